@@ -1,0 +1,260 @@
+/*
+ * mpgos.h - C-ABI of the GB300 ensemble explicit Runge-Kutta integrator.
+ *
+ * This is the boundary that replaces the host object of the reference,
+ * class ProblemSolver in SourceCodes/SingleSystem_PerThread_Interface.cuh:117-208
+ * (and the kernel launch it performs in Solve(), :1279-1285). Plain C types
+ * only: opaque handles, pointers, sizes and int status codes.
+ *
+ * Two pieces meet at this ABI:
+ *   - the runtime (libmpgos_runtime.so) owns device memory, pinned host
+ *     buffers, the stream, CUDA graphs, timing and the autotuner;
+ *   - a system plugin (libmpgos_<system>.so, or the user's own translation
+ *     unit through the C++ drop-in header mpgos/SingleSystem_PerThread_Interface.cuh)
+ *     holds the sm_103a kernels instantiated for one set of user device hooks
+ *     (the PerThread_* templates of the reference, e.g.
+ *     Tutorials_SingleSystem_PerThread/T1_Reference/Reference_SystemDefinition.cuh:6-76)
+ *     and hands the runtime an mpgos_pt_kernels table.
+ *
+ * Error convention: every function returns MPGOS_OK (0) or a positive error
+ * code; mpgos_last_error() returns a thread-local message for the last error.
+ * The reference prints and calls exit(1) instead
+ * (SingleSystem_PerThread_Interface.cuh:13-22, :566-581); the C++ drop-in
+ * header restores that behaviour on top of these codes.
+ */
+#ifndef MPGOS_H
+#define MPGOS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MPGOS_ABI_VERSION 1
+
+/* ---- status codes ------------------------------------------------------ */
+enum mpgos_status {
+    MPGOS_OK              = 0,
+    MPGOS_ERR_ARGUMENT    = 1, /* bad index, option, variable or value      */
+    MPGOS_ERR_CUDA        = 2, /* a CUDA runtime call failed                */
+    MPGOS_ERR_MEMORY      = 3, /* device or pinned host allocation failed   */
+    MPGOS_ERR_SHAPE       = 4, /* kernel table does not match the request   */
+    MPGOS_ERR_UNSUPPORTED = 5  /* mode or feature not compiled in           */
+};
+
+/* ---- Algorithms (SingleSystem_PerThread_Interface.cuh:33) --------------- */
+enum mpgos_algorithm { MPGOS_RK4 = 0, MPGOS_RKCK45 = 1 };
+
+/* ---- ListOfVariables (SingleSystem_PerThread_Interface.cuh:35-47) -------- */
+enum mpgos_variable {
+    MPGOS_ALL                       = 0,
+    MPGOS_TIME_DOMAIN               = 1,  /* [2][NT]                 */
+    MPGOS_ACTUAL_STATE              = 2,  /* [SD][NT]                */
+    MPGOS_ACTUAL_TIME               = 3,  /* [NT]                    */
+    MPGOS_CONTROL_PARAMETERS        = 4,  /* [NCP][NT]               */
+    MPGOS_SHARED_PARAMETERS         = 5,  /* [NSP]                   */
+    MPGOS_INTEGER_SHARED_PARAMETERS = 6,  /* [NISP] (int32)          */
+    MPGOS_ACCESSORIES               = 7,  /* [NA][NT]                */
+    MPGOS_INTEGER_ACCESSORIES       = 8,  /* [NIA][NT] (int32)       */
+    MPGOS_DENSE_OUTPUT              = 9,  /* index + time + state    */
+    MPGOS_DENSE_INDEX               = 10, /* [NT] (int32)            */
+    MPGOS_DENSE_TIME                = 11, /* [NDO][NT]               */
+    MPGOS_DENSE_STATE               = 12, /* [NDO][SD][NT]           */
+    /* extensions (no counterpart in the reference) */
+    MPGOS_STATUS                    = 32, /* [NT] int32 bit flags of the last Solve  */
+    MPGOS_ACCEPTED_STEPS            = 33, /* [NT] int32, accepted steps, last Solve  */
+    MPGOS_REJECTED_STEPS            = 34  /* [NT] int32, rejected attempts, last Solve */
+};
+
+/* ---- ListOfSolverOptions (SingleSystem_PerThread_Interface.cuh:49-62) ---- */
+enum mpgos_option {
+    MPGOS_THREADS_PER_BLOCK            = 0,
+    MPGOS_INITIAL_TIME_STEP            = 1,
+    MPGOS_ACTIVE_NUMBER_OF_THREADS     = 2,
+    MPGOS_MAXIMUM_TIME_STEP            = 3,
+    MPGOS_MINIMUM_TIME_STEP            = 4,
+    MPGOS_TIME_STEP_GROW_LIMIT         = 5,
+    MPGOS_TIME_STEP_SHRINK_LIMIT       = 6,
+    MPGOS_RELATIVE_TOLERANCE           = 7,  /* indexed by component  */
+    MPGOS_ABSOLUTE_TOLERANCE           = 8,  /* indexed by component  */
+    MPGOS_EVENT_TOLERANCE              = 9,  /* indexed by event      */
+    MPGOS_EVENT_DIRECTION              = 10, /* indexed by event      */
+    MPGOS_DENSE_OUTPUT_MINIMUM_TIME_STEP = 11,
+    MPGOS_DENSE_OUTPUT_SAVE_FREQUENCY  = 12,
+    MPGOS_PREFER_SHARED_MEMORY         = 13,
+    /* extensions */
+    MPGOS_KERNEL_MODE                  = 32, /* MPGOS_MODE_* bit set             */
+    MPGOS_MAXIMUM_ATTEMPTS             = 33  /* step attempts per instance and launch */
+};
+
+/* ---- kernel modes (extensions) -----------------------------------------
+ * PLAIN        reference arithmetic: one instance per thread, static grid,
+ *              controller with FP64 pow/div exactly as
+ *              SingleSystem_PerThread_ExplicitRungeKutta_ErrorControllers.cuh:23-85.
+ * FAST_CONTROL step-size factor from FP32 log2/exp2 of the tolerance ratio and
+ *              integer-pipe compares on FP64 bit patterns; accept/reject
+ *              decisions are unchanged, the new step size differs from the
+ *              FP64 pow by about 1e-7 relative.
+ * PERSISTENT   one resident grid; every lane pulls the next instance from a
+ *              device work counter when its instance finishes.
+ * FP32_STAGE   right-hand side and stage sums in FP32; state update, time,
+ *              error norm, step control and events in FP64 (RKCK45 only).
+ * CHOSEN       FAST_CONTROL | PERSISTENT.
+ */
+#define MPGOS_MODE_PLAIN        0
+#define MPGOS_MODE_FAST_CONTROL 1
+#define MPGOS_MODE_PERSISTENT   2
+#define MPGOS_MODE_FP32_STAGE   4
+#define MPGOS_MODE_CHOSEN       (MPGOS_MODE_FAST_CONTROL | MPGOS_MODE_PERSISTENT)
+
+/* ---- per-instance status flags (MPGOS_STATUS), extensions --------------
+ * The reference reports these conditions with device printf only
+ * (SingleSystem_PerThread_ExplicitRungeKutta_ErrorControllers.cuh:15,66,73,
+ *  SingleSystem_PerThread_EventHandling.cuh:38). */
+#define MPGOS_INSTANCE_OK               0
+#define MPGOS_INSTANCE_NONFINITE        1  /* stopped: state not finite            */
+#define MPGOS_INSTANCE_MINIMUM_STEP     2  /* warning: continued at minimum step    */
+#define MPGOS_INSTANCE_EVENT_OMITTED    4  /* warning: event step below minimum     */
+#define MPGOS_INSTANCE_ATTEMPT_LIMIT    8  /* stopped: MPGOS_MAXIMUM_ATTEMPTS hit   */
+
+/* ---- kernel table handed from a system plugin to the runtime ----------- */
+
+/* Compile-time shape of a system plugin (template parameters of the
+ * reference's ProblemSolver, SingleSystem_PerThread_Interface.cuh:117). */
+typedef struct mpgos_pt_shape {
+    int32_t sd, ncp, nsp, nisp, ne, na, nia;
+    int32_t algorithm;       /* mpgos_algorithm             */
+    int32_t precision_bytes; /* 8 = double, 4 = float      */
+    int32_t modes;           /* MPGOS_MODE_* bits compiled  */
+} mpgos_pt_shape;
+
+/* Everything one launch needs. Mirrors the by-value kernel arguments of the
+ * reference (Struct_ThreadConfiguration, Struct_GlobalVariables,
+ * Struct_SharedMemoryUsage, Struct_SolverOptions,
+ * SingleSystem_PerThread_Interface.cuh:72-115), plus the extensions. Device
+ * pointers; floating-point arrays are in the table's precision. */
+typedef struct mpgos_pt_launch {
+    int64_t nt;           /* instances allocated (SoA stride)       */
+    int64_t n_active;     /* instances integrated: 0 .. n_active-1  */
+    int32_t ndo;          /* dense-output slots per instance        */
+    int32_t mode;         /* MPGOS_MODE_* bits                      */
+    int32_t prefer_shared;
+    int32_t dense_save_frequency;
+    int64_t max_attempts;
+    double  initial_dt, max_dt, min_dt, grow_limit, shrink_limit, dense_min_dt;
+
+    void*          time_domain;
+    void*          actual_state;
+    void*          actual_time;
+    void*          control_parameters;
+    const void*    shared_parameters;
+    const int32_t* integer_shared_parameters;
+    void*          accessories;
+    int32_t*       integer_accessories;
+    const void*    relative_tolerance;
+    const void*    absolute_tolerance;
+    const void*    event_tolerance;
+    const int32_t* event_direction;
+    int32_t*       dense_index;
+    void*          dense_time;
+    void*          dense_state;
+    int32_t*       status;          /* [NT] or NULL */
+    int32_t*       accepted_steps;  /* [NT] or NULL */
+    int32_t*       rejected_steps;  /* [NT] or NULL */
+    uint32_t*      work_counter;    /* PERSISTENT: one zeroed counter */
+} mpgos_pt_launch;
+
+typedef struct mpgos_pt_kernels {
+    int32_t        abi_version;     /* MPGOS_ABI_VERSION */
+    mpgos_pt_shape shape;
+    const char*    name;
+    /* Launch on the given cudaStream_t; returns a cudaError_t value. */
+    int (*launch)(const mpgos_pt_launch* args, int grid, int block, size_t dynamic_smem, void* stream);
+    /* Resident blocks per SM for (mode, block, dynamic smem); cudaError_t. */
+    int (*occupancy)(int32_t mode, int block, size_t dynamic_smem, int* blocks_per_sm);
+} mpgos_pt_kernels;
+
+/* ---- solver object (ProblemSolver, SingleSystem_PerThread_Interface.cuh:117-208) */
+typedef struct mpgos_pt_solver mpgos_pt_solver;
+
+/* ProblemSolver(int device), :309-518: stream, event, pinned host + device
+ * buffers sized for nt instances and ndo dense-output slots; defaults of
+ * :475-496 (tolerances 1e-8, event tolerance 1e-6, direction 0). */
+int mpgos_pt_create(const mpgos_pt_kernels* kernels, int64_t nt, int32_t ndo,
+                    int device, mpgos_pt_solver** out);
+/* ~ProblemSolver, :521-555. */
+int mpgos_pt_destroy(mpgos_pt_solver* solver);
+/* Compiled shape, instance count and dense slots of a solver. */
+int mpgos_pt_get_shape(const mpgos_pt_solver* solver, mpgos_pt_shape* shape,
+                       int64_t* nt, int32_t* ndo);
+
+/* SolverOption(option, value) and SolverOption(option, index, value),
+ * :611-703. index is ignored by the non-indexed options. Tolerance and event
+ * options are pushed to the device immediately, as :679-694 do. */
+int mpgos_pt_set_option(mpgos_pt_solver* solver, int32_t option, int32_t index, double value);
+int mpgos_pt_get_option(const mpgos_pt_solver* solver, int32_t option, int32_t index, double* value);
+
+/* Pinned host buffer of a variable (the h_* arrays of :399-409) and its
+ * element count. SetHost/GetHost (:706-1080) become plain stores and loads
+ * at index pid + serial*NT (dense state: pid + comp*NT + step*NT*SD). */
+int mpgos_pt_host_buffer(mpgos_pt_solver* solver, int32_t variable, void** ptr, int64_t* count);
+/* Device buffer of a variable (for callers that keep data resident in HBM). */
+int mpgos_pt_device_buffer(mpgos_pt_solver* solver, int32_t variable, void** ptr, int64_t* count);
+
+/* SynchroniseFromHostToDevice / SynchroniseFromDeviceToHost, :833-965.
+ * Asynchronous on the solver's stream. */
+int mpgos_pt_sync_h2d(mpgos_pt_solver* solver, int32_t variable);
+int mpgos_pt_sync_d2h(mpgos_pt_solver* solver, int32_t variable);
+
+/* Solve(), :1279-1285: one asynchronous launch on the solver's stream. The
+ * step size restarts from InitialTimeStep on every launch, as
+ * SingleSystem_PerThread_Solver.cuh:138-139 does. */
+int mpgos_pt_solve(mpgos_pt_solver* solver);
+/* n_phases consecutive Solve() calls, captured once into a CUDA graph and
+ * replayed (extension). Bit-identical to n_phases calls of mpgos_pt_solve. If
+ * stream_accessory >= 0, the accessory column stream_accessory is copied after
+ * every phase into the device buffer phase_output[phase][NT]. */
+int mpgos_pt_solve_phases(mpgos_pt_solver* solver, int32_t n_phases,
+                          int32_t stream_accessory, void* phase_output);
+
+/* InsertSynchronisationPoint / SynchroniseSolver / SynchroniseDevice,
+ * :1288-1312. */
+int mpgos_pt_insert_sync_point(mpgos_pt_solver* solver);
+int mpgos_pt_sync_solver(mpgos_pt_solver* solver);
+int mpgos_pt_sync_device(mpgos_pt_solver* solver);
+
+/* Stream of the solver as a cudaStream_t (extension). */
+int mpgos_pt_stream(mpgos_pt_solver* solver, void** stream);
+
+/* Launch configuration the next Solve() will use (extension). */
+int mpgos_pt_launch_config(mpgos_pt_solver* solver, int* grid, int* block, int32_t* mode);
+
+/* Time with CUDA events on the solver's stream (extension): start, then stop
+ * returns the elapsed milliseconds after synchronising the stop event. */
+int mpgos_pt_timer_start(mpgos_pt_solver* solver);
+int mpgos_pt_timer_stop(mpgos_pt_solver* solver, float* milliseconds);
+
+/* Autotuner (extension): times one Solve() per candidate (block size x
+ * static/persistent mapping) on a scratch copy of the current device state,
+ * restores the state, keeps the fastest configuration and, if cache_path is
+ * not NULL, records it in a JSON cache keyed by system, shape, NT and GPU. */
+int mpgos_pt_autotune(mpgos_pt_solver* solver, int32_t fast_control, const char* cache_path);
+
+/* Thread-local message of the last failing call ("" if none). */
+const char* mpgos_last_error(void);
+
+/* Runtime ABI version (MPGOS_ABI_VERSION). */
+int mpgos_abi_version(void);
+
+/* ---- entry point exported by every system plugin --------------------- */
+/* Kernel table for (algorithm, precision_bytes), or NULL if not compiled. */
+typedef const mpgos_pt_kernels* (*mpgos_pt_system_fn)(int32_t algorithm, int32_t precision_bytes);
+const mpgos_pt_kernels* mpgos_pt_system_kernels(int32_t algorithm, int32_t precision_bytes);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MPGOS_H */

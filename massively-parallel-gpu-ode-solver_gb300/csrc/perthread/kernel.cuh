@@ -1,0 +1,454 @@
+// Per-thread ensemble solver kernels for sm_103a.
+//
+// One ODE instance per lane, the whole integration loop of one launch inside
+// the kernel, state in registers, SoA [field][NT] arrays in HBM - the execution
+// model of the reference kernel SingleSystem_PerThread
+// (SourceCodes/SingleSystem_PerThread_Solver.cuh:11-437), re-organised for GB300:
+//
+//  * The per-instance loop is a state machine that performs one step attempt
+//    per iteration. A lane whose instance has finished writes it back and, in
+//    PERSISTENT mode, pulls the next instance index from a device work counter
+//    inside the same iteration, so the warp keeps stepping with all lanes busy
+//    instead of idling until its slowest lane finishes. This replaces the
+//    reference's one-thread-one-instance launch and its NumberOfActiveThreads
+//    tail guard (SingleSystem_PerThread_Solver.cuh:91).
+//  * Tolerances, event options and the shared parameters are staged once per
+//    CTA in shared memory behind a barrier.
+//  * Every instance loop is bounded by MaximumAttempts; an instance that hits
+//    it stops with MPGOS_INSTANCE_ATTEMPT_LIMIT instead of spinning.
+//  * Per-instance status flags and accepted/rejected step counts replace the
+//    reference's device printf warnings.
+//
+// The user hooks (PerThread_OdeFunction, PerThread_EventFunction,
+// PerThread_ActionAfterEventDetection, PerThread_ActionAfterSuccessfulTimeStep,
+// PerThread_Initialization, PerThread_Finalization) must be declared before
+// this header is included, exactly as with the reference interface header.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "mpgos.h"
+#include "numerics.cuh"
+
+// Largest block the kernels are compiled for (register budget 65536 / 256).
+#ifndef MPGOS_MAX_BLOCK
+#define MPGOS_MAX_BLOCK 256
+#endif
+
+namespace mpgos {
+namespace pt {
+
+template <int SD_, int NCP_, int NSP_, int NISP_, int NE_, int NA_, int NIA_>
+struct Shape {
+    static constexpr int SD = SD_, NCP = NCP_, NSP = NSP_, NISP = NISP_, NE = NE_, NA = NA_, NIA = NIA_;
+};
+
+// Kernel arguments in the kernel's precision (the reference passes the same
+// information as Struct_ThreadConfiguration / Struct_GlobalVariables /
+// Struct_SharedMemoryUsage / Struct_SolverOptions,
+// SingleSystem_PerThread_Interface.cuh:72-115).
+template <class P>
+struct Args {
+    long long nt;
+    long long n_active;
+    P* td;
+    P* x;
+    P* t;
+    P* cp;
+    const P* sp;
+    const int* spi;
+    P* acc;
+    int* acci;
+    const P* rtol;
+    const P* atol;
+    const P* etol;
+    const int* edir;
+    int* didx;
+    P* dtime;
+    P* dstate;
+    int* status;
+    int* n_acc;
+    int* n_rej;
+    unsigned int* work;
+    int prefer_shared;
+    Options<P> o;
+};
+
+// Registers of one instance between step attempts.
+template <class S, class P>
+struct Instance {
+    static constexpr int SD = S::SD;
+    long long i;
+    P td[2];
+    P x[SD];
+    P cp[AtLeastOne<S::NCP>::value];
+    P acc[AtLeastOne<S::NA>::value];
+    int acci[AtLeastOne<S::NIA>::value];
+    P ga[AtLeastOne<S::NE>::value];
+    P t, dt, new_dt, dense_next;
+    int didx, skipped, terminate, udt, status, nacc, nrej;
+    long long attempts;
+};
+
+// Block-shared copies of the per-block constant data.
+template <class S, class P>
+struct Staged {
+    P* sp;
+    int* spi;
+    const P* rtol;
+    const P* atol;
+    const P* etol;
+    const int* edir;
+};
+
+template <class S, int ALG, class P, int MODE>
+struct Solver {
+    static constexpr int SD = S::SD, NCP = S::NCP, NSP = S::NSP, NISP = S::NISP;
+    static constexpr int NE = S::NE, NA = S::NA, NIA = S::NIA;
+    static constexpr bool PERSISTENT = (MODE & MPGOS_MODE_PERSISTENT) != 0;
+    // FAST_CONTROL and FP32_STAGE apply to FP64 instances of the adaptive scheme.
+    static constexpr bool IS_DOUBLE = sizeof(P) == 8;
+    static constexpr bool FAST = ((MODE & MPGOS_MODE_FAST_CONTROL) != 0) && IS_DOUBLE && ALG == MPGOS_RKCK45;
+    static constexpr bool F32S = ((MODE & MPGOS_MODE_FP32_STAGE) != 0) && IS_DOUBLE && ALG == MPGOS_RKCK45;
+    using Inst = Instance<S, P>;
+
+    // Load instance i and run the start-of-launch part of the reference loop
+    // (SingleSystem_PerThread_Solver.cuh:117-193).
+    __device__ static void begin(Inst& s, long long i, const Args<P>& a, const Staged<S, P>& g,
+                                 float* cpf, float* accf)
+    {
+        const long long nt = a.nt;
+        s.i = i;
+#pragma unroll
+        for (int k = 0; k < 2; k++) s.td[k] = a.td[i + k * nt];
+#pragma unroll
+        for (int k = 0; k < SD; k++) s.x[k] = a.x[i + k * nt];
+#pragma unroll
+        for (int k = 0; k < NCP; k++) s.cp[k] = a.cp[i + k * nt];
+#pragma unroll
+        for (int k = 0; k < NA; k++) s.acc[k] = a.acc[i + k * nt];
+#pragma unroll
+        for (int k = 0; k < NIA; k++) s.acci[k] = a.acci[i + k * nt];
+        s.t          = a.t[i];
+        s.dt         = a.o.initial_dt;
+        s.new_dt     = a.o.initial_dt;
+        s.didx       = a.didx[i];
+        s.skipped    = 0;
+        s.terminate  = 0;
+        s.udt        = 0;
+        s.status     = 0;
+        s.nacc       = 0;
+        s.nrej       = 0;
+        s.attempts   = 0;
+        s.dense_next = s.t;
+
+        const int ti = static_cast<int>(i), nti = static_cast<int>(nt);
+        PerThread_Initialization(ti, nti, s.didx, s.t, s.dt, s.td, s.x, s.cp, g.sp, g.spi, s.acc, s.acci);
+        if (NE > 0)
+            PerThread_EventFunction(ti, nti, s.ga, s.t, s.dt, s.td, s.x, s.cp, g.sp, g.spi, s.acc, s.acci);
+        if (a.o.ndo > 0)
+            dense_store<SD, P>(i, nt, 1, s.didx, a.o.ndo, a.dtime, a.dstate, s.t, s.x, s.skipped,
+                               s.dense_next, a.o.dense_min_dt, s.td[1]);
+        if (F32S) refresh_f32(s, cpf, accf);
+    }
+
+    __device__ static void refresh_f32(const Inst& s, float* cpf, float* accf)
+    {
+#pragma unroll
+        for (int k = 0; k < NCP; k++) cpf[k] = static_cast<float>(s.cp[k]);
+#pragma unroll
+        for (int k = 0; k < NA; k++) accf[k] = static_cast<float>(s.acc[k]);
+    }
+
+    // One step attempt: the body of the reference's while loop
+    // (SingleSystem_PerThread_Solver.cuh:197-393).
+    __device__ static void attempt(Inst& s, const Args<P>& a, const Staged<S, P>& g, float* cpf,
+                                   float* spf, float* accf)
+    {
+        const Options<P>& o = a.o;
+        if (s.attempts >= o.max_attempts) {
+            s.status |= MPGOS_INSTANCE_ATTEMPT_LIMIT;
+            s.terminate = 1;
+            return;
+        }
+        s.attempts++;
+
+        const int ti = static_cast<int>(s.i), nti = static_cast<int>(a.nt);
+        int update = 1, finite = 1, end_reached = 0;
+        P xn[SD];
+        P err[SD];
+        s.dt = s.new_dt;
+        if (s.dt > (s.td[1] - s.t)) {
+            s.dt        = s.td[1] - s.t;
+            end_reached = 1;
+        }
+
+        if (ALG == MPGOS_RK4) {
+            step_rk4<SD, P>(ti, nti, s.t, s.dt, s.x, xn, finite, s.cp, g.sp, g.spi, s.acc, s.acci);
+            control_rk4<P>(o, finite, s.terminate, s.new_dt, s.status);
+        } else {
+            if constexpr (F32S) {
+                step_rkck45_f32stage<SD, NCP, NA>(ti, nti, s.t, s.dt, s.x, xn, err, finite, cpf, spf, g.spi,
+                                                  accf, s.acci);
+            } else {
+                step_rkck45<SD, P, FAST>(ti, nti, s.t, s.dt, s.x, xn, err, finite, s.cp, g.sp, g.spi, s.acc,
+                                         s.acci);
+            }
+            if constexpr (FAST) {
+                control_rkck45_fast<SD>(o, s.dt, s.x, xn, err, g.rtol, g.atol, update, finite, s.terminate,
+                                        s.new_dt, s.status);
+            } else {
+                control_rkck45_plain<SD, P>(o, s.dt, s.x, xn, err, g.rtol, g.atol, update, finite, s.terminate,
+                                            s.new_dt, s.status);
+            }
+        }
+
+        P gn[AtLeastOne<NE>::value];
+        if (NE > 0) {
+            PerThread_EventFunction(ti, nti, gn, s.t + s.dt, s.dt, s.td, xn, s.cp, g.sp, g.spi, s.acc, s.acci);
+            event_step_control<NE, P>(update, s.terminate, s.ga, gn, g.etol, g.edir, s.dt, s.new_dt, o.min_dt,
+                                      s.status);
+        }
+
+        if (update == 1) {
+            s.nacc++;
+            s.t += s.dt;
+#pragma unroll
+            for (int k = 0; k < SD; k++) s.x[k] = xn[k];
+
+            PerThread_ActionAfterSuccessfulTimeStep(ti, nti, s.udt, s.t, s.dt, s.td, s.x, s.cp, g.sp, g.spi,
+                                                    s.acc, s.acci);
+            if (NE > 0) {
+                for (int e = 0; e < NE; e++) {
+                    if (event_detected<P>(s.ga[e], gn[e], g.etol[e], g.edir[e]))
+                        PerThread_ActionAfterEventDetection(ti, nti, e, s.udt, s.t, s.dt, s.td, s.x, s.cp, g.sp,
+                                                            g.spi, s.acc, s.acci);
+                }
+                PerThread_EventFunction(ti, nti, gn, s.t, s.dt, s.td, s.x, s.cp, g.sp, g.spi, s.acc, s.acci);
+#pragma unroll
+                for (int e = 0; e < NE; e++) s.ga[e] = gn[e];
+            }
+            if (o.ndo > 0) {
+                const int store = dense_condition<P>(s.t, s.dense_next, s.didx, s.skipped, end_reached, s.udt,
+                                                     o.ndo, o.dense_freq);
+                dense_store<SD, P>(s.i, a.nt, store, s.didx, o.ndo, a.dtime, a.dstate, s.t, s.x, s.skipped,
+                                   s.dense_next, o.dense_min_dt, s.td[1]);
+            }
+            if (F32S && NA > 0) refresh_f32(s, cpf, accf);
+            if ((end_reached == 1) || (s.udt == 1)) s.terminate = 1;
+        } else {
+            s.nrej++;
+        }
+    }
+
+    // Finalization hook and write-back (SingleSystem_PerThread_Solver.cuh:397-435).
+    __device__ static void end(Inst& s, const Args<P>& a, const Staged<S, P>& g)
+    {
+        const long long i = s.i, nt = a.nt;
+        const int ti = static_cast<int>(i), nti = static_cast<int>(nt);
+        PerThread_Finalization(ti, nti, s.didx, s.t, s.dt, s.td, s.x, s.cp, g.sp, g.spi, s.acc, s.acci);
+#pragma unroll
+        for (int k = 0; k < 2; k++) a.td[i + k * nt] = s.td[k];
+#pragma unroll
+        for (int k = 0; k < SD; k++) a.x[i + k * nt] = s.x[k];
+#pragma unroll
+        for (int k = 0; k < NCP; k++) a.cp[i + k * nt] = s.cp[k];
+#pragma unroll
+        for (int k = 0; k < NA; k++) a.acc[i + k * nt] = s.acc[k];
+#pragma unroll
+        for (int k = 0; k < NIA; k++) a.acci[i + k * nt] = s.acci[k];
+        a.t[i]    = s.t;
+        a.didx[i] = s.didx;
+        if (a.status) a.status[i] = s.status;
+        if (a.n_acc) a.n_acc[i] = s.nacc;
+        if (a.n_rej) a.n_rej[i] = s.nrej;
+    }
+
+    // Next instance for a lane whose instance finished: warp-aggregated
+    // atomic on the work counter; the counter counts instances handed out
+    // beyond the first one per lane.
+    __device__ static long long next_index(const Args<P>& a, long long total_threads)
+    {
+        if (!PERSISTENT) return a.n_active;
+        const unsigned mask   = __activemask();
+        const int lane        = threadIdx.x & 31;
+        const int leader      = __ffs(mask) - 1;
+        const unsigned rank   = __popc(mask & ((1u << lane) - 1u));
+        unsigned base = 0;
+        if (lane == leader) base = atomicAdd(a.work, static_cast<unsigned>(__popc(mask)));
+        base = __shfl_sync(mask, base, leader);
+        return total_threads + static_cast<long long>(base) + rank;
+    }
+};
+
+// Dynamic shared memory: [NSP] P, then [NISP] int.
+template <class S, class P>
+__host__ __device__ constexpr size_t dynamic_smem_bytes()
+{
+    return sizeof(P) * S::NSP + sizeof(int) * S::NISP;
+}
+
+template <class S, int ALG, class P, int MODE>
+__global__ void __launch_bounds__(MPGOS_MAX_BLOCK) perthread_kernel(Args<P> a)
+{
+    using Sv = Solver<S, ALG, P, MODE>;
+    constexpr int SD = S::SD, NSP = S::NSP, NISP = S::NISP, NE = S::NE;
+    constexpr bool ADAPTIVE = (ALG == MPGOS_RKCK45);
+
+    extern __shared__ __align__(16) unsigned char mpgos_dyn_smem[];
+    __shared__ P s_rtol[ADAPTIVE ? SD : 1];
+    __shared__ P s_atol[ADAPTIVE ? SD : 1];
+    __shared__ P s_etol[AtLeastOne<NE>::value];
+    __shared__ int s_edir[AtLeastOne<NE>::value];
+    __shared__ float s_spf[AtLeastOne<NSP>::value];
+
+    P* dyn_sp   = reinterpret_cast<P*>(mpgos_dyn_smem);
+    int* dyn_spi = reinterpret_cast<int*>(mpgos_dyn_smem + sizeof(P) * NSP);
+
+    for (int k = threadIdx.x; k < SD; k += blockDim.x) {
+        if (ADAPTIVE) {
+            s_rtol[k] = a.rtol[k];
+            s_atol[k] = a.atol[k];
+        }
+    }
+    for (int k = threadIdx.x; k < NE; k += blockDim.x) {
+        s_etol[k] = a.etol[k];
+        s_edir[k] = a.edir[k];
+    }
+    if (a.prefer_shared) {
+        for (int k = threadIdx.x; k < NSP; k += blockDim.x) dyn_sp[k] = a.sp[k];
+        for (int k = threadIdx.x; k < NISP; k += blockDim.x) dyn_spi[k] = a.spi[k];
+    }
+    if (Sv::F32S) {
+        for (int k = threadIdx.x; k < NSP; k += blockDim.x) s_spf[k] = static_cast<float>(a.sp[k]);
+    }
+    __syncthreads();
+
+    Staged<S, P> g;
+    g.sp   = a.prefer_shared ? dyn_sp : const_cast<P*>(a.sp);
+    g.spi  = a.prefer_shared ? dyn_spi : const_cast<int*>(a.spi);
+    g.rtol = s_rtol;
+    g.atol = s_atol;
+    g.etol = s_etol;
+    g.edir = s_edir;
+
+    float cpf[AtLeastOne<S::NCP>::value];
+    float accf[AtLeastOne<S::NA>::value];
+
+    const long long total = static_cast<long long>(gridDim.x) * blockDim.x;
+    long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= a.n_active) return;
+
+    typename Sv::Inst s;
+    Sv::begin(s, i, a, g, cpf, accf);
+    while (true) {
+        if (s.terminate) {
+            Sv::end(s, a, g);
+            i = Sv::next_index(a, total);
+            if (i >= a.n_active) break;
+            Sv::begin(s, i, a, g, cpf, accf);
+        }
+        Sv::attempt(s, a, g, cpf, s_spf, accf);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Kernel table: the launch side of the plugin ABI (mpgos_pt_kernels in mpgos.h).
+// ---------------------------------------------------------------------------
+template <class P>
+Args<P> make_args(const mpgos_pt_launch& L)
+{
+    Args<P> a;
+    a.nt            = L.nt;
+    a.n_active      = L.n_active;
+    a.td            = static_cast<P*>(L.time_domain);
+    a.x             = static_cast<P*>(L.actual_state);
+    a.t             = static_cast<P*>(L.actual_time);
+    a.cp            = static_cast<P*>(L.control_parameters);
+    a.sp            = static_cast<const P*>(L.shared_parameters);
+    a.spi           = L.integer_shared_parameters;
+    a.acc           = static_cast<P*>(L.accessories);
+    a.acci          = L.integer_accessories;
+    a.rtol          = static_cast<const P*>(L.relative_tolerance);
+    a.atol          = static_cast<const P*>(L.absolute_tolerance);
+    a.etol          = static_cast<const P*>(L.event_tolerance);
+    a.edir          = L.event_direction;
+    a.didx          = L.dense_index;
+    a.dtime         = static_cast<P*>(L.dense_time);
+    a.dstate        = static_cast<P*>(L.dense_state);
+    a.status        = L.status;
+    a.n_acc         = L.accepted_steps;
+    a.n_rej         = L.rejected_steps;
+    a.work          = L.work_counter;
+    a.prefer_shared = L.prefer_shared;
+    a.o.initial_dt   = static_cast<P>(L.initial_dt);
+    a.o.max_dt       = static_cast<P>(L.max_dt);
+    a.o.min_dt       = static_cast<P>(L.min_dt);
+    a.o.grow         = static_cast<P>(L.grow_limit);
+    a.o.shrink       = static_cast<P>(L.shrink_limit);
+    a.o.dense_min_dt = static_cast<P>(L.dense_min_dt);
+    a.o.min_dt_guard = a.o.min_dt * static_cast<P>(1.01);
+    a.o.dense_freq   = L.dense_save_frequency;
+    a.o.ndo          = L.ndo;
+    a.o.max_attempts = L.max_attempts;
+    return a;
+}
+
+template <class S, int ALG, class P>
+struct KernelTable {
+    static constexpr bool DOUBLE_ADAPTIVE = sizeof(P) == 8 && ALG == MPGOS_RKCK45;
+    static constexpr int MODES =
+        MPGOS_MODE_PERSISTENT | (DOUBLE_ADAPTIVE ? (MPGOS_MODE_FAST_CONTROL | MPGOS_MODE_FP32_STAGE) : 0);
+
+    // Modes a table can run; the runtime only asks for these.
+    static void* kernel_for(int mode)
+    {
+        switch (mode) {
+            case 0: return reinterpret_cast<void*>(&perthread_kernel<S, ALG, P, 0>);
+            case 2: return reinterpret_cast<void*>(&perthread_kernel<S, ALG, P, 2>);
+            default: break;
+        }
+        if constexpr (DOUBLE_ADAPTIVE) {
+            switch (mode) {
+                case 1: return reinterpret_cast<void*>(&perthread_kernel<S, ALG, P, 1>);
+                case 3: return reinterpret_cast<void*>(&perthread_kernel<S, ALG, P, 3>);
+                case 5: return reinterpret_cast<void*>(&perthread_kernel<S, ALG, P, 5>);
+                case 7: return reinterpret_cast<void*>(&perthread_kernel<S, ALG, P, 7>);
+                default: break;
+            }
+        }
+        return nullptr;
+    }
+
+    static int launch(const mpgos_pt_launch* L, int grid, int block, size_t smem, void* stream)
+    {
+        void* fn = kernel_for(L->mode);
+        if (fn == nullptr) return static_cast<int>(cudaErrorInvalidValue);
+        Args<P> a = make_args<P>(*L);
+        void* params[] = {&a};
+        return static_cast<int>(cudaLaunchKernel(fn, dim3(grid), dim3(block), params, smem,
+                                                 static_cast<cudaStream_t>(stream)));
+    }
+
+    static int occupancy(int32_t mode, int block, size_t smem, int* blocks)
+    {
+        void* fn = kernel_for(mode);
+        if (fn == nullptr) return static_cast<int>(cudaErrorInvalidValue);
+        return static_cast<int>(cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, fn, block, smem));
+    }
+
+    static const mpgos_pt_kernels* get(const char* name)
+    {
+        static mpgos_pt_kernels table = {
+            MPGOS_ABI_VERSION,
+            {S::SD, S::NCP, S::NSP, S::NISP, S::NE, S::NA, S::NIA, ALG, static_cast<int32_t>(sizeof(P)), MODES},
+            name,
+            &launch,
+            &occupancy};
+        return &table;
+    }
+};
+
+}  // namespace pt
+}  // namespace mpgos

@@ -1,0 +1,129 @@
+"""In-tree build of the native libraries (no pip install, no cmake).
+
+Outputs, all under ``massively-parallel-gpu-ode-solver_gb300/_build/``:
+
+* ``libmpgos_runtime.so``   host runtime implementing the C-ABI of ``include/mpgos.h``
+* ``libmpgos_<system>.so``  one system plugin per hook file in ``systems/``
+  (sm_103a kernels for that system's user hooks)
+
+Every CUDA translation unit is compiled with
+``-gencode arch=compute_103a,code=sm_103a`` only. Units are compiled in
+parallel and skipped when their output is newer than every input.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+from pathlib import Path
+
+PKG_ROOT = Path(__file__).resolve().parent.parent          # massively-parallel-gpu-ode-solver_gb300/
+REPO_ROOT = PKG_ROOT.parent
+BUILD_DIR = PKG_ROOT / "_build"
+INCLUDE_DIR = REPO_ROOT / "include"
+CSRC = PKG_ROOT / "csrc"
+SYSTEMS_DIR = PKG_ROOT / "systems"
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+# System plugins built by default: name -> source file (hook file + plugin export).
+SYSTEMS = ["lorenz", "duffing", "duffing_param", "duffing_events", "bouncing_ball", "keller_miksis"]
+
+
+def nvcc_path() -> str:
+    cand = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    return cand
+
+
+def cuda_home() -> Path:
+    return Path(nvcc_path()).resolve().parent.parent
+
+
+def _newer(out: Path, deps) -> bool:
+    if not out.exists():
+        return False
+    t = out.stat().st_mtime
+    return all(Path(d).stat().st_mtime <= t for d in deps)
+
+
+def _deps_glob(*dirs) -> list:
+    out = []
+    for d in dirs:
+        for ext in ("*.cuh", "*.h", "*.cu", "*.cpp", "*.hpp"):
+            out.extend(Path(d).rglob(ext))
+    return out
+
+
+def _run(cmd: list, what: str) -> None:
+    proc = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if proc.returncode != 0:
+        raise RuntimeError(f"build of {what} failed (exit {proc.returncode}):\n{' '.join(cmd)}\n{proc.stdout}")
+
+
+def _common_flags() -> list:
+    lib = cuda_home() / "lib64"
+    return [
+        "-O3", "-std=c++17", "-lineinfo", "-shared", "-Xcompiler", "-fPIC",
+        "-Xcompiler", "-fvisibility=hidden", "-cudart", "shared",
+        f"-I{INCLUDE_DIR}", f"-I{CSRC / 'perthread'}", f"-I{SYSTEMS_DIR}",
+        "-Xlinker", f"-rpath,{lib}", "-Xlinker", "-rpath,$ORIGIN",
+    ]
+
+
+def runtime_lib() -> Path:
+    return BUILD_DIR / "libmpgos_runtime.so"
+
+
+def system_lib(name: str) -> Path:
+    return BUILD_DIR / f"libmpgos_{name}.so"
+
+
+def build_runtime(force: bool = False) -> Path:
+    out = runtime_lib()
+    src = CSRC / "runtime" / "runtime.cpp"
+    deps = [src, INCLUDE_DIR / "mpgos.h"]
+    if not force and _newer(out, deps):
+        return out
+    cmd = [nvcc_path(), "-x", "cu", *ARCH, *_common_flags(), str(src), "-o", str(out)]
+    _run(cmd, "libmpgos_runtime.so")
+    return out
+
+
+def build_system(name: str, force: bool = False, extra: list | None = None) -> Path:
+    out = system_lib(name)
+    src = SYSTEMS_DIR / f"{name}.cu"
+    deps = [src, SYSTEMS_DIR / f"{name}.cuh", INCLUDE_DIR / "mpgos.h", *_deps_glob(CSRC / "perthread")]
+    if not force and _newer(out, deps):
+        return out
+    cmd = [nvcc_path(), *ARCH, *_common_flags(), *(extra or []), str(src), "-o", str(out)]
+    _run(cmd, f"libmpgos_{name}.so")
+    return out
+
+
+def build_all(force: bool = False, systems=None, jobs: int | None = None) -> dict:
+    """Build the runtime and every system plugin; returns {name: path}."""
+    BUILD_DIR.mkdir(parents=True, exist_ok=True)
+    systems = list(systems or SYSTEMS)
+    jobs = jobs or max(1, min(len(systems) + 1, os.cpu_count() or 4))
+    results = {}
+    with cf.ThreadPoolExecutor(max_workers=jobs) as ex:
+        futs = {ex.submit(build_runtime, force): "runtime"}
+        for s in systems:
+            futs[ex.submit(build_system, s, force)] = s
+        errors = []
+        for f in cf.as_completed(futs):
+            try:
+                results[futs[f]] = f.result()
+            except Exception as e:  # collect all failures, then raise once
+                errors.append(str(e))
+        if errors:
+            raise RuntimeError("\n\n".join(errors))
+    return results
+
+
+if __name__ == "__main__":
+    import sys
+    r = build_all(force="--force" in sys.argv)
+    for k, v in sorted(r.items()):
+        print(f"{k}: {v}")

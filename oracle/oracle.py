@@ -1,0 +1,133 @@
+"""Python front end of the CPU oracle (and of the pinned reference CPU build).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() and
+by bench.py's CPU-baseline leg, as the checker. The product never imports it.
+
+``run_oracle(case)`` integrates a ``mpgos_gb300.workloads.Case`` with the
+oracle (oracle_perthread.cpp), ``run_ref_cpu(case)`` with the reference's own
+solver kernel compiled for the CPU (only where the reference checkout exists).
+Both return the same result dictionary as ``workloads.run_gpu``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import time
+
+import numpy as np
+
+from . import build_oracle as _b
+
+_libs: dict = {}
+_ref_libs: dict = {}
+
+_D = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_I = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+
+
+def _oracle(system: str):
+    if system not in _libs:
+        path = _b.build_oracle(system)
+        lib = C.CDLL(str(path))
+        lib.oracle_pt_solve.restype = C.c_int
+        lib.oracle_pt_solve.argtypes = [
+            C.c_int, C.c_longlong, C.c_longlong, C.c_longlong, C.c_int,
+            _D, _D, _D, _D, _D, _I, _D, _I, _D, _D, _D, _I, _I, _D, _D, _I, _I, _I, _D, C.c_int, C.c_longlong, C.c_int]
+        lib.oracle_pt_threads.restype = C.c_int
+        _libs[system] = lib
+    return _libs[system]
+
+
+def _ref(system: str):
+    if system not in _ref_libs:
+        path = _b.build_ref(system)
+        if path is None:
+            raise FileNotFoundError("reference checkout not available: reference CPU build cannot be made")
+        lib = C.CDLL(str(path))
+        lib.ref_cpu_solve.restype = C.c_int
+        lib.ref_cpu_solve.argtypes = [
+            C.c_int, C.c_longlong, C.c_longlong, C.c_int,
+            _D, _D, _D, _D, _D, _I, _D, _I, _D, _D, _D, _I, _I, _D, _D, _D, C.c_int]
+        _ref_libs[system] = lib
+    return _ref_libs[system]
+
+
+def max_threads(system: str = "lorenz") -> int:
+    return int(_oracle(system).oracle_pt_threads())
+
+
+def _prepare(case):
+    a = {k: np.ascontiguousarray(v.copy()) for k, v in case.arrays.items()}
+    for k in ("acci", "didx", "spi"):
+        a[k] = np.ascontiguousarray(a[k].astype(np.int32))
+    pad = lambda v, dt: np.ascontiguousarray(np.concatenate([np.asarray(v, dtype=dt), np.zeros(1, dt)]))
+    tol = dict(rtol=pad(case.rtol, np.float64), atol=pad(case.atol, np.float64), etol=pad(case.etol, np.float64),
+               edir=pad(case.edir, np.int32), sp=pad(a["sp"], np.float64), spi=pad(a["spi"], np.int32))
+    for k in ("cp", "acc", "acci", "dtime", "dstate"):
+        if a[k].size == 0:   # zero-sized fields still need a valid pointer
+            a[k] = np.zeros(1, dtype=a[k].dtype)
+    o = case.options
+    opt6 = np.array([o["initial_dt"], o["max_dt"], o["min_dt"], o["grow"], o["shrink"], o["dense_min_dt"]])
+    return a, tol, opt6
+
+
+def _results(case, a, status, nacc, nrej):
+    sd, ncp, nsp, nisp, ne, na, nia = case.shape
+    nt = case.nt
+    out = dict(td=a["td"], x=a["x"], t=a["t"], didx=a["didx"], status=status, nacc=nacc, nrej=nrej,
+               cp=a["cp"].reshape(ncp, nt) if ncp else np.zeros((0, nt)),
+               acc=a["acc"].reshape(na, nt) if na else np.zeros((0, nt)),
+               acci=a["acci"].reshape(nia, nt) if nia else np.zeros((0, nt), dtype=np.int32))
+    if case.ndo:
+        out["dtime"] = a["dtime"]
+        out["dstate"] = a["dstate"]
+    return out
+
+
+def run_oracle(case, threads: int = 0, first: int = 0, count: int | None = None) -> dict:
+    """Integrate ``case`` (all its phases) with the CPU oracle."""
+    lib = _oracle(case.system)
+    a, tol, opt6 = _prepare(case)
+    nt = case.nt
+    n_active = case.n_active if case.n_active is not None else nt
+    count = n_active - first if count is None else count
+    status = np.zeros(nt, np.int32)
+    nacc = np.zeros(nt, np.int32)
+    nrej = np.zeros(nt, np.int32)
+    o = case.options
+    for _ in range(case.phases):
+        rc = lib.oracle_pt_solve(case.algorithm, nt, first, count, case.ndo, a["td"], a["x"], a["t"], a["cp"],
+                                 tol["sp"], tol["spi"], a["acc"], a["acci"], tol["rtol"], tol["atol"], tol["etol"],
+                                 tol["edir"], a["didx"], a["dtime"], a["dstate"], status, nacc, nrej, opt6,
+                                 int(o["dense_freq"]), int(o["max_attempts"]), int(threads))
+        if rc != 0:
+            raise RuntimeError(f"oracle_pt_solve failed with {rc}")
+    return _results(case, a, status, nacc, nrej)
+
+
+def time_oracle(case, threads: int = 0) -> float:
+    """Wall-clock seconds of one oracle run of ``case``."""
+    t0 = time.perf_counter()
+    run_oracle(case, threads=threads)
+    return time.perf_counter() - t0
+
+
+def run_ref_cpu(case) -> dict:
+    """Integrate ``case`` with the reference's own kernel compiled for the CPU
+    (nt in {64, 256, 1024}, ndo in {0, 16})."""
+    lib = _ref(case.system)
+    a, tol, opt6 = _prepare(case)
+    nt = case.nt
+    n_active = case.n_active if case.n_active is not None else nt
+    # The reference kernel reads the event options for every component index
+    # below SD (SingleSystem_PerThread_Solver.cuh:60); pad them to SD entries.
+    sd = case.shape[0]
+    etol = np.ascontiguousarray(np.concatenate([tol["etol"], np.zeros(sd)]))
+    edir = np.ascontiguousarray(np.concatenate([tol["edir"], np.zeros(sd, np.int32)]))
+    for _ in range(case.phases):
+        rc = lib.ref_cpu_solve(case.algorithm, nt, n_active, case.ndo, a["td"], a["x"], a["t"], a["cp"], tol["sp"],
+                               tol["spi"], a["acc"], a["acci"], tol["rtol"], tol["atol"], etol, edir, a["didx"],
+                               a["dtime"], a["dstate"], opt6, int(case.options["dense_freq"]))
+        if rc != 0:
+            raise RuntimeError(f"ref_cpu_solve: (nt={nt}, ndo={case.ndo}) not compiled")
+    z = np.zeros(nt, np.int32)
+    return _results(case, a, z, z.copy(), z.copy())

@@ -1,0 +1,137 @@
+// CPU build of the reference's own per-thread solver kernel, used to pin the
+// oracle.
+//
+// TEST INFRASTRUCTURE ONLY. oracle/build_oracle.py compiles this file with
+// g++ against the reference's unmodified SourceCodes/SingleSystem_PerThread_Solver.cuh
+// (and the headers it includes) where they lie in the reference checkout,
+// into oracle/_ref/libref_cpu_<system>.so (git-ignored). Nothing from the
+// reference is copied into this repository.
+//
+// The kernel template SingleSystem_PerThread<NT,...> is executed on the CPU
+// by calling it once per instance with a one-thread block (blockDim.x = 1,
+// threadIdx.x = 0, blockIdx.x = instance): with one thread per block every
+// block-shared load loop of the kernel loads all entries itself. NT is a
+// template argument of the reference kernel, so the entry point is compiled
+// for a fixed list of ensemble sizes (MPGOS_REF_NT_LIST).
+//
+// Compile: -DMPGOS_SYSTEM_HEADER="<hooks>.cuh" -I<reference>/SourceCodes.
+#include "host_shim.hpp"
+
+#include <cstdint>
+
+// CUDA spellings the reference kernel uses.
+#define __global__
+#define __shared__
+struct MpgosHostDim3 {
+    unsigned x, y, z;
+};
+static MpgosHostDim3 threadIdx{0, 0, 0};
+static MpgosHostDim3 blockIdx{0, 0, 0};
+static MpgosHostDim3 blockDim{1, 1, 1};
+static inline int max(int a, int b) { return a > b ? a : b; }
+static inline int min(int a, int b) { return a < b ? a : b; }
+static inline int __float_as_int(float f) { int i; std::memcpy(&i, &f, 4); return i; }
+static inline float __int_as_float(int i) { float f; std::memcpy(&f, &i, 4); return f; }
+static inline long long __double_as_longlong(double d) { long long i; std::memcpy(&i, &d, 8); return i; }
+static inline double __longlong_as_double(long long i) { double d; std::memcpy(&d, &i, 8); return d; }
+static inline int atomicCAS(int* a, int c, int v) { int o = *a; if (o == c) *a = v; return o; }
+static inline unsigned long long atomicCAS(unsigned long long* a, unsigned long long c, unsigned long long v)
+{
+    unsigned long long o = *a;
+    if (o == c) *a = v;
+    return o;
+}
+// Backing store of the kernel's `extern __shared__ int DynamicSharedMemory[]`.
+int DynamicSharedMemory[1 << 14];
+
+// Kernel-argument types and enum of SingleSystem_PerThread_Interface.cuh:33,72-115
+// (the interface header itself is host code for the GPU build and is not
+// compiled here). Field order and types as in the reference.
+enum Algorithms { RK4, RKCK45 };
+struct Struct_ThreadConfiguration {
+    int GridSize;
+    int BlockSize;
+    int NumberOfActiveThreads;
+};
+template <class Precision>
+struct Struct_GlobalVariables {
+    Precision* d_TimeDomain;
+    Precision* d_ActualState;
+    Precision* d_ActualTime;
+    Precision* d_ControlParameters;
+    Precision* d_SharedParameters;
+    int* d_IntegerSharedParameters;
+    Precision* d_Accessories;
+    int* d_IntegerAccessories;
+    Precision* d_RelativeTolerance;
+    Precision* d_AbsoluteTolerance;
+    Precision* d_EventTolerance;
+    int* d_EventDirection;
+    int* d_DenseOutputIndex;
+    Precision* d_DenseOutputTimeInstances;
+    Precision* d_DenseOutputStates;
+};
+struct Struct_SharedMemoryUsage {
+    int PreferSharedMemory;
+    int IsAdaptive;
+};
+template <class Precision>
+struct Struct_SolverOptions {
+    Precision InitialTimeStep;
+    Precision MaximumTimeStep;
+    Precision MinimumTimeStep;
+    Precision TimeStepGrowLimit;
+    Precision TimeStepShrinkLimit;
+    int DenseOutputSaveFrequency;
+    Precision DenseOutputMinimumTimeStep;
+};
+
+#include MPGOS_SYSTEM_HEADER
+
+#include "SingleSystem_PerThread_Solver.cuh"
+
+#ifndef MPGOS_REF_NT_LIST
+#define MPGOS_REF_NT_LIST X(64) X(256) X(1024)
+#endif
+
+namespace {
+constexpr int SD = MPGOS_SYS_SD, NCP = MPGOS_SYS_NCP, NSP = MPGOS_SYS_NSP, NISP = MPGOS_SYS_NISP;
+constexpr int NE = MPGOS_SYS_NE, NA = MPGOS_SYS_NA, NIA = MPGOS_SYS_NIA;
+
+template <int NT, int NDO, Algorithms ALG>
+void run(long long n_active, const Struct_GlobalVariables<double>& g, const Struct_SolverOptions<double>& o)
+{
+    Struct_ThreadConfiguration tc{(int)NT, 1, (int)n_active};
+    Struct_SharedMemoryUsage sm{1, ALG == RK4 ? 0 : 1};
+    blockDim.x = 1;
+    threadIdx.x = 0;
+    for (long long i = 0; i < n_active; i++) {
+        blockIdx.x = (unsigned)i;
+        SingleSystem_PerThread<NT, SD, NCP, NSP, NISP, NE, NA, NIA, NDO, ALG, double>(tc, g, sm, o);
+    }
+}
+}  // namespace
+
+extern "C" {
+
+// Returns 0 on success, 2 if (nt, ndo) is not in the compiled list.
+// ndo must be 0 or 16 (the NDO template argument of the compiled kernels).
+int ref_cpu_solve(int algorithm, long long nt, long long n_active, int ndo, double* td, double* x, double* t,
+                  double* cp, double* sp, int* spi, double* acc, int* acci, double* rtol, double* atol, double* etol,
+                  int* edir, int* didx, double* dtime, double* dstate, const double* opt6, int dense_freq)
+{
+    Struct_GlobalVariables<double> g{td, x, t, cp, sp, spi, acc, acci, rtol, atol, etol, edir, didx, dtime, dstate};
+    Struct_SolverOptions<double> o{opt6[0], opt6[1], opt6[2], opt6[3], opt6[4], dense_freq, opt6[5]};
+#define X(N)                                                                  \
+    if (nt == N) {                                                            \
+        if (ndo == 0 && algorithm == 0) { run<N, 0, RK4>(n_active, g, o); return 0; }     \
+        if (ndo == 0 && algorithm == 1) { run<N, 0, RKCK45>(n_active, g, o); return 0; }  \
+        if (ndo == 16 && algorithm == 0) { run<N, 16, RK4>(n_active, g, o); return 0; }   \
+        if (ndo == 16 && algorithm == 1) { run<N, 16, RKCK45>(n_active, g, o); return 0; } \
+    }
+    MPGOS_REF_NT_LIST
+#undef X
+    return 2;
+}
+
+}  // extern "C"
