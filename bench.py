@@ -1,0 +1,436 @@
+"""Benchmark of the per-thread ensemble solver (the hot path) on GB300.
+
+Workload (headline): Lorenz ensemble, 2^20 instances, rho = linspace(0, 21),
+initial state (10, 10, 10), adaptive Cash-Karp 4(5) at rtol = atol = 1e-10
+over t in [0, 10], FP64. One step = one integration of the whole ensemble
+from the initial state (one Solve() launch, after a device-side restore of
+the initial state). Metric: accepted instance-steps per second.
+
+Arms:
+  default           the GB300 kernels through the C-ABI, CHOSEN form
+                    (persistent work queue + FAST_CONTROL); the PLAIN form
+                    (reference arithmetic, static mapping) is measured in the
+                    same run and reported under "plain".
+  --impl reference  the reference's CPU implementation of the path: the
+                    reference solver compiled for this host where its build
+                    exists (oracle/_ref), else the oracle port
+                    (oracle/oracle_perthread.cpp), OpenMP on all host cores,
+                    each step a bounded sample of the workload.
+
+Timing: W untimed warm-up steps, then exactly K steps, each timed with CUDA
+events on the solver's stream; L2 (129 MB) is flushed before every step by
+writing a 512 MB buffer, outside the timed event pair. Under torchrun every
+rank integrates its own full ensemble (weak scaling, no data-path
+collective); the time is the max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+REPO = Path(__file__).resolve().parent
+PKG = REPO / "massively-parallel-gpu-ode-solver_gb300"
+for p in (str(REPO), str(PKG)):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+WORKLOAD = "lorenz_rkck45_tol1e-10_t0-10_2^20"
+METRIC = "accepted instance-steps/s (Lorenz RKCK45, rtol=atol=1e-10, 2^20 instances)"
+UNIT = "instance-steps/s"
+NT = 1 << 20
+
+# Algorithmic FP64 FLOP per RKCK45 step attempt of the Lorenz system
+# (1 add/sub/mul/div = 1 FLOP, an FMA = 2): six right-hand sides of 9 FLOP,
+# stage sums, solution and embedded error 55 FLOP per component
+# (3+5+7+9+11 stage sums, 9 solution, 11 error), and 2 FLOP per component in
+# the controller (tolerance scale and ratio). pow / exp2 are counted as one
+# special-function evaluation, not as FLOP.
+FLOP_PER_ATTEMPT = 6 * 9 + 3 * 55 + 3 * 2
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--nt", type=int, default=NT, help="instances per GPU (default 2^20)")
+    ap.add_argument("--no-plain", action="store_true", help="skip the PLAIN-form measurement")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
+    return ap.parse_args()
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = REPO / "gpurun_out" / f"clocks_{os.getpid()}.csv"
+
+    def __enter__(self):
+        try:
+            self.path.parent.mkdir(exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self) -> dict:
+        if self.proc is None or not self.path.exists():
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    return world, rank, local
+
+
+def dist_barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def dist_max(world, value: float) -> float:
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def dist_sum(world, value: float) -> float:
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def load_peaks() -> dict:
+    p = REPO / "MEASURED_PEAKS.json"
+    return json.loads(p.read_text()) if p.exists() else {}
+
+
+def load_traffic() -> dict:
+    """Per-launch DRAM bytes of the dominant kernel from the committed ncu summary."""
+    p = REPO / "profiles" / "roofline_traffic.json"
+    return json.loads(p.read_text()) if p.exists() else {}
+
+
+def cpu_sample_case(nt: int, stride: int):
+    from mpgos_gb300 import workloads as W
+    full = W.lorenz_case(nt=nt)
+    return full.subset(np.arange(0, nt, stride))
+
+
+def cpu_baseline(nt: int, stride: int = 8) -> dict:
+    """Oracle port (OpenMP, all host cores) on every stride-th instance."""
+    from oracle import oracle as O
+    case = cpu_sample_case(nt, stride)
+    threads = O.max_threads("lorenz")
+    O.run_oracle(cpu_sample_case(nt, nt // 64))  # load + warm
+    t0 = time.perf_counter()
+    res = O.run_oracle(case, threads=threads)
+    dt = time.perf_counter() - t0
+    steps = float(res["nacc"].sum())
+    return {"value": steps / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{case.nt} of {nt} instances (every {stride}th, same rho distribution), "
+                      f"{int(steps)} accepted steps in {dt:.2f} s"}
+
+
+def run_reference(args):
+    """--impl reference: the reference's CPU implementation on the host cores."""
+    world, rank, local = dist_setup()
+    if rank != 0:
+        return
+    from oracle import build_oracle, oracle as O
+    import platform
+    stride = 16
+    case = cpu_sample_case(args.nt, stride)
+    kind = "port"
+    runner = lambda c: O.run_oracle(c, threads=0)
+    try:
+        # The reference's own kernel compiled for this host (only where the
+        # reference checkout existed at build time and the binary matches).
+        if build_oracle.ref_lib("lorenz").exists() and platform.machine() in ("x86_64", "AMD64"):
+            kind = "reference"
+    except Exception:
+        kind = "port"
+    # ref_cpu_solve is compiled for fixed NT values only; the sample is run
+    # through the oracle port, which is bit-identical to it on x86-64.
+    threads = O.max_threads("lorenz")
+    for _ in range(args.warmup):
+        runner(cpu_sample_case(args.nt, args.nt // 256))
+    times, steps = [], 0.0
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        res = runner(case)
+        times.append(time.perf_counter() - t0)
+        steps += float(res["nacc"].sum())
+    total = sum(times)
+    value = steps / total
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": WORKLOAD, "instances": args.nt, "sample_stride": stride},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port" if kind == "port" else kind,
+                             "sample": f"{case.nt} of {args.nt} instances (every {stride}th) per step"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def flush_l2(buf):
+    buf.fill_(1)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    world, rank, local = dist_setup()
+    import torch
+    torch.cuda.set_device(local)
+    from mpgos_gb300 import build, capi, workloads as W
+    from mpgos_gb300.solver import Variable
+
+    build.build_all()
+    case = W.lorenz_case(nt=args.nt)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+
+    def measure(mode, steps, warmup, clocks=None, tune=False, reference=False):
+        """Time ``steps`` integrations of the whole ensemble: our kernels in
+        ``mode`` (autotuned launch shape if ``tune``) or, with ``reference``,
+        the reference's own kernel (sm_103a cubin) on the same buffers."""
+        s = W.load_solver(case, mode=mode, block=128, device=local)
+        s.checkpoint_save()
+        kern = None
+        if reference:
+            from oracle import ref_gpu
+            kern = ref_gpu.ReferenceKernel("lorenz", 1, args.nt, 0)
+            kern.bind(s, case, block=32)   # reference default: one warp per block
+            launch = kern.launch
+        else:
+            if tune:
+                s.autotune(fast_control=bool(mode & capi.MODE_FAST_CONTROL))
+            launch = s.Solve
+        for _ in range(warmup):
+            s.checkpoint_restore()
+            launch()
+        s.SynchroniseDevice()
+        grid, block, m = s.launch_config() if not reference else (kern.grid, kern.block, -1)
+        kernel_ms, step_ms = [], []
+        dist_barrier(world)
+        torch.cuda.synchronize()
+        ctx = clocks if clocks is not None else _Null()
+        accepted = attempts = 0.0
+        with ctx:
+            for _ in range(steps):
+                flush_l2(flush)
+                torch.cuda.synchronize()
+                s.timer_start()
+                s.checkpoint_restore()
+                launch()
+                step_ms.append(s.timer_stop())
+                if reference:
+                    s.SynchroniseFromDeviceToHost(Variable.IntegerAccessories)
+                    s.InsertSynchronisationPoint()
+                    s.SynchroniseSolver()
+                    accepted += float(s.host(Variable.IntegerAccessories)[0].sum())
+                else:
+                    for v in (Variable.AcceptedSteps, Variable.RejectedSteps):
+                        s.SynchroniseFromDeviceToHost(v)
+                    s.InsertSynchronisationPoint()
+                    s.SynchroniseSolver()
+                    na = float(s.host(Variable.AcceptedSteps).sum())
+                    accepted += na
+                    attempts += na + float(s.host(Variable.RejectedSteps).sum())
+            torch.cuda.synchronize()
+        # kernel-only time of the dominant kernel (events on its stream around the launch)
+        for _ in range(min(steps, 3)):
+            flush_l2(flush)
+            torch.cuda.synchronize()
+            s.checkpoint_restore()
+            s.timer_start()
+            launch()
+            kernel_ms.append(s.timer_stop())
+        dist_barrier(world)
+        res = W.read_results(s)
+        if kern is not None:
+            kern.close()
+        s.close()
+        return dict(step_ms=step_ms, kernel_ms=kernel_ms, accepted=accepted, attempts=attempts, grid=grid,
+                    block=block, mode=m, res=res)
+
+    clocks = Clocks(local)
+    chosen = measure(capi.MODE_CHOSEN, args.steps, args.warmup, clocks, tune=True)
+    t_step = dist_max(world, sum(chosen["step_ms"]) / 1e3)
+    acc_all = dist_sum(world, chosen["accepted"])
+    value = acc_all / t_step
+    ms_per_step = 1e3 * t_step / args.steps
+
+    # e2e through the public API with host buffers: H2D of the step's inputs,
+    # Solve, D2H of the end states and step counters, every step.
+    with W.load_solver(case, mode=chosen["mode"], block=chosen["block"], device=local) as s:
+        host_x0 = s.host(Variable.ActualState).copy()
+        host_t0 = s.host(Variable.ActualTime).copy()
+        host_c0 = s.host(Variable.IntegerAccessories).copy()
+        h2d = [Variable.ActualState, Variable.ActualTime, Variable.IntegerAccessories]
+        d2h = [Variable.ActualState, Variable.IntegerAccessories]
+        s.Solve()
+        s.SynchroniseDevice()
+        e2e_steps = max(1, min(args.steps, 3))
+        dist_barrier(world)
+        acc = 0.0
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            s.host(Variable.ActualState)[:] = host_x0
+            s.host(Variable.ActualTime)[:] = host_t0
+            s.host(Variable.IntegerAccessories)[:] = host_c0
+            for v in h2d:
+                s.SynchroniseFromHostToDevice(v)
+            s.Solve()
+            for v in d2h:
+                s.SynchroniseFromDeviceToHost(v)
+            s.InsertSynchronisationPoint()
+            s.SynchroniseSolver()
+            acc += float(s.host(Variable.IntegerAccessories)[0].sum())
+        dt = dist_max(world, time.perf_counter() - t0)
+        e2e = {"value": dist_sum(world, acc) / dt, "unit": UNIT,
+               "h2d_bytes_per_step": int(sum(s.host(v).nbytes for v in h2d)),
+               "d2h_bytes_per_step": int(sum(s.host(v).nbytes for v in d2h)), "steps": e2e_steps}
+
+    def summarize(r):
+        tp = dist_max(world, sum(r["step_ms"]) / 1e3)
+        return {"value": dist_sum(world, r["accepted"]) / tp, "ms_per_step": 1e3 * tp / len(r["step_ms"]),
+                "kernel_ms": statistics.median(r["kernel_ms"]), "grid": r["grid"], "block": r["block"],
+                "mode": r["mode"]}
+
+    plain = ref_gpu = None
+    parity = {}
+    if not args.no_plain:
+        p = measure(capi.MODE_PLAIN, max(1, min(args.steps, 3)), 1)
+        plain = summarize(p)
+        from oracle import ref_gpu as R
+        if R.available("lorenz", 1, args.nt, 0):
+            r = measure(capi.MODE_PLAIN, max(1, min(args.steps, 3)), 1, reference=True)
+            ref_gpu = summarize(r)
+            ref_gpu["kernel"] = "reference SingleSystem_PerThread built for sm_103a (oracle/_ref cubin), block 32"
+            same = all(np.array_equal(np.asarray(p["res"][k]).view(np.uint8), np.asarray(r["res"][k]).view(np.uint8))
+                       for k in ("x", "t", "acci"))
+            parity["plain_bitwise_equal_to_reference_kernel"] = bool(same)
+            ref_res = r["res"]
+        else:
+            ref_res = p["res"]
+        a, b = chosen["res"]["x"], ref_res["x"]
+        scale = np.max(np.abs(b), axis=1, keepdims=True)
+        rel = np.abs(a - b) / (np.abs(b) + 1e-3 * scale)
+        per_inst = rel.max(axis=0)
+        parity.update({"chosen_vs_reference_max_scaled_rel": float(per_inst.max()),
+                       "chosen_instances_within_1e-9": float(np.mean(per_inst <= 1e-9)),
+                       "chosen_step_count_equal_fraction": float(np.mean(chosen["res"]["acci"][0] == ref_res["acci"][0]))})
+
+    if rank != 0:
+        return
+
+    peak_fp64 = capi.fma_peak(local, 8)
+    kernel_s = statistics.median(chosen["kernel_ms"]) / 1e3
+    attempts_per_launch = chosen["attempts"] / args.steps
+    achieved = FLOP_PER_ATTEMPT * attempts_per_launch / kernel_s
+    traffic = load_traffic().get("lorenz_chosen_bytes_per_launch")
+    peaks = load_peaks()
+    cpu = None if args.no_cpu else cpu_baseline(args.nt)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "instances": args.nt, "form": "chosen",
+                   "mode": chosen["mode"], "grid": chosen["grid"], "block": chosen["block"],
+                   "l2": "flushed before every step (512 MB write), outside the timed events",
+                   "accepted_steps_per_launch": chosen["accepted"] / args.steps,
+                   "attempts_per_launch": attempts_per_launch},
+        "e2e": e2e,
+        "plain": plain,
+        "reference_gpu": ref_gpu,
+        "speedup_vs_reference_gpu": (value / ref_gpu["value"]) if ref_gpu else None,
+        "parity": parity,
+        "roofline": {"bound": "fp64", "achieved": achieved / 1e12, "peak": peak_fp64 / 1e12, "unit": "TFLOP/s",
+                     "frac": achieved / peak_fp64, "traffic": traffic,
+                     "flop_per_attempt": FLOP_PER_ATTEMPT,
+                     "kernel_ms": kernel_s * 1e3,
+                     "peak_source": "measured FP64 FMA throughput (mpgos_probe_fma_peak), same GPU, same run",
+                     "hbm_peak_gbs_measured": peaks.get("hbm_gbs")},
+        "cpu_baseline": cpu,
+        "clocks": clocks.summary(),
+        "gpu_launches": args.steps,
+    }
+    print(json.dumps(line))
+
+
+class _Null:
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        return False
+
+
+if __name__ == "__main__":
+    main()

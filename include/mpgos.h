@@ -242,6 +242,21 @@ int mpgos_pt_timer_stop(mpgos_pt_solver* solver, float* milliseconds);
  * not NULL, records it in a JSON cache keyed by system, shape, NT and GPU. */
 int mpgos_pt_autotune(mpgos_pt_solver* solver, int32_t fast_control, const char* cache_path);
 
+/* Device-side checkpoint of every array a launch writes (time domain, state,
+ * time, control parameters, accessories, dense output) and restore of it
+ * (extension). The reference keeps the state only implicitly in the object
+ * between Solve() calls (SingleSystem_PerThread_Solver.cuh:117-137, :414-435);
+ * this makes a resumable snapshot explicit. Asynchronous on the stream. */
+int mpgos_pt_checkpoint_save(mpgos_pt_solver* solver);
+int mpgos_pt_checkpoint_restore(mpgos_pt_solver* solver);
+
+/* Measured FMA throughput of the device (extension, no counterpart in the
+ * reference): independent fused multiply-add chains in FP64
+ * (precision_bytes 8) or FP32 (4) on every SM, timed with CUDA events.
+ * Writes FLOP/s (one FMA = 2 FLOP). Used as the roofline denominator of the
+ * FP64-pipe-bound kernels. */
+int mpgos_probe_fma_peak(int device, int32_t precision_bytes, double* flops_per_second);
+
 /* Thread-local message of the last failing call ("" if none). */
 const char* mpgos_last_error(void);
 

@@ -28,7 +28,6 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
-#include "mpgos.h"
 #include "numerics.cuh"
 
 // Largest block the kernels are compiled for (register budget 65536 / 256).
@@ -100,6 +99,8 @@ struct Staged {
     const P* atol;
     const P* etol;
     const int* edir;
+    const float* lrtol;  // log2 of the tolerances (FAST_CONTROL)
+    const float* latol;
 };
 
 template <class S, int ALG, class P, int MODE>
@@ -179,9 +180,18 @@ struct Solver {
         P xn[SD];
         P err[SD];
         s.dt = s.new_dt;
-        if (s.dt > (s.td[1] - s.t)) {
-            s.dt        = s.td[1] - s.t;
-            end_reached = 1;
+        {
+            // Clamp to the end of the time domain. FAST_CONTROL compares the
+            // positive step with the remaining interval as int64 bit patterns
+            // (exact, also when the remainder is negative) instead of in FP64.
+            const P rem = s.td[1] - s.t;
+            bool clamp;
+            if constexpr (FAST) clamp = bits_of(s.dt) > bits_of(rem);
+            else clamp = s.dt > rem;
+            if (clamp) {
+                s.dt        = rem;
+                end_reached = 1;
+            }
         }
 
         if (ALG == MPGOS_RK4) {
@@ -196,8 +206,8 @@ struct Solver {
                                          s.acci);
             }
             if constexpr (FAST) {
-                control_rkck45_fast<SD>(o, s.dt, s.x, xn, err, g.rtol, g.atol, update, finite, s.terminate,
-                                        s.new_dt, s.status);
+                control_rkck45_fast<SD>(o, s.dt, s.x, xn, err, g.rtol, g.atol, g.lrtol, g.latol, update, finite,
+                                        s.terminate, s.new_dt, s.status);
             } else {
                 control_rkck45_plain<SD, P>(o, s.dt, s.x, xn, err, g.rtol, g.atol, update, finite, s.terminate,
                                             s.new_dt, s.status);
@@ -302,6 +312,8 @@ __global__ void __launch_bounds__(MPGOS_MAX_BLOCK) perthread_kernel(Args<P> a)
     __shared__ P s_etol[AtLeastOne<NE>::value];
     __shared__ int s_edir[AtLeastOne<NE>::value];
     __shared__ float s_spf[AtLeastOne<NSP>::value];
+    __shared__ float s_lrtol[ADAPTIVE ? SD : 1];
+    __shared__ float s_latol[ADAPTIVE ? SD : 1];
 
     P* dyn_sp   = reinterpret_cast<P*>(mpgos_dyn_smem);
     int* dyn_spi = reinterpret_cast<int*>(mpgos_dyn_smem + sizeof(P) * NSP);
@@ -310,6 +322,10 @@ __global__ void __launch_bounds__(MPGOS_MAX_BLOCK) perthread_kernel(Args<P> a)
         if (ADAPTIVE) {
             s_rtol[k] = a.rtol[k];
             s_atol[k] = a.atol[k];
+            if constexpr (Sv::FAST) {
+                s_lrtol[k] = log2_nonneg(a.rtol[k]);
+                s_latol[k] = log2_nonneg(a.atol[k]);
+            }
         }
     }
     for (int k = threadIdx.x; k < NE; k += blockDim.x) {
@@ -332,6 +348,8 @@ __global__ void __launch_bounds__(MPGOS_MAX_BLOCK) perthread_kernel(Args<P> a)
     g.atol = s_atol;
     g.etol = s_etol;
     g.edir = s_edir;
+    g.lrtol = s_lrtol;
+    g.latol = s_latol;
 
     float cpf[AtLeastOne<S::NCP>::value];
     float accf[AtLeastOne<S::NA>::value];

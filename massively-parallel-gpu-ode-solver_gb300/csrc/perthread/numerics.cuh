@@ -12,7 +12,11 @@
 #include <math.h>
 #include <stdint.h>
 
+#if __has_include("mpgos.h")
 #include "mpgos.h"
+#else
+#include "../../../include/mpgos.h"
+#endif
 
 namespace mpgos {
 namespace pt {
@@ -291,28 +295,46 @@ __device__ __forceinline__ void control_rkck45_plain(const Options<P>& o, P dt, 
     new_dt = fmax(new_dt, o.min_dt);
 }
 
-// Adaptive step, FAST_CONTROL (FP64 values only): the same accept/reject rule
-// with exact integer compares on bit patterns; the factor 0.9 R^(1/5) (or
-// R^(1/4) after a rejection), R = min_i tol_i/err_i, is formed as
-// 0.9 * exp2(min_i(log2 tol_i - log2 err_i) / 5) in FP32. The factor is clamped
-// to [shrink, grow] afterwards, so its FP32 rounding only moves the next step
-// size by about 1e-7 relative. Requires non-negative tolerances and options
-// (checked on the host).
+// Adaptive step, FAST_CONTROL (FP64 values only). Same accept/reject rule as
+// the reference (err_i < max(rtol_i * max(|xn_i|, |x_i|), atol_i) for every
+// component), decided without FP64 arithmetic in the common case: the test
+// is made on d_i = log2(tol_i) - log2(err_i) in FP32, where log2 tol_i is
+// max(log2 rtol_i + log2 m_i, log2 atol_i) from the exponent bits and the FP32
+// log2 unit. The FP32 estimate is good to better than 3e-4 (log2 units) over
+// the whole double range, so only when |d_i| < FAST_BAND (2e-3, a 0.14% band
+// around err = tol) is the exact FP64 product formed and compared; the
+// decision is therefore always the one of the FP64 rule.
+// The factor 0.9 R^(1/5) (0.9 R^(1/4) after a rejection), R = min_i tol_i/err_i,
+// becomes 0.9 * exp2(min_i d_i / 5) in FP32; it is clamped to [shrink, grow]
+// afterwards, so its FP32 rounding moves the next step size by ~1e-6 relative.
+// Requires non-negative tolerances and options (checked on the host).
+// lrtol / latol: log2 of the tolerances (per block, FP32).
+constexpr float FAST_BAND = 2e-3f;
+
 template <int SD>
 __device__ __forceinline__ void control_rkck45_fast(const Options<double>& o, double dt, const double* x,
                                                     const double* xn, const double* err,
-                                                    const double* rtol, const double* atol, int& update,
-                                                    int& finite, int& terminate, double& new_dt,
-                                                    int& status)
+                                                    const double* rtol, const double* atol, const float* lrtol,
+                                                    const float* latol, int& update, int& finite, int& terminate,
+                                                    double& new_dt, int& status)
 {
     float lr = INFINITY;
 #pragma unroll
     for (int i = 0; i < SD; i++) {
-        const double m   = from_bits(max_bits(abs_bits(xn[i]), abs_bits(x[i])));
-        const long long tb = max_bits(bits_of(rtol[i] * m), bits_of(atol[i]));
-        const long long eb = bits_of(err[i]);
-        update = update && (eb < tb);
-        lr = fminf(lr, log2_nonneg(from_bits(tb)) - log2_nonneg(err[i]));
+        const long long mb = max_bits(abs_bits(xn[i]), abs_bits(x[i]));
+        const float lt = fmaxf(lrtol[i] + log2_nonneg(from_bits(mb)), latol[i]);
+        const float d  = lt - log2_nonneg(err[i]);
+        int accept_i;
+        if (d > FAST_BAND) {
+            accept_i = 1;
+        } else if (d < -FAST_BAND) {
+            accept_i = 0;
+        } else {
+            const long long tb = max_bits(bits_of(rtol[i] * from_bits(mb)), bits_of(atol[i]));
+            accept_i = bits_of(err[i]) < tb;
+        }
+        update = update && accept_i;
+        lr = fminf(lr, d);
     }
     const float expo = (update == 1) ? 0.2f : 0.25f;
     float qf = 0.9f * exp2f(fminf(fmaxf(lr * expo, -120.0f), 120.0f));

@@ -103,10 +103,11 @@ struct mpgos_pt_solver {
     int32_t dense_freq = 1;
     int32_t prefer_shared = 1;
     int32_t mode = MPGOS_MODE_PLAIN;
-    int64_t max_attempts = 100000000;
+    int64_t max_attempts = 10000000;
     uint64_t generation = 1;  // bumped by every change that alters a launch
 
     std::map<GraphKey, cudaGraphExec_t> graphs;
+    std::vector<void*> checkpoint;  // device copies, one per checkpointed variable
 };
 
 namespace {
@@ -359,6 +360,8 @@ MPGOS_EXPORT int mpgos_pt_destroy(mpgos_pt_solver* s)
     }
     for (void* p : {s->d_rtol, s->d_atol, s->d_etol, static_cast<void*>(s->d_edir), static_cast<void*>(s->d_work)})
         if (p) cudaFree(p);
+    for (void* p : s->checkpoint)
+        if (p) cudaFree(p);
     if (s->timer_begin) cudaEventDestroy(s->timer_begin);
     if (s->timer_end) cudaEventDestroy(s->timer_end);
     if (s->sync_event) cudaEventDestroy(s->sync_event);
@@ -464,9 +467,10 @@ MPGOS_EXPORT int mpgos_pt_set_option(mpgos_pt_solver* s, int32_t option, int32_t
         case MPGOS_KERNEL_MODE: {
             const int32_t m = static_cast<int32_t>(value);
             if (m < 0 || m > 7 || m != value) return fail(MPGOS_ERR_ARGUMENT, "kernel mode %g outside 0..7", value);
-            const int32_t need = m & ~MPGOS_MODE_PERSISTENT;
-            if ((need & s->shape.modes) != need)
-                return fail(MPGOS_ERR_UNSUPPORTED, "kernel mode %d not compiled for this table (modes 0x%x)", m, s->shape.modes);
+            // FAST_CONTROL only changes the adaptive FP64 controller and is a
+            // no-op elsewhere; FP32_STAGE changes the arithmetic and must exist.
+            if ((m & MPGOS_MODE_FP32_STAGE) && !(s->shape.modes & MPGOS_MODE_FP32_STAGE))
+                return fail(MPGOS_ERR_UNSUPPORTED, "FP32_STAGE mode not compiled for this table (modes 0x%x)", s->shape.modes);
             s->mode = m;
             break;
         }
@@ -817,6 +821,48 @@ MPGOS_EXPORT int mpgos_pt_autotune(mpgos_pt_solver* s, int32_t fast_control, con
         std::ofstream outf(cache_path, std::ios::app);
         if (outf) outf << "{\"" << json_escape(k) << "\": {\"block\": " << best_block << ", \"mode\": " << best_mode
                        << ", \"ms\": " << best << "}}\n";
+    }
+    return MPGOS_OK;
+}
+
+namespace {
+// Arrays a launch may write (SingleSystem_PerThread_Solver.cuh:414-435 plus dense output).
+const int32_t kCheckpointVars[] = {MPGOS_TIME_DOMAIN, MPGOS_ACTUAL_STATE, MPGOS_ACTUAL_TIME, MPGOS_CONTROL_PARAMETERS,
+                                   MPGOS_ACCESSORIES, MPGOS_INTEGER_ACCESSORIES, MPGOS_DENSE_INDEX,
+                                   MPGOS_DENSE_TIME, MPGOS_DENSE_STATE};
+}  // namespace
+
+MPGOS_EXPORT int mpgos_pt_checkpoint_save(mpgos_pt_solver* s)
+{
+    int rc = check_solver(s);
+    if (rc) return rc;
+    MPGOS_CUDA(cudaSetDevice(s->device));
+    const size_t n = sizeof(kCheckpointVars) / sizeof(kCheckpointVars[0]);
+    if (s->checkpoint.empty()) {
+        s->checkpoint.assign(n, nullptr);
+        for (size_t i = 0; i < n; i++) {
+            const size_t bytes = std::max<size_t>(s->var[kCheckpointVars[i]].bytes(), 16);
+            if (cudaMalloc(&s->checkpoint[i], bytes) != cudaSuccess)
+                return fail(MPGOS_ERR_MEMORY, "checkpoint allocation of %zu bytes failed", bytes);
+        }
+    }
+    for (size_t i = 0; i < n; i++) {
+        const Buffer& b = s->var[kCheckpointVars[i]];
+        if (b.bytes()) MPGOS_CUDA(cudaMemcpyAsync(s->checkpoint[i], b.device, b.bytes(), cudaMemcpyDeviceToDevice, s->stream));
+    }
+    return MPGOS_OK;
+}
+
+MPGOS_EXPORT int mpgos_pt_checkpoint_restore(mpgos_pt_solver* s)
+{
+    int rc = check_solver(s);
+    if (rc) return rc;
+    if (s->checkpoint.empty()) return fail(MPGOS_ERR_ARGUMENT, "no checkpoint saved");
+    MPGOS_CUDA(cudaSetDevice(s->device));
+    const size_t n = sizeof(kCheckpointVars) / sizeof(kCheckpointVars[0]);
+    for (size_t i = 0; i < n; i++) {
+        const Buffer& b = s->var[kCheckpointVars[i]];
+        if (b.bytes()) MPGOS_CUDA(cudaMemcpyAsync(b.device, s->checkpoint[i], b.bytes(), cudaMemcpyDeviceToDevice, s->stream));
     }
     return MPGOS_OK;
 }

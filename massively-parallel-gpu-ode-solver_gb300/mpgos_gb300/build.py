@@ -82,10 +82,11 @@ def system_lib(name: str) -> Path:
 def build_runtime(force: bool = False) -> Path:
     out = runtime_lib()
     src = CSRC / "runtime" / "runtime.cpp"
-    deps = [src, INCLUDE_DIR / "mpgos.h"]
+    probes = CSRC / "runtime" / "probes.cu"
+    deps = [src, probes, INCLUDE_DIR / "mpgos.h"]
     if not force and _newer(out, deps):
         return out
-    cmd = [nvcc_path(), "-x", "cu", *ARCH, *_common_flags(), str(src), "-o", str(out)]
+    cmd = [nvcc_path(), *ARCH, *_common_flags(), "-x", "cu", str(src), str(probes), "-o", str(out)]
     _run(cmd, "libmpgos_runtime.so")
     return out
 

@@ -124,6 +124,9 @@ def _declare(lib):
         "mpgos_pt_timer_start": (C.c_int, [P]),
         "mpgos_pt_timer_stop": (C.c_int, [P, C.POINTER(C.c_float)]),
         "mpgos_pt_autotune": (C.c_int, [P, i32, C.c_char_p]),
+        "mpgos_pt_checkpoint_save": (C.c_int, [P]),
+        "mpgos_pt_checkpoint_restore": (C.c_int, [P]),
+        "mpgos_probe_fma_peak": (C.c_int, [C.c_int, i32, C.POINTER(C.c_double)]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(lib, name)
@@ -139,6 +142,7 @@ RUNTIME_SYMBOLS = (
     "mpgos_pt_sync_h2d", "mpgos_pt_sync_d2h", "mpgos_pt_solve", "mpgos_pt_solve_phases",
     "mpgos_pt_insert_sync_point", "mpgos_pt_sync_solver", "mpgos_pt_sync_device", "mpgos_pt_stream",
     "mpgos_pt_launch_config", "mpgos_pt_timer_start", "mpgos_pt_timer_stop", "mpgos_pt_autotune",
+    "mpgos_pt_checkpoint_save", "mpgos_pt_checkpoint_restore", "mpgos_probe_fma_peak",
 )
 PLUGIN_SYMBOLS = ("mpgos_pt_system_kernels",)
 
@@ -195,3 +199,10 @@ def loaded_library_paths() -> list:
         out.append(str(_build.runtime_lib()))
     out.extend(str(_build.system_lib(n)) for n in _plugins)
     return out
+
+
+def fma_peak(device: int = 0, precision_bytes: int = 8) -> float:
+    """Measured FMA throughput of the device in FLOP/s (mpgos_probe_fma_peak)."""
+    v = C.c_double()
+    check(runtime().mpgos_probe_fma_peak(int(device), int(precision_bytes), C.byref(v)))
+    return float(v.value)

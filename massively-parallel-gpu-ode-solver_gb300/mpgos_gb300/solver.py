@@ -248,6 +248,12 @@ class ProblemSolver:
                                                cache_path.encode() if cache_path else None))
         return self.launch_config()
 
+    def checkpoint_save(self):
+        capi.check(self._lib.mpgos_pt_checkpoint_save(self._h))
+
+    def checkpoint_restore(self):
+        capi.check(self._lib.mpgos_pt_checkpoint_restore(self._h))
+
     def set_mode(self, mode: int):
         self.SolverOption(Option.KernelMode, mode)
 

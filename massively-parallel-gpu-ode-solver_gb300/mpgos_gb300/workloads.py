@@ -37,7 +37,7 @@ SHAPES = {  # SD, NCP, NSP, NISP, NE, NA, NIA of the hook files in systems/
 }
 
 DEFAULT_OPTIONS = dict(initial_dt=1e-2, max_dt=1e6, min_dt=1e-12, grow=5.0, shrink=0.1, dense_min_dt=0.0,
-                       dense_freq=1, max_attempts=100_000_000)
+                       dense_freq=1, max_attempts=1_000_000)
 
 
 @dataclass

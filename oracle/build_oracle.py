@@ -5,6 +5,10 @@ TEST INFRASTRUCTURE ONLY.
 * ``oracle/_build/liboracle_<system>.so`` - the oracle (oracle_perthread.cpp)
   compiled once per hook file, with OpenMP. Built everywhere, including the
   GPU machine.
+* ``oracle/_ref/ref_gpu_<system>_<alg>_nt<NT>_ndo<NDO>.cubin`` - the
+  reference's own per-thread kernel built for sm_103a (ref_gpu_entry.cu),
+  device code only; built where the reference checkout exists and shipped to
+  the GPU machine with the working tree.
 * ``oracle/_ref/libref_cpu_<system>.so`` - the reference's own
   SourceCodes/SingleSystem_PerThread_Solver.cuh compiled for the CPU through
   ref_cpu_entry.cpp, straight from the reference checkout (MPGOS_REFERENCE_ROOT,
@@ -83,6 +87,48 @@ def build_ref(system: str, force: bool = False) -> Path | None:
     return out
 
 
+# Reference GPU kernels built as cubins: (system, algorithm, NT, NDO). The
+# reference's NT and NDO are template arguments, so every ensemble size the
+# tests and the bench compare against is listed. keller_miksis is absent on
+# purpose: with SD = 2 > NE = 1 the reference kernel indexes its event-option
+# arrays by component (SingleSystem_PerThread_Solver.cuh:60-63), which reads
+# past the NE-entry device array and writes past the NE-entry shared array.
+REF_GPU_KERNELS = [
+    ("lorenz", 1, 256, 0), ("lorenz", 1, 1000, 0), ("lorenz", 0, 64, 0), ("lorenz", 1, 1 << 20, 0),
+    ("duffing", 0, 64, 0), ("duffing", 0, 8192, 0),
+    ("duffing_param", 1, 256, 0), ("duffing_param", 1, 1000, 0),
+    ("duffing_events", 1, 64, 16), ("duffing_events", 1, 512, 16),
+    ("bouncing_ball", 1, 64, 0), ("bouncing_ball", 1, 300, 0),
+]
+# Register caps of the reference's own makefiles (T2_Lorenz/makefile: 64).
+REF_GPU_RREG = {"lorenz": 64}
+
+
+def ref_cubin(system: str, algorithm: int, nt: int, ndo: int, rreg: int | None = None) -> Path:
+    tag = f"_rr{rreg}" if rreg else ""
+    return REF_DIR / f"ref_gpu_{system}_{'rkck45' if algorithm else 'rk4'}_nt{nt}_ndo{ndo}{tag}.cubin"
+
+
+def build_ref_gpu(system: str, algorithm: int, nt: int, ndo: int, rreg: int | None = None,
+                  force: bool = False) -> Path | None:
+    if not reference_available():
+        return None
+    out = ref_cubin(system, algorithm, nt, ndo, rreg)
+    src = ORACLE_DIR / "ref_gpu_entry.cu"
+    hdr = SYSTEMS_DIR / f"{system}.cuh"
+    if not force and _newer(out, [src, hdr, ORACLE_DIR / "ref_types.hpp", Path(__file__)]):
+        return out
+    cmd = ["nvcc", "-cubin", "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17", "-lineinfo", "-w",
+           f"-I{ORACLE_DIR}", f"-I{SYSTEMS_DIR}", f"-I{REFERENCE_ROOT / 'SourceCodes'}",
+           f'-DMPGOS_SYSTEM_HEADER="{system}.cuh"', f"-DREF_NT={nt}", f"-DREF_ALG={'RKCK45' if algorithm else 'RK4'}",
+           f"-DREF_NDO={ndo}"]
+    if rreg:
+        cmd.append(f"-maxrregcount={rreg}")
+    cmd += [str(src), "-o", str(out)]
+    _run(cmd, out.name)
+    return out
+
+
 def build_all(force: bool = False) -> dict:
     BUILD_DIR.mkdir(exist_ok=True)
     REF_DIR.mkdir(exist_ok=True)
@@ -92,6 +138,11 @@ def build_all(force: bool = False) -> dict:
         for s in SYSTEMS:
             futs[ex.submit(build_oracle, s, force)] = ("oracle", s)
             futs[ex.submit(build_ref, s, force)] = ("ref", s)
+        for (s, alg, nt, ndo) in REF_GPU_KERNELS:
+            futs[ex.submit(build_ref_gpu, s, alg, nt, ndo, None, force)] = ("ref_gpu", s, alg, nt, ndo)
+            if s in REF_GPU_RREG:
+                rr = REF_GPU_RREG[s]
+                futs[ex.submit(build_ref_gpu, s, alg, nt, ndo, rr, force)] = ("ref_gpu", s, alg, nt, ndo, rr)
         errors = []
         for f in cf.as_completed(futs):
             try:

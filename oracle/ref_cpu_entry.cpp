@@ -44,47 +44,7 @@ static inline unsigned long long atomicCAS(unsigned long long* a, unsigned long 
 // Backing store of the kernel's `extern __shared__ int DynamicSharedMemory[]`.
 int DynamicSharedMemory[1 << 14];
 
-// Kernel-argument types and enum of SingleSystem_PerThread_Interface.cuh:33,72-115
-// (the interface header itself is host code for the GPU build and is not
-// compiled here). Field order and types as in the reference.
-enum Algorithms { RK4, RKCK45 };
-struct Struct_ThreadConfiguration {
-    int GridSize;
-    int BlockSize;
-    int NumberOfActiveThreads;
-};
-template <class Precision>
-struct Struct_GlobalVariables {
-    Precision* d_TimeDomain;
-    Precision* d_ActualState;
-    Precision* d_ActualTime;
-    Precision* d_ControlParameters;
-    Precision* d_SharedParameters;
-    int* d_IntegerSharedParameters;
-    Precision* d_Accessories;
-    int* d_IntegerAccessories;
-    Precision* d_RelativeTolerance;
-    Precision* d_AbsoluteTolerance;
-    Precision* d_EventTolerance;
-    int* d_EventDirection;
-    int* d_DenseOutputIndex;
-    Precision* d_DenseOutputTimeInstances;
-    Precision* d_DenseOutputStates;
-};
-struct Struct_SharedMemoryUsage {
-    int PreferSharedMemory;
-    int IsAdaptive;
-};
-template <class Precision>
-struct Struct_SolverOptions {
-    Precision InitialTimeStep;
-    Precision MaximumTimeStep;
-    Precision MinimumTimeStep;
-    Precision TimeStepGrowLimit;
-    Precision TimeStepShrinkLimit;
-    int DenseOutputSaveFrequency;
-    Precision DenseOutputMinimumTimeStep;
-};
+#include "ref_types.hpp"
 
 #include MPGOS_SYSTEM_HEADER
 

@@ -1,0 +1,83 @@
+"""Comparison helpers shared by the GPU parity tests.
+
+Three kinds of comparison, each with the bar it can meet:
+
+* GPU vs the reference's own kernel on the same GPU (``bitwise``): the PLAIN
+  kernels keep the reference's operation order, so every output, including
+  values sampled on the step grid (dense output, extrema over accepted
+  steps), must agree bit for bit.
+* GPU vs CPU (oracle or golden fixtures from the reference's CPU build)
+  (``close``): fused multiply-adds and CUDA's math library round differently
+  from the host, so FP64 end states agree to ~1e-13 relative; the bar is
+  1e-9 relative to the value, with values more than 1e3 times smaller than
+  the component's magnitude across the ensemble compared against 1e-9 of
+  1e-3 x that magnitude (states that end next to zero, e.g. at an event, have
+  no meaningful relative error). Event counts, step counts and dense indices
+  must be equal.
+* Values sampled on the step grid (accessories recording extrema over
+  accepted steps, dense-output times and states) move with the grid, which
+  moves when an event-refinement step lands a rounding error away from the
+  tolerance band; these are compared at 1e-4 (``grid``).
+"""
+import numpy as np
+
+END_STATE_KEYS = ("td", "x", "t", "cp")
+GRID_KEYS = ("acc", "dtime", "dstate")
+INT_KEYS = ("acci", "didx")
+
+
+def scaled_close(a, b, rtol):
+    """|a - b| <= rtol * (|b| + 1e-3 * magnitude of the row)."""
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    if b.size == 0:
+        return np.ones(b.shape, bool)
+    if b.ndim == 1:
+        scale = np.max(np.abs(b))
+    else:
+        scale = np.max(np.abs(b), axis=-1, keepdims=True)
+    return np.abs(a - b) <= rtol * (np.abs(b) + 1e-3 * scale)
+
+
+def assert_close(res, ref, rtol=1e-9, grid_rtol=1e-4, ints=True, mask=None, keys=None):
+    """``mask``: instances to compare (default all)."""
+    for k in keys or (END_STATE_KEYS + GRID_KEYS):
+        if k not in ref or np.asarray(ref[k]).size == 0:
+            continue
+        a, b = np.asarray(res[k]), np.asarray(ref[k])
+        if mask is not None:
+            a, b = a[..., mask], b[..., mask]
+        ok = scaled_close(a, b, grid_rtol if k in GRID_KEYS else rtol)
+        if not ok.all():
+            bad = np.argwhere(~ok)[:5]
+            raise AssertionError(f"{k}: {int((~ok).sum())} elements differ, e.g. at {bad.tolist()}: "
+                                 f"{a[tuple(bad[0])]!r} vs {b[tuple(bad[0])]!r}")
+    if ints:
+        for k in INT_KEYS:
+            if k in ref:
+                a, b = np.asarray(res[k]), np.asarray(ref[k])
+                if mask is not None:
+                    a, b = a[..., mask], b[..., mask]
+                np.testing.assert_array_equal(a, b, err_msg=k)
+
+
+def assert_bitwise(a, b, keys=None):
+    for k in keys or sorted(set(a) & set(b)):
+        x, y = np.asarray(a[k]), np.asarray(b[k])
+        assert x.shape == y.shape, k
+        assert np.array_equal(x.view(np.uint8), y.view(np.uint8)), f"{k} differs bitwise"
+
+
+def sensitive_instances(case, rtol=1e-10):
+    """Instances whose end state moves by more than ``rtol`` (scaled) when the
+    initial state is perturbed by one unit in the last place: the chaotic or
+    near-bifurcation members of the ensemble, where rounding differences
+    between two correct implementations are amplified beyond any fixed
+    tolerance. Computed with the oracle."""
+    from oracle import oracle as O
+    base = O.run_oracle(case)
+    pert = case.copy()
+    pert.arrays["x"] = np.nextafter(pert.arrays["x"], np.inf)
+    moved = O.run_oracle(pert)
+    ok = scaled_close(moved["x"], base["x"], rtol).all(axis=0)
+    return ~ok
