@@ -118,6 +118,7 @@ enum mpgos_option {
 #define MPGOS_INSTANCE_MINIMUM_STEP     2  /* warning: continued at minimum step    */
 #define MPGOS_INSTANCE_EVENT_OMITTED    4  /* warning: event step below minimum     */
 #define MPGOS_INSTANCE_ATTEMPT_LIMIT    8  /* stopped: MPGOS_MAXIMUM_ATTEMPTS hit   */
+#define MPGOS_INSTANCE_TAPE_OVERFLOW   16  /* adjoint: more accepted steps than the tape holds */
 
 /* ---- kernel table handed from a system plugin to the runtime ----------- */
 
@@ -166,6 +167,17 @@ typedef struct mpgos_pt_launch {
     uint32_t*      work_counter;    /* PERSISTENT: one zeroed counter */
 } mpgos_pt_launch;
 
+/* Adjoint tape (extension): frozen step sizes and state checkpoints of a
+ * recorded forward pass, device pointers, FP64. */
+typedef struct mpgos_pt_tape {
+    int32_t  segment;    /* accepted steps between checkpoints (<= 64)      */
+    int32_t  max_steps;  /* tape capacity in accepted steps per instance    */
+    double*  dt;         /* [max_steps][NT]                                 */
+    double*  ckpt_x;     /* [max_steps/segment + 1][SD][NT]                 */
+    double*  ckpt_t;     /* [max_steps/segment + 1][NT]                     */
+    int32_t* n_steps;    /* [NT] accepted steps recorded                    */
+} mpgos_pt_tape;
+
 typedef struct mpgos_pt_kernels {
     int32_t        abi_version;     /* MPGOS_ABI_VERSION */
     mpgos_pt_shape shape;
@@ -174,6 +186,13 @@ typedef struct mpgos_pt_kernels {
     int (*launch)(const mpgos_pt_launch* args, int grid, int block, size_t dynamic_smem, void* stream);
     /* Resident blocks per SM for (mode, block, dynamic smem); cudaError_t. */
     int (*occupancy)(int32_t mode, int block, size_t dynamic_smem, int* blocks_per_sm);
+    /* Adjoint (NULL when not compiled): forward launch that records the tape,
+     * and the reverse launch (one instance per thread) computing
+     * dL/dx(t0) [SD][NT] and dL/dcPAR [NCP][NT] from dL/dx(T) [SD][NT]. */
+    int (*launch_record)(const mpgos_pt_launch* args, const mpgos_pt_tape* tape, int grid, int block,
+                         size_t dynamic_smem, void* stream);
+    int (*launch_adjoint)(const mpgos_pt_launch* args, const mpgos_pt_tape* tape, const double* dL_dxT,
+                          double* dL_dx0, double* dL_dp, int grid, int block, size_t dynamic_smem, void* stream);
 } mpgos_pt_kernels;
 
 /* ---- solver object (ProblemSolver, SingleSystem_PerThread_Interface.cuh:117-208) */
@@ -249,6 +268,20 @@ int mpgos_pt_autotune(mpgos_pt_solver* solver, int32_t fast_control, const char*
  * this makes a resumable snapshot explicit. Asynchronous on the stream. */
 int mpgos_pt_checkpoint_save(mpgos_pt_solver* solver);
 int mpgos_pt_checkpoint_restore(mpgos_pt_solver* solver);
+
+/* Discrete adjoint (extension, no counterpart in the reference).
+ * mpgos_pt_solve_record: one Solve() that also records the tape (every
+ * accepted step size, a checkpoint every `segment` accepted steps; capacity
+ * max_steps accepted steps per instance, device memory owned by the solver).
+ * mpgos_pt_adjoint: reverse pass over the recorded tape. Device pointers,
+ * FP64: dL_dxT [SD][NT] in, dL_dx0 [SD][NT] and dL_dp [NCP][NT] out; the
+ * gradient of the discrete map with the recorded step sequence frozen.
+ * Instances whose step count exceeded the tape get MPGOS_INSTANCE_TAPE_OVERFLOW
+ * in MPGOS_STATUS and no gradient. Asynchronous on the solver's stream. */
+int mpgos_pt_solve_record(mpgos_pt_solver* solver, int32_t max_steps, int32_t segment);
+int mpgos_pt_adjoint(mpgos_pt_solver* solver, const double* dL_dxT, double* dL_dx0, double* dL_dp);
+/* Device pointers and sizes of the recorded tape (read-only view). */
+int mpgos_pt_tape_info(const mpgos_pt_solver* solver, mpgos_pt_tape* tape);
 
 /* Measured FMA throughput of the device (extension, no counterpart in the
  * reference): independent fused multiply-add chains in FP64

@@ -1,0 +1,278 @@
+// Discrete adjoint of the per-thread explicit Runge-Kutta integration
+// (extension: the reference has no differentiation).
+//
+// Forward (recording) pass: the ordinary solver kernel compiled with
+// MODE_RECORD (kernel.cuh) stores, per instance, every accepted step size (the
+// frozen step sequence, including event-refined and end-clamped steps) and a
+// checkpoint of time and state every SEG accepted steps.
+//
+// Reverse pass (this file, one instance per thread): for each segment, last
+// first, the states at every step of the segment are recomputed from the
+// checkpoint with the recorded step sizes (bit-identical to the forward pass:
+// the same stepper code), then the adjoint is propagated backwards through the
+// Runge-Kutta stages of every step:
+//     kappa_i = dt b_i lambda + sum_{j>i} dt a_ji xi_j,   xi_i = J_x(X_i)^T kappa_i,
+//     mu     += J_p(X_i)^T kappa_i,                        lambda <- lambda + sum_i xi_i,
+// where J = [df/dx | df/dp] at the stage points comes from one evaluation of
+// the user's PerThread_OdeFunction instantiated with dual numbers. The result
+// is the exact gradient of the discrete map with the step sequence frozen,
+// d L / d x(t0) and d L / d cPAR, for a terminal loss whose gradient
+// d L / d x(T) the caller supplies.
+//
+// Scope: the control parameters are the differentiated parameters; hooks
+// that change the state outside the right-hand side (event actions, step
+// actions, Initialization) are not differentiated.
+#pragma once
+
+#include "dual.cuh"
+#include "kernel.cuh"
+
+namespace mpgos {
+namespace pt {
+
+// Butcher tableaux of the two schemes (mathematical coefficients; the
+// reference's RK4 accumulates k1 + 2k2 + 2k3 + k4, which is this tableau).
+template <int ALG> struct Tableau;
+template <> struct Tableau<MPGOS_RKCK45> {
+    static constexpr int S = 6;
+    __device__ static double a(int i, int j) {
+        const double A[6][5] = {{0, 0, 0, 0, 0},
+                                {1.0 / 5.0, 0, 0, 0, 0},
+                                {3.0 / 40.0, 9.0 / 40.0, 0, 0, 0},
+                                {3.0 / 10.0, -9.0 / 10.0, 6.0 / 5.0, 0, 0},
+                                {-11.0 / 54.0, 5.0 / 2.0, -70.0 / 27.0, 35.0 / 27.0, 0},
+                                {1631.0 / 55296.0, 175.0 / 512.0, 575.0 / 13824.0, 44275.0 / 110592.0, 253.0 / 4096.0}};
+        return A[i][j];
+    }
+    __device__ static double b(int i) {
+        const double B[6] = {37.0 / 378.0, 0.0, 250.0 / 621.0, 125.0 / 594.0, 0.0, 512.0 / 1771.0};
+        return B[i];
+    }
+    __device__ static double c(int i) {
+        const double Cc[6] = {0.0, 1.0 / 5.0, 3.0 / 10.0, 3.0 / 5.0, 1.0, 7.0 / 8.0};
+        return Cc[i];
+    }
+};
+template <> struct Tableau<MPGOS_RK4> {
+    static constexpr int S = 4;
+    __device__ static double a(int i, int j) {
+        const double A[4][3] = {{0, 0, 0}, {0.5, 0, 0}, {0, 0.5, 0}, {0, 0, 1.0}};
+        return A[i][j];
+    }
+    __device__ static double b(int i) {
+        const double B[4] = {1.0 / 6.0, 1.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0};
+        return B[i];
+    }
+    __device__ static double c(int i) {
+        const double Cc[4] = {0.0, 0.5, 0.5, 1.0};
+        return Cc[i];
+    }
+};
+
+// Maximum segment length compiled into the reverse kernel (local-memory
+// buffer of the replayed states).
+constexpr int MAX_SEG = 64;
+
+template <class S, int ALG>
+__global__ void __launch_bounds__(MPGOS_MAX_BLOCK) adjoint_kernel(Args<double> a, Tape tp, const double* dLdxT,
+                                                                  double* dLdx0, double* dLdp)
+{
+    constexpr int SD = S::SD, NCP = S::NCP, NSP = S::NSP, NISP = S::NISP, NA = S::NA, NIA = S::NIA;
+    constexpr int N = SD + NCP;  // dual directions: state, then control parameters
+    using D = ad::Dual<N>;
+    using TB = Tableau<ALG>;
+    constexpr int ST = TB::S;
+
+    extern __shared__ __align__(16) unsigned char mpgos_dyn_smem[];
+    double* sp = reinterpret_cast<double*>(mpgos_dyn_smem);
+    int* spi   = reinterpret_cast<int*>(mpgos_dyn_smem + sizeof(double) * NSP);
+    for (int k = threadIdx.x; k < NSP; k += blockDim.x) sp[k] = a.sp[k];
+    for (int k = threadIdx.x; k < NISP; k += blockDim.x) spi[k] = a.spi[k];
+    __syncthreads();
+
+    const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= a.n_active) return;
+    const long long nt = a.nt;
+    const int ti = static_cast<int>(i), nti = static_cast<int>(nt);
+
+    double cp[AtLeastOne<NCP>::value];
+    double acc[AtLeastOne<NA>::value];
+    int acci[AtLeastOne<NIA>::value];
+#pragma unroll
+    for (int k = 0; k < NCP; k++) cp[k] = a.cp[i + k * nt];
+#pragma unroll
+    for (int k = 0; k < NA; k++) acc[k] = a.acc[i + k * nt];
+#pragma unroll
+    for (int k = 0; k < NIA; k++) acci[k] = a.acci[i + k * nt];
+
+    // dual copies of the constant inputs
+    D cpd[AtLeastOne<NCP>::value];
+    D spd[AtLeastOne<NSP>::value];
+    D accd[AtLeastOne<NA>::value];
+#pragma unroll
+    for (int k = 0; k < NCP; k++) {
+        cpd[k] = D(cp[k]);
+        cpd[k].d[SD + k] = 1.0;
+    }
+    for (int k = 0; k < NSP; k++) spd[k] = D(sp[k]);
+#pragma unroll
+    for (int k = 0; k < NA; k++) accd[k] = D(acc[k]);
+
+    double lam[SD];
+    double mu[AtLeastOne<NCP>::value];
+#pragma unroll
+    for (int d = 0; d < SD; d++) lam[d] = dLdxT[d * nt + i];
+#pragma unroll
+    for (int k = 0; k < NCP; k++) mu[k] = 0.0;
+
+    const int n = tp.n_steps[i];
+    int status = a.status ? a.status[i] : 0;
+    if (n > tp.max_steps) status |= MPGOS_INSTANCE_TAPE_OVERFLOW;
+
+    double xs[MAX_SEG][SD];
+    double ts[MAX_SEG];
+    const int seg = tp.seg;
+
+    if (!(status & MPGOS_INSTANCE_TAPE_OVERFLOW) && n > 0) {
+        for (int sgm = (n - 1) / seg; sgm >= 0; sgm--) {
+            const int k0 = sgm * seg;
+            const int k1 = min(n, k0 + seg);
+            // replay the segment with the recorded steps
+            double x[SD];
+            double t = tp.ckpt_t[static_cast<long long>(sgm) * nt + i];
+#pragma unroll
+            for (int d = 0; d < SD; d++) x[d] = tp.ckpt_x[(static_cast<long long>(sgm) * SD + d) * nt + i];
+            for (int k = k0; k < k1; k++) {
+                const double dt = tp.dt[static_cast<long long>(k) * nt + i];
+#pragma unroll
+                for (int d = 0; d < SD; d++) xs[k - k0][d] = x[d];
+                ts[k - k0] = t;
+                if (k + 1 < k1) {
+                    double xn[SD], err[SD];
+                    int finite = 1;
+                    if (ALG == MPGOS_RK4)
+                        step_rk4<SD, double>(ti, nti, t, dt, x, xn, finite, cp, sp, spi, acc, acci);
+                    else
+                        step_rkck45<SD, double, true>(ti, nti, t, dt, x, xn, err, finite, cp, sp, spi, acc, acci);
+#pragma unroll
+                    for (int d = 0; d < SD; d++) x[d] = xn[d];
+                    t += dt;
+                }
+            }
+            // reverse through the segment
+            for (int k = k1 - 1; k >= k0; k--) {
+                const double dt = tp.dt[static_cast<long long>(k) * nt + i];
+                const double* xk = xs[k - k0];
+                const double tk  = ts[k - k0];
+                double K[ST][SD];
+                double J[ST][SD][N];
+                for (int st = 0; st < ST; st++) {
+                    D Xd[SD];
+                    D Fd[SD];
+#pragma unroll
+                    for (int d = 0; d < SD; d++) {
+                        double sum = 0.0;
+                        for (int j = 0; j < st; j++) sum += TB::a(st, j) * K[j][d];
+                        Xd[d] = D(xk[d] + dt * sum);
+                        Xd[d].d[d] = 1.0;
+                    }
+                    const D Td(tk + TB::c(st) * dt);
+                    PerThread_OdeFunction(ti, nti, Fd, Xd, Td, cpd, spd, spi, accd, acci);
+#pragma unroll
+                    for (int d = 0; d < SD; d++) {
+                        K[st][d] = Fd[d].v;
+#pragma unroll
+                        for (int q = 0; q < N; q++) J[st][d][q] = Fd[d].d[q];
+                    }
+                }
+                double kap[ST][SD];
+                for (int st = 0; st < ST; st++)
+#pragma unroll
+                    for (int d = 0; d < SD; d++) kap[st][d] = dt * TB::b(st) * lam[d];
+                double dlam[SD];
+#pragma unroll
+                for (int d = 0; d < SD; d++) dlam[d] = 0.0;
+                for (int st = ST - 1; st >= 0; st--) {
+                    double xi[SD];
+#pragma unroll
+                    for (int r = 0; r < SD; r++) {
+                        double v = 0.0;
+#pragma unroll
+                        for (int d = 0; d < SD; d++) v += J[st][d][r] * kap[st][d];
+                        xi[r] = v;
+                    }
+#pragma unroll
+                    for (int q = 0; q < NCP; q++) {
+                        double v = 0.0;
+#pragma unroll
+                        for (int d = 0; d < SD; d++) v += J[st][d][SD + q] * kap[st][d];
+                        mu[q] += v;
+                    }
+                    for (int j = 0; j < st; j++) {
+                        const double w = dt * TB::a(st, j);
+                        if (w != 0.0) {
+#pragma unroll
+                            for (int d = 0; d < SD; d++) kap[j][d] += w * xi[d];
+                        }
+                    }
+#pragma unroll
+                    for (int d = 0; d < SD; d++) dlam[d] += xi[d];
+                }
+#pragma unroll
+                for (int d = 0; d < SD; d++) lam[d] += dlam[d];
+            }
+        }
+    }
+#pragma unroll
+    for (int d = 0; d < SD; d++) dLdx0[d * nt + i] = lam[d];
+#pragma unroll
+    for (int q = 0; q < NCP; q++) dLdp[q * nt + i] = mu[q];
+    if (a.status) a.status[i] = status;
+}
+
+}  // namespace pt
+}  // namespace mpgos
+
+namespace mpgos {
+namespace pt {
+
+// Launch side of the adjoint (mpgos_pt_kernels::launch_record / launch_adjoint).
+template <class S, int ALG>
+struct AdjointTable {
+    static Tape tape_of(const mpgos_pt_tape& t)
+    {
+        return Tape{t.segment, t.max_steps, t.dt, t.ckpt_x, t.ckpt_t, t.n_steps};
+    }
+
+    static int launch_record(const mpgos_pt_launch* L, const mpgos_pt_tape* tape, int grid, int block, size_t smem,
+                             void* stream)
+    {
+        if (tape == nullptr || tape->segment < 1 || tape->segment > MAX_SEG) return static_cast<int>(cudaErrorInvalidValue);
+        void* fn = nullptr;
+        switch (L->mode & (MPGOS_MODE_FAST_CONTROL | MPGOS_MODE_PERSISTENT)) {
+            case 0: fn = reinterpret_cast<void*>(&perthread_kernel<S, ALG, double, MODE_RECORD>); break;
+            case 1: fn = reinterpret_cast<void*>(&perthread_kernel<S, ALG, double, MODE_RECORD | 1>); break;
+            case 2: fn = reinterpret_cast<void*>(&perthread_kernel<S, ALG, double, MODE_RECORD | 2>); break;
+            default: fn = reinterpret_cast<void*>(&perthread_kernel<S, ALG, double, MODE_RECORD | 3>); break;
+        }
+        Args<double> a = make_args<double>(*L);
+        a.tape = tape_of(*tape);
+        void* params[] = {&a};
+        return static_cast<int>(cudaLaunchKernel(fn, dim3(grid), dim3(block), params, smem,
+                                                 static_cast<cudaStream_t>(stream)));
+    }
+
+    static int launch_adjoint(const mpgos_pt_launch* L, const mpgos_pt_tape* tape, const double* dLdxT,
+                              double* dLdx0, double* dLdp, int grid, int block, size_t smem, void* stream)
+    {
+        if (tape == nullptr || tape->segment < 1 || tape->segment > MAX_SEG) return static_cast<int>(cudaErrorInvalidValue);
+        Args<double> a = make_args<double>(*L);
+        Tape t = tape_of(*tape);
+        void* params[] = {&a, &t, &dLdxT, &dLdx0, &dLdp};
+        return static_cast<int>(cudaLaunchKernel(reinterpret_cast<void*>(&adjoint_kernel<S, ALG>), dim3(grid),
+                                                 dim3(block), params, smem, static_cast<cudaStream_t>(stream)));
+    }
+};
+
+}  // namespace pt
+}  // namespace mpgos

@@ -1,0 +1,141 @@
+// Forward-mode dual numbers for differentiating user hooks unchanged.
+//
+// The reference's hooks are templates on Precision
+// (Tutorials_SingleSystem_PerThread/T1_Reference/Reference_SystemDefinition.cuh:5-13).
+// Instantiating PerThread_OdeFunction with Precision = Dual<N> evaluates the
+// right-hand side and, in the same pass, its derivatives along N seeded
+// directions: with the state components and the control parameters seeded
+// as unit directions this yields the full Jacobian [df/dx | df/dp], from which
+// the adjoint kernel forms vector-Jacobian products.
+//
+// Arithmetic, comparisons and the math functions the hooks use (cos, sin,
+// pow, sqrt, exp, log, fabs/abs, sincospi) are overloaded and found by
+// argument-dependent lookup. The value part always calls CUDA's own function;
+// derivative parts use the analytic derivative identities. A dual whose
+// derivative part is identically zero (the time argument, shared parameters)
+// skips the derivative evaluation of transcendental functions.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <math.h>
+
+namespace mpgos {
+namespace ad {
+
+template <int N>
+struct Dual {
+    double v;
+    double d[N];
+
+    __host__ __device__ Dual() : v(0.0) {
+#pragma unroll
+        for (int i = 0; i < N; i++) d[i] = 0.0;
+    }
+    __host__ __device__ Dual(double x) : v(x) {  // NOLINT: implicit, hooks write static_cast<Precision>(c)
+#pragma unroll
+        for (int i = 0; i < N; i++) d[i] = 0.0;
+    }
+    __host__ __device__ explicit operator double() const { return v; }
+
+    __device__ bool constant() const {
+        bool z = true;
+#pragma unroll
+        for (int i = 0; i < N; i++) z = z && (d[i] == 0.0);
+        return z;
+    }
+
+    __device__ Dual& operator+=(const Dual& b) { v += b.v; for (int i = 0; i < N; i++) d[i] += b.d[i]; return *this; }
+    __device__ Dual& operator-=(const Dual& b) { v -= b.v; for (int i = 0; i < N; i++) d[i] -= b.d[i]; return *this; }
+    __device__ Dual& operator*=(const Dual& b) { *this = *this * b; return *this; }
+    __device__ Dual& operator/=(const Dual& b) { *this = *this / b; return *this; }
+    __device__ Dual& operator++() { v += 1.0; return *this; }
+
+    // chain rule helper: f(v) with derivative f'(v)
+    __device__ Dual chain(double fv, double dfv) const {
+        Dual r;
+        r.v = fv;
+#pragma unroll
+        for (int i = 0; i < N; i++) r.d[i] = dfv * d[i];
+        return r;
+    }
+
+    friend __device__ Dual operator-(const Dual& a) { Dual r; r.v = -a.v; for (int i = 0; i < N; i++) r.d[i] = -a.d[i]; return r; }
+    friend __device__ Dual operator+(const Dual& a) { return a; }
+    friend __device__ Dual operator+(const Dual& a, const Dual& b) { Dual r; r.v = a.v + b.v; for (int i = 0; i < N; i++) r.d[i] = a.d[i] + b.d[i]; return r; }
+    friend __device__ Dual operator-(const Dual& a, const Dual& b) { Dual r; r.v = a.v - b.v; for (int i = 0; i < N; i++) r.d[i] = a.d[i] - b.d[i]; return r; }
+    friend __device__ Dual operator*(const Dual& a, const Dual& b) {
+        Dual r;
+        r.v = a.v * b.v;
+#pragma unroll
+        for (int i = 0; i < N; i++) r.d[i] = a.d[i] * b.v + a.v * b.d[i];
+        return r;
+    }
+    friend __device__ Dual operator/(const Dual& a, const Dual& b) {
+        Dual r;
+        const double inv = 1.0 / b.v;
+        r.v = a.v * inv;
+#pragma unroll
+        for (int i = 0; i < N; i++) r.d[i] = (a.d[i] - r.v * b.d[i]) * inv;
+        return r;
+    }
+    friend __device__ Dual operator+(const Dual& a, double b) { Dual r = a; r.v += b; return r; }
+    friend __device__ Dual operator+(double a, const Dual& b) { Dual r = b; r.v += a; return r; }
+    friend __device__ Dual operator-(const Dual& a, double b) { Dual r = a; r.v -= b; return r; }
+    friend __device__ Dual operator-(double a, const Dual& b) { Dual r = -b; r.v += a; return r; }
+    friend __device__ Dual operator*(const Dual& a, double b) { Dual r; r.v = a.v * b; for (int i = 0; i < N; i++) r.d[i] = a.d[i] * b; return r; }
+    friend __device__ Dual operator*(double a, const Dual& b) { return b * a; }
+    friend __device__ Dual operator/(const Dual& a, double b) { return a * (1.0 / b); }
+    friend __device__ Dual operator/(double a, const Dual& b) { return Dual(a) / b; }
+
+    friend __device__ bool operator<(const Dual& a, const Dual& b) { return a.v < b.v; }
+    friend __device__ bool operator>(const Dual& a, const Dual& b) { return a.v > b.v; }
+    friend __device__ bool operator<=(const Dual& a, const Dual& b) { return a.v <= b.v; }
+    friend __device__ bool operator>=(const Dual& a, const Dual& b) { return a.v >= b.v; }
+    friend __device__ bool operator==(const Dual& a, const Dual& b) { return a.v == b.v; }
+    friend __device__ bool operator!=(const Dual& a, const Dual& b) { return a.v != b.v; }
+
+    // ---- math functions (found by ADL from the hooks) ----
+    friend __device__ Dual cos(const Dual& a) {
+        if (a.constant()) return Dual(::cos(a.v));
+        double s, c;
+        ::sincos(a.v, &s, &c);
+        return a.chain(c, -s);
+    }
+    friend __device__ Dual sin(const Dual& a) {
+        if (a.constant()) return Dual(::sin(a.v));
+        double s, c;
+        ::sincos(a.v, &s, &c);
+        return a.chain(s, c);
+    }
+    friend __device__ Dual exp(const Dual& a) { const double e = ::exp(a.v); return a.chain(e, e); }
+    friend __device__ Dual log(const Dual& a) { return a.chain(::log(a.v), 1.0 / a.v); }
+    friend __device__ Dual sqrt(const Dual& a) { const double s = ::sqrt(a.v); return a.chain(s, 0.5 / s); }
+    friend __device__ Dual fabs(const Dual& a) { return a.v < 0.0 ? -a : a; }
+    friend __device__ Dual abs(const Dual& a) { return a.v < 0.0 ? -a : a; }
+    friend __device__ Dual pow(const Dual& a, double e) {
+        const double p = ::pow(a.v, e);
+        return a.chain(p, e * ::pow(a.v, e - 1.0));
+    }
+    friend __device__ Dual pow(const Dual& a, const Dual& b) {
+        // d(a^b) = b a^(b-1) da + a^b ln(a) db
+        const double p = ::pow(a.v, b.v);
+        Dual r;
+        r.v = p;
+        const double da = b.v * ::pow(a.v, b.v - 1.0);
+        const bool bconst = b.constant();
+        const double db = bconst ? 0.0 : p * ::log(a.v);
+#pragma unroll
+        for (int i = 0; i < N; i++) r.d[i] = da * a.d[i] + db * b.d[i];
+        return r;
+    }
+    friend __device__ void sincospi(const Dual& a, Dual* s, Dual* c) {
+        double sv, cv;
+        ::sincospi(a.v, &sv, &cv);
+        const double w = 3.14159265358979323846;
+        *s = a.chain(sv, w * cv);
+        *c = a.chain(cv, -w * sv);
+    }
+};
+
+}  // namespace ad
+}  // namespace mpgos

@@ -43,6 +43,19 @@ struct Shape {
     static constexpr int SD = SD_, NCP = NCP_, NSP = NSP_, NISP = NISP_, NE = NE_, NA = NA_, NIA = NIA_;
 };
 
+// Device-side view of the adjoint tape (mpgos_pt_tape in mpgos.h).
+struct Tape {
+    int seg;
+    int max_steps;
+    double* dt;      // [max_steps][NT]
+    double* ckpt_x;  // [max_steps/seg + 1][SD][NT]
+    double* ckpt_t;  // [max_steps/seg + 1][NT]
+    int* n_steps;    // [NT]
+};
+
+// Kernel-internal mode bit: the forward launch records the adjoint tape.
+constexpr int MODE_RECORD = 8;
+
 // Kernel arguments in the kernel's precision (the reference passes the same
 // information as Struct_ThreadConfiguration / Struct_GlobalVariables /
 // Struct_SharedMemoryUsage / Struct_SolverOptions,
@@ -72,6 +85,7 @@ struct Args {
     unsigned int* work;
     int prefer_shared;
     Options<P> o;
+    Tape tape;
 };
 
 // Registers of one instance between step attempts.
@@ -112,6 +126,7 @@ struct Solver {
     static constexpr bool IS_DOUBLE = sizeof(P) == 8;
     static constexpr bool FAST = ((MODE & MPGOS_MODE_FAST_CONTROL) != 0) && IS_DOUBLE && ALG == MPGOS_RKCK45;
     static constexpr bool F32S = ((MODE & MPGOS_MODE_FP32_STAGE) != 0) && IS_DOUBLE && ALG == MPGOS_RKCK45;
+    static constexpr bool RECORD = ((MODE & MODE_RECORD) != 0) && IS_DOUBLE;
     using Inst = Instance<S, P>;
 
     // Load instance i and run the start-of-launch part of the reference loop
@@ -152,6 +167,12 @@ struct Solver {
             dense_store<SD, P>(i, nt, 1, s.didx, a.o.ndo, a.dtime, a.dstate, s.t, s.x, s.skipped,
                                s.dense_next, a.o.dense_min_dt, s.td[1]);
         if (F32S) refresh_f32(s, cpf, accf);
+        if constexpr (RECORD) {
+            // checkpoint 0: the state the first step starts from
+            a.tape.ckpt_t[i] = s.t;
+#pragma unroll
+            for (int d = 0; d < SD; d++) a.tape.ckpt_x[d * nt + i] = s.x[d];
+        }
     }
 
     __device__ static void refresh_f32(const Inst& s, float* cpf, float* accf)
@@ -246,6 +267,21 @@ struct Solver {
                                    s.dense_next, o.dense_min_dt, s.td[1]);
             }
             if (F32S && NA > 0) refresh_f32(s, cpf, accf);
+            if constexpr (RECORD) {
+                // frozen step size of accepted step nacc, checkpoint every seg steps
+                const int k = s.nacc - 1;
+                if (k < a.tape.max_steps) {
+                    a.tape.dt[static_cast<long long>(k) * a.nt + s.i] = s.dt;
+                    if (s.nacc % a.tape.seg == 0) {
+                        const long long c = s.nacc / a.tape.seg;
+                        a.tape.ckpt_t[c * a.nt + s.i] = s.t;
+#pragma unroll
+                        for (int d = 0; d < SD; d++) a.tape.ckpt_x[(c * SD + d) * a.nt + s.i] = s.x[d];
+                    }
+                } else {
+                    s.status |= MPGOS_INSTANCE_TAPE_OVERFLOW;
+                }
+            }
             if ((end_reached == 1) || (s.udt == 1)) s.terminate = 1;
         } else {
             s.nrej++;
@@ -273,6 +309,7 @@ struct Solver {
         if (a.status) a.status[i] = s.status;
         if (a.n_acc) a.n_acc[i] = s.nacc;
         if (a.n_rej) a.n_rej[i] = s.nrej;
+        if constexpr (RECORD) a.tape.n_steps[i] = s.nacc;
     }
 
     // Next instance for a lane whose instance finished: warp-aggregated
@@ -413,6 +450,11 @@ Args<P> make_args(const mpgos_pt_launch& L)
     return a;
 }
 
+// Adjoint launchers, filled in by adjoint.cuh's AdjointTable where compiled.
+using RecordFn  = int (*)(const mpgos_pt_launch*, const mpgos_pt_tape*, int, int, size_t, void*);
+using AdjointFn = int (*)(const mpgos_pt_launch*, const mpgos_pt_tape*, const double*, double*, double*, int, int,
+                          size_t, void*);
+
 template <class S, int ALG, class P>
 struct KernelTable {
     static constexpr bool DOUBLE_ADAPTIVE = sizeof(P) == 8 && ALG == MPGOS_RKCK45;
@@ -456,14 +498,16 @@ struct KernelTable {
         return static_cast<int>(cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, fn, block, smem));
     }
 
-    static const mpgos_pt_kernels* get(const char* name)
+    static const mpgos_pt_kernels* get(const char* name, RecordFn record = nullptr, AdjointFn adjoint = nullptr)
     {
         static mpgos_pt_kernels table = {
             MPGOS_ABI_VERSION,
             {S::SD, S::NCP, S::NSP, S::NISP, S::NE, S::NA, S::NIA, ALG, static_cast<int32_t>(sizeof(P)), MODES},
             name,
             &launch,
-            &occupancy};
+            &occupancy,
+            record,
+            adjoint};
         return &table;
     }
 };

@@ -108,6 +108,10 @@ struct mpgos_pt_solver {
 
     std::map<GraphKey, cudaGraphExec_t> graphs;
     std::vector<void*> checkpoint;  // device copies, one per checkpointed variable
+
+    // adjoint tape (device memory, allocated by the first recording solve)
+    mpgos_pt_tape tape{};
+    size_t tape_bytes = 0;
 };
 
 namespace {
@@ -361,6 +365,9 @@ MPGOS_EXPORT int mpgos_pt_destroy(mpgos_pt_solver* s)
     for (void* p : {s->d_rtol, s->d_atol, s->d_etol, static_cast<void*>(s->d_edir), static_cast<void*>(s->d_work)})
         if (p) cudaFree(p);
     for (void* p : s->checkpoint)
+        if (p) cudaFree(p);
+    for (void* p : {static_cast<void*>(s->tape.dt), static_cast<void*>(s->tape.ckpt_x),
+                    static_cast<void*>(s->tape.ckpt_t), static_cast<void*>(s->tape.n_steps)})
         if (p) cudaFree(p);
     if (s->timer_begin) cudaEventDestroy(s->timer_begin);
     if (s->timer_end) cudaEventDestroy(s->timer_end);
@@ -864,5 +871,75 @@ MPGOS_EXPORT int mpgos_pt_checkpoint_restore(mpgos_pt_solver* s)
         const Buffer& b = s->var[kCheckpointVars[i]];
         if (b.bytes()) MPGOS_CUDA(cudaMemcpyAsync(b.device, s->checkpoint[i], b.bytes(), cudaMemcpyDeviceToDevice, s->stream));
     }
+    return MPGOS_OK;
+}
+
+// ---- discrete adjoint -----------------------------------------------------------
+MPGOS_EXPORT int mpgos_pt_solve_record(mpgos_pt_solver* s, int32_t max_steps, int32_t segment)
+{
+    int rc = check_solver(s);
+    if (rc) return rc;
+    if (s->k->launch_record == nullptr || s->shape.precision_bytes != 8)
+        return fail(MPGOS_ERR_UNSUPPORTED, "system %s has no adjoint kernels compiled (FP64 only)", s->k->name);
+    if (max_steps < 1 || segment < 1 || segment > 64)
+        return fail(MPGOS_ERR_ARGUMENT, "tape: max_steps %d must be >= 1 and segment %d within 1..64", max_steps, segment);
+    MPGOS_CUDA(cudaSetDevice(s->device));
+    const size_t nt = static_cast<size_t>(s->nt), sd = static_cast<size_t>(s->shape.sd);
+    const size_t nck = static_cast<size_t>(max_steps / segment + 1);
+    if (s->tape.max_steps != max_steps || s->tape.segment != segment || s->tape.dt == nullptr) {
+        MPGOS_CUDA(cudaStreamSynchronize(s->stream));
+        for (void* p : {static_cast<void*>(s->tape.dt), static_cast<void*>(s->tape.ckpt_x),
+                        static_cast<void*>(s->tape.ckpt_t), static_cast<void*>(s->tape.n_steps)})
+            if (p) cudaFree(p);
+        s->tape = mpgos_pt_tape{};
+        const size_t b_dt = static_cast<size_t>(max_steps) * nt * 8, b_cx = nck * sd * nt * 8, b_ct = nck * nt * 8;
+        if (cudaMalloc(reinterpret_cast<void**>(&s->tape.dt), b_dt) != cudaSuccess ||
+            cudaMalloc(reinterpret_cast<void**>(&s->tape.ckpt_x), b_cx) != cudaSuccess ||
+            cudaMalloc(reinterpret_cast<void**>(&s->tape.ckpt_t), b_ct) != cudaSuccess ||
+            cudaMalloc(reinterpret_cast<void**>(&s->tape.n_steps), nt * 4) != cudaSuccess) {
+            s->tape.max_steps = 0;
+            return fail(MPGOS_ERR_MEMORY, "adjoint tape allocation (%zu bytes) failed", b_dt + b_cx + b_ct + nt * 4);
+        }
+        s->tape.max_steps = max_steps;
+        s->tape.segment = segment;
+        s->tape_bytes = b_dt + b_cx + b_ct + nt * 4;
+    }
+    if (s->n_active <= 0) return MPGOS_OK;
+    const int32_t m = effective_mode(s, s->mode) & (MPGOS_MODE_FAST_CONTROL | MPGOS_MODE_PERSISTENT);
+    int grid = 0;
+    if ((rc = grid_for(s, m, s->block, &grid))) return rc;
+    if (m & MPGOS_MODE_PERSISTENT) MPGOS_CUDA(cudaMemsetAsync(s->d_work, 0, sizeof(uint32_t), s->stream));
+    mpgos_pt_launch L;
+    fill_launch(s, L, m);
+    rc = s->k->launch_record(&L, &s->tape, grid, s->block, dynamic_smem(s), s->stream);
+    if (rc != 0) return fail(MPGOS_ERR_CUDA, "recording launch failed: %s", cudaGetErrorString((cudaError_t)rc));
+    return MPGOS_OK;
+}
+
+MPGOS_EXPORT int mpgos_pt_adjoint(mpgos_pt_solver* s, const double* dLdxT, double* dLdx0, double* dLdp)
+{
+    int rc = check_solver(s);
+    if (rc) return rc;
+    if (s->k->launch_adjoint == nullptr) return fail(MPGOS_ERR_UNSUPPORTED, "system %s has no adjoint kernels", s->k->name);
+    if (s->tape.dt == nullptr) return fail(MPGOS_ERR_ARGUMENT, "no recorded forward pass (call mpgos_pt_solve_record first)");
+    if (dLdxT == nullptr || dLdx0 == nullptr || (dLdp == nullptr && s->shape.ncp > 0))
+        return fail(MPGOS_ERR_ARGUMENT, "null gradient buffer");
+    if (s->n_active <= 0) return MPGOS_OK;
+    MPGOS_CUDA(cudaSetDevice(s->device));
+    const int block = 64;
+    const int64_t grid = (s->n_active + block - 1) / block;
+    mpgos_pt_launch L;
+    fill_launch(s, L, 0);
+    rc = s->k->launch_adjoint(&L, &s->tape, dLdxT, dLdx0, dLdp, static_cast<int>(grid), block, dynamic_smem(s), s->stream);
+    if (rc != 0) return fail(MPGOS_ERR_CUDA, "adjoint launch failed: %s", cudaGetErrorString((cudaError_t)rc));
+    return MPGOS_OK;
+}
+
+MPGOS_EXPORT int mpgos_pt_tape_info(const mpgos_pt_solver* s, mpgos_pt_tape* tape)
+{
+    int rc = check_solver(s);
+    if (rc) return rc;
+    if (tape == nullptr) return fail(MPGOS_ERR_ARGUMENT, "null tape pointer");
+    *tape = s->tape;
     return MPGOS_OK;
 }

@@ -28,7 +28,8 @@ SYSTEMS_DIR = PKG_ROOT / "systems"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 # System plugins built by default: name -> source file (hook file + plugin export).
-SYSTEMS = ["lorenz", "duffing", "duffing_param", "duffing_events", "bouncing_ball", "keller_miksis"]
+SYSTEMS = ["lorenz", "duffing", "duffing_param", "duffing_param_sens", "duffing_events", "bouncing_ball",
+           "keller_miksis"]
 
 
 def nvcc_path() -> str:

@@ -76,6 +76,7 @@ INSTANCE_NONFINITE = 1
 INSTANCE_MINIMUM_STEP = 2
 INSTANCE_EVENT_OMITTED = 4
 INSTANCE_ATTEMPT_LIMIT = 8
+INSTANCE_TAPE_OVERFLOW = 16
 
 ABI_VERSION = 1
 
@@ -85,6 +86,11 @@ class Shape(C.Structure):
                 ("sd", "ncp", "nsp", "nisp", "ne", "na", "nia", "algorithm", "precision_bytes", "modes")]
 
 
+class Tape(C.Structure):
+    _fields_ = [("segment", C.c_int32), ("max_steps", C.c_int32), ("dt", C.c_void_p), ("ckpt_x", C.c_void_p),
+                ("ckpt_t", C.c_void_p), ("n_steps", C.c_void_p)]
+
+
 class KernelTable(C.Structure):
     _fields_ = [
         ("abi_version", C.c_int32),
@@ -92,6 +98,8 @@ class KernelTable(C.Structure):
         ("name", C.c_char_p),
         ("launch", C.c_void_p),
         ("occupancy", C.c_void_p),
+        ("launch_record", C.c_void_p),
+        ("launch_adjoint", C.c_void_p),
     ]
 
 
@@ -127,6 +135,9 @@ def _declare(lib):
         "mpgos_pt_checkpoint_save": (C.c_int, [P]),
         "mpgos_pt_checkpoint_restore": (C.c_int, [P]),
         "mpgos_probe_fma_peak": (C.c_int, [C.c_int, i32, C.POINTER(C.c_double)]),
+        "mpgos_pt_solve_record": (C.c_int, [P, i32, i32]),
+        "mpgos_pt_adjoint": (C.c_int, [P, P, P, P]),
+        "mpgos_pt_tape_info": (C.c_int, [P, C.POINTER(Tape)]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(lib, name)
@@ -143,6 +154,7 @@ RUNTIME_SYMBOLS = (
     "mpgos_pt_insert_sync_point", "mpgos_pt_sync_solver", "mpgos_pt_sync_device", "mpgos_pt_stream",
     "mpgos_pt_launch_config", "mpgos_pt_timer_start", "mpgos_pt_timer_stop", "mpgos_pt_autotune",
     "mpgos_pt_checkpoint_save", "mpgos_pt_checkpoint_restore", "mpgos_probe_fma_peak",
+    "mpgos_pt_solve_record", "mpgos_pt_adjoint", "mpgos_pt_tape_info",
 )
 PLUGIN_SYMBOLS = ("mpgos_pt_system_kernels",)
 

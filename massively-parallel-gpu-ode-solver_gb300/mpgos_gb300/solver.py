@@ -254,6 +254,22 @@ class ProblemSolver:
     def checkpoint_restore(self):
         capi.check(self._lib.mpgos_pt_checkpoint_restore(self._h))
 
+    def SolveRecord(self, max_steps: int, segment: int = 32):
+        """One Solve() that records the adjoint tape (frozen step sizes and a
+        checkpoint every ``segment`` accepted steps)."""
+        capi.check(self._lib.mpgos_pt_solve_record(self._h, int(max_steps), int(segment)))
+
+    def Adjoint(self, dLdxT_ptr: int, dLdx0_ptr: int, dLdp_ptr: int):
+        """Reverse pass over the recorded tape; device pointers, FP64,
+        [SD][NT] in, [SD][NT] and [NCP][NT] out."""
+        capi.check(self._lib.mpgos_pt_adjoint(self._h, C.c_void_p(dLdxT_ptr), C.c_void_p(dLdx0_ptr),
+                                              C.c_void_p(dLdp_ptr or None)))
+
+    def tape_info(self):
+        t = capi.Tape()
+        capi.check(self._lib.mpgos_pt_tape_info(self._h, C.byref(t)))
+        return t
+
     def set_mode(self, mode: int):
         self.SolverOption(Option.KernelMode, mode)
 

@@ -31,6 +31,7 @@ SHAPES = {  # SD, NCP, NSP, NISP, NE, NA, NIA of the hook files in systems/
     "lorenz": (3, 1, 0, 0, 0, 0, 1),
     "duffing": (2, 1, 1, 0, 0, 1, 1),
     "duffing_param": (2, 2, 0, 0, 0, 0, 1),
+    "duffing_param_sens": (10, 2, 0, 0, 0, 0, 1),
     "duffing_events": (2, 1, 1, 1, 2, 2, 2),
     "bouncing_ball": (2, 1, 1, 1, 2, 1, 2),
     "keller_miksis": (2, 21, 0, 0, 1, 1, 2),
@@ -162,6 +163,21 @@ def duffing_param_targets(nt: int, seed: int = 20261203) -> np.ndarray:
     """Per-instance terminal targets ~ N(0, 0.5^2) of the adjoint loss."""
     rng = np.random.default_rng(seed + 1)
     return rng.normal(0.0, 0.5, (2, nt))
+
+
+def duffing_param_sens_case(base: Case, tol: float = 1e-12) -> Case:
+    """The forward-sensitivity system of ``base`` (a duffing_param case):
+    state plus d(state)/d(x0, v0, k, B), starting from the identity block."""
+    c = empty_case("duffing_param_sens", 1, base.nt)
+    for k in ("td", "t", "cp"):
+        c.arrays[k] = base.arrays[k].copy()
+    c.arrays["x"][:2] = base.arrays["x"]
+    c.arrays["x"][2] = 1.0   # dx0/dx0(0)
+    c.arrays["x"][5] = 1.0   # dx1/dx1(0)
+    c.rtol[:] = tol
+    c.atol[:] = tol
+    c.options = dict(base.options)
+    return c
 
 
 def duffing_events_case(nt: int = 256, periods: int = 4, ndo: int = 16, seed: int = 7, stop_after: int = 0,

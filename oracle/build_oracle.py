@@ -32,7 +32,8 @@ BUILD_DIR = ORACLE_DIR / "_build"
 REF_DIR = ORACLE_DIR / "_ref"
 REFERENCE_ROOT = Path(os.environ.get("MPGOS_REFERENCE_ROOT", "/root/reference"))
 
-SYSTEMS = ["lorenz", "duffing", "duffing_param", "duffing_events", "bouncing_ball", "keller_miksis"]
+SYSTEMS = ["lorenz", "duffing", "duffing_param", "duffing_param_sens", "duffing_events", "bouncing_ball",
+           "keller_miksis"]
 FLAGS = ["-O3", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math"]
 
 

@@ -51,6 +51,28 @@ def _ref(system: str):
     return _ref_libs[system]
 
 
+def replay(case, dt_tape: np.ndarray, n_steps: np.ndarray, x0=None, cp=None, threads: int = 0) -> np.ndarray:
+    """End states of ``case`` integrated with a frozen step sequence
+    (``dt_tape`` [max_steps][NT], ``n_steps`` [NT]); optional replacement
+    initial states / control parameters. Returns x(T) [SD][NT]."""
+    lib = _oracle(case.system)
+    if not hasattr(lib.oracle_pt_replay, "_typed"):
+        lib.oracle_pt_replay.restype = C.c_int
+        lib.oracle_pt_replay.argtypes = [C.c_int, C.c_longlong, C.c_longlong, C.c_longlong, _D, _D, _D, _D, _I, _D,
+                                         _I, _D, _I, C.c_int]
+        lib.oracle_pt_replay._typed = True
+    a, tol, _ = _prepare(case)
+    x = np.ascontiguousarray((a["x"] if x0 is None else np.asarray(x0, np.float64)).copy())
+    cpa = a["cp"] if cp is None else np.ascontiguousarray(np.asarray(cp, np.float64))
+    t = np.ascontiguousarray(a["t"].copy())
+    rc = lib.oracle_pt_replay(case.algorithm, case.nt, 0, case.nt, x, t, cpa, tol["sp"], tol["spi"], a["acc"],
+                              a["acci"], np.ascontiguousarray(dt_tape, dtype=np.float64),
+                              np.ascontiguousarray(n_steps, dtype=np.int32), int(threads))
+    if rc != 0:
+        raise RuntimeError(f"oracle_pt_replay failed with {rc}")
+    return x
+
+
 def max_threads(system: str = "lorenz") -> int:
     return int(_oracle(system).oracle_pt_threads())
 

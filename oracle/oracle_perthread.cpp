@@ -314,6 +314,53 @@ int oracle_pt_solve(int algorithm, long long nt, long long first, long long coun
     return 0;
 }
 
+// Integrate instances [first, first+count) with a given step sequence:
+// dt[k*nt + i] for k < n_steps[i] (the frozen step sizes of a recorded GPU
+// forward pass), no step-size control, no events. x, t are updated in place.
+// This is the discrete map whose derivative the GPU adjoint computes, so
+// central differences of it check the adjoint without step-selection noise.
+int oracle_pt_replay(int algorithm, long long nt, long long first, long long count, double* x, double* t,
+                     const double* cp, const double* sp, const int* spi, const double* acc, const int* acci,
+                     const double* dt, const int* n_steps, int threads)
+{
+    if (nt < 1 || first < 0 || count < 0 || first + count > nt || (algorithm != 0 && algorithm != 1)) return 1;
+#ifdef _OPENMP
+    if (threads > 0) omp_set_num_threads(threads);
+#pragma omp parallel
+#endif
+    {
+        std::vector<double> spc(sp, sp + NSP);
+        std::vector<int> spic(spi, spi + NISP);
+        spc.push_back(0.0);
+        spic.push_back(0);
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 64)
+#endif
+        for (long long i = first; i < first + count; i++) {
+            double xi[SD], xn[SD], err[SD], cpi[one_at_least<NCP>()], acci_d[one_at_least<NA>()];
+            int accii[one_at_least<NIA>()];
+            for (int k = 0; k < SD; k++) xi[k] = x[i + k * nt];
+            for (int k = 0; k < NCP; k++) cpi[k] = cp[i + k * nt];
+            for (int k = 0; k < NA; k++) acci_d[k] = acc[i + k * nt];
+            for (int k = 0; k < NIA; k++) accii[k] = acci[i + k * nt];
+            double ti = t[i];
+            for (int s = 0; s < n_steps[i]; s++) {
+                const double h = dt[(long long)s * nt + i];
+                int finite = 1;
+                if (algorithm == 0)
+                    rk4((int)i, (int)nt, ti, h, xi, xn, finite, cpi, spc.data(), spic.data(), acci_d, accii);
+                else
+                    rkck45((int)i, (int)nt, ti, h, xi, xn, err, finite, cpi, spc.data(), spic.data(), acci_d, accii);
+                for (int k = 0; k < SD; k++) xi[k] = xn[k];
+                ti += h;
+            }
+            for (int k = 0; k < SD; k++) x[i + k * nt] = xi[k];
+            t[i] = ti;
+        }
+    }
+    return 0;
+}
+
 int oracle_pt_threads(void)
 {
 #ifdef _OPENMP

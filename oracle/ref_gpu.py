@@ -64,6 +64,7 @@ def _driver():
             "cuMemAlloc_v2": [C.POINTER(C.c_uint64), C.c_size_t],
             "cuMemFree_v2": [C.c_uint64],
             "cuMemcpyHtoD_v2": [C.c_uint64, P, C.c_size_t],
+            "cuMemcpyDtoH_v2": [P, C.c_uint64, C.c_size_t],
             "cuCtxGetCurrent": [C.POINTER(P)],
             "cuGetErrorString": [C.c_int, C.POINTER(C.c_char_p)],
         }.items():
@@ -180,3 +181,11 @@ def run_ref_gpu(case, block: int = 64, rreg: int | None = None, device: int = 0)
                 k.launch()
             s.SynchroniseDevice()
         return W.read_results(s)
+
+
+def device_to_host(ptr: int, shape, dtype) -> np.ndarray:
+    """Copy a device array (raw pointer) to a new host array (test helper)."""
+    out = np.empty(shape, dtype=dtype)
+    if out.nbytes:
+        _ck(_driver().cuMemcpyDtoH_v2(out.ctypes.data, int(ptr), out.nbytes), "cuMemcpyDtoH")
+    return out
