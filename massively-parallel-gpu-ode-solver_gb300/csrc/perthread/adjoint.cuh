@@ -73,6 +73,80 @@ template <> struct Tableau<MPGOS_RK4> {
 // buffer of the replayed states).
 constexpr int MAX_SEG = 64;
 
+// Local-memory budget (doubles) for keeping a whole segment's stage Jacobians.
+constexpr int JBUF_DOUBLES = 4096;
+
+// Stage values K and Jacobians J = [df/dx | df/dp] of one step from (x, t)
+// with step dt, by dual-number evaluation of the user's right-hand side at
+// the stage points X_st = x + dt * sum_j a_st,j K_j.
+template <class TB, int ST, int SD, int N, class D>
+__device__ __forceinline__ void dual_stages(int ti, int nti, const double* x, double t, double dt, D* cpd, D* spd,
+                                            int* spi, D* accd, int* acci, double (&K)[ST][SD],
+                                            double (&J)[ST][SD][N])
+{
+    for (int st = 0; st < ST; st++) {
+        D Xd[SD];
+        D Fd[SD];
+#pragma unroll
+        for (int d = 0; d < SD; d++) {
+            double sum = 0.0;
+            for (int j = 0; j < st; j++) sum += TB::a(st, j) * K[j][d];
+            Xd[d] = D(x[d] + dt * sum);
+            Xd[d].d[d] = 1.0;
+        }
+        const D Td(t + TB::c(st) * dt);
+        PerThread_OdeFunction(ti, nti, Fd, Xd, Td, cpd, spd, spi, accd, acci);
+#pragma unroll
+        for (int d = 0; d < SD; d++) {
+            K[st][d] = Fd[d].v;
+#pragma unroll
+            for (int q = 0; q < N; q++) J[st][d][q] = Fd[d].d[q];
+        }
+    }
+}
+
+// Adjoint of one Runge-Kutta step with frozen dt: lambda <- lambda + sum_i xi_i,
+// mu += sum_i J_p,i^T kappa_i (see the header comment).
+template <class TB, int ST, int SD, int N, int NCP>
+__device__ __forceinline__ void reverse_step(const double (&J)[ST][SD][N], double dt, double* lam, double* mu)
+{
+    double kap[ST][SD];
+    for (int st = 0; st < ST; st++)
+#pragma unroll
+        for (int d = 0; d < SD; d++) kap[st][d] = dt * TB::b(st) * lam[d];
+    double dlam[SD];
+#pragma unroll
+    for (int d = 0; d < SD; d++) dlam[d] = 0.0;
+    for (int st = ST - 1; st >= 0; st--) {
+        double xi[SD];
+#pragma unroll
+        for (int r = 0; r < SD; r++) {
+            double v = 0.0;
+#pragma unroll
+            for (int d = 0; d < SD; d++) v += J[st][d][r] * kap[st][d];
+            xi[r] = v;
+        }
+#pragma unroll
+        for (int q = 0; q < NCP; q++) {
+            double v = 0.0;
+#pragma unroll
+            for (int d = 0; d < SD; d++) v += J[st][d][SD + q] * kap[st][d];
+            mu[q] += v;
+        }
+        for (int j = 0; j < st; j++) {
+            const double w = dt * TB::a(st, j);
+            if (w != 0.0) {
+#pragma unroll
+                for (int d = 0; d < SD; d++) kap[j][d] += w * xi[d];
+            }
+        }
+#pragma unroll
+        for (int d = 0; d < SD; d++) dlam[d] += xi[d];
+    }
+#pragma unroll
+    for (int d = 0; d < SD; d++) lam[d] += dlam[d];
+}
+
 template <class S, int ALG>
 __global__ void __launch_bounds__(MPGOS_MAX_BLOCK) adjoint_kernel(Args<double> a, Tape tp, const double* dLdxT,
                                                                   double* dLdx0, double* dLdp)
@@ -82,6 +156,9 @@ __global__ void __launch_bounds__(MPGOS_MAX_BLOCK) adjoint_kernel(Args<double> a
     using D = ad::Dual<N>;
     using TB = Tableau<ALG>;
     constexpr int ST = TB::S;
+    // Keep a segment's stage Jacobians when they fit the local-memory budget;
+    // otherwise replay the states and re-evaluate the dual stages per step.
+    constexpr bool STORE_J = MAX_SEG * ST * SD * N <= JBUF_DOUBLES;
 
     extern __shared__ __align__(16) unsigned char mpgos_dyn_smem[];
     double* sp = reinterpret_cast<double*>(mpgos_dyn_smem);
@@ -129,10 +206,44 @@ __global__ void __launch_bounds__(MPGOS_MAX_BLOCK) adjoint_kernel(Args<double> a
     int status = a.status ? a.status[i] : 0;
     if (n > tp.max_steps) status |= MPGOS_INSTANCE_TAPE_OVERFLOW;
 
-    double xs[MAX_SEG][SD];
-    double ts[MAX_SEG];
     const int seg = tp.seg;
 
+    if constexpr (STORE_J) {
+        // One forward pass per segment with dual-number stages: the stage
+        // values advance the state (tableau form of the step), the stage
+        // Jacobians are kept in local memory, then the segment is swept
+        // backwards with algebra only. One right-hand-side evaluation per
+        // stage and step in the whole reverse pass.
+        double Jseg[MAX_SEG][ST][SD][N];
+        if (!(status & MPGOS_INSTANCE_TAPE_OVERFLOW) && n > 0) {
+            for (int sgm = (n - 1) / seg; sgm >= 0; sgm--) {
+                const int k0 = sgm * seg;
+                const int k1 = min(n, k0 + seg);
+                double x[SD];
+                double t = tp.ckpt_t[static_cast<long long>(sgm) * nt + i];
+#pragma unroll
+                for (int d = 0; d < SD; d++) x[d] = tp.ckpt_x[(static_cast<long long>(sgm) * SD + d) * nt + i];
+                for (int k = k0; k < k1; k++) {
+                    const double dt = tp.dt[static_cast<long long>(k) * nt + i];
+                    double K[ST][SD];
+                    dual_stages<TB, ST, SD, N>(ti, nti, x, t, dt, cpd, spd, spi, accd, acci, K, Jseg[k - k0]);
+                    if (k + 1 < k1) {
+#pragma unroll
+                        for (int d = 0; d < SD; d++) {
+                            double sum = 0.0;
+                            for (int st = 0; st < ST; st++) sum += TB::b(st) * K[st][d];
+                            x[d] = x[d] + dt * sum;
+                        }
+                        t += dt;
+                    }
+                }
+                for (int k = k1 - 1; k >= k0; k--)
+                    reverse_step<TB, ST, SD, N, NCP>(Jseg[k - k0], tp.dt[static_cast<long long>(k) * nt + i], lam, mu);
+            }
+        }
+    } else {
+    double xs[MAX_SEG][SD];
+    double ts[MAX_SEG];
     if (!(status & MPGOS_INSTANCE_TAPE_OVERFLOW) && n > 0) {
         for (int sgm = (n - 1) / seg; sgm >= 0; sgm--) {
             const int k0 = sgm * seg;
@@ -159,69 +270,16 @@ __global__ void __launch_bounds__(MPGOS_MAX_BLOCK) adjoint_kernel(Args<double> a
                     t += dt;
                 }
             }
-            // reverse through the segment
+            // reverse through the segment, re-evaluating the dual stages
             for (int k = k1 - 1; k >= k0; k--) {
                 const double dt = tp.dt[static_cast<long long>(k) * nt + i];
-                const double* xk = xs[k - k0];
-                const double tk  = ts[k - k0];
                 double K[ST][SD];
                 double J[ST][SD][N];
-                for (int st = 0; st < ST; st++) {
-                    D Xd[SD];
-                    D Fd[SD];
-#pragma unroll
-                    for (int d = 0; d < SD; d++) {
-                        double sum = 0.0;
-                        for (int j = 0; j < st; j++) sum += TB::a(st, j) * K[j][d];
-                        Xd[d] = D(xk[d] + dt * sum);
-                        Xd[d].d[d] = 1.0;
-                    }
-                    const D Td(tk + TB::c(st) * dt);
-                    PerThread_OdeFunction(ti, nti, Fd, Xd, Td, cpd, spd, spi, accd, acci);
-#pragma unroll
-                    for (int d = 0; d < SD; d++) {
-                        K[st][d] = Fd[d].v;
-#pragma unroll
-                        for (int q = 0; q < N; q++) J[st][d][q] = Fd[d].d[q];
-                    }
-                }
-                double kap[ST][SD];
-                for (int st = 0; st < ST; st++)
-#pragma unroll
-                    for (int d = 0; d < SD; d++) kap[st][d] = dt * TB::b(st) * lam[d];
-                double dlam[SD];
-#pragma unroll
-                for (int d = 0; d < SD; d++) dlam[d] = 0.0;
-                for (int st = ST - 1; st >= 0; st--) {
-                    double xi[SD];
-#pragma unroll
-                    for (int r = 0; r < SD; r++) {
-                        double v = 0.0;
-#pragma unroll
-                        for (int d = 0; d < SD; d++) v += J[st][d][r] * kap[st][d];
-                        xi[r] = v;
-                    }
-#pragma unroll
-                    for (int q = 0; q < NCP; q++) {
-                        double v = 0.0;
-#pragma unroll
-                        for (int d = 0; d < SD; d++) v += J[st][d][SD + q] * kap[st][d];
-                        mu[q] += v;
-                    }
-                    for (int j = 0; j < st; j++) {
-                        const double w = dt * TB::a(st, j);
-                        if (w != 0.0) {
-#pragma unroll
-                            for (int d = 0; d < SD; d++) kap[j][d] += w * xi[d];
-                        }
-                    }
-#pragma unroll
-                    for (int d = 0; d < SD; d++) dlam[d] += xi[d];
-                }
-#pragma unroll
-                for (int d = 0; d < SD; d++) lam[d] += dlam[d];
+                dual_stages<TB, ST, SD, N>(ti, nti, xs[k - k0], ts[k - k0], dt, cpd, spd, spi, accd, acci, K, J);
+                reverse_step<TB, ST, SD, N, NCP>(J, dt, lam, mu);
             }
         }
+    }
     }
 #pragma unroll
     for (int d = 0; d < SD; d++) dLdx0[d * nt + i] = lam[d];

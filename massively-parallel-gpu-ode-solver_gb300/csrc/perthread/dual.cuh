@@ -37,11 +37,13 @@ struct Dual {
     }
     __host__ __device__ explicit operator double() const { return v; }
 
+    // True when every derivative is +-0 (tested on the bit patterns, which
+    // keeps the FP64 pipe free).
     __device__ bool constant() const {
-        bool z = true;
+        long long z = 0;
 #pragma unroll
-        for (int i = 0; i < N; i++) z = z && (d[i] == 0.0);
-        return z;
+        for (int i = 0; i < N; i++) z |= (__double_as_longlong(d[i]) << 1);
+        return z == 0;
     }
 
     __device__ Dual& operator+=(const Dual& b) { v += b.v; for (int i = 0; i < N; i++) d[i] += b.d[i]; return *this; }

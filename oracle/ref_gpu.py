@@ -14,6 +14,13 @@ argument structs) on the device buffers of a GB300 ``ProblemSolver``, whose
 SoA layout is the reference's. Tolerance and event arrays are separate device
 copies padded to max(SD, NE) entries, because the reference kernel reads the
 event options for every index below SD (SingleSystem_PerThread_Solver.cuh:60).
+
+Launches use one warp per block (the reference's default BlockSize, the warp
+size, SingleSystem_PerThread_Interface.cuh:343): the reference kernel stages
+tolerances and event options into shared memory from threads 0..SD-1 and
+reads them from every thread without a barrier
+(SingleSystem_PerThread_Solver.cuh:37-65), so with several warps per block the
+later warps can read the shared arrays before they are written.
 """
 from __future__ import annotations
 
@@ -170,7 +177,7 @@ class ReferenceKernel:
                                      self.params, None), "cuLaunchKernel")
 
 
-def run_ref_gpu(case, block: int = 64, rreg: int | None = None, device: int = 0) -> dict:
+def run_ref_gpu(case, block: int = 32, rreg: int | None = None, device: int = 0) -> dict:
     """Integrate ``case`` (all phases) with the reference kernel on the GPU."""
     from mpgos_gb300 import workloads as W
     with W.load_solver(case, mode=0, device=device) as s:

@@ -56,18 +56,33 @@ GOLDEN = [(p.stem, *load(p)) for p in golden_files()]
 def test_plain_is_bitwise_identical_to_reference_kernel(name, case, native_libs):
     if not _ref_available(case):
         pytest.skip("no reference cubin for this case (see oracle/build_oracle.REF_GPU_KERNELS)")
-    ref = R.run_ref_gpu(case, block=64)
+    ref = R.run_ref_gpu(case)  # one warp per block, the reference's default
     for mode in (0, 2):  # static and persistent mapping
         assert_bitwise(W.run_gpu(case, mode=mode, block=64), ref,
                        keys=["td", "x", "t", "cp", "acc", "acci", "didx"] + (["dtime", "dstate"] if case.ndo else []))
 
 
 # ---- parity with the reference CPU build (golden fixtures) ------------------
+_CALM = {}
+
+
+def calm_instances(name, case):
+    """Instances that are not chaotic (parity.sensitive_instances), cached."""
+    if name not in _CALM:
+        _CALM[name] = ~sensitive_instances(case)
+    return _CALM[name]
+
+
 @pytest.mark.parametrize("mode", list(MODES), ids=str)
 @pytest.mark.parametrize("name,case,ref", GOLDEN, ids=lambda v: v if isinstance(v, str) else "")
-def test_gpu_matches_reference_golden(name, case, ref, mode, native_libs):
+def test_gpu_matches_reference_golden(name, case, ref, mode, native_libs, oracle_libs):
+    """PLAIN and PERSISTENT: every instance. FAST_CONTROL forms: every
+    non-chaotic instance (their step sizes differ by ~1e-6 relative)."""
     res = W.run_gpu(case, mode=MODES[mode], block=64)
-    assert_close(res, ref)
+    mask = calm_instances(name, case) if MODES[mode] & capi.MODE_FAST_CONTROL else None
+    if mask is not None:
+        assert mask.mean() > 0.8, mask.mean()
+    assert_close(res, ref, mask=mask)
     assert np.all(res["status"] & (capi.INSTANCE_NONFINITE | capi.INSTANCE_ATTEMPT_LIMIT) == 0)
 
 
@@ -77,10 +92,11 @@ def test_gpu_matches_reference_golden(name, case, ref, mode, native_libs):
 def test_gpu_matches_oracle(name, case, mode, native_libs, oracle_libs):
     ref = O.run_oracle(case)
     res = W.run_gpu(case, mode=MODES[mode], block=96)
-    assert_close(res, ref)
-    np.testing.assert_array_equal(res["nacc"], ref["nacc"])
-    np.testing.assert_array_equal(res["nrej"], ref["nrej"])
-    np.testing.assert_array_equal(res["status"], ref["status"])
+    mask = calm_instances(name, case) if MODES[mode] & capi.MODE_FAST_CONTROL else np.ones(case.nt, bool)
+    assert mask.mean() > 0.8, mask.mean()
+    assert_close(res, ref, mask=mask)
+    for k in ("nacc", "nrej", "status"):
+        np.testing.assert_array_equal(res[k][mask], ref[k][mask], err_msg=k)
 
 
 @pytest.mark.parametrize("fast", [0, 1])
@@ -131,7 +147,7 @@ def test_lorenz_full_size(native_libs, oracle_libs):
     assert chosen["acci"][0].sum() == chosen["nacc"].sum()
     if _ref_available(case):
         plain = W.run_gpu(case, mode=0, block=64)
-        assert_bitwise(plain, R.run_ref_gpu(case, block=64), keys=["x", "t", "acci"])
+        assert_bitwise(plain, R.run_ref_gpu(case), keys=["x", "t", "acci"])
     idx = np.unique(np.concatenate([np.linspace(0, case.nt - 1, 448).astype(np.int64),
                                     np.random.default_rng(1).integers(0, case.nt, 64)]))
     sub = case.subset(idx)
@@ -145,31 +161,41 @@ def test_lorenz_full_size(native_libs, oracle_libs):
 
 
 def test_fp32_stage_mode_error_is_bounded(native_libs, oracle_libs):
-    case = W.lorenz_case(nt=4096, tol=1e-6)
+    """FP32 stages at rtol = atol = 1e-6 on the non-chaotic Lorenz range:
+    end-state error against the FP64 oracle of the same tolerance."""
+    case = W.lorenz_case(nt=4096, tol=1e-6, rho=(0.0, 13.9))
     ref = O.run_oracle(case)
     res = W.run_gpu(case, mode=capi.MODE_FP32_STAGE | capi.MODE_CHOSEN, block=128)
     assert np.all(np.isfinite(res["x"])) and np.all(res["t"] == 10.0)
-    calm = ~sensitive_instances(case, rtol=1e-6)
-    assert scaled_close(res["x"][:, calm], ref["x"][:, calm], 1e-3).all()
+    assert np.quantile(scaled_rel(res["x"], ref["x"]), 0.99) < 1e-4
 
 
 def test_float_precision_table(native_libs, oracle_libs):
-    case = W.lorenz_case(nt=512, tol=1e-6)
+    """Precision = float (the reference's float build) at 1e-5."""
+    case = W.lorenz_case(nt=512, tol=1e-5, rho=(0.0, 13.9))
     ref = O.run_oracle(case)
     res = W.run_gpu(case, mode=0, precision="float")
-    calm = ~sensitive_instances(case, rtol=1e-5)
-    assert scaled_close(res["x"][:, calm], ref["x"][:, calm], 1e-2).all()
+    assert np.all(res["t"] == np.float32(10.0))
+    assert np.quantile(scaled_rel(res["x"], ref["x"]), 0.99) < 1e-3
 
 
-def test_status_flags_and_attempt_limit(native_libs):
+def scaled_rel(a, b):
+    scale = np.max(np.abs(b), axis=1, keepdims=True)
+    return np.max(np.abs(a - b) / (np.abs(b) + 1e-3 * scale), axis=0)
+
+
+@pytest.mark.parametrize("mode", [0, 3])
+def test_status_flags_and_attempt_limit(mode, native_libs, oracle_libs):
     case = W.lorenz_case(nt=64)
-    case.options["max_attempts"] = 10
     case.arrays["x"][0, 5] = np.nan
-    res = W.run_gpu(case, mode=3)
-    assert res["status"][5] & capi.INSTANCE_NONFINITE
-    others = np.delete(np.arange(64), 5)
-    assert np.all(res["status"][others] & capi.INSTANCE_ATTEMPT_LIMIT)
-    assert np.all(res["nacc"][others] + res["nrej"][others] == 10)
+    res = W.run_gpu(case, mode=mode)
+    ref = O.run_oracle(case)
+    assert res["status"][5] == capi.INSTANCE_NONFINITE      # shrinks to the minimum step, then stops
+    np.testing.assert_array_equal(res["status"], ref["status"])
+    case.options["max_attempts"] = 10
+    res = W.run_gpu(case, mode=mode)
+    assert np.all(res["status"] & capi.INSTANCE_ATTEMPT_LIMIT)
+    assert np.all(res["nacc"] + res["nrej"] == 10)
 
 
 def test_two_solver_objects_alternate(native_libs):
