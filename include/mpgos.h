@@ -296,6 +296,115 @@ const char* mpgos_last_error(void);
 /* Runtime ABI version (MPGOS_ABI_VERSION). */
 int mpgos_abi_version(void);
 
+/* =========================================================================
+ * Coupled per-block solver (CoupledSystems_PerBlock_Interface.cuh:135-248):
+ * NS systems of UPS coupled units. Unit-scope arrays are [field][NS*UPS]
+ * with unit u of system s at s*UPS + u, system-scope arrays [field][NS]; the
+ * coupling matrix is stored as the reference stores it for its (CBW, CCI)
+ * (CoupledSystems_PerBlock_Interface.cuh:426-438, :993-1080).
+ * ========================================================================= */
+
+/* ListOfVariables of the coupled interface (CoupledSystems_PerBlock_Interface.cuh:33-52). */
+enum mpgos_cb_variable {
+    MPGOS_CB_ALL = 0, MPGOS_CB_TIME_DOMAIN = 1, MPGOS_CB_ACTUAL_TIME = 2, MPGOS_CB_ACTUAL_STATE = 3,
+    MPGOS_CB_UNIT_PARAMETERS = 4, MPGOS_CB_SYSTEM_PARAMETERS = 5, MPGOS_CB_GLOBAL_PARAMETERS = 6,
+    MPGOS_CB_INTEGER_GLOBAL_PARAMETERS = 7, MPGOS_CB_UNIT_ACCESSORIES = 8, MPGOS_CB_INTEGER_UNIT_ACCESSORIES = 9,
+    MPGOS_CB_SYSTEM_ACCESSORIES = 10, MPGOS_CB_INTEGER_SYSTEM_ACCESSORIES = 11, MPGOS_CB_COUPLING_MATRIX = 12,
+    MPGOS_CB_COUPLING_STRENGTH = 13, MPGOS_CB_COUPLING_INDEX = 14, MPGOS_CB_DENSE_OUTPUT = 15,
+    MPGOS_CB_DENSE_INDEX = 16, MPGOS_CB_DENSE_TIME = 17, MPGOS_CB_DENSE_STATE = 18,
+    /* extensions: per system, last Solve */
+    MPGOS_CB_STATUS = 32, MPGOS_CB_ACCEPTED_STEPS = 33, MPGOS_CB_REJECTED_STEPS = 34
+};
+
+/* ListOfSolverOptions of the coupled interface (CoupledSystems_PerBlock_Interface.cuh:53-66). */
+enum mpgos_cb_option {
+    MPGOS_CB_INITIAL_TIME_STEP = 0, MPGOS_CB_ACTIVE_SYSTEMS = 1, MPGOS_CB_MAXIMUM_TIME_STEP = 2,
+    MPGOS_CB_MINIMUM_TIME_STEP = 3, MPGOS_CB_TIME_STEP_GROW_LIMIT = 4, MPGOS_CB_TIME_STEP_SHRINK_LIMIT = 5,
+    MPGOS_CB_RELATIVE_TOLERANCE = 6, MPGOS_CB_ABSOLUTE_TOLERANCE = 7, MPGOS_CB_EVENT_TOLERANCE = 8,
+    MPGOS_CB_EVENT_DIRECTION = 9, MPGOS_CB_DENSE_OUTPUT_SAVE_FREQUENCY = 10,
+    MPGOS_CB_DENSE_OUTPUT_MINIMUM_TIME_STEP = 11, MPGOS_CB_SHARED_GLOBAL_VARIABLES = 12,
+    MPGOS_CB_SHARED_COUPLING_MATRICES = 13,
+    /* extensions */
+    MPGOS_CB_KERNEL_MODE = 32,          /* 0 or MPGOS_MODE_PERSISTENT       */
+    MPGOS_CB_MAXIMUM_ATTEMPTS = 33,     /* step attempts per system         */
+    MPGOS_CB_WARPS_PER_BLOCK = 34       /* systems per CTA (one per warp)   */
+};
+
+typedef struct mpgos_cb_shape {
+    int32_t ups, ud, nc, cbw, cci, nup, nsp, ngp, nigp, nua, niua, nsa, nisa, ne;
+    int32_t algorithm, precision_bytes;
+    int32_t matrix_entries;  /* stored entries of one coupling matrix */
+} mpgos_cb_shape;
+
+typedef struct mpgos_cb_launch {
+    int64_t ns, n_active;
+    int32_t ndo, mode, shared_global, shared_coupling, dense_save_frequency, reserved;
+    int64_t max_attempts;
+    double  initial_dt, max_dt, min_dt, grow_limit, shrink_limit, dense_min_dt;
+    void*          time_domain;                 /* [2][NS]        */
+    void*          actual_time;                 /* [NS]           */
+    void*          system_parameters;           /* [NSP][NS]      */
+    void*          system_accessories;          /* [NSA][NS]      */
+    int32_t*       integer_system_accessories;  /* [NISA][NS]     */
+    void*          coupling_strength;           /* [NC][NS]       */
+    int32_t*       dense_index;                 /* [NS]           */
+    void*          dense_time;                  /* [NDO][NS]      */
+    void*          actual_state;                /* [UD][NS*UPS]   */
+    void*          unit_parameters;             /* [NUP][NS*UPS]  */
+    void*          unit_accessories;            /* [NUA][NS*UPS]  */
+    int32_t*       integer_unit_accessories;    /* [NIUA][NS*UPS] */
+    void*          dense_state;                 /* [NDO][UD][NS*UPS] */
+    const void*    global_parameters;           /* [NGP]          */
+    const int32_t* integer_global_parameters;   /* [NIGP]         */
+    const void*    coupling_matrix;             /* [NC][matrix_entries] */
+    const int32_t* coupling_index;              /* [NC]           */
+    const void*    relative_tolerance;          /* [UD]           */
+    const void*    absolute_tolerance;          /* [UD]           */
+    const void*    event_tolerance;             /* [NE]           */
+    const int32_t* event_direction;             /* [NE]           */
+    int32_t*       status;                      /* [NS]           */
+    int32_t*       accepted_steps;              /* [NS]           */
+    int32_t*       rejected_steps;              /* [NS]           */
+    uint32_t*      work_counter;
+} mpgos_cb_launch;
+
+typedef struct mpgos_cb_kernels {
+    int32_t        abi_version;
+    mpgos_cb_shape shape;
+    const char*    name;
+    int (*launch)(const mpgos_cb_launch* args, int grid, int block, size_t dynamic_smem, void* stream);
+    int (*occupancy)(int32_t mode, int block, size_t dynamic_smem, int* blocks_per_sm);
+    size_t (*dynamic_smem)(int warps_per_block, int shared_global, int shared_coupling);
+} mpgos_cb_kernels;
+
+typedef struct mpgos_cb_solver mpgos_cb_solver;
+
+/* ProblemSolver(int) / ~ProblemSolver of the coupled interface. */
+int mpgos_cb_create(const mpgos_cb_kernels* kernels, int64_t ns, int32_t ndo, int device, mpgos_cb_solver** out);
+int mpgos_cb_destroy(mpgos_cb_solver* solver);
+int mpgos_cb_get_shape(const mpgos_cb_solver* solver, mpgos_cb_shape* shape, int64_t* ns, int32_t* ndo);
+/* SolverOption (CoupledSystems_PerBlock_Interface.cuh:760-860). */
+int mpgos_cb_set_option(mpgos_cb_solver* solver, int32_t option, int32_t index, double value);
+/* Pinned host / device buffer of a variable and its element count. */
+int mpgos_cb_host_buffer(mpgos_cb_solver* solver, int32_t variable, void** ptr, int64_t* count);
+int mpgos_cb_device_buffer(mpgos_cb_solver* solver, int32_t variable, void** ptr, int64_t* count);
+/* SynchroniseFromHostToDevice / SynchroniseFromDeviceToHost. */
+int mpgos_cb_sync_h2d(mpgos_cb_solver* solver, int32_t variable);
+int mpgos_cb_sync_d2h(mpgos_cb_solver* solver, int32_t variable);
+/* Solve() (CoupledSystems_PerBlock_Interface.cuh:1947-1966): one launch. */
+int mpgos_cb_solve(mpgos_cb_solver* solver);
+int mpgos_cb_insert_sync_point(mpgos_cb_solver* solver);
+int mpgos_cb_sync_solver(mpgos_cb_solver* solver);
+int mpgos_cb_timer_start(mpgos_cb_solver* solver);
+int mpgos_cb_timer_stop(mpgos_cb_solver* solver, float* milliseconds);
+int mpgos_cb_stream(mpgos_cb_solver* solver, void** stream);
+int mpgos_cb_checkpoint_save(mpgos_cb_solver* solver);
+int mpgos_cb_checkpoint_restore(mpgos_cb_solver* solver);
+
+/* Coupled kernel table of a coupled-system plugin, or NULL. */
+typedef const mpgos_cb_kernels* (*mpgos_cb_system_fn)(int32_t algorithm, int32_t precision_bytes);
+const mpgos_cb_kernels* mpgos_cb_system_kernels(int32_t algorithm, int32_t precision_bytes);
+
 /* ---- entry point exported by every system plugin --------------------- */
 /* Kernel table for (algorithm, precision_bytes), or NULL if not compiled. */
 typedef const mpgos_pt_kernels* (*mpgos_pt_system_fn)(int32_t algorithm, int32_t precision_bytes);

@@ -1,0 +1,789 @@
+// Coupled per-block ensemble solver for sm_103a: one warp per system.
+//
+// The reference integrates a system of UPS coupled units with one thread per
+// unit inside a block (four kernel variants by launch shape,
+// SourceCodes/CoupledSystmes_PerBlock_Solver.cuh:10,786,1507,2214, chosen in
+// CoupledSystems_PerBlock_Interface.cuh:1949-1966), system-scope variables in
+// shared memory, per-system reductions through shared-memory atomics
+// (atomicAnd, a CAS-loop atomicFMIN) and a __syncthreads between every phase
+// of a step. Here one warp owns one system:
+//
+//  * units are spread over the 32 lanes (UPL = ceil(UPS/32) units per lane),
+//    their state, stages and parameters live in registers;
+//  * system-scope variables (time domain, time, step, dense index, user
+//    termination flag, system parameters and accessories) live in a per-warp
+//    slot of shared memory, because the hooks take them by reference exactly
+//    as in the reference;
+//  * the coupling matrix is staged once per CTA in shared memory (all four
+//    storages of the reference: full, banded, circular-banded, full circular)
+//    and the coupling matrix-vector product of every stage reads the coupling
+//    terms as shared-memory broadcasts;
+//  * accept/reject, the error ratio and the event step are warp reductions
+//    (__all_sync, shuffles) and the phases are separated by __syncwarp only,
+//    so systems never wait for each other; in PERSISTENT mode a warp pulls
+//    the next system from a device counter when its system finishes.
+//
+// Arithmetic (stage sums, coupling accumulation, controller with safety
+// factor 0.8, event secant step) keeps the reference's operation order
+// (CoupledSystems_PerBlock_ExplicitRungeKutta_Steppers.cuh:1483-2014,
+// ..._ErrorControllers.cuh:320-423, CoupledSystems_PerBlock_EventHandling.cuh:149-214).
+//
+// The user hooks (CoupledSystems_PerBlock_OdeFunction, _EventFunction,
+// _ActionAfterEventDetection, _ActionAfterSuccessfulTimeStep,
+// _Initialization, _Finalization) must be declared before this header.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../perthread/numerics.cuh"
+
+#ifndef MPGOS_CB_MAX_BLOCK
+#define MPGOS_CB_MAX_BLOCK 256
+#endif
+
+namespace mpgos {
+namespace cb {
+
+using pt::AtLeastOne;
+using pt::Options;
+
+template <int UPS_, int UD_, int NC_, int CBW_, int CCI_, int NUP_, int NSP_, int NGP_, int NIGP_, int NUA_,
+          int NIUA_, int NSA_, int NISA_, int NE_>
+struct Shape {
+    static constexpr int UPS = UPS_, UD = UD_, NC = NC_, CBW = CBW_, CCI = CCI_, NUP = NUP_, NSP = NSP_;
+    static constexpr int NGP = NGP_, NIGP = NIGP_, NUA = NUA_, NIUA = NIUA_, NSA = NSA_, NISA = NISA_, NE = NE_;
+    static constexpr int UPL = (UPS + 31) / 32;  // units per lane
+    // entries of one stored coupling matrix (CoupledSystems_PerBlock_Interface.cuh:426-438)
+    static constexpr int MAT = (CCI == 0 && CBW == 0)  ? UPS * UPS
+                               : (CCI == 0 && CBW > 0) ? UPS * (2 * CBW + 1)
+                               : (CCI == 1 && CBW > 0) ? (2 * CBW + 1)
+                                                       : UPS;
+};
+
+template <class P>
+struct Args {
+    long long ns, n_active;
+    // system scope [field][NS]
+    P* td;
+    P* t;
+    P* sp;
+    P* sacc;
+    int* isacc;
+    P* cstr;
+    int* didx;
+    P* dtime;
+    // unit scope [field][NS*UPS], unit u of system s at s*UPS + u
+    P* x;
+    P* up;
+    P* uacc;
+    int* iuacc;
+    P* dstate;
+    // global scope
+    const P* gp;
+    const int* igp;
+    const P* cmat;
+    const int* cidx;
+    const P* rtol;
+    const P* atol;
+    const P* etol;
+    const int* edir;
+    // per system, this launch
+    int* status;
+    int* n_acc;
+    int* n_rej;
+    unsigned int* work;
+    int shared_global;
+    int shared_coupling;
+    Options<P> o;
+};
+
+// Per-warp (per-system) shared-memory slot.
+template <class S, class P>
+struct WarpSlot {
+    P td[2];
+    P t, dt, newdt, dense_next, evdt, ratio;
+    P sp[AtLeastOne<S::NSP>::value];
+    P sacc[AtLeastOne<S::NSA>::value];
+    P cstr[AtLeastOne<S::NC>::value];
+    P cpt[S::UPS][AtLeastOne<S::NC>::value];
+    int isacc[AtLeastOne<S::NISA>::value];
+    int didx, udt, skipped, update;
+};
+
+template <class S, class P>
+__host__ __device__ constexpr size_t block_smem_bytes()
+{
+    return 0;
+}
+
+// Coupling value of coupling i for unit `unit`: ComputeCouplingValue of
+// CoupledSystems_PerBlock_ExplicitRungeKutta_Steppers.cuh:2552-2633.
+template <class S, class P>
+__device__ __forceinline__ P coupling_value(const P* M, const WarpSlot<S, P>& w, int unit, int i)
+{
+    constexpr int UPS = S::UPS, CBW = S::CBW, CCI = S::CCI;
+    P v = 0;
+    if (CCI == 0 && CBW == 0) {
+        const int shift = i * UPS * UPS;
+        for (int col = 0; col < UPS; col++) v += M[unit + col * UPS + shift] * w.cpt[col][i];
+    } else if (CCI == 0 && CBW > 0) {
+        const int shift = i * UPS * (2 * CBW + 1);
+        for (int dg = 0; dg < 2 * CBW + 1; dg++) {
+            int su = unit + dg - CBW;
+            if (su >= UPS) su -= UPS;
+            if (su < 0) su += UPS;
+            v += M[unit + dg * UPS + shift] * w.cpt[su][i];
+        }
+    } else if (CCI == 1 && CBW > 0) {
+        const int shift = i * (2 * CBW + 1);
+        for (int dg = 0; dg < 2 * CBW + 1; dg++) {
+            int su = unit + dg - CBW;
+            if (su >= UPS) su -= UPS;
+            if (su < 0) su += UPS;
+            v += M[dg + shift] * w.cpt[su][i];
+        }
+    } else {
+        const int shift = i * UPS;
+        for (int dg = 0; dg < UPS; dg++) {
+            int su = unit + dg - CBW;
+            if (su >= UPS) su -= UPS;
+            if (su < 0) su += UPS;
+            v += M[dg + shift] * w.cpt[su][i];
+        }
+    }
+    return v;
+}
+
+__device__ __forceinline__ bool warp_all(bool p) { return __all_sync(0xffffffffu, p); }
+__device__ __forceinline__ bool warp_any(bool p) { return __any_sync(0xffffffffu, p); }
+template <class P>
+__device__ __forceinline__ P warp_min(P v)
+{
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, off));
+    return v;
+}
+
+template <class S, int ALG, class P, int MODE>
+struct Solver {
+    static constexpr int UPS = S::UPS, UD = S::UD, NC = S::NC, NUP = S::NUP, NUA = S::NUA, NIUA = S::NIUA;
+    static constexpr int NE = S::NE, UPL = S::UPL, NSP = S::NSP, NSA = S::NSA, NISA = S::NISA;
+    static constexpr bool PERSISTENT = (MODE & MPGOS_MODE_PERSISTENT) != 0;
+    using Slot = WarpSlot<S, P>;
+
+    // Registers of the lane's units.
+    struct Units {
+        P x[UPL][UD];
+        P up[UPL][AtLeastOne<NUP>::value];
+        P uacc[UPL][AtLeastOne<NUA>::value];
+        int iuacc[UPL][AtLeastOne<NIUA>::value];
+        P ga[UPL][AtLeastOne<NE>::value];
+        P cpf[UPL][AtLeastOne<NC>::value];
+    };
+
+    __device__ static bool has(int lane, int j) { return lane + 32 * j < UPS; }
+    __device__ static int unit_of(int lane, int j) { return lane + 32 * j; }
+
+    // One right-hand side for all of the lane's units at stage point X, then
+    // the coupling term added (the stepper stage of
+    // CoupledSystems_PerBlock_ExplicitRungeKutta_Steppers.cuh:1733-1762).
+    __device__ static void stage_rhs(long long s, int lane, Slot& w, Units& u, const P* gp, const int* igp, const P* M,
+                                     const int* cidx, P T, P (&X)[UPL][UD], P (&F)[UPL][UD])
+    {
+        const int sid = static_cast<int>(s);
+#pragma unroll
+        for (int j = 0; j < UPL; j++) {
+            if (has(lane, j)) {
+                const int uid = unit_of(lane, j);
+                CoupledSystems_PerBlock_OdeFunction<P>(sid, uid, F[j], X[j], T, u.up[j], w.sp, const_cast<P*>(gp),
+                                                       const_cast<int*>(igp), u.uacc[j], u.iuacc[j], w.sacc, w.isacc,
+                                                       w.cpt[uid], u.cpf[j]);
+            }
+        }
+        __syncwarp();
+#pragma unroll
+        for (int j = 0; j < UPL; j++) {
+            if (has(lane, j)) {
+                const int uid = unit_of(lane, j);
+                for (int i = 0; i < NC; i++) {
+                    const P value = coupling_value<S, P>(M, w, uid, i);
+                    const int c = cidx[i];  // validated on the host; guarded against a stale device copy
+                    if (c >= 0 && c < UD) F[j][c] += w.cstr[i] * u.cpf[j][i] * value;
+                }
+            }
+        }
+        __syncwarp();
+    }
+
+    // RK4 step: CoupledSystems_PerBlock_ExplicitRungeKutta_Steppers.cuh:1483-1692.
+    __device__ static void step_rk4(long long s, int lane, Slot& w, Units& u, const P* gp, const int* igp, const P* M,
+                                    const int* cidx, P t, P dt, P (&xn)[UPL][UD], int& finite)
+    {
+        P X[UPL][UD], k[UPL][UD];
+        stage_rhs(s, lane, w, u, gp, igp, M, cidx, t, u.x, xn);
+        P T = t + static_cast<P>(0.5) * dt;
+#pragma unroll
+        for (int j = 0; j < UPL; j++)
+#pragma unroll
+            for (int d = 0; d < UD; d++) X[j][d] = u.x[j][d] + xn[j][d] * static_cast<P>(0.5) * dt;
+        stage_rhs(s, lane, w, u, gp, igp, M, cidx, T, X, k);
+#pragma unroll
+        for (int j = 0; j < UPL; j++)
+#pragma unroll
+            for (int d = 0; d < UD; d++) {
+                xn[j][d] += 2 * k[j][d];
+                X[j][d] = u.x[j][d] + k[j][d] * static_cast<P>(0.5) * dt;
+            }
+        stage_rhs(s, lane, w, u, gp, igp, M, cidx, T, X, k);
+        T = t + dt;
+#pragma unroll
+        for (int j = 0; j < UPL; j++)
+#pragma unroll
+            for (int d = 0; d < UD; d++) {
+                xn[j][d] += static_cast<P>(2.0) * k[j][d];
+                X[j][d] = u.x[j][d] + k[j][d] * dt;
+            }
+        stage_rhs(s, lane, w, u, gp, igp, M, cidx, T, X, k);
+#pragma unroll
+        for (int j = 0; j < UPL; j++)
+#pragma unroll
+            for (int d = 0; d < UD; d++) {
+                xn[j][d] = u.x[j][d] + dt * (xn[j][d] + k[j][d]) * static_cast<P>(1.0 / 6.0);
+                if (has(lane, j) && isfinite(xn[j][d]) == 0) finite = 0;
+            }
+    }
+
+    // Cash-Karp 4(5) step: CoupledSystems_PerBlock_ExplicitRungeKutta_Steppers.cuh:1695-2014.
+    __device__ static void step_rkck45(long long s, int lane, Slot& w, Units& u, const P* gp, const int* igp,
+                                       const P* M, const int* cidx, P t, P dt, P (&xn)[UPL][UD],
+                                       P (&err)[UPL][UD], int& finite)
+    {
+        P X[UPL][UD];
+        P k1[UPL][UD], k2[UPL][UD], k3[UPL][UD], k4[UPL][UD], k5[UPL][UD], k6[UPL][UD];
+        stage_rhs(s, lane, w, u, gp, igp, M, cidx, t, u.x, k1);
+#pragma unroll
+        for (int j = 0; j < UPL; j++)
+#pragma unroll
+            for (int d = 0; d < UD; d++) X[j][d] = u.x[j][d] + (k1[j][d] * static_cast<P>(1.0 / 5.0)) * dt;
+        stage_rhs(s, lane, w, u, gp, igp, M, cidx, t + static_cast<P>(1.0 / 5.0) * dt, X, k2);
+#pragma unroll
+        for (int j = 0; j < UPL; j++)
+#pragma unroll
+            for (int d = 0; d < UD; d++)
+                X[j][d] = u.x[j][d] + (k1[j][d] * static_cast<P>(3.0 / 40.0) + k2[j][d] * static_cast<P>(9.0 / 40.0)) * dt;
+        stage_rhs(s, lane, w, u, gp, igp, M, cidx, t + static_cast<P>(3.0 / 10.0) * dt, X, k3);
+#pragma unroll
+        for (int j = 0; j < UPL; j++)
+#pragma unroll
+            for (int d = 0; d < UD; d++)
+                X[j][d] = u.x[j][d] + (k1[j][d] * static_cast<P>(3.0 / 10.0) + k2[j][d] * static_cast<P>(-9.0 / 10.0) +
+                                       k3[j][d] * static_cast<P>(6.0 / 5.0)) * dt;
+        stage_rhs(s, lane, w, u, gp, igp, M, cidx, t + static_cast<P>(3.0 / 5.0) * dt, X, k4);
+#pragma unroll
+        for (int j = 0; j < UPL; j++)
+#pragma unroll
+            for (int d = 0; d < UD; d++)
+                X[j][d] = u.x[j][d] + (k1[j][d] * static_cast<P>(-11.0 / 54.0) + k2[j][d] * static_cast<P>(5.0 / 2.0) +
+                                       k3[j][d] * static_cast<P>(-70.0 / 27.0) +
+                                       k4[j][d] * static_cast<P>(35.0 / 27.0)) * dt;
+        stage_rhs(s, lane, w, u, gp, igp, M, cidx, t + dt, X, k5);
+#pragma unroll
+        for (int j = 0; j < UPL; j++)
+#pragma unroll
+            for (int d = 0; d < UD; d++)
+                X[j][d] = u.x[j][d] + (k1[j][d] * static_cast<P>(1631.0 / 55296.0) +
+                                       k2[j][d] * static_cast<P>(175.0 / 512.0) +
+                                       k3[j][d] * static_cast<P>(575.0 / 13824.0) +
+                                       k4[j][d] * static_cast<P>(44275.0 / 110592.0) +
+                                       k5[j][d] * static_cast<P>(253.0 / 4096.0)) * dt;
+        stage_rhs(s, lane, w, u, gp, igp, M, cidx, t + static_cast<P>(7.0 / 8.0) * dt, X, k6);
+#pragma unroll
+        for (int j = 0; j < UPL; j++)
+#pragma unroll
+            for (int d = 0; d < UD; d++) {
+                xn[j][d] = u.x[j][d] + (k1[j][d] * static_cast<P>(37.0 / 378.0) +
+                                        k3[j][d] * static_cast<P>(250.0 / 621.0) +
+                                        k4[j][d] * static_cast<P>(125.0 / 594.0) +
+                                        k6[j][d] * static_cast<P>(512.0 / 1771.0)) * dt;
+                P e = k1[j][d] * (static_cast<P>(37.0 / 378.0 - 2825.0 / 27648.0)) +
+                      k3[j][d] * (static_cast<P>(250.0 / 621.0 - 18575.0 / 48384.0)) +
+                      k4[j][d] * (static_cast<P>(125.0 / 594.0 - 13525.0 / 55296.0)) +
+                      k5[j][d] * (static_cast<P>(0.0 - 277.0 / 14336.0)) +
+                      k6[j][d] * (static_cast<P>(512.0 / 1771.0 - 1.0 / 4.0));
+                err[j][d] = dt * abs(e) + static_cast<P>(1e-18);
+                if (has(lane, j) && ((isfinite(xn[j][d]) == 0) || (isfinite(err[j][d]) == 0))) finite = 0;
+            }
+    }
+
+    // Integrate system s with the calling warp: the body of the reference's
+    // MultipleSystems_SingleBlockLaunch kernel for one system
+    // (CoupledSystmes_PerBlock_Solver.cuh:1575-2211).
+    __device__ static void system(long long s, int lane, Slot& w, const Args<P>& a, const P* gp, const int* igp,
+                                  const P* M, const int* cidx, const P* rtol, const P* atol, const P* etol,
+                                  const int* edir)
+    {
+        const long long ns = a.ns, nu = a.ns * UPS;
+        const Options<P>& o = a.o;
+        const int sid = static_cast<int>(s);
+        Units u;
+        // ---- load: system scope into the slot, unit scope into registers
+        if (lane == 0) {
+            w.td[0] = a.td[s];
+            w.td[1] = a.td[s + ns];
+            w.t = a.t[s];
+            w.dt = o.initial_dt;
+            w.newdt = o.initial_dt;
+            w.didx = a.didx[s];
+            w.udt = 0;
+            w.skipped = 0;
+            w.dense_next = w.t;
+        }
+        for (int k = lane; k < NSP; k += 32) w.sp[k] = a.sp[s + k * ns];
+        for (int k = lane; k < NSA; k += 32) w.sacc[k] = a.sacc[s + k * ns];
+        for (int k = lane; k < NISA; k += 32) w.isacc[k] = a.isacc[s + k * ns];
+        for (int k = lane; k < NC; k += 32) w.cstr[k] = a.cstr[s + k * ns];
+#pragma unroll
+        for (int j = 0; j < UPL; j++) {
+            if (!has(lane, j)) continue;
+            const long long g = s * UPS + unit_of(lane, j);
+#pragma unroll
+            for (int d = 0; d < UD; d++) u.x[j][d] = a.x[g + d * nu];
+#pragma unroll
+            for (int k = 0; k < NUP; k++) u.up[j][k] = a.up[g + k * nu];
+#pragma unroll
+            for (int k = 0; k < NUA; k++) u.uacc[j][k] = a.uacc[g + k * nu];
+#pragma unroll
+            for (int k = 0; k < NIUA; k++) u.iuacc[j][k] = a.iuacc[g + k * nu];
+        }
+        __syncwarp();
+
+        P* gpm = const_cast<P*>(gp);
+        int* igpm = const_cast<int*>(igp);
+#pragma unroll
+        for (int j = 0; j < UPL; j++)
+            if (has(lane, j))
+                CoupledSystems_PerBlock_Initialization<P>(sid, unit_of(lane, j), w.didx, w.t, w.dt, w.td, u.x[j],
+                                                          u.up[j], w.sp, gpm, igpm, u.uacc[j], u.iuacc[j], w.sacc,
+                                                          w.isacc);
+        __syncwarp();
+        if (NE > 0) {
+#pragma unroll
+            for (int j = 0; j < UPL; j++)
+                if (has(lane, j))
+                    CoupledSystems_PerBlock_EventFunction<P>(sid, unit_of(lane, j), u.ga[j], w.t, w.dt, w.td, u.x[j],
+                                                             u.up[j], w.sp, gpm, igpm, u.uacc[j], u.iuacc[j], w.sacc,
+                                                             w.isacc);
+            __syncwarp();
+        }
+        if (o.ndo > 0) dense_store(s, lane, w, u, a, 1, 1);
+
+        int status = 0, nacc = 0, nrej = 0, terminate = 0;
+        long long attempts = 0;
+        while (!terminate) {
+            if (attempts >= o.max_attempts) {
+                status |= MPGOS_INSTANCE_ATTEMPT_LIMIT;
+                break;
+            }
+            attempts++;
+            // ---- time stepping (CoupledSystmes_PerBlock_Solver.cuh:1839-1858)
+            int update = 1, finite = 1, end_reached = 0;
+            P dt = w.newdt;
+            const P t = w.t;
+            if (dt > (w.td[1] - t)) {
+                dt = w.td[1] - t;
+                end_reached = 1;
+            }
+            __syncwarp();
+            if (lane == 0) w.dt = dt;
+            __syncwarp();
+
+            // ---- stepper
+            P xn[UPL][UD], err[UPL][UD];
+            if (ALG == MPGOS_RK4) {
+                step_rk4(s, lane, w, u, gp, igp, M, cidx, t, dt, xn, finite);
+            } else {
+                step_rkck45(s, lane, w, u, gp, igp, M, cidx, t, dt, xn, err, finite);
+            }
+            finite = warp_all(finite != 0) ? 1 : 0;
+
+            // ---- controller (..._ErrorControllers.cuh:320-423 for RKCK45, safety factor 0.8)
+            P newdt;
+            if (ALG == MPGOS_RK4) {
+                // ..._ErrorControllers.cuh:286-316: a non-finite step stops
+                // the system without being accepted
+                if (finite == 0) {
+                    terminate = 1;
+                    update = 0;
+                    status |= MPGOS_INSTANCE_NONFINITE;
+                }
+                newdt = o.initial_dt;
+            } else {
+                P ratio = 1e30;
+                int lane_update = 1;
+#pragma unroll
+                for (int j = 0; j < UPL; j++) {
+                    if (!has(lane, j)) continue;
+                    for (int d = 0; d < UD; d++) {
+                        const P tol = fmax(rtol[d] * fmax(fabs(xn[j][d]), fabs(u.x[j][d])), atol[d]);
+                        lane_update = lane_update & (err[j][d] < tol);
+                        ratio = fmin(ratio, tol / err[j][d]);
+                    }
+                }
+                update = warp_all(lane_update != 0) ? 1 : 0;
+                ratio = warp_min(ratio);
+                P q = (update == 1) ? static_cast<P>(0.8) * pow(ratio, static_cast<P>(1.0 / 5.0))
+                                    : static_cast<P>(0.8) * pow(ratio, static_cast<P>(1.0 / 4.0));
+                if (isfinite(q) == 0) finite = 0;
+                if (finite == 0) {
+                    q = o.shrink;
+                    update = 0;
+                    if (dt < o.min_dt_guard) {
+                        terminate = 1;
+                        status |= MPGOS_INSTANCE_NONFINITE;
+                    }
+                } else if (dt < o.min_dt_guard) {
+                    update = 1;
+                    status |= MPGOS_INSTANCE_MINIMUM_STEP;
+                }
+                q = fmin(q, o.grow);
+                q = fmax(q, o.shrink);
+                newdt = dt * q;
+                newdt = fmin(newdt, o.max_dt);
+                newdt = fmax(newdt, o.min_dt);
+            }
+            if (lane == 0) w.newdt = newdt;
+            __syncwarp();
+
+            // ---- events (CoupledSystems_PerBlock_EventHandling.cuh:149-214)
+            P gn[UPL][AtLeastOne<NE>::value];
+            if (NE > 0) {
+#pragma unroll
+                for (int j = 0; j < UPL; j++)
+                    if (has(lane, j))
+                        CoupledSystems_PerBlock_EventFunction<P>(sid, unit_of(lane, j), gn[j], t + dt, w.newdt, w.td,
+                                                                 xn[j], u.up[j], w.sp, gpm, igpm, u.uacc[j],
+                                                                 u.iuacc[j], w.sacc, w.isacc);
+                __syncwarp();
+                P evdt = dt;
+                int corrected = 0;
+                if (update == 1 && terminate == 0) {
+#pragma unroll
+                    for (int j = 0; j < UPL; j++) {
+                        if (!has(lane, j)) continue;
+                        for (int e = 0; e < NE; e++) {
+                            if (((u.ga[j][e] > etol[e]) && (gn[j][e] < -etol[e]) && (edir[e] <= 0)) ||
+                                ((u.ga[j][e] < -etol[e]) && (gn[j][e] > etol[e]) && (edir[e] >= 0))) {
+                                evdt = fmin(evdt, -u.ga[j][e] / (gn[j][e] - u.ga[j][e]) * dt);
+                                corrected = 1;
+                            }
+                        }
+                    }
+                }
+                corrected = warp_any(corrected != 0) ? 1 : 0;
+                evdt = warp_min(evdt);
+                if (corrected == 1) {
+                    if (evdt < o.min_dt) {
+                        status |= MPGOS_INSTANCE_EVENT_OMITTED;
+                    } else {
+                        newdt = evdt;
+                        update = 0;
+                        if (lane == 0) w.newdt = newdt;
+                    }
+                }
+                __syncwarp();
+            }
+
+            // ---- accept (CoupledSystmes_PerBlock_Solver.cuh:1975-2075)
+            if (update == 1) {
+                nacc++;
+                if (lane == 0) w.t += dt;
+#pragma unroll
+                for (int j = 0; j < UPL; j++)
+#pragma unroll
+                    for (int d = 0; d < UD; d++) u.x[j][d] = xn[j][d];
+                __syncwarp();
+#pragma unroll
+                for (int j = 0; j < UPL; j++)
+                    if (has(lane, j))
+                        CoupledSystems_PerBlock_ActionAfterSuccessfulTimeStep<P>(
+                            sid, unit_of(lane, j), w.udt, w.t, w.dt, w.td, u.x[j], u.up[j], w.sp, gpm, igpm,
+                            u.uacc[j], u.iuacc[j], w.sacc, w.isacc);
+                __syncwarp();
+                if (NE > 0) {
+#pragma unroll
+                    for (int j = 0; j < UPL; j++) {
+                        if (!has(lane, j)) continue;
+                        for (int e = 0; e < NE; e++) {
+                            if (pt::event_detected<P>(u.ga[j][e], gn[j][e], etol[e], edir[e]))
+                                CoupledSystems_PerBlock_ActionAfterEventDetection<P>(
+                                    sid, unit_of(lane, j), e, w.udt, w.t, w.dt, w.td, u.x[j], u.up[j], w.sp, gpm,
+                                    igpm, u.uacc[j], u.iuacc[j], w.sacc, w.isacc);
+                        }
+                    }
+                    __syncwarp();
+#pragma unroll
+                    for (int j = 0; j < UPL; j++)
+                        if (has(lane, j))
+                            CoupledSystems_PerBlock_EventFunction<P>(sid, unit_of(lane, j), gn[j], w.t, w.newdt,
+                                                                     w.td, u.x[j], u.up[j], w.sp, gpm, igpm,
+                                                                     u.uacc[j], u.iuacc[j], w.sacc, w.isacc);
+                    __syncwarp();
+#pragma unroll
+                    for (int j = 0; j < UPL; j++)
+#pragma unroll
+                        for (int e = 0; e < NE; e++) u.ga[j][e] = gn[j][e];
+                }
+            } else {
+                nrej++;
+            }
+            if (o.ndo > 0) dense_store(s, lane, w, u, a, update, 0, end_reached);
+            __syncwarp();
+            if (update == 1 && ((end_reached == 1) || (w.udt == 1))) terminate = 1;
+            __syncwarp();
+        }
+
+        // ---- finalisation and write back (CoupledSystmes_PerBlock_Solver.cuh:2128-2210)
+#pragma unroll
+        for (int j = 0; j < UPL; j++)
+            if (has(lane, j))
+                CoupledSystems_PerBlock_Finalization<P>(sid, unit_of(lane, j), w.didx, w.t, w.dt, w.td, u.x[j],
+                                                        u.up[j], w.sp, gpm, igpm, u.uacc[j], u.iuacc[j], w.sacc,
+                                                        w.isacc);
+        __syncwarp();
+#pragma unroll
+        for (int j = 0; j < UPL; j++) {
+            if (!has(lane, j)) continue;
+            const long long g = s * UPS + unit_of(lane, j);
+#pragma unroll
+            for (int d = 0; d < UD; d++) a.x[g + d * nu] = u.x[j][d];
+#pragma unroll
+            for (int k = 0; k < NUA; k++) a.uacc[g + k * nu] = u.uacc[j][k];
+#pragma unroll
+            for (int k = 0; k < NIUA; k++) a.iuacc[g + k * nu] = u.iuacc[j][k];
+        }
+        if (lane == 0) {
+            a.t[s] = w.t;
+            a.td[s] = w.td[0];
+            a.td[s + ns] = w.td[1];
+            a.didx[s] = w.didx;
+            if (a.status) a.status[s] = status;
+            if (a.n_acc) a.n_acc[s] = nacc;
+            if (a.n_rej) a.n_rej[s] = nrej;
+        }
+        for (int k = lane; k < NSA; k += 32) a.sacc[s + k * ns] = w.sacc[k];
+        for (int k = lane; k < NISA; k += 32) a.isacc[s + k * ns] = w.isacc[k];
+        __syncwarp();
+    }
+
+    // Dense output of one system (CoupledSystems_PerBlock_DenseOutput.cuh:210-312).
+    // initial = 1: the unconditional store before the loop.
+    __device__ static void dense_store(long long s, int lane, Slot& w, const Units& u, const Args<P>& a, int update,
+                                       int initial, int end_reached = 0)
+    {
+        const Options<P>& o = a.o;
+        int store;
+        if (initial) {
+            store = 1;
+        } else if (update == 1) {
+            store = ((w.didx < o.ndo) && (w.dense_next < w.t) && (w.skipped >= (o.dense_freq - 1))) ? 1 : 0;
+            if ((w.didx < o.ndo) && ((end_reached == 1) || (w.udt == 1))) store = 1;
+        } else {
+            store = 0;
+        }
+        const long long nu = a.ns * UPS;
+        if (store == 1 && w.didx < o.ndo) {
+#pragma unroll
+            for (int j = 0; j < UPL; j++) {
+                if (!has(lane, j)) continue;
+                const long long g = s * UPS + unit_of(lane, j);
+#pragma unroll
+                for (int d = 0; d < UD; d++)
+                    a.dstate[g + d * nu + static_cast<long long>(w.didx) * nu * UD] = u.x[j][d];
+            }
+            if (lane == 0) a.dtime[s + static_cast<long long>(w.didx) * a.ns] = w.t;
+        }
+        __syncwarp();
+        if (lane == 0) {
+            if (store == 1) {
+                if (w.didx < o.ndo) w.didx++;
+                w.skipped = 0;
+                w.dense_next = fmin(w.t + o.dense_min_dt, w.td[1]);
+            }
+            if (store == 0 && update == 1) w.skipped++;
+        }
+        __syncwarp();
+    }
+};
+
+// Dynamic shared memory: [global parameters NGP][coupling matrices NC*MAT]
+// [integer global parameters NIGP], padded to 16 bytes, then one WarpSlot per
+// warp.
+template <class S, class P>
+__host__ __device__ constexpr size_t block_part_bytes(int shared_global, int shared_coupling)
+{
+    const size_t b = sizeof(P) * ((shared_global ? S::NGP : 0) + (shared_coupling ? S::NC * S::MAT : 0)) +
+                     sizeof(int) * (shared_global ? S::NIGP : 0);
+    return (b + 15) / 16 * 16;
+}
+
+template <class S, class P>
+__host__ __device__ constexpr size_t dynamic_smem_bytes(int warps, int shared_global, int shared_coupling)
+{
+    return block_part_bytes<S, P>(shared_global, shared_coupling) + static_cast<size_t>(warps) * sizeof(WarpSlot<S, P>);
+}
+
+template <class S, int ALG, class P, int MODE>
+__global__ void __launch_bounds__(MPGOS_CB_MAX_BLOCK) coupled_kernel(Args<P> a)
+{
+    using Sv = Solver<S, ALG, P, MODE>;
+    constexpr int UD = S::UD, NE = S::NE, NC = S::NC, NGP = S::NGP, NIGP = S::NIGP;
+    constexpr bool ADAPTIVE = (ALG == MPGOS_RKCK45);
+    extern __shared__ __align__(16) unsigned char mpgos_cb_smem[];
+    __shared__ P s_rtol[ADAPTIVE ? UD : 1];
+    __shared__ P s_atol[ADAPTIVE ? UD : 1];
+    __shared__ P s_etol[AtLeastOne<NE>::value];
+    __shared__ int s_edir[AtLeastOne<NE>::value];
+    __shared__ int s_cidx[AtLeastOne<NC>::value];
+
+    const int sg = a.shared_global, sc = a.shared_coupling;
+    P* dyn_gp = reinterpret_cast<P*>(mpgos_cb_smem);
+    P* dyn_m = dyn_gp + (sg ? NGP : 0);
+    int* dyn_igp = reinterpret_cast<int*>(dyn_m + (sc ? NC * S::MAT : 0));
+    using Slot = WarpSlot<S, P>;
+    Slot* slots = reinterpret_cast<Slot*>(mpgos_cb_smem + block_part_bytes<S, P>(sg, sc));
+
+    for (int k = threadIdx.x; k < UD; k += blockDim.x) {
+        if (ADAPTIVE) {
+            s_rtol[k] = a.rtol[k];
+            s_atol[k] = a.atol[k];
+        }
+    }
+    for (int k = threadIdx.x; k < NE; k += blockDim.x) {
+        s_etol[k] = a.etol[k];
+        s_edir[k] = a.edir[k];
+    }
+    for (int k = threadIdx.x; k < NC; k += blockDim.x) s_cidx[k] = a.cidx[k];
+    if (sg) {
+        for (int k = threadIdx.x; k < NGP; k += blockDim.x) dyn_gp[k] = a.gp[k];
+        for (int k = threadIdx.x; k < NIGP; k += blockDim.x) dyn_igp[k] = a.igp[k];
+    }
+    if (sc)
+        for (int k = threadIdx.x; k < NC * S::MAT; k += blockDim.x) dyn_m[k] = a.cmat[k];
+    __syncthreads();
+
+    const P* gp = sg ? dyn_gp : a.gp;
+    const int* igp = sg ? dyn_igp : a.igp;
+    const P* M = sc ? dyn_m : a.cmat;
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int warps = blockDim.x >> 5;
+    Slot& w = slots[warp];
+
+    long long s = static_cast<long long>(blockIdx.x) * warps + warp;
+    const long long total = static_cast<long long>(gridDim.x) * warps;
+    while (s < a.n_active) {
+        Sv::system(s, lane, w, a, gp, igp, M, s_cidx, s_rtol, s_atol, s_etol, s_edir);
+        if (!Sv::PERSISTENT) break;
+        unsigned next = 0;
+        if (lane == 0) next = atomicAdd(a.work, 1u);
+        next = __shfl_sync(0xffffffffu, next, 0);
+        s = total + static_cast<long long>(next);
+    }
+}
+
+// ---- launch table --------------------------------------------------------------
+template <class P>
+Args<P> make_args(const mpgos_cb_launch& L)
+{
+    Args<P> a;
+    a.ns = L.ns;
+    a.n_active = L.n_active;
+    a.td = static_cast<P*>(L.time_domain);
+    a.t = static_cast<P*>(L.actual_time);
+    a.sp = static_cast<P*>(L.system_parameters);
+    a.sacc = static_cast<P*>(L.system_accessories);
+    a.isacc = L.integer_system_accessories;
+    a.cstr = static_cast<P*>(L.coupling_strength);
+    a.didx = L.dense_index;
+    a.dtime = static_cast<P*>(L.dense_time);
+    a.x = static_cast<P*>(L.actual_state);
+    a.up = static_cast<P*>(L.unit_parameters);
+    a.uacc = static_cast<P*>(L.unit_accessories);
+    a.iuacc = L.integer_unit_accessories;
+    a.dstate = static_cast<P*>(L.dense_state);
+    a.gp = static_cast<const P*>(L.global_parameters);
+    a.igp = L.integer_global_parameters;
+    a.cmat = static_cast<const P*>(L.coupling_matrix);
+    a.cidx = L.coupling_index;
+    a.rtol = static_cast<const P*>(L.relative_tolerance);
+    a.atol = static_cast<const P*>(L.absolute_tolerance);
+    a.etol = static_cast<const P*>(L.event_tolerance);
+    a.edir = L.event_direction;
+    a.status = L.status;
+    a.n_acc = L.accepted_steps;
+    a.n_rej = L.rejected_steps;
+    a.work = L.work_counter;
+    a.shared_global = L.shared_global;
+    a.shared_coupling = L.shared_coupling;
+    a.o.initial_dt = static_cast<P>(L.initial_dt);
+    a.o.max_dt = static_cast<P>(L.max_dt);
+    a.o.min_dt = static_cast<P>(L.min_dt);
+    a.o.grow = static_cast<P>(L.grow_limit);
+    a.o.shrink = static_cast<P>(L.shrink_limit);
+    a.o.dense_min_dt = static_cast<P>(L.dense_min_dt);
+    a.o.min_dt_guard = a.o.min_dt * static_cast<P>(1.01);
+    a.o.dense_freq = L.dense_save_frequency;
+    a.o.ndo = L.ndo;
+    a.o.max_attempts = L.max_attempts;
+    return a;
+}
+
+template <class S, int ALG, class P>
+struct KernelTable {
+    static void* kernel_for(int mode)
+    {
+        return (mode & MPGOS_MODE_PERSISTENT) ? reinterpret_cast<void*>(&coupled_kernel<S, ALG, P, MPGOS_MODE_PERSISTENT>)
+                                              : reinterpret_cast<void*>(&coupled_kernel<S, ALG, P, 0>);
+    }
+    static int launch(const mpgos_cb_launch* L, int grid, int block, size_t smem, void* stream)
+    {
+        Args<P> a = make_args<P>(*L);
+        void* params[] = {&a};
+        void* fn = kernel_for(L->mode);
+        if (smem > 48 * 1024) {
+            cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+            if (e != cudaSuccess) return static_cast<int>(e);
+        }
+        return static_cast<int>(cudaLaunchKernel(fn, dim3(grid), dim3(block), params, smem,
+                                                 static_cast<cudaStream_t>(stream)));
+    }
+    static int occupancy(int32_t mode, int block, size_t smem, int* blocks)
+    {
+        void* fn = kernel_for(mode);
+        if (smem > 48 * 1024) {
+            cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+            if (e != cudaSuccess) return static_cast<int>(e);
+        }
+        return static_cast<int>(cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, fn, block, smem));
+    }
+    static size_t smem(int warps, int shared_global, int shared_coupling)
+    {
+        return dynamic_smem_bytes<S, P>(warps, shared_global, shared_coupling);
+    }
+    static const mpgos_cb_kernels* get(const char* name)
+    {
+        static mpgos_cb_kernels table = {
+            MPGOS_ABI_VERSION,
+            {S::UPS, S::UD, S::NC, S::CBW, S::CCI, S::NUP, S::NSP, S::NGP, S::NIGP, S::NUA, S::NIUA, S::NSA, S::NISA,
+             S::NE, ALG, static_cast<int32_t>(sizeof(P)), S::MAT},
+            name,
+            &launch,
+            &occupancy,
+            &smem};
+        return &table;
+    }
+};
+
+}  // namespace cb
+}  // namespace mpgos

@@ -74,6 +74,15 @@ struct GraphKey {
 
 }  // namespace
 
+// Entry for the coupled-solver runtime (runtime_coupled.cpp): same error slot.
+namespace mpgos_runtime {
+int set_error(int code, const char* msg)
+{
+    g_last_error = msg;
+    return code;
+}
+}  // namespace mpgos_runtime
+
 struct mpgos_pt_solver {
     const mpgos_pt_kernels* k = nullptr;
     mpgos_pt_shape shape{};

@@ -5,6 +5,8 @@ Outputs, all under ``massively-parallel-gpu-ode-solver_gb300/_build/``:
 * ``libmpgos_runtime.so``   host runtime implementing the C-ABI of ``include/mpgos.h``
 * ``libmpgos_<system>.so``  one system plugin per hook file in ``systems/``
   (sm_103a kernels for that system's user hooks)
+* ``libmpgos_<ring>.so``    coupled-system plugins (one warp per system),
+  one per ``systems/<ring>.cu`` in ``COUPLED``
 
 Every CUDA translation unit is compiled with
 ``-gencode arch=compute_103a,code=sm_103a`` only. Units are compiled in
@@ -30,6 +32,9 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # System plugins built by default: name -> source file (hook file + plugin export).
 SYSTEMS = ["lorenz", "duffing", "duffing_param", "duffing_param_sens", "duffing_events", "bouncing_ball",
            "keller_miksis"]
+# Coupled-system plugins: the ring of Duffing oscillators with 64 units and,
+# at 16 units, each of the four coupling-matrix storages.
+COUPLED = ["ring64", "ring16_full", "ring16_band", "ring16_circband", "ring16_circ"]
 
 
 def nvcc_path() -> str:
@@ -67,7 +72,7 @@ def _common_flags() -> list:
     return [
         "-O3", "-std=c++17", "-lineinfo", "-shared", "-Xcompiler", "-fPIC",
         "-Xcompiler", "-fvisibility=hidden", "-cudart", "shared",
-        f"-I{INCLUDE_DIR}", f"-I{CSRC / 'perthread'}", f"-I{SYSTEMS_DIR}",
+        f"-I{INCLUDE_DIR}", f"-I{CSRC / 'perthread'}", f"-I{CSRC / 'coupled'}", f"-I{SYSTEMS_DIR}",
         "-Xlinker", f"-rpath,{lib}", "-Xlinker", "-rpath,$ORIGIN",
     ]
 
@@ -82,12 +87,11 @@ def system_lib(name: str) -> Path:
 
 def build_runtime(force: bool = False) -> Path:
     out = runtime_lib()
-    src = CSRC / "runtime" / "runtime.cpp"
-    probes = CSRC / "runtime" / "probes.cu"
-    deps = [src, probes, INCLUDE_DIR / "mpgos.h"]
+    srcs = [CSRC / "runtime" / "runtime.cpp", CSRC / "runtime" / "runtime_coupled.cpp", CSRC / "runtime" / "probes.cu"]
+    deps = [*srcs, INCLUDE_DIR / "mpgos.h"]
     if not force and _newer(out, deps):
         return out
-    cmd = [nvcc_path(), *ARCH, *_common_flags(), "-x", "cu", str(src), str(probes), "-o", str(out)]
+    cmd = [nvcc_path(), *ARCH, *_common_flags(), "-x", "cu", *map(str, srcs), "-o", str(out)]
     _run(cmd, "libmpgos_runtime.so")
     return out
 
@@ -95,7 +99,8 @@ def build_runtime(force: bool = False) -> Path:
 def build_system(name: str, force: bool = False, extra: list | None = None) -> Path:
     out = system_lib(name)
     src = SYSTEMS_DIR / f"{name}.cu"
-    deps = [src, SYSTEMS_DIR / f"{name}.cuh", INCLUDE_DIR / "mpgos.h", *_deps_glob(CSRC / "perthread")]
+    deps = [src, INCLUDE_DIR / "mpgos.h", *_deps_glob(CSRC / "perthread", CSRC / "coupled"),
+            *SYSTEMS_DIR.glob("*.cuh")]
     if not force and _newer(out, deps):
         return out
     cmd = [nvcc_path(), *ARCH, *_common_flags(), *(extra or []), str(src), "-o", str(out)]
@@ -106,7 +111,7 @@ def build_system(name: str, force: bool = False, extra: list | None = None) -> P
 def build_all(force: bool = False, systems=None, jobs: int | None = None) -> dict:
     """Build the runtime and every system plugin; returns {name: path}."""
     BUILD_DIR.mkdir(parents=True, exist_ok=True)
-    systems = list(systems or SYSTEMS)
+    systems = list(systems or (SYSTEMS + COUPLED))
     jobs = jobs or max(1, min(len(systems) + 1, os.cpu_count() or 4))
     results = {}
     with cf.ThreadPoolExecutor(max_workers=jobs) as ex:

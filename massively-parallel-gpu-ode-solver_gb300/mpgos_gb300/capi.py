@@ -81,6 +81,69 @@ INSTANCE_TAPE_OVERFLOW = 16
 ABI_VERSION = 1
 
 
+# Coupled per-block solver (CoupledSystems_PerBlock_Interface.cuh:33-66).
+class CbVariable(IntEnum):
+    All = 0
+    TimeDomain = 1
+    ActualTime = 2
+    ActualState = 3
+    UnitParameters = 4
+    SystemParameters = 5
+    GlobalParameters = 6
+    IntegerGlobalParameters = 7
+    UnitAccessories = 8
+    IntegerUnitAccessories = 9
+    SystemAccessories = 10
+    IntegerSystemAccessories = 11
+    CouplingMatrix = 12
+    CouplingStrength = 13
+    CouplingIndex = 14
+    DenseOutput = 15
+    DenseIndex = 16
+    DenseTime = 17
+    DenseState = 18
+    Status = 32
+    AcceptedSteps = 33
+    RejectedSteps = 34
+
+
+class CbOption(IntEnum):
+    InitialTimeStep = 0
+    ActiveSystems = 1
+    MaximumTimeStep = 2
+    MinimumTimeStep = 3
+    TimeStepGrowLimit = 4
+    TimeStepShrinkLimit = 5
+    RelativeTolerance = 6
+    AbsoluteTolerance = 7
+    EventTolerance = 8
+    EventDirection = 9
+    DenseOutputSaveFrequency = 10
+    DenseOutputMinimumTimeStep = 11
+    SharedGlobalVariables = 12
+    SharedCouplingMatrices = 13
+    KernelMode = 32
+    MaximumAttempts = 33
+    WarpsPerBlock = 34
+
+
+class CbShape(C.Structure):
+    _fields_ = [(n, C.c_int32) for n in
+                ("ups", "ud", "nc", "cbw", "cci", "nup", "nsp", "ngp", "nigp", "nua", "niua", "nsa", "nisa", "ne",
+                 "algorithm", "precision_bytes", "matrix_entries")]
+
+
+class CbKernelTable(C.Structure):
+    _fields_ = [
+        ("abi_version", C.c_int32),
+        ("shape", CbShape),
+        ("name", C.c_char_p),
+        ("launch", C.c_void_p),
+        ("occupancy", C.c_void_p),
+        ("dynamic_smem", C.c_void_p),
+    ]
+
+
 class Shape(C.Structure):
     _fields_ = [(n, C.c_int32) for n in
                 ("sd", "ncp", "nsp", "nisp", "ne", "na", "nia", "algorithm", "precision_bytes", "modes")]
@@ -138,6 +201,22 @@ def _declare(lib):
         "mpgos_pt_solve_record": (C.c_int, [P, i32, i32]),
         "mpgos_pt_adjoint": (C.c_int, [P, P, P, P]),
         "mpgos_pt_tape_info": (C.c_int, [P, C.POINTER(Tape)]),
+        "mpgos_cb_create": (C.c_int, [P, i64, i32, C.c_int, C.POINTER(P)]),
+        "mpgos_cb_destroy": (C.c_int, [P]),
+        "mpgos_cb_get_shape": (C.c_int, [P, C.POINTER(CbShape), C.POINTER(i64), C.POINTER(i32)]),
+        "mpgos_cb_set_option": (C.c_int, [P, i32, i32, C.c_double]),
+        "mpgos_cb_host_buffer": (C.c_int, [P, i32, C.POINTER(P), C.POINTER(i64)]),
+        "mpgos_cb_device_buffer": (C.c_int, [P, i32, C.POINTER(P), C.POINTER(i64)]),
+        "mpgos_cb_sync_h2d": (C.c_int, [P, i32]),
+        "mpgos_cb_sync_d2h": (C.c_int, [P, i32]),
+        "mpgos_cb_solve": (C.c_int, [P]),
+        "mpgos_cb_insert_sync_point": (C.c_int, [P]),
+        "mpgos_cb_sync_solver": (C.c_int, [P]),
+        "mpgos_cb_timer_start": (C.c_int, [P]),
+        "mpgos_cb_timer_stop": (C.c_int, [P, C.POINTER(C.c_float)]),
+        "mpgos_cb_stream": (C.c_int, [P, C.POINTER(P)]),
+        "mpgos_cb_checkpoint_save": (C.c_int, [P]),
+        "mpgos_cb_checkpoint_restore": (C.c_int, [P]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(lib, name)
@@ -155,8 +234,14 @@ RUNTIME_SYMBOLS = (
     "mpgos_pt_launch_config", "mpgos_pt_timer_start", "mpgos_pt_timer_stop", "mpgos_pt_autotune",
     "mpgos_pt_checkpoint_save", "mpgos_pt_checkpoint_restore", "mpgos_probe_fma_peak",
     "mpgos_pt_solve_record", "mpgos_pt_adjoint", "mpgos_pt_tape_info",
+    "mpgos_cb_create", "mpgos_cb_destroy", "mpgos_cb_get_shape", "mpgos_cb_set_option", "mpgos_cb_host_buffer",
+    "mpgos_cb_device_buffer", "mpgos_cb_sync_h2d", "mpgos_cb_sync_d2h", "mpgos_cb_solve",
+    "mpgos_cb_insert_sync_point", "mpgos_cb_sync_solver", "mpgos_cb_timer_start", "mpgos_cb_timer_stop",
+    "mpgos_cb_stream", "mpgos_cb_checkpoint_save", "mpgos_cb_checkpoint_restore",
 )
-PLUGIN_SYMBOLS = ("mpgos_pt_system_kernels",)
+# mpgos_pt_system_kernels: per-thread system plugins; mpgos_cb_system_kernels:
+# coupled-system plugins.
+PLUGIN_SYMBOLS = ("mpgos_pt_system_kernels", "mpgos_cb_system_kernels")
 
 
 def runtime():
@@ -174,21 +259,42 @@ def runtime():
 
 
 def plugin(name: str):
-    """Load (once) the system plugin libmpgos_<name>.so."""
+    """Load (once) the system plugin libmpgos_<name>.so (per-thread or
+    coupled: whichever of the two entry points it exports is declared)."""
     if name not in _plugins:
         path = _build.system_lib(name)
         if not path.exists():
             raise FileNotFoundError(f"{path} is missing: run __graft_entry__.build()")
         lib = C.CDLL(str(path))
-        fn = lib.mpgos_pt_system_kernels
-        fn.restype = C.c_void_p
-        fn.argtypes = [C.c_int32, C.c_int32]
+        for sym in PLUGIN_SYMBOLS:
+            if hasattr(lib, sym):
+                fn = getattr(lib, sym)
+                fn.restype = C.c_void_p
+                fn.argtypes = [C.c_int32, C.c_int32]
         _plugins[name] = lib
     return _plugins[name]
 
 
+def coupled_kernel_table(system: str, algorithm: int, precision_bytes: int) -> int:
+    lib = plugin(system)
+    if not hasattr(lib, "mpgos_cb_system_kernels"):
+        raise MpgosError(5, f"{system!r} is not a coupled-system plugin")
+    ptr = lib.mpgos_cb_system_kernels(int(algorithm), int(precision_bytes))
+    if not ptr:
+        raise MpgosError(5, f"coupled system {system!r} has no kernels for algorithm {algorithm}, "
+                            f"{precision_bytes}-byte precision")
+    return ptr
+
+
+def coupled_kernel_table_info(ptr: int) -> CbKernelTable:
+    return CbKernelTable.from_address(ptr)
+
+
 def kernel_table(system: str, algorithm: int, precision_bytes: int) -> int:
-    ptr = plugin(system).mpgos_pt_system_kernels(int(algorithm), int(precision_bytes))
+    lib = plugin(system)
+    if not hasattr(lib, "mpgos_pt_system_kernels"):
+        raise MpgosError(5, f"{system!r} is not a per-thread system plugin")
+    ptr = lib.mpgos_pt_system_kernels(int(algorithm), int(precision_bytes))
     if not ptr:
         raise MpgosError(5, f"system {system!r} has no kernels for algorithm {algorithm}, {precision_bytes}-byte precision")
     return ptr

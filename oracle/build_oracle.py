@@ -9,6 +9,12 @@ TEST INFRASTRUCTURE ONLY.
   reference's own per-thread kernel built for sm_103a (ref_gpu_entry.cu),
   device code only; built where the reference checkout exists and shipped to
   the GPU machine with the working tree.
+* ``oracle/_build/liboracle_cb_<system>.so`` - the coupled-solver oracle
+  (oracle_coupled.cpp) compiled once per coupled-system plugin source
+  ``systems/<system>.cu`` (its hook file and coupling storage).
+* ``oracle/_ref/ref_gpu_cb_<system>_<alg>_ns<NS>_tpb<TPB>_spb<SPB>_ndo<NDO>.cubin``
+  - the reference's own coupled kernel (MultipleSystems_SingleBlockLaunch)
+  built for sm_103a (ref_gpu_coupled_entry.cu).
 * ``oracle/_ref/libref_cpu_<system>.so`` - the reference's own
   SourceCodes/SingleSystem_PerThread_Solver.cuh compiled for the CPU through
   ref_cpu_entry.cpp, straight from the reference checkout (MPGOS_REFERENCE_ROOT,
@@ -35,6 +41,78 @@ REFERENCE_ROOT = Path(os.environ.get("MPGOS_REFERENCE_ROOT", "/root/reference"))
 SYSTEMS = ["lorenz", "duffing", "duffing_param", "duffing_param_sens", "duffing_events", "bouncing_ball",
            "keller_miksis"]
 FLAGS = ["-O3", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math"]
+# Coupled-system plugins (the product's build list): the oracle and the
+# reference cubins read hook file, UPS, CBW and CCI from systems/<name>.cu.
+COUPLED = ["ring64", "ring16_full", "ring16_band", "ring16_circband", "ring16_circ"]
+
+
+def coupled_defs(system: str) -> dict:
+    """{"header": hook file, "UPS": .., "CBW": .., "CCI": ..} of a coupled plugin."""
+    import re
+    text = (SYSTEMS_DIR / f"{system}.cu").read_text()
+    out = {"header": re.search(r'#include\s+"([^"/]+\.cuh)"', text).group(1)}
+    for k in ("UPS", "CBW", "CCI"):
+        out[k] = int(re.search(rf"#define\s+MPGOS_SYS_{k}\s+(\d+)", text).group(1))
+    return out
+
+
+def _coupled_macros(system: str) -> list:
+    d = coupled_defs(system)
+    return [f'-DMPGOS_SYSTEM_HEADER="{d["header"]}"', f"-DMPGOS_SYS_UPS={d['UPS']}", f"-DMPGOS_SYS_CBW={d['CBW']}",
+            f"-DMPGOS_SYS_CCI={d['CCI']}"]
+
+
+def oracle_cb_lib(system: str) -> Path:
+    return BUILD_DIR / f"liboracle_cb_{system}.so"
+
+
+def build_oracle_coupled(system: str, force: bool = False) -> Path:
+    out = oracle_cb_lib(system)
+    src = ORACLE_DIR / "oracle_coupled.cpp"
+    d = coupled_defs(system)
+    deps = [src, SYSTEMS_DIR / d["header"], SYSTEMS_DIR / f"{system}.cu", ORACLE_DIR / "host_shim.hpp", Path(__file__)]
+    if not force and _newer(out, deps):
+        return out
+    cmd = ["g++", *FLAGS, "-fopenmp", f"-I{ORACLE_DIR}", f"-I{SYSTEMS_DIR}", *_coupled_macros(system), str(src),
+           "-o", str(out)]
+    _run(cmd, out.name)
+    return out
+
+
+# Reference coupled kernels built as cubins: (system, algorithm, NS, TPB, SPB,
+# NDO), all with SPB * UPS == TPB and NS a multiple of SPB, so that the
+# reference's unit layout has no thread padding and coincides with the GB300
+# layout. The 16384-system ring64 cubins serve the full-size parity test and
+# the reference-kernel timing (two launch shapes: 2 and 4 systems per block).
+REF_GPU_CB_KERNELS = [
+    ("ring16_full", 1, 256, 64, 4, 0), ("ring16_band", 1, 256, 64, 4, 0), ("ring16_circband", 1, 256, 64, 4, 0),
+    ("ring16_circ", 1, 256, 64, 4, 0), ("ring16_full", 0, 256, 64, 4, 0), ("ring16_full", 1, 256, 64, 4, 8),
+    ("ring64", 1, 512, 128, 2, 0), ("ring64", 1, 16384, 128, 2, 0), ("ring64", 1, 16384, 256, 4, 0),
+]
+
+
+def ref_cb_cubin(system: str, algorithm: int, ns: int, tpb: int, spb: int, ndo: int) -> Path:
+    alg = "rkck45" if algorithm else "rk4"
+    return REF_DIR / f"ref_gpu_cb_{system}_{alg}_ns{ns}_tpb{tpb}_spb{spb}_ndo{ndo}.cubin"
+
+
+def build_ref_gpu_coupled(system: str, algorithm: int, ns: int, tpb: int, spb: int, ndo: int,
+                          force: bool = False) -> Path | None:
+    if not (REFERENCE_ROOT / "SourceCodes" / "CoupledSystmes_PerBlock_Solver.cuh").exists():
+        return None
+    out = ref_cb_cubin(system, algorithm, ns, tpb, spb, ndo)
+    src = ORACLE_DIR / "ref_gpu_coupled_entry.cu"
+    d = coupled_defs(system)
+    deps = [src, SYSTEMS_DIR / d["header"], SYSTEMS_DIR / f"{system}.cu", ORACLE_DIR / "ref_types_coupled.hpp",
+            Path(__file__)]
+    if not force and _newer(out, deps):
+        return out
+    cmd = ["nvcc", "-cubin", "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17", "-lineinfo", "-w",
+           f"-I{ORACLE_DIR}", f"-I{SYSTEMS_DIR}", f"-I{REFERENCE_ROOT / 'SourceCodes'}", *_coupled_macros(system),
+           f"-DREF_NS={ns}", f"-DREF_TPB={tpb}", f"-DREF_SPB={spb}", f"-DREF_NDO={ndo}",
+           f"-DREF_ALG={'RKCK45' if algorithm else 'RK4'}", str(src), "-o", str(out)]
+    _run(cmd, out.name)
+    return out
 
 
 def oracle_lib(system: str) -> Path:
@@ -139,6 +217,10 @@ def build_all(force: bool = False) -> dict:
         for s in SYSTEMS:
             futs[ex.submit(build_oracle, s, force)] = ("oracle", s)
             futs[ex.submit(build_ref, s, force)] = ("ref", s)
+        for s in COUPLED:
+            futs[ex.submit(build_oracle_coupled, s, force)] = ("oracle_cb", s)
+        for k in REF_GPU_CB_KERNELS:
+            futs[ex.submit(build_ref_gpu_coupled, *k, force)] = ("ref_gpu_cb", *k)
         for (s, alg, nt, ndo) in REF_GPU_KERNELS:
             futs[ex.submit(build_ref_gpu, s, alg, nt, ndo, None, force)] = ("ref_gpu", s, alg, nt, ndo)
             if s in REF_GPU_RREG:

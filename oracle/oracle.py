@@ -153,3 +153,79 @@ def run_ref_cpu(case) -> dict:
             raise RuntimeError(f"ref_cpu_solve: (nt={nt}, ndo={case.ndo}) not compiled")
     z = np.zeros(nt, np.int32)
     return _results(case, a, z, z.copy(), z.copy())
+
+
+# ---- coupled per-block solver -------------------------------------------------
+class _CbArrays(C.Structure):
+    _fields_ = [("ns", C.c_longlong)] + [(n, C.c_void_p) for n in (
+        "td", "t", "sp", "sacc", "cstr", "dtime", "x", "up", "uacc", "dstate", "isacc", "didx", "iuacc", "gp", "cmat",
+        "rtol", "atol", "etol", "igp", "cidx", "edir", "status", "nacc", "nrej")]
+
+
+class _CbOpts(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("initial_dt", "max_dt", "min_dt", "grow", "shrink", "dense_min_dt")] + [
+        ("dense_freq", C.c_int), ("ndo", C.c_int), ("max_attempts", C.c_longlong)]
+
+
+_cb_libs: dict = {}
+
+
+def _oracle_cb(system: str):
+    if system not in _cb_libs:
+        lib = C.CDLL(str(_b.build_oracle_coupled(system)))
+        lib.oracle_cb_solve.restype = C.c_int
+        lib.oracle_cb_solve.argtypes = [C.POINTER(_CbArrays), C.POINTER(_CbOpts), C.c_int, C.c_longlong, C.c_longlong,
+                                        C.c_int]
+        lib.oracle_cb_shape.restype = None
+        lib.oracle_cb_shape.argtypes = [C.POINTER(C.c_int)]
+        _cb_libs[system] = lib
+    return _cb_libs[system]
+
+
+def oracle_cb_shape(system: str) -> tuple:
+    """(UPS, UD, NC, CBW, CCI, NUP, NSP, NGP, NIGP, NUA, NIUA, NSA, NISA, NE, MAT)."""
+    out = (C.c_int * 15)()
+    _oracle_cb(system).oracle_cb_shape(out)
+    return tuple(out)
+
+
+def run_oracle_coupled(case, threads: int = 0, first: int = 0, count: int | None = None) -> dict:
+    """Integrate a ``coupled_workloads.CbCase`` (all phases) with the coupled
+    oracle; systems [first, first + count) only when given (the others keep
+    their inputs). Returns the dictionary of ``run_coupled_gpu``."""
+    lib = _oracle_cb(case.system)
+    a = case.arrays
+    f64 = lambda v: np.ascontiguousarray(np.array(v, dtype=np.float64, copy=True))
+    i32 = lambda v: np.ascontiguousarray(np.array(v, dtype=np.int32, copy=True))
+    ns = case.ns
+    st = dict(td=f64(a["td"]), t=f64(a["t"]), sp=f64(a["sp"]), sacc=f64(a["sacc"]), cstr=f64(a["cstr"]),
+              dtime=f64(a["dtime"]), x=f64(a["x"]), up=f64(a["up"]), uacc=f64(a["uacc"]), dstate=f64(a["dstate"]),
+              isacc=i32(a["isacc"]), didx=i32(a["didx"]), iuacc=i32(a["iuacc"]), gp=f64(a["gp"]),
+              cmat=f64(case.stored_matrix()), rtol=f64(case.rtol), atol=f64(case.atol), etol=f64(case.etol),
+              igp=i32(a["igp"]), cidx=i32(a["cidx"]), edir=i32(case.edir), status=np.zeros(ns, np.int32),
+              nacc=np.zeros(ns, np.int32), nrej=np.zeros(ns, np.int32))
+    pad = {k: (v if v.size else np.zeros(2, v.dtype)) for k, v in st.items()}
+    arr = _CbArrays(ns, *[pad[n].ctypes.data for n, _ in _CbArrays._fields_[1:]])
+    o = case.options
+    opts = _CbOpts(o["initial_dt"], o["max_dt"], o["min_dt"], o["grow"], o["shrink"], o["dense_min_dt"],
+                   int(o["dense_freq"]), int(case.ndo), int(o["max_attempts"]))
+    n_active = case.n_active if case.n_active is not None else ns
+    count = n_active - first if count is None else count
+    for _ in range(case.phases):
+        rc = lib.oracle_cb_solve(C.byref(arr), C.byref(opts), int(case.algorithm), int(first), int(count), int(threads))
+        if rc != 0:
+            raise RuntimeError(f"oracle_cb_solve failed with {rc}")
+    out = {k: st[k] for k in ("td", "t", "x", "didx", "status", "nacc", "nrej", "iuacc", "uacc", "isacc", "sacc")}
+    if case.ndo:
+        out["dtime"], out["dstate"] = st["dtime"], st["dstate"]
+    return out
+
+
+def time_oracle_coupled(case, threads: int = 0, count: int | None = None) -> tuple:
+    """Wall time of the coupled oracle on the first ``count`` systems; returns
+    (seconds, accepted system-steps)."""
+    t0 = time.perf_counter()
+    r = run_oracle_coupled(case, threads=threads, first=0, count=count)
+    dt = time.perf_counter() - t0
+    n = case.ns if count is None else count
+    return dt, int(r["nacc"][:n].sum())

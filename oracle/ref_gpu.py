@@ -196,3 +196,111 @@ def device_to_host(ptr: int, shape, dtype) -> np.ndarray:
     if out.nbytes:
         _ck(_driver().cuMemcpyDtoH_v2(out.ctypes.data, int(ptr), out.nbytes), "cuMemcpyDtoH")
     return out
+
+
+# ---- coupled per-block solver -----------------------------------------------------
+class CbThreadConfiguration(C.Structure):
+    _fields_ = [(n, C.c_int) for n in ("LogicalThreadsPerBlock", "NumberOfBlockLaunches", "ThreadPaddingPerBlock",
+                                       "BlockSize", "GridSize", "TotalLogicalThreads")]
+
+
+class CbGlobalVariables(C.Structure):
+    _fields_ = [(n, C.c_void_p) for n in (
+        "d_TimeDomain", "d_ActualState", "d_ActualTime", "d_UnitParameters", "d_SystemParameters",
+        "d_GlobalParameters", "d_IntegerGlobalParameters", "d_UnitAccessories", "d_IntegerUnitAccessories",
+        "d_SystemAccessories", "d_IntegerSystemAccessories", "d_CouplingMatrix", "d_CouplingStrength",
+        "d_CouplingIndex", "d_DenseOutputIndex", "d_DenseOutputTimeInstances", "d_DenseOutputStates",
+        "d_RelativeTolerance", "d_AbsoluteTolerance", "d_EventTolerance", "d_EventDirection")]
+
+
+class CbSharedMemoryUsage(C.Structure):
+    _fields_ = [("GlobalVariables", C.c_bool), ("CouplingMatrices", C.c_bool), ("SingleCouplingMatrixSize", C.c_int),
+                ("IsAdaptive", C.c_int)]
+
+
+class CbSolverOptions(C.Structure):
+    _fields_ = [("InitialTimeStep", C.c_double), ("ActiveSystems", C.c_int), ("MaximumTimeStep", C.c_double),
+                ("MinimumTimeStep", C.c_double), ("TimeStepGrowLimit", C.c_double),
+                ("TimeStepShrinkLimit", C.c_double), ("DenseOutputSaveFrequency", C.c_int),
+                ("DenseOutputMinimumTimeStep", C.c_double)]
+
+
+def coupled_available(system: str, algorithm: int, ns: int, tpb: int, spb: int, ndo: int) -> bool:
+    return _b.ref_cb_cubin(system, algorithm, ns, tpb, spb, ndo).exists()
+
+
+class CoupledReferenceKernel(ReferenceKernel):
+    """The reference's MultipleSystems_SingleBlockLaunch coupled kernel
+    (CoupledSystmes_PerBlock_Solver.cuh:1507-2211) for one (system,
+    algorithm, NS, TPB, SPB, NDO), launched as the reference's Solve() does
+    (CoupledSystems_PerBlock_Interface.cuh:1947-1966: grid ceil(NS/SPB),
+    block TPB, dynamic shared memory for the global parameters and, when
+    shared, the coupling matrices, :540-544) on the device buffers of a GB300
+    ``CoupledProblemSolver``. SPB * TPB layouts without thread padding only,
+    where the reference's unit layout is the GB300 one."""
+
+    def __init__(self, system: str, algorithm: int, ns: int, tpb: int, spb: int, ndo: int = 0):
+        path = _b.ref_cb_cubin(system, algorithm, ns, tpb, spb, ndo)
+        if not path.exists():
+            raise FileNotFoundError(f"{path} not built (needs the reference checkout at build time)")
+        cu = _driver()
+        ctx = C.c_void_p()
+        _ck(cu.cuCtxGetCurrent(C.byref(ctx)), "cuCtxGetCurrent")
+        if not ctx.value:
+            raise RuntimeError("no current CUDA context: create a solver on the device first")
+        self.mod = C.c_void_p()
+        _ck(cu.cuModuleLoad(C.byref(self.mod), str(path).encode()), f"cuModuleLoad({path.name})")
+        n = C.c_uint()
+        _ck(cu.cuModuleGetFunctionCount(C.byref(n), self.mod), "cuModuleGetFunctionCount")
+        if n.value != 1:
+            raise RuntimeError(f"{path.name}: expected one kernel, found {n.value}")
+        funcs = (C.c_void_p * 1)()
+        _ck(cu.cuModuleEnumerateFunctions(funcs, 1, self.mod), "cuModuleEnumerateFunctions")
+        self.fn = C.c_void_p(funcs[0])
+        self.system, self.algorithm, self.ns, self.tpb, self.spb, self.ndo = system, algorithm, ns, tpb, spb, ndo
+        self._dev = []
+
+    def bind(self, solver, case, shared_global: int = 1, shared_coupling: int = 0):
+        """Prepare a launch on the buffers of ``solver`` (holding ``case``);
+        the defaults are the reference's (SharedGlobalVariables on,
+        SharedCouplingMatrices off unless circular)."""
+        from mpgos_gb300.capi import CbVariable as V
+        ups = solver.UPS
+        if solver.NS != self.ns or solver.NDO != self.ndo or self.spb * ups != self.tpb or self.ns % self.spb:
+            raise ValueError("solver shape does not match the compiled reference kernel")
+        if solver.CCI == 1:
+            shared_coupling = 1  # the reference forces it (CoupledSystems_PerBlock_Interface.cuh:524-527)
+        d = solver.device_ptr
+        self.gv = CbGlobalVariables(
+            d(V.TimeDomain), d(V.ActualState), d(V.ActualTime), d(V.UnitParameters), d(V.SystemParameters),
+            d(V.GlobalParameters), d(V.IntegerGlobalParameters), d(V.UnitAccessories), d(V.IntegerUnitAccessories),
+            d(V.SystemAccessories), d(V.IntegerSystemAccessories), d(V.CouplingMatrix), d(V.CouplingStrength),
+            d(V.CouplingIndex), d(V.DenseIndex), d(V.DenseTime), d(V.DenseState),
+            self._upload(np.asarray(case.rtol, np.float64)), self._upload(np.asarray(case.atol, np.float64)),
+            self._upload(np.asarray(case.etol, np.float64)), self._upload(np.asarray(case.edir, np.int32)))
+        grid = self.ns // self.spb
+        self.tc = CbThreadConfiguration(self.tpb, 1, 0, self.tpb, grid, self.ns * ups)
+        self.smu = CbSharedMemoryUsage(bool(shared_global), bool(shared_coupling), solver.MAT,
+                                       1 if self.algorithm == 1 else 0)
+        o = case.options
+        n_active = case.n_active if case.n_active is not None else case.ns
+        self.so = CbSolverOptions(o["initial_dt"], n_active, o["max_dt"], o["min_dt"], o["grow"], o["shrink"],
+                                  int(o["dense_freq"]), o["dense_min_dt"])
+        self.grid, self.block = grid, self.tpb
+        self.smem = shared_global * (solver.NGP * 8 + solver.NiGP * 4) + shared_coupling * solver.NC * solver.MAT * 8
+        self.stream = solver.stream()
+        self.params = (C.c_void_p * 4)(C.addressof(self.tc), C.addressof(self.gv), C.addressof(self.smu),
+                                      C.addressof(self.so))
+
+
+def run_ref_gpu_coupled(case, tpb: int, spb: int, device: int = 0, shared_coupling: int = 0) -> dict:
+    """Integrate a ``CbCase`` (all phases) with the reference coupled kernel."""
+    from mpgos_gb300 import coupled_workloads as CW
+    with CW.load_coupled_solver(case, device=device) as s:
+        s.SynchroniseDevice()
+        with CoupledReferenceKernel(case.system, case.algorithm, case.ns, tpb, spb, case.ndo) as k:
+            k.bind(s, case, shared_global=1, shared_coupling=shared_coupling)
+            for _ in range(case.phases):
+                k.launch()
+            s.SynchroniseDevice()
+        return CW.read_coupled_results(s)

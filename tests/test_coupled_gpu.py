@@ -1,0 +1,150 @@
+"""GPU parity tests of the coupled per-block solver (one warp per system).
+
+* Against the reference's own coupled kernel (MultipleSystems_SingleBlockLaunch
+  built for sm_103a, oracle/_ref cubins, launched on the same device buffers):
+  every output bit-identical, for the four coupling storages, RK4 and RKCK45,
+  dense output, and the 16384 x 64-unit ring at full ensemble size.
+* The mapping (warps per CTA, persistent work queue, coupling matrix in shared
+  or global memory) changes nothing: bit-identical.
+* Against the CPU oracle: end states within 1e-9 of the component's scale or
+  within 1e3 x the oracle's own spread under tiny perturbations; crossing
+  counts and step counts equal on the systems the perturbations leave
+  unchanged (see test_coupled_matches_oracle for the allowance).
+"""
+import numpy as np
+import pytest
+
+from tests.parity import assert_bitwise, scaled_close
+from mpgos_gb300 import capi, coupled_workloads as CW
+from oracle import oracle as O, ref_gpu as R
+
+pytestmark = pytest.mark.gpu
+
+KEYS = ["td", "t", "x", "iuacc", "isacc", "didx"]
+
+
+def _ref(case, tpb, spb):
+    if not R.coupled_available(case.system, case.algorithm, case.ns, tpb, spb, case.ndo):
+        pytest.skip("reference coupled cubin not built (oracle/build_oracle.REF_GPU_CB_KERNELS)")
+    return R.run_ref_gpu_coupled(case, tpb, spb)
+
+
+REF_CASES = [
+    ("ring16_full", dict(), 64, 4),
+    ("ring16_band", dict(), 64, 4),
+    ("ring16_circband", dict(), 64, 4),
+    ("ring16_circ", dict(), 64, 4),
+    ("ring16_full", dict(algorithm=0), 64, 4),
+    ("ring16_full", dict(ndo=8), 64, 4),
+    ("ring64", dict(), 128, 2),
+]
+
+
+@pytest.mark.parametrize("system,kw,tpb,spb", REF_CASES,
+                         ids=["full", "band", "circband", "circ", "full_rk4", "full_dense", "ring64"])
+def test_coupled_is_bitwise_identical_to_reference_kernel(system, kw, tpb, spb, native_libs):
+    ns = 512 if system == "ring64" else 256
+    case = CW.ring_case(system, ns=ns, periods=2, seed=11, **kw)
+    if case.ndo:
+        case.options["dense_min_dt"] = 0.5
+    ref = _ref(case, tpb, spb)
+    res = CW.run_coupled_gpu(case, mode=0, warps=4)
+    assert np.all(res["status"] == 0)
+    assert_bitwise(res, ref, keys=KEYS + (["dtime", "dstate"] if case.ndo else []))
+    # the persistent work queue integrates the same systems in another order
+    assert_bitwise(CW.run_coupled_gpu(case, mode=capi.MODE_PERSISTENT, warps=2), ref, keys=KEYS)
+
+
+def test_mapping_does_not_change_results(native_libs):
+    case = CW.ring_case("ring64", ns=96, periods=1, seed=12)
+    base = CW.run_coupled_gpu(case, mode=0, warps=1)
+    for warps in (2, 4, 8):
+        assert_bitwise(base, CW.run_coupled_gpu(case, mode=0, warps=warps))
+    assert_bitwise(base, CW.run_coupled_gpu(case, mode=capi.MODE_PERSISTENT, warps=4))
+    c = case.copy()
+    c.options["shared_coupling"] = 0
+    c.options["shared_global"] = 0
+    assert_bitwise(base, CW.run_coupled_gpu(c, mode=0, warps=4))
+
+
+def test_active_systems_and_phases(native_libs):
+    case = CW.ring_case("ring16_full", ns=64, periods=1, seed=13)
+    case.n_active = 40
+    res = CW.run_coupled_gpu(case, mode=capi.MODE_PERSISTENT, warps=4)
+    assert np.all(res["t"][:40] == case.arrays["td"][1, :40])
+    np.testing.assert_array_equal(res["x"][:, 40 * 16:], case.arrays["x"][:, 40 * 16:])
+    # two launches of one period each == the oracle's two phases
+    c2 = CW.ring_case("ring16_full", ns=64, periods=1, seed=13)
+    c2.phases = 2
+    two = CW.run_coupled_gpu(c2, mode=0, warps=4)
+    ora = O.run_oracle_coupled(c2)
+    assert scaled_close(two["x"], ora["x"], 1e-9).mean() > 0.9
+
+
+def _spread(case):
+    """The oracle's own sensitivity: end-state spread and the systems whose
+    integer outputs stay unchanged under four tiny perturbations (initial
+    states one ulp up and down, tolerances 1e-12 relative up and down)."""
+    base = O.run_oracle_coupled(case)
+    spread = np.zeros_like(base["x"])
+    stable = np.ones(case.ns, bool)
+    for kind, sign in (("x", np.inf), ("x", -np.inf), ("tol", 1.0), ("tol", -1.0)):
+        pert = case.copy()
+        if kind == "x":
+            pert.arrays["x"] = np.nextafter(pert.arrays["x"], sign)
+        else:
+            pert.rtol = pert.rtol * (1.0 + sign * 1e-12)
+            pert.atol = pert.atol * (1.0 + sign * 1e-12)
+        moved = O.run_oracle_coupled(pert)
+        spread = np.maximum(spread, np.abs(moved["x"] - base["x"]))
+        same = np.all(moved["iuacc"].reshape(-1, case.ns, case.ups) == base["iuacc"].reshape(-1, case.ns, case.ups),
+                      axis=(0, 2))
+        stable &= same & (moved["nacc"] == base["nacc"]) & (moved["nrej"] == base["nrej"])
+    return base, spread, stable
+
+
+@pytest.mark.parametrize("system", ["ring16_full", "ring16_band", "ring64"])
+def test_coupled_matches_oracle(system, native_libs, oracle_libs):
+    """End states: every element within the bar. Integer outputs (crossing
+    counts, step counts): equal on the systems whose integers the oracle's
+    own perturbations leave unchanged, with at most 2% of those allowed to
+    differ: every accepted event landing must fall inside the event band,
+    and a landing whose event value is a rounding error from the band edge
+    takes one more refinement step under any change of rounding, which a
+    finite set of perturbations samples but cannot exhaust."""
+    ns, periods = (128, 1) if system == "ring64" else (256, 2)
+    case = CW.ring_case(system, ns=ns, periods=periods, seed=14)
+    ora, spread, stable = _spread(case)
+    assert stable.mean() > 0.5
+    res = CW.run_coupled_gpu(case, mode=capi.MODE_PERSISTENT, warps=4)
+    mag = np.max(np.abs(case.arrays["x"]), axis=-1)
+    ok = scaled_close(res["x"], ora["x"], 1e-9, mag, floor=1.0) | (np.abs(res["x"] - ora["x"]) <= 1e3 * spread)
+    assert ok.all(), f"{int((~ok).sum())} end-state elements outside the bar"
+    same = np.all(res["iuacc"].reshape(-1, case.ns, case.ups) == ora["iuacc"].reshape(-1, case.ns, case.ups),
+                  axis=(0, 2))
+    for k in ("nacc", "nrej", "status"):
+        same &= res[k] == ora[k]
+    assert (~same[stable]).sum() <= max(1, int(0.02 * stable.sum())), \
+        f"{int((~same[stable]).sum())} of {int(stable.sum())} stable systems differ in integer outputs"
+    np.testing.assert_array_equal(res["isacc"][0], res["nacc"])
+
+
+def test_coupled_full_ensemble_matches_reference_kernel(native_libs):
+    """16384 rings of 64 units with the dense coupling matrix (the coupled
+    configuration at full ensemble size; two forcing periods): crossing
+    counts per unit, step counts per system and end states bit-identical to
+    the reference kernel."""
+    case = CW.ring_case("ring64", ns=16384, periods=2, seed=5)
+    ref = _ref(case, 128, 2)
+    res = CW.run_coupled_gpu(case, mode=capi.MODE_PERSISTENT, warps=4)
+    assert np.all(res["status"] == 0)
+    assert_bitwise(res, ref, keys=KEYS)
+
+
+def test_attempt_limit_is_reported(native_libs):
+    case = CW.ring_case("ring16_full", ns=32, periods=2, seed=15)
+    case.options["max_attempts"] = 50
+    res = CW.run_coupled_gpu(case, mode=0, warps=4)
+    assert np.all(res["status"] & capi.INSTANCE_ATTEMPT_LIMIT)
+    assert np.all(res["nacc"] + res["nrej"] == 50)
+    assert np.all(res["t"] < case.arrays["td"][1])
