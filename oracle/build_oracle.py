@@ -9,6 +9,12 @@ TEST INFRASTRUCTURE ONLY.
   reference's own per-thread kernel built for sm_103a (ref_gpu_entry.cu),
   device code only; built where the reference checkout exists and shipped to
   the GPU machine with the working tree.
+* ``oracle/_build/liboracle_fma_<system>.so`` / ``liboracle_cb_fma_<system>.so``
+  - the same oracles with multiply-adds contracted into fused multiply-adds
+  (``-ffp-contract=fast``, plus ``-mfma`` on x86-64 where FMA is not in the
+  base instruction set). Not a reference: the tests measure how far the
+  oracle's own results move when only the rounding of multiply-adds changes,
+  which is the difference between the GPU and the host arithmetic.
 * ``oracle/_build/liboracle_cb_<system>.so`` - the coupled-solver oracle
   (oracle_coupled.cpp) compiled once per coupled-system plugin source
   ``systems/<system>.cu`` (its hook file and coupling storage).
@@ -62,19 +68,19 @@ def _coupled_macros(system: str) -> list:
             f"-DMPGOS_SYS_CCI={d['CCI']}"]
 
 
-def oracle_cb_lib(system: str) -> Path:
-    return BUILD_DIR / f"liboracle_cb_{system}.so"
+def oracle_cb_lib(system: str, fma: bool = False) -> Path:
+    return BUILD_DIR / f"liboracle_cb_{'fma_' if fma else ''}{system}.so"
 
 
-def build_oracle_coupled(system: str, force: bool = False) -> Path:
-    out = oracle_cb_lib(system)
+def build_oracle_coupled(system: str, force: bool = False, fma: bool = False) -> Path:
+    out = oracle_cb_lib(system, fma)
     src = ORACLE_DIR / "oracle_coupled.cpp"
     d = coupled_defs(system)
     deps = [src, SYSTEMS_DIR / d["header"], SYSTEMS_DIR / f"{system}.cu", ORACLE_DIR / "host_shim.hpp", Path(__file__)]
     if not force and _newer(out, deps):
         return out
-    cmd = ["g++", *FLAGS, "-fopenmp", f"-I{ORACLE_DIR}", f"-I{SYSTEMS_DIR}", *_coupled_macros(system), str(src),
-           "-o", str(out)]
+    cmd = ["g++", *(_fma_flags() if fma else FLAGS), "-fopenmp", f"-I{ORACLE_DIR}", f"-I{SYSTEMS_DIR}",
+           *_coupled_macros(system), str(src), "-o", str(out)]
     _run(cmd, out.name)
     return out
 
@@ -115,8 +121,16 @@ def build_ref_gpu_coupled(system: str, algorithm: int, ns: int, tpb: int, spb: i
     return out
 
 
-def oracle_lib(system: str) -> Path:
-    return BUILD_DIR / f"liboracle_{system}.so"
+def oracle_lib(system: str, fma: bool = False) -> Path:
+    return BUILD_DIR / f"liboracle_{'fma_' if fma else ''}{system}.so"
+
+
+def _fma_flags() -> list:
+    import platform
+    flags = [f for f in FLAGS if f != "-ffp-contract=off"] + ["-ffp-contract=fast"]
+    if platform.machine() in ("x86_64", "AMD64"):
+        flags.append("-mfma")
+    return flags
 
 
 def ref_lib(system: str) -> Path:
@@ -140,13 +154,13 @@ def _run(cmd, what):
         raise RuntimeError(f"build of {what} failed:\n{' '.join(map(str, cmd))}\n{p.stdout}")
 
 
-def build_oracle(system: str, force: bool = False) -> Path:
-    out = oracle_lib(system)
+def build_oracle(system: str, force: bool = False, fma: bool = False) -> Path:
+    out = oracle_lib(system, fma)
     src = ORACLE_DIR / "oracle_perthread.cpp"
     hdr = SYSTEMS_DIR / f"{system}.cuh"
     if not force and _newer(out, [src, hdr, ORACLE_DIR / "host_shim.hpp", Path(__file__)]):
         return out
-    cmd = ["g++", *FLAGS, "-fopenmp", f"-I{ORACLE_DIR}", f"-I{SYSTEMS_DIR}",
+    cmd = ["g++", *(_fma_flags() if fma else FLAGS), "-fopenmp", f"-I{ORACLE_DIR}", f"-I{SYSTEMS_DIR}",
            f'-DMPGOS_SYSTEM_HEADER="{system}.cuh"', str(src), "-o", str(out)]
     _run(cmd, out.name)
     return out
@@ -216,9 +230,11 @@ def build_all(force: bool = False) -> dict:
         futs = {}
         for s in SYSTEMS:
             futs[ex.submit(build_oracle, s, force)] = ("oracle", s)
+            futs[ex.submit(build_oracle, s, force, True)] = ("oracle_fma", s)
             futs[ex.submit(build_ref, s, force)] = ("ref", s)
         for s in COUPLED:
             futs[ex.submit(build_oracle_coupled, s, force)] = ("oracle_cb", s)
+            futs[ex.submit(build_oracle_coupled, s, force, True)] = ("oracle_cb_fma", s)
         for k in REF_GPU_CB_KERNELS:
             futs[ex.submit(build_ref_gpu_coupled, *k, force)] = ("ref_gpu_cb", *k)
         for (s, alg, nt, ndo) in REF_GPU_KERNELS:

@@ -24,17 +24,18 @@ _D = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 _I = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
 
 
-def _oracle(system: str):
-    if system not in _libs:
-        path = _b.build_oracle(system)
+def _oracle(system: str, fma: bool = False):
+    key = (system, fma)
+    if key not in _libs:
+        path = _b.build_oracle(system, fma=fma)
         lib = C.CDLL(str(path))
         lib.oracle_pt_solve.restype = C.c_int
         lib.oracle_pt_solve.argtypes = [
             C.c_int, C.c_longlong, C.c_longlong, C.c_longlong, C.c_int,
             _D, _D, _D, _D, _D, _I, _D, _I, _D, _D, _D, _I, _I, _D, _D, _I, _I, _I, _D, C.c_int, C.c_longlong, C.c_int]
         lib.oracle_pt_threads.restype = C.c_int
-        _libs[system] = lib
-    return _libs[system]
+        _libs[key] = lib
+    return _libs[key]
 
 
 def _ref(system: str):
@@ -105,9 +106,11 @@ def _results(case, a, status, nacc, nrej):
     return out
 
 
-def run_oracle(case, threads: int = 0, first: int = 0, count: int | None = None) -> dict:
-    """Integrate ``case`` (all its phases) with the CPU oracle."""
-    lib = _oracle(case.system)
+def run_oracle(case, threads: int = 0, first: int = 0, count: int | None = None, fma: bool = False) -> dict:
+    """Integrate ``case`` (all its phases) with the CPU oracle; ``fma``: the
+    build with contracted multiply-adds (a rounding perturbation, not a
+    reference)."""
+    lib = _oracle(case.system, fma)
     a, tol, opt6 = _prepare(case)
     nt = case.nt
     n_active = case.n_active if case.n_active is not None else nt
@@ -170,16 +173,17 @@ class _CbOpts(C.Structure):
 _cb_libs: dict = {}
 
 
-def _oracle_cb(system: str):
-    if system not in _cb_libs:
-        lib = C.CDLL(str(_b.build_oracle_coupled(system)))
+def _oracle_cb(system: str, fma: bool = False):
+    key = (system, fma)
+    if key not in _cb_libs:
+        lib = C.CDLL(str(_b.build_oracle_coupled(system, fma=fma)))
         lib.oracle_cb_solve.restype = C.c_int
         lib.oracle_cb_solve.argtypes = [C.POINTER(_CbArrays), C.POINTER(_CbOpts), C.c_int, C.c_longlong, C.c_longlong,
                                         C.c_int]
         lib.oracle_cb_shape.restype = None
         lib.oracle_cb_shape.argtypes = [C.POINTER(C.c_int)]
-        _cb_libs[system] = lib
-    return _cb_libs[system]
+        _cb_libs[key] = lib
+    return _cb_libs[key]
 
 
 def oracle_cb_shape(system: str) -> tuple:
@@ -189,11 +193,12 @@ def oracle_cb_shape(system: str) -> tuple:
     return tuple(out)
 
 
-def run_oracle_coupled(case, threads: int = 0, first: int = 0, count: int | None = None) -> dict:
+def run_oracle_coupled(case, threads: int = 0, first: int = 0, count: int | None = None, fma: bool = False) -> dict:
     """Integrate a ``coupled_workloads.CbCase`` (all phases) with the coupled
     oracle; systems [first, first + count) only when given (the others keep
-    their inputs). Returns the dictionary of ``run_coupled_gpu``."""
-    lib = _oracle_cb(case.system)
+    their inputs); ``fma``: the contracted build. Returns the dictionary of
+    ``run_coupled_gpu``."""
+    lib = _oracle_cb(case.system, fma)
     a = case.arrays
     f64 = lambda v: np.ascontiguousarray(np.array(v, dtype=np.float64, copy=True))
     i32 = lambda v: np.ascontiguousarray(np.array(v, dtype=np.int32, copy=True))

@@ -79,14 +79,16 @@ _SPREAD_CACHE = {}
 
 
 def perturbation_spread(case, rel=0.0, key=None, tol_rel=0.0):
-    """What a tiny change of the inputs does to the CPU reference itself: the
-    oracle is run on ``case`` and on ``case`` with every initial state moved
-    by one unit in the last place (``rel`` = 0) or by ``rel`` relative and,
-    with ``tol_rel`` > 0, once more with the tolerances moved by ``tol_rel``
-    relative (which moves every step size by about tol_rel / 5: the step grid
-    shift that a step-size factor rounded differently produces). Returns
-    (|difference| per float output, the largest over the perturbations;
-    mask of instances whose integer outputs no perturbation changed).
+    """What tiny changes do to the CPU reference itself. The oracle is run on
+    ``case`` and on three variants: every initial state moved by one unit in
+    the last place (``rel`` = 0) or by ``rel`` relative; the same inputs with
+    multiply-adds contracted into fused multiply-adds (the rounding change
+    between host and GPU arithmetic, which event refinements and impacts can
+    amplify far beyond one ulp); and, with ``tol_rel`` > 0, the tolerances
+    moved by ``tol_rel`` relative (which moves every step size by about
+    tol_rel / 5: the step-grid shift of a step-size factor rounded
+    differently). Returns (|difference| per float output, the largest over
+    the variants; mask of instances whose integer outputs no variant changed).
     Cached under ``key``."""
     from oracle import oracle as O
     ck = (key, rel, tol_rel)
@@ -96,7 +98,7 @@ def perturbation_spread(case, rel=0.0, key=None, tol_rel=0.0):
     pert = case.copy()
     x = pert.arrays["x"]
     pert.arrays["x"] = np.nextafter(x, np.inf) if rel == 0.0 else x * (1.0 + rel) + (x == 0) * rel
-    runs = [O.run_oracle(pert)]
+    runs = [O.run_oracle(pert), O.run_oracle(case, fma=True)]
     if tol_rel > 0.0:
         pt = case.copy()
         pt.rtol = pt.rtol * (1.0 + tol_rel)

@@ -83,19 +83,20 @@ def test_active_systems_and_phases(native_libs):
 
 def _spread(case):
     """The oracle's own sensitivity: end-state spread and the systems whose
-    integer outputs stay unchanged under four tiny perturbations (initial
-    states one ulp up and down, tolerances 1e-12 relative up and down)."""
+    integer outputs stay unchanged under five tiny perturbations (initial
+    states one ulp up and down, tolerances 1e-12 relative up and down, and
+    multiply-adds contracted into fused multiply-adds)."""
     base = O.run_oracle_coupled(case)
     spread = np.zeros_like(base["x"])
     stable = np.ones(case.ns, bool)
-    for kind, sign in (("x", np.inf), ("x", -np.inf), ("tol", 1.0), ("tol", -1.0)):
+    for kind, sign in (("x", np.inf), ("x", -np.inf), ("tol", 1.0), ("tol", -1.0), ("fma", 0)):
         pert = case.copy()
         if kind == "x":
             pert.arrays["x"] = np.nextafter(pert.arrays["x"], sign)
-        else:
+        elif kind == "tol":
             pert.rtol = pert.rtol * (1.0 + sign * 1e-12)
             pert.atol = pert.atol * (1.0 + sign * 1e-12)
-        moved = O.run_oracle_coupled(pert)
+        moved = O.run_oracle_coupled(pert, fma=(kind == "fma"))
         spread = np.maximum(spread, np.abs(moved["x"] - base["x"]))
         same = np.all(moved["iuacc"].reshape(-1, case.ns, case.ups) == base["iuacc"].reshape(-1, case.ns, case.ups),
                       axis=(0, 2))
