@@ -283,6 +283,25 @@ int mpgos_pt_adjoint(mpgos_pt_solver* solver, const double* dL_dxT, double* dL_d
 /* Device pointers and sizes of the recorded tape (read-only view). */
 int mpgos_pt_tape_info(const mpgos_pt_solver* solver, mpgos_pt_tape* tape);
 
+/* mpgos_pt_solve_record without device allocation (no counterpart in the
+ * reference): records the same tape as mpgos_pt_solve_record, bit for bit, into
+ * a file-scope static device array of MPGOS_STATIC_TAPE_BYTES held by the
+ * runtime library, instead of buffers it cudaMalloc's. No cudaMalloc, cudaFree
+ * or other allocating call is made; the per-instance step counts are cleared
+ * with cudaMemsetAsync on the solver's stream. A tape larger than
+ * MPGOS_STATIC_TAPE_BYTES (dt: max_steps x NT doubles, checkpoints:
+ * (max_steps / segment + 1) x (SD + 1) x NT doubles, counts: NT ints, each part
+ * rounded up to 256 bytes) is rejected with MPGOS_ERR_ARGUMENT and a message.
+ * mpgos_pt_adjoint and mpgos_pt_tape_info then read this tape until the next
+ * mpgos_pt_solve_record. There is one such array per device and process:
+ * overlapping calls (two solvers, or a second call before the first's reverse
+ * pass has finished on the stream) race on it. The first call on a device
+ * looks up the array's address (cudaGetSymbolAddress, which loads the
+ * runtime's device module), so make that first call before any stream
+ * capture begins. */
+#define MPGOS_STATIC_TAPE_BYTES (16u * 1024u * 1024u)
+int mpgos_pt_solve_record_static(mpgos_pt_solver* solver, int32_t max_steps, int32_t segment);
+
 /* Measured FMA throughput of the device (extension, no counterpart in the
  * reference): independent fused multiply-add chains in FP64
  * (precision_bytes 8) or FP32 (4) on every SM, timed with CUDA events.

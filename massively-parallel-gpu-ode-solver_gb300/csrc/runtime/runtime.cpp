@@ -20,6 +20,7 @@
 #include <cstring>
 #include <fstream>
 #include <map>
+#include <mutex>
 #include <sstream>
 #include <string>
 #include <vector>
@@ -121,6 +122,10 @@ struct mpgos_pt_solver {
     // adjoint tape (device memory, allocated by the first recording solve)
     mpgos_pt_tape tape{};
     size_t tape_bytes = 0;
+    // Tape views into the static device scratch of mpgos_pt_solve_record_static;
+    // use_static_tape selects which tape the reverse pass reads.
+    mpgos_pt_tape static_tape{};
+    bool use_static_tape = false;
 };
 
 namespace {
@@ -922,6 +927,7 @@ MPGOS_EXPORT int mpgos_pt_solve_record(mpgos_pt_solver* s, int32_t max_steps, in
     fill_launch(s, L, m);
     rc = s->k->launch_record(&L, &s->tape, grid, s->block, dynamic_smem(s), s->stream);
     if (rc != 0) return fail(MPGOS_ERR_CUDA, "recording launch failed: %s", cudaGetErrorString((cudaError_t)rc));
+    s->use_static_tape = false;
     return MPGOS_OK;
 }
 
@@ -930,7 +936,8 @@ MPGOS_EXPORT int mpgos_pt_adjoint(mpgos_pt_solver* s, const double* dLdxT, doubl
     int rc = check_solver(s);
     if (rc) return rc;
     if (s->k->launch_adjoint == nullptr) return fail(MPGOS_ERR_UNSUPPORTED, "system %s has no adjoint kernels", s->k->name);
-    if (s->tape.dt == nullptr) return fail(MPGOS_ERR_ARGUMENT, "no recorded forward pass (call mpgos_pt_solve_record first)");
+    const mpgos_pt_tape& tape = s->use_static_tape ? s->static_tape : s->tape;
+    if (tape.dt == nullptr) return fail(MPGOS_ERR_ARGUMENT, "no recorded forward pass (call mpgos_pt_solve_record first)");
     if (dLdxT == nullptr || dLdx0 == nullptr || (dLdp == nullptr && s->shape.ncp > 0))
         return fail(MPGOS_ERR_ARGUMENT, "null gradient buffer");
     if (s->n_active <= 0) return MPGOS_OK;
@@ -939,7 +946,7 @@ MPGOS_EXPORT int mpgos_pt_adjoint(mpgos_pt_solver* s, const double* dLdxT, doubl
     const int64_t grid = (s->n_active + block - 1) / block;
     mpgos_pt_launch L;
     fill_launch(s, L, 0);
-    rc = s->k->launch_adjoint(&L, &s->tape, dLdxT, dLdx0, dLdp, static_cast<int>(grid), block, dynamic_smem(s), s->stream);
+    rc = s->k->launch_adjoint(&L, &tape, dLdxT, dLdx0, dLdp, static_cast<int>(grid), block, dynamic_smem(s), s->stream);
     if (rc != 0) return fail(MPGOS_ERR_CUDA, "adjoint launch failed: %s", cudaGetErrorString((cudaError_t)rc));
     return MPGOS_OK;
 }
@@ -949,6 +956,82 @@ MPGOS_EXPORT int mpgos_pt_tape_info(const mpgos_pt_solver* s, mpgos_pt_tape* tap
     int rc = check_solver(s);
     if (rc) return rc;
     if (tape == nullptr) return fail(MPGOS_ERR_ARGUMENT, "null tape pointer");
-    *tape = s->tape;
+    *tape = s->use_static_tape ? s->static_tape : s->tape;
+    return MPGOS_OK;
+}
+
+// ---- recording into static device scratch ------------------------------------
+// The tape of mpgos_pt_solve_record_static lives in this file-scope device
+// array instead of cudaMalloc'd buffers: [dt][ckpt_x][ckpt_t][n_steps], each
+// part starting on a 256-byte boundary.
+static __device__ __align__(256) unsigned char g_static_tape[MPGOS_STATIC_TAPE_BYTES];
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_static_tape_mu;
+void* g_static_tape_addr[kMaxDevices] = {};
+
+size_t align256(size_t b) { return (b + 255) / 256 * 256; }
+
+// Device address of g_static_tape on the current device (looked up once per
+// device; the lookup loads this library's device module on first use).
+int static_tape_base(int device, unsigned char** base)
+{
+    if (device < 0 || device >= kMaxDevices) return fail(MPGOS_ERR_ARGUMENT, "device ordinal %d out of range", device);
+    std::lock_guard<std::mutex> lock(g_static_tape_mu);
+    if (g_static_tape_addr[device] == nullptr) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_static_tape);
+        if (e != cudaSuccess || p == nullptr)
+            return fail(MPGOS_ERR_CUDA, "cudaGetSymbolAddress(static tape) on device %d failed: %s", device,
+                        cudaGetErrorString(e));
+        g_static_tape_addr[device] = p;
+    }
+    *base = static_cast<unsigned char*>(g_static_tape_addr[device]);
+    return MPGOS_OK;
+}
+}  // namespace
+
+MPGOS_EXPORT int mpgos_pt_solve_record_static(mpgos_pt_solver* s, int32_t max_steps, int32_t segment)
+{
+    int rc = check_solver(s);
+    if (rc) return rc;
+    if (s->k->launch_record == nullptr || s->shape.precision_bytes != 8)
+        return fail(MPGOS_ERR_UNSUPPORTED, "system %s has no adjoint kernels compiled (FP64 only)", s->k->name);
+    if (max_steps < 1 || segment < 1 || segment > 64)
+        return fail(MPGOS_ERR_ARGUMENT, "tape: max_steps %d must be >= 1 and segment %d within 1..64", max_steps, segment);
+    const size_t nt = static_cast<size_t>(s->nt), sd = static_cast<size_t>(s->shape.sd);
+    const size_t nck = static_cast<size_t>(max_steps / segment + 1);
+    const size_t b_dt = align256(static_cast<size_t>(max_steps) * nt * 8), b_cx = align256(nck * sd * nt * 8);
+    const size_t b_ct = align256(nck * nt * 8), b_n = align256(nt * 4);
+    const size_t need = b_dt + b_cx + b_ct + b_n;
+    if (need > MPGOS_STATIC_TAPE_BYTES)
+        return fail(MPGOS_ERR_ARGUMENT,
+                    "static tape: %zu bytes needed for %zu instances x %d steps (checkpoint every %d), only %zu "
+                    "available (MPGOS_STATIC_TAPE_BYTES); use mpgos_pt_solve_record",
+                    need, nt, max_steps, segment, static_cast<size_t>(MPGOS_STATIC_TAPE_BYTES));
+    MPGOS_CUDA(cudaSetDevice(s->device));
+    unsigned char* base = nullptr;
+    if ((rc = static_tape_base(s->device, &base))) return rc;
+    mpgos_pt_tape t{};
+    t.segment = segment;
+    t.max_steps = max_steps;
+    t.dt = reinterpret_cast<double*>(base);
+    t.ckpt_x = reinterpret_cast<double*>(base + b_dt);
+    t.ckpt_t = reinterpret_cast<double*>(base + b_dt + b_cx);
+    t.n_steps = reinterpret_cast<int32_t*>(base + b_dt + b_cx + b_ct);
+    s->static_tape = t;
+    s->use_static_tape = true;
+    // step counts of instances this launch does not integrate read as zero
+    MPGOS_CUDA(cudaMemsetAsync(t.n_steps, 0, nt * 4, s->stream));
+    if (s->n_active <= 0) return MPGOS_OK;
+    const int32_t m = effective_mode(s, s->mode) & (MPGOS_MODE_FAST_CONTROL | MPGOS_MODE_PERSISTENT);
+    int grid = 0;
+    if ((rc = grid_for(s, m, s->block, &grid))) return rc;
+    if (m & MPGOS_MODE_PERSISTENT) MPGOS_CUDA(cudaMemsetAsync(s->d_work, 0, sizeof(uint32_t), s->stream));
+    mpgos_pt_launch L;
+    fill_launch(s, L, m);
+    rc = s->k->launch_record(&L, &s->static_tape, grid, s->block, dynamic_smem(s), s->stream);
+    if (rc != 0) return fail(MPGOS_ERR_CUDA, "recording launch failed: %s", cudaGetErrorString((cudaError_t)rc));
     return MPGOS_OK;
 }

@@ -79,6 +79,7 @@ INSTANCE_ATTEMPT_LIMIT = 8
 INSTANCE_TAPE_OVERFLOW = 16
 
 ABI_VERSION = 1
+STATIC_TAPE_BYTES = 16 * 1024 * 1024  # MPGOS_STATIC_TAPE_BYTES of mpgos.h
 
 
 # Coupled per-block solver (CoupledSystems_PerBlock_Interface.cuh:33-66).
@@ -201,6 +202,7 @@ def _declare(lib):
         "mpgos_pt_solve_record": (C.c_int, [P, i32, i32]),
         "mpgos_pt_adjoint": (C.c_int, [P, P, P, P]),
         "mpgos_pt_tape_info": (C.c_int, [P, C.POINTER(Tape)]),
+        "mpgos_pt_solve_record_static": (C.c_int, [P, i32, i32]),
         "mpgos_cb_create": (C.c_int, [P, i64, i32, C.c_int, C.POINTER(P)]),
         "mpgos_cb_destroy": (C.c_int, [P]),
         "mpgos_cb_get_shape": (C.c_int, [P, C.POINTER(CbShape), C.POINTER(i64), C.POINTER(i32)]),
@@ -233,7 +235,7 @@ RUNTIME_SYMBOLS = (
     "mpgos_pt_insert_sync_point", "mpgos_pt_sync_solver", "mpgos_pt_sync_device", "mpgos_pt_stream",
     "mpgos_pt_launch_config", "mpgos_pt_timer_start", "mpgos_pt_timer_stop", "mpgos_pt_autotune",
     "mpgos_pt_checkpoint_save", "mpgos_pt_checkpoint_restore", "mpgos_probe_fma_peak",
-    "mpgos_pt_solve_record", "mpgos_pt_adjoint", "mpgos_pt_tape_info",
+    "mpgos_pt_solve_record", "mpgos_pt_adjoint", "mpgos_pt_tape_info", "mpgos_pt_solve_record_static",
     "mpgos_cb_create", "mpgos_cb_destroy", "mpgos_cb_get_shape", "mpgos_cb_set_option", "mpgos_cb_host_buffer",
     "mpgos_cb_device_buffer", "mpgos_cb_sync_h2d", "mpgos_cb_sync_d2h", "mpgos_cb_solve",
     "mpgos_cb_insert_sync_point", "mpgos_cb_sync_solver", "mpgos_cb_timer_start", "mpgos_cb_timer_stop",

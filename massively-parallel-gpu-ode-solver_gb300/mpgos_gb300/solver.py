@@ -259,6 +259,13 @@ class ProblemSolver:
         checkpoint every ``segment`` accepted steps)."""
         capi.check(self._lib.mpgos_pt_solve_record(self._h, int(max_steps), int(segment)))
 
+    def SolveRecordStatic(self, max_steps: int, segment: int = 32):
+        """SolveRecord into the runtime's static device scratch
+        (mpgos_pt_solve_record_static): no device allocation; at most
+        MPGOS_STATIC_TAPE_BYTES of tape; one scratch per device and process,
+        so concurrent recordings race."""
+        capi.check(self._lib.mpgos_pt_solve_record_static(self._h, int(max_steps), int(segment)))
+
     def Adjoint(self, dLdxT_ptr: int, dLdx0_ptr: int, dLdp_ptr: int):
         """Reverse pass over the recorded tape; device pointers, FP64,
         [SD][NT] in, [SD][NT] and [NCP][NT] out."""
