@@ -7,10 +7,14 @@ from the initial state (one Solve() launch, after a device-side restore of
 the initial state). Metric: accepted instance-steps per second.
 
 Arms:
-  default           the GB300 kernels through the C-ABI, CHOSEN form
-                    (persistent work queue + FAST_CONTROL); the PLAIN form
-                    (reference arithmetic, static mapping) is measured in the
-                    same run and reported under "plain".
+  default           the GB300 kernels through the C-ABI, chosen form:
+                    DF_STAGE (double-float stage arithmetic on the FP32 pipe,
+                    log-domain step control) on the persistent work queue,
+                    launch shape autotuned. Measured in the same run and
+                    reported beside it: the FP64 FAST_CONTROL form ("fast_fp64"),
+                    the PLAIN form (reference arithmetic, static mapping,
+                    "plain") and the reference's own kernel built for sm_103a
+                    ("reference_gpu").
   --impl reference  the reference's CPU implementation of the path: the
                     reference solver compiled for this host where its build
                     exists (oracle/_ref), else the oracle port
@@ -44,6 +48,7 @@ for p in (str(REPO), str(PKG)):
         sys.path.insert(0, p)
 
 WORKLOAD = "lorenz_rkck45_tol1e-10_t0-10_2^20"
+CHOSEN_MODE = 16 | 2   # MPGOS_MODE_DF_STAGE | MPGOS_MODE_PERSISTENT (the autotuner may drop persistence)
 METRIC = "accepted instance-steps/s (Lorenz RKCK45, rtol=atol=1e-10, 2^20 instances)"
 UNIT = "instance-steps/s"
 NT = 1 << 20
@@ -269,7 +274,7 @@ def main():
             launch = kern.launch
         else:
             if tune:
-                s.autotune(fast_control=bool(mode & capi.MODE_FAST_CONTROL))
+                s.autotune(arithmetic=mode & (capi.MODE_FAST_CONTROL | capi.MODE_DF_STAGE))
             launch = s.Solve
         for _ in range(warmup):
             s.checkpoint_restore()
@@ -320,7 +325,7 @@ def main():
                     block=block, mode=m, res=res)
 
     clocks = Clocks(local)
-    chosen = measure(capi.MODE_CHOSEN, args.steps, args.warmup, clocks, tune=True)
+    chosen = measure(CHOSEN_MODE, args.steps, args.warmup, clocks, tune=True)
     t_step = dist_max(world, sum(chosen["step_ms"]) / 1e3)
     acc_all = dist_sum(world, chosen["accepted"])
     value = acc_all / t_step
@@ -363,6 +368,7 @@ def main():
                 "kernel_ms": statistics.median(r["kernel_ms"]), "grid": r["grid"], "block": r["block"],
                 "mode": r["mode"]}
 
+    fast = summarize(measure(capi.MODE_CHOSEN, max(1, min(args.steps, 3)), 1, tune=True))
     plain = ref_gpu = None
     parity = {}
     if not args.no_plain:
@@ -391,31 +397,41 @@ def main():
         return
 
     peak_fp64 = capi.fma_peak(local, 8)
+    peak_fp32_ops = capi.fma_peak(local, 4) / 2.0   # FP32 FMA instructions per second
     kernel_s = statistics.median(chosen["kernel_ms"]) / 1e3
     attempts_per_launch = chosen["attempts"] / args.steps
-    achieved = FLOP_PER_ATTEMPT * attempts_per_launch / kernel_s
-    traffic = load_traffic().get("lorenz_chosen_bytes_per_launch")
+    prof = load_traffic()
+    fp32_ops = prof.get("lorenz_df_fp32_thread_ops_per_attempt")
+    traffic = prof.get("lorenz_df_dram_bytes_per_launch")
+    achieved = (fp32_ops * attempts_per_launch / kernel_s) if fp32_ops else None
     peaks = load_peaks()
     cpu = None if args.no_cpu else cpu_baseline(args.nt)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "instances": args.nt, "form": "chosen",
+        "vs_baseline": None, "dtype": "df64 (float pairs, ~48-bit) stages; f64 state in HBM", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "instances": args.nt, "form": "chosen: DF_STAGE + persistent",
                    "mode": chosen["mode"], "grid": chosen["grid"], "block": chosen["block"],
                    "l2": "flushed before every step (512 MB write), outside the timed events",
                    "accepted_steps_per_launch": chosen["accepted"] / args.steps,
                    "attempts_per_launch": attempts_per_launch},
         "e2e": e2e,
+        "fast_fp64": fast,
         "plain": plain,
         "reference_gpu": ref_gpu,
         "speedup_vs_reference_gpu": (value / ref_gpu["value"]) if ref_gpu else None,
         "parity": parity,
-        "roofline": {"bound": "fp64", "achieved": achieved / 1e12, "peak": peak_fp64 / 1e12, "unit": "TFLOP/s",
-                     "frac": achieved / peak_fp64, "traffic": traffic,
-                     "flop_per_attempt": FLOP_PER_ATTEMPT,
+        "roofline": {"bound": "fp32_pipe",
+                     "achieved": achieved / 1e12 if achieved else None,
+                     "peak": peak_fp32_ops / 1e12, "unit": "T FP32-pipe thread-ops/s",
+                     "frac": achieved / peak_fp32_ops if achieved else None, "traffic": traffic,
+                     "fp32_thread_ops_per_attempt": fp32_ops,
+                     "ops_source": "FFMA+FADD+FMUL thread instructions per step attempt, ncu capture "
+                                   "(profiles/perthread_df_kernel_lorenz.md)",
                      "kernel_ms": kernel_s * 1e3,
-                     "peak_source": "measured FP64 FMA throughput (mpgos_probe_fma_peak), same GPU, same run",
+                     "peak_source": "measured FP32 FMA throughput (mpgos_probe_fma_peak), same GPU, same run",
+                     "algorithmic_fp64_equivalent_tflops": FLOP_PER_ATTEMPT * attempts_per_launch / kernel_s / 1e12,
+                     "fp64_fma_peak_tflops": peak_fp64 / 1e12,
                      "hbm_peak_gbs_measured": peaks.get("hbm_gbs")},
         "cpu_baseline": cpu,
         "clocks": clocks.summary(),

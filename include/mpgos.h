@@ -107,6 +107,12 @@ enum mpgos_option {
 #define MPGOS_MODE_FAST_CONTROL 1
 #define MPGOS_MODE_PERSISTENT   2
 #define MPGOS_MODE_FP32_STAGE   4
+/* DF_STAGE: every per-instance quantity of the adaptive FP64 scheme in
+ * double-float arithmetic (pairs of floats, ~48 significant bits) on the FP32
+ * pipe, with a log-domain step-size factor; results agree with the FP64
+ * kernels to ~1e-13 relative on non-chaotic instances. Exclusive with
+ * FP32_STAGE; FAST_CONTROL is implied. */
+#define MPGOS_MODE_DF_STAGE     16
 #define MPGOS_MODE_CHOSEN       (MPGOS_MODE_FAST_CONTROL | MPGOS_MODE_PERSISTENT)
 
 /* ---- per-instance status flags (MPGOS_STATUS), extensions --------------
@@ -258,8 +264,11 @@ int mpgos_pt_timer_stop(mpgos_pt_solver* solver, float* milliseconds);
 /* Autotuner (extension): times one Solve() per candidate (block size x
  * static/persistent mapping) on a scratch copy of the current device state,
  * restores the state, keeps the fastest configuration and, if cache_path is
- * not NULL, records it in a JSON cache keyed by system, shape, NT and GPU. */
-int mpgos_pt_autotune(mpgos_pt_solver* solver, int32_t fast_control, const char* cache_path);
+ * not NULL, records it in a JSON cache keyed by system, shape, NT and GPU.
+ * `arithmetic` fixes the arithmetic the candidates share: 0 the reference's,
+ * MPGOS_MODE_DF_STAGE double-float stages, any other non-zero value
+ * FAST_CONTROL (each where compiled, else the reference's). */
+int mpgos_pt_autotune(mpgos_pt_solver* solver, int32_t arithmetic, const char* cache_path);
 
 /* Device-side checkpoint of every array a launch writes (time domain, state,
  * time, control parameters, accessories, dense output) and restore of it

@@ -1,0 +1,312 @@
+// Per-thread RKCK45 solver in double-float arithmetic (DF_STAGE mode).
+//
+// Every per-instance quantity of one launch (state, stages, time, step,
+// error, tolerances, event values) is a double-float (dfloat.cuh: ~48
+// significant bits) evaluated on the FP32 pipe; FP64 is touched only to load
+// the instance, to round back on write-back and for transcendental functions
+// inside user hooks. The algorithm is the reference's loop
+// (SingleSystem_PerThread_Solver.cuh:117-435) with the Cash-Karp stepper
+// instantiated for dfloat, the reference's event handling and dense output,
+// and this controller:
+//   accept  iff err_i < max(rtol_i * max(|xn_i|, |x_i|), atol_i) for all i,
+//           compared exactly in double-float;
+//   factor  0.9 * (min_i tol_i / err_i)^(1/5) (1/4 after a rejection),
+//           formed as 0.9 * exp2(min_i (log2 tol_i - log2 err_i) / 5) in FP32
+//           from the leading floats (relative error ~1e-7, like FAST_CONTROL),
+//           clamped to [shrink, grow]; the new step is dt * factor in
+//           double-float, clamped to [min_dt, max_dt].
+// The last step of the time domain ends exactly on its upper bound.
+//
+// Precision: the stage sums and the right-hand side carry ~4e-15 relative
+// rounding per operation instead of 1.1e-16; against a local error of order
+// the tolerance (1e-10 in the headline configuration) this moves the end
+// states of non-chaotic instances by ~1e-13 relative and the embedded error
+// estimate by ~1e-6 relative, both far inside the 1e-9 parity bar. The
+// exponent range is float's (|values| within ~1e-38..3e38); systems whose
+// states or parameters leave it must not use this mode.
+#pragma once
+
+#include "dfloat.cuh"
+
+namespace mpgos {
+namespace pt {
+
+using df::dfloat;
+
+struct DfOptions {
+    dfloat initial_dt, max_dt, min_dt, min_dt_guard, dense_min_dt;
+    float grow, shrink;
+    int ndo, dense_freq;
+    long long max_attempts;
+};
+
+template <class S>
+struct DfInstance {
+    static constexpr int SD = S::SD;
+    long long i;
+    dfloat td[2];
+    dfloat x[SD];
+    dfloat cp[AtLeastOne<S::NCP>::value];
+    dfloat acc[AtLeastOne<S::NA>::value];
+    int acci[AtLeastOne<S::NIA>::value];
+    dfloat ga[AtLeastOne<S::NE>::value];
+    dfloat t, dt, new_dt, dense_next;
+    int didx, skipped, terminate, udt, status, nacc, nrej;
+    long long attempts;
+};
+
+template <class S>
+struct DfStaged {
+    dfloat* sp;
+    int* spi;
+    const dfloat* rtol;
+    const dfloat* atol;
+    const dfloat* etol;
+    const int* edir;
+};
+
+// Controller of DF_STAGE (see the file comment).
+template <int SD>
+__device__ __forceinline__ void control_rkck45_df(const DfOptions& o, dfloat dt, const dfloat* x, const dfloat* xn,
+                                                  const dfloat* err, const dfloat* rtol, const dfloat* atol,
+                                                  int& update, int& finite, int& terminate, dfloat& new_dt,
+                                                  int& status)
+{
+    float lr = INFINITY;
+#pragma unroll
+    for (int i = 0; i < SD; i++) {
+        const dfloat tol = df::fmax(rtol[i] * df::fmax(df::abs(xn[i]), df::abs(x[i])), atol[i]);
+        update = update && (err[i] < tol);
+        lr = fminf(lr, __log2f(tol.hi) - __log2f(err[i].hi));
+    }
+    const float expo = (update == 1) ? 0.2f : 0.25f;
+    float q = 0.9f * exp2f(fminf(fmaxf(lr * expo, -120.0f), 120.0f));
+    if (finite == 0) {
+        q      = o.shrink;
+        update = 0;
+        if (dt < o.min_dt_guard) {
+            terminate = 1;
+            status |= MPGOS_INSTANCE_NONFINITE;
+        }
+    } else if (dt < o.min_dt_guard) {
+        update = 1;
+        status |= MPGOS_INSTANCE_MINIMUM_STEP;
+    }
+    q      = fminf(q, o.grow);
+    q      = fmaxf(q, o.shrink);
+    new_dt = df::mul_f(dt, q);
+    new_dt = df::fmin(new_dt, o.max_dt);
+    new_dt = df::fmax(new_dt, o.min_dt);
+}
+
+template <int SD>
+__device__ __forceinline__ void dense_store_df(long long i, long long nt, int store, int& didx, int ndo,
+                                               double* dtime, double* dstate, dfloat t, const dfloat* x,
+                                               int& skipped, dfloat& dense_next, dfloat dense_min_dt, dfloat upper)
+{
+    if (store == 1) {
+        if (didx < ndo) {
+            dtime[i + static_cast<long long>(didx) * nt] = static_cast<double>(t);
+            long long idx = i + static_cast<long long>(didx) * nt * SD;
+#pragma unroll
+            for (int c = 0; c < SD; c++) {
+                dstate[idx] = static_cast<double>(x[c]);
+                idx += nt;
+            }
+            didx++;
+        }
+        skipped    = 0;
+        dense_next = df::fmin(t + dense_min_dt, upper);
+    } else {
+        skipped++;
+    }
+}
+
+template <class S, int MODE>
+struct DfSolver {
+    static constexpr int SD = S::SD, NCP = S::NCP, NE = S::NE, NA = S::NA, NIA = S::NIA;
+    static constexpr bool PERSISTENT = (MODE & MPGOS_MODE_PERSISTENT) != 0;
+    using Inst = DfInstance<S>;
+
+    __device__ static void begin(Inst& s, long long i, const Args<double>& a, const DfStaged<S>& g,
+                                 const DfOptions& o)
+    {
+        const long long nt = a.nt;
+        s.i = i;
+#pragma unroll
+        for (int k = 0; k < 2; k++) s.td[k] = dfloat(a.td[i + k * nt]);
+#pragma unroll
+        for (int k = 0; k < SD; k++) s.x[k] = dfloat(a.x[i + k * nt]);
+#pragma unroll
+        for (int k = 0; k < NCP; k++) s.cp[k] = dfloat(a.cp[i + k * nt]);
+#pragma unroll
+        for (int k = 0; k < NA; k++) s.acc[k] = dfloat(a.acc[i + k * nt]);
+#pragma unroll
+        for (int k = 0; k < NIA; k++) s.acci[k] = a.acci[i + k * nt];
+        s.t          = dfloat(a.t[i]);
+        s.dt         = o.initial_dt;
+        s.new_dt     = o.initial_dt;
+        s.didx       = a.didx[i];
+        s.skipped    = 0;
+        s.terminate  = 0;
+        s.udt        = 0;
+        s.status     = 0;
+        s.nacc       = 0;
+        s.nrej       = 0;
+        s.attempts   = 0;
+        s.dense_next = s.t;
+        const int ti = static_cast<int>(i), nti = static_cast<int>(nt);
+        PerThread_Initialization(ti, nti, s.didx, s.t, s.dt, s.td, s.x, s.cp, g.sp, g.spi, s.acc, s.acci);
+        if (NE > 0)
+            PerThread_EventFunction(ti, nti, s.ga, s.t, s.dt, s.td, s.x, s.cp, g.sp, g.spi, s.acc, s.acci);
+        if (o.ndo > 0)
+            dense_store_df<SD>(i, nt, 1, s.didx, o.ndo, a.dtime, a.dstate, s.t, s.x, s.skipped, s.dense_next,
+                               o.dense_min_dt, s.td[1]);
+    }
+
+    __device__ static void attempt(Inst& s, const Args<double>& a, const DfStaged<S>& g, const DfOptions& o)
+    {
+        if (s.attempts >= o.max_attempts) {
+            s.status |= MPGOS_INSTANCE_ATTEMPT_LIMIT;
+            s.terminate = 1;
+            return;
+        }
+        s.attempts++;
+        const int ti = static_cast<int>(s.i), nti = static_cast<int>(a.nt);
+        int update = 1, finite = 1, end_reached = 0;
+        dfloat xn[SD], err[SD];
+        s.dt = s.new_dt;
+        const dfloat rem = s.td[1] - s.t;
+        if (s.dt > rem) {
+            s.dt        = rem;
+            end_reached = 1;
+        }
+        step_rkck45<SD, dfloat, false>(ti, nti, s.t, s.dt, s.x, xn, err, finite, s.cp, g.sp, g.spi, s.acc, s.acci);
+        control_rkck45_df<SD>(o, s.dt, s.x, xn, err, g.rtol, g.atol, update, finite, s.terminate, s.new_dt,
+                              s.status);
+
+        dfloat gn[AtLeastOne<NE>::value];
+        if (NE > 0) {
+            PerThread_EventFunction(ti, nti, gn, s.t + s.dt, s.dt, s.td, xn, s.cp, g.sp, g.spi, s.acc, s.acci);
+            event_step_control<NE, dfloat>(update, s.terminate, s.ga, gn, g.etol, g.edir, s.dt, s.new_dt, o.min_dt,
+                                           s.status);
+        }
+
+        if (update == 1) {
+            s.nacc++;
+            s.t = (end_reached == 1) ? s.td[1] : s.t + s.dt;
+#pragma unroll
+            for (int k = 0; k < SD; k++) s.x[k] = xn[k];
+            PerThread_ActionAfterSuccessfulTimeStep(ti, nti, s.udt, s.t, s.dt, s.td, s.x, s.cp, g.sp, g.spi,
+                                                    s.acc, s.acci);
+            if (NE > 0) {
+                for (int e = 0; e < NE; e++) {
+                    if (event_detected<dfloat>(s.ga[e], gn[e], g.etol[e], g.edir[e]))
+                        PerThread_ActionAfterEventDetection(ti, nti, e, s.udt, s.t, s.dt, s.td, s.x, s.cp, g.sp,
+                                                            g.spi, s.acc, s.acci);
+                }
+                PerThread_EventFunction(ti, nti, gn, s.t, s.dt, s.td, s.x, s.cp, g.sp, g.spi, s.acc, s.acci);
+#pragma unroll
+                for (int e = 0; e < NE; e++) s.ga[e] = gn[e];
+            }
+            if (o.ndo > 0) {
+                const int store = dense_condition<dfloat>(s.t, s.dense_next, s.didx, s.skipped, end_reached, s.udt,
+                                                          o.ndo, o.dense_freq);
+                dense_store_df<SD>(s.i, a.nt, store, s.didx, o.ndo, a.dtime, a.dstate, s.t, s.x, s.skipped,
+                                   s.dense_next, o.dense_min_dt, s.td[1]);
+            }
+            if ((end_reached == 1) || (s.udt == 1)) s.terminate = 1;
+        } else {
+            s.nrej++;
+        }
+    }
+
+    __device__ static void end(Inst& s, const Args<double>& a, const DfStaged<S>& g)
+    {
+        const long long i = s.i, nt = a.nt;
+        const int ti = static_cast<int>(i), nti = static_cast<int>(nt);
+        PerThread_Finalization(ti, nti, s.didx, s.t, s.dt, s.td, s.x, s.cp, g.sp, g.spi, s.acc, s.acci);
+#pragma unroll
+        for (int k = 0; k < 2; k++) a.td[i + k * nt] = static_cast<double>(s.td[k]);
+#pragma unroll
+        for (int k = 0; k < SD; k++) a.x[i + k * nt] = static_cast<double>(s.x[k]);
+#pragma unroll
+        for (int k = 0; k < NCP; k++) a.cp[i + k * nt] = static_cast<double>(s.cp[k]);
+#pragma unroll
+        for (int k = 0; k < NA; k++) a.acc[i + k * nt] = static_cast<double>(s.acc[k]);
+#pragma unroll
+        for (int k = 0; k < NIA; k++) a.acci[i + k * nt] = s.acci[k];
+        a.t[i]    = static_cast<double>(s.t);
+        a.didx[i] = s.didx;
+        if (a.status) a.status[i] = s.status;
+        if (a.n_acc) a.n_acc[i] = s.nacc;
+        if (a.n_rej) a.n_rej[i] = s.nrej;
+    }
+};
+
+// DF_STAGE kernel: same launch contract as perthread_kernel<S, RKCK45, double, *>.
+template <class S, int MODE>
+__global__ void __launch_bounds__(MPGOS_MAX_BLOCK) perthread_df_kernel(Args<double> a)
+{
+    using Sv = DfSolver<S, MODE>;
+    constexpr int SD = S::SD, NSP = S::NSP, NISP = S::NISP, NE = S::NE;
+    extern __shared__ __align__(16) unsigned char mpgos_dyn_smem[];
+    __shared__ dfloat s_rtol[SD];
+    __shared__ dfloat s_atol[SD];
+    __shared__ dfloat s_etol[AtLeastOne<NE>::value];
+    __shared__ int s_edir[AtLeastOne<NE>::value];
+    __shared__ dfloat s_sp[AtLeastOne<NSP>::value];
+    int* dyn_spi = reinterpret_cast<int*>(mpgos_dyn_smem + sizeof(double) * NSP);
+
+    for (int k = threadIdx.x; k < SD; k += blockDim.x) {
+        s_rtol[k] = dfloat(a.rtol[k]);
+        s_atol[k] = dfloat(a.atol[k]);
+    }
+    for (int k = threadIdx.x; k < NE; k += blockDim.x) {
+        s_etol[k] = dfloat(a.etol[k]);
+        s_edir[k] = a.edir[k];
+    }
+    for (int k = threadIdx.x; k < NSP; k += blockDim.x) s_sp[k] = dfloat(a.sp[k]);
+    if (a.prefer_shared)
+        for (int k = threadIdx.x; k < NISP; k += blockDim.x) dyn_spi[k] = a.spi[k];
+    __syncthreads();
+
+    DfStaged<S> g;
+    g.sp   = s_sp;
+    g.spi  = a.prefer_shared ? dyn_spi : const_cast<int*>(a.spi);
+    g.rtol = s_rtol;
+    g.atol = s_atol;
+    g.etol = s_etol;
+    g.edir = s_edir;
+
+    DfOptions o;
+    o.initial_dt   = dfloat(a.o.initial_dt);
+    o.max_dt       = dfloat(a.o.max_dt);
+    o.min_dt       = dfloat(a.o.min_dt);
+    o.min_dt_guard = dfloat(a.o.min_dt_guard);
+    o.dense_min_dt = dfloat(a.o.dense_min_dt);
+    o.grow         = static_cast<float>(a.o.grow);
+    o.shrink       = static_cast<float>(a.o.shrink);
+    o.ndo          = a.o.ndo;
+    o.dense_freq   = a.o.dense_freq;
+    o.max_attempts = a.o.max_attempts;
+
+    const long long total = static_cast<long long>(gridDim.x) * blockDim.x;
+    long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= a.n_active) return;
+
+    typename Sv::Inst s;
+    Sv::begin(s, i, a, g, o);
+    while (true) {
+        if (s.terminate) {
+            Sv::end(s, a, g);
+            i = Solver<S, MPGOS_RKCK45, double, MODE>::next_index(a, total);
+            if (i >= a.n_active) break;
+            Sv::begin(s, i, a, g, o);
+        }
+        Sv::attempt(s, a, g, o);
+    }
+}
+
+}  // namespace pt
+}  // namespace mpgos

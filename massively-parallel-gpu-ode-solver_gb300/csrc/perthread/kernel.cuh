@@ -408,6 +408,14 @@ __global__ void __launch_bounds__(MPGOS_MAX_BLOCK) perthread_kernel(Args<P> a)
     }
 }
 
+}  // namespace pt
+}  // namespace mpgos
+
+#include "df_solver.cuh"
+
+namespace mpgos {
+namespace pt {
+
 // ---------------------------------------------------------------------------
 // Kernel table: the launch side of the plugin ABI (mpgos_pt_kernels in mpgos.h).
 // ---------------------------------------------------------------------------
@@ -459,7 +467,8 @@ template <class S, int ALG, class P>
 struct KernelTable {
     static constexpr bool DOUBLE_ADAPTIVE = sizeof(P) == 8 && ALG == MPGOS_RKCK45;
     static constexpr int MODES =
-        MPGOS_MODE_PERSISTENT | (DOUBLE_ADAPTIVE ? (MPGOS_MODE_FAST_CONTROL | MPGOS_MODE_FP32_STAGE) : 0);
+        MPGOS_MODE_PERSISTENT |
+        (DOUBLE_ADAPTIVE ? (MPGOS_MODE_FAST_CONTROL | MPGOS_MODE_FP32_STAGE | MPGOS_MODE_DF_STAGE) : 0);
 
     // Modes a table can run; the runtime only asks for these.
     static void* kernel_for(int mode)
@@ -475,6 +484,10 @@ struct KernelTable {
                 case 3: return reinterpret_cast<void*>(&perthread_kernel<S, ALG, P, 3>);
                 case 5: return reinterpret_cast<void*>(&perthread_kernel<S, ALG, P, 5>);
                 case 7: return reinterpret_cast<void*>(&perthread_kernel<S, ALG, P, 7>);
+                case MPGOS_MODE_DF_STAGE: return reinterpret_cast<void*>(&perthread_df_kernel<S, MPGOS_MODE_DF_STAGE>);
+                case MPGOS_MODE_DF_STAGE | MPGOS_MODE_PERSISTENT:
+                    return reinterpret_cast<void*>(
+                        &perthread_df_kernel<S, MPGOS_MODE_DF_STAGE | MPGOS_MODE_PERSISTENT>);
                 default: break;
             }
         }

@@ -170,7 +170,7 @@ __device__ __forceinline__ void step_rkck45(int tid, int nt, P t, P dt, P* x, P*
               static_cast<P>(0.0 - 277.0 / 14336.0) * k5[i] +
               static_cast<P>(512.0 / 1771.0 - 1.0 / 4.0) * k6[i];
         err[i] = dt * abs(e) + 1e-18;
-        if (BITCHECK) {
+        if constexpr (BITCHECK) {
             if (!finite_bits(xn[i]) || !finite_bits(err[i])) finite = 0;
         } else {
             if ((isfinite(xn[i]) == 0) || (isfinite(err[i]) == 0)) finite = 0;

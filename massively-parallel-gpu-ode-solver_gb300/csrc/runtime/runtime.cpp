@@ -217,6 +217,7 @@ size_t dynamic_smem(const mpgos_pt_solver* s)
 int32_t effective_mode(const mpgos_pt_solver* s, int32_t mode)
 {
     int32_t m = mode & (s->shape.modes | MPGOS_MODE_PERSISTENT);
+    if (m & MPGOS_MODE_DF_STAGE) return MPGOS_MODE_DF_STAGE | (m & MPGOS_MODE_PERSISTENT);
     if (m & MPGOS_MODE_FP32_STAGE) m |= MPGOS_MODE_FAST_CONTROL;  // compiled together
     return m;
 }
@@ -487,11 +488,17 @@ MPGOS_EXPORT int mpgos_pt_set_option(mpgos_pt_solver* s, int32_t option, int32_t
             break;
         case MPGOS_KERNEL_MODE: {
             const int32_t m = static_cast<int32_t>(value);
-            if (m < 0 || m > 7 || m != value) return fail(MPGOS_ERR_ARGUMENT, "kernel mode %g outside 0..7", value);
+            if (m < 0 || m > 23 || (m & 8) || m != value)
+                return fail(MPGOS_ERR_ARGUMENT, "kernel mode %g is not a set of MPGOS_MODE_* bits", value);
             // FAST_CONTROL only changes the adaptive FP64 controller and is a
-            // no-op elsewhere; FP32_STAGE changes the arithmetic and must exist.
+            // no-op elsewhere; FP32_STAGE and DF_STAGE change the arithmetic
+            // and must exist.
             if ((m & MPGOS_MODE_FP32_STAGE) && !(s->shape.modes & MPGOS_MODE_FP32_STAGE))
                 return fail(MPGOS_ERR_UNSUPPORTED, "FP32_STAGE mode not compiled for this table (modes 0x%x)", s->shape.modes);
+            if ((m & MPGOS_MODE_DF_STAGE) && !(s->shape.modes & MPGOS_MODE_DF_STAGE))
+                return fail(MPGOS_ERR_UNSUPPORTED, "DF_STAGE mode not compiled for this table (modes 0x%x)", s->shape.modes);
+            if ((m & MPGOS_MODE_DF_STAGE) && (m & MPGOS_MODE_FP32_STAGE))
+                return fail(MPGOS_ERR_ARGUMENT, "DF_STAGE and FP32_STAGE are exclusive");
             s->mode = m;
             break;
         }
@@ -744,13 +751,17 @@ MPGOS_EXPORT int mpgos_pt_timer_stop(mpgos_pt_solver* s, float* ms)
     return MPGOS_OK;
 }
 
-MPGOS_EXPORT int mpgos_pt_autotune(mpgos_pt_solver* s, int32_t fast_control, const char* cache_path)
+MPGOS_EXPORT int mpgos_pt_autotune(mpgos_pt_solver* s, int32_t arithmetic, const char* cache_path)
 {
     int rc = check_solver(s);
     if (rc) return rc;
     if (s->n_active <= 0) return MPGOS_OK;
     MPGOS_CUDA(cudaSetDevice(s->device));
-    const int32_t base = (fast_control && (s->shape.modes & MPGOS_MODE_FAST_CONTROL)) ? MPGOS_MODE_FAST_CONTROL : 0;
+    int32_t base = 0;
+    if ((arithmetic & MPGOS_MODE_DF_STAGE) && (s->shape.modes & MPGOS_MODE_DF_STAGE))
+        base = MPGOS_MODE_DF_STAGE;
+    else if (arithmetic && (s->shape.modes & MPGOS_MODE_FAST_CONTROL))
+        base = MPGOS_MODE_FAST_CONTROL;
 
     std::ostringstream key;
     key << s->k->name << "/sd" << s->shape.sd << "/alg" << s->shape.algorithm << "/p" << s->shape.precision_bytes

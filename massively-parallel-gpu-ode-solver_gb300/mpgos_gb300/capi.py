@@ -69,6 +69,7 @@ MODE_PLAIN = 0
 MODE_FAST_CONTROL = 1
 MODE_PERSISTENT = 2
 MODE_FP32_STAGE = 4
+MODE_DF_STAGE = 16
 MODE_CHOSEN = MODE_FAST_CONTROL | MODE_PERSISTENT
 
 INSTANCE_OK = 0

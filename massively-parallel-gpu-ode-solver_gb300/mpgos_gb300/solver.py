@@ -243,9 +243,11 @@ class ProblemSolver:
         capi.check(self._lib.mpgos_pt_timer_stop(self._h, C.byref(ms)))
         return float(ms.value)
 
-    def autotune(self, fast_control: bool = True, cache_path: str | None = None):
-        capi.check(self._lib.mpgos_pt_autotune(self._h, int(bool(fast_control)),
-                                               cache_path.encode() if cache_path else None))
+    def autotune(self, fast_control: bool = True, cache_path: str | None = None, arithmetic: int | None = None):
+        """Pick block size and mapping by timing; ``arithmetic`` (a MPGOS_MODE_*
+        value: 0, MODE_FAST_CONTROL or MODE_DF_STAGE) overrides ``fast_control``."""
+        arith = int(bool(fast_control)) if arithmetic is None else int(arithmetic)
+        capi.check(self._lib.mpgos_pt_autotune(self._h, arith, cache_path.encode() if cache_path else None))
         return self.launch_config()
 
     def checkpoint_save(self):

@@ -366,3 +366,50 @@ def run_gpu(case: Case, mode: int = 0, block: int | None = None, graph: bool = F
             for _ in range(case.phases):
                 s.Solve()
         return read_results(s)
+
+
+def _main(argv=None) -> int:
+    """Integrate one synthetic ensemble on the GPU and print a summary line:
+    ``python -m mpgos_gb300.workloads --case lorenz --nt 262144 --mode 18
+    --block 128 --launches 2`` (the command the kernel profiles are taken
+    with: every launch is a full integration from the initial state)."""
+    import argparse
+    import json
+    import time
+
+    ap = argparse.ArgumentParser(prog="python -m mpgos_gb300.workloads")
+    ap.add_argument("--case", default="lorenz", choices=["lorenz", "keller_miksis", "duffing_param", "duffing_rk4"])
+    ap.add_argument("--nt", type=int, default=1 << 18)
+    ap.add_argument("--mode", type=int, default=0, help="MPGOS_MODE_* bits")
+    ap.add_argument("--block", type=int, default=128)
+    ap.add_argument("--launches", type=int, default=1)
+    a = ap.parse_args(argv)
+    if a.case == "lorenz":
+        case = lorenz_case(nt=a.nt)
+    elif a.case == "keller_miksis":
+        side = max(1, int(round(math.sqrt(a.nt))))
+        case = keller_miksis_case(n_amp=side, n_freq=max(1, a.nt // side))
+    elif a.case == "duffing_param":
+        case = duffing_param_case(nt=a.nt)
+    else:
+        case = duffing_rk4_case(nt=a.nt)
+    from .solver import Variable
+    with load_solver(case, mode=a.mode, block=a.block) as s:
+        s.checkpoint_save()
+        times = []
+        for _ in range(a.launches):
+            s.checkpoint_restore()
+            s.SynchroniseDevice()
+            t0 = time.perf_counter()
+            s.Solve()
+            s.SynchroniseDevice()
+            times.append(time.perf_counter() - t0)
+        res = read_results(s)
+    print(json.dumps({"case": a.case, "nt": case.nt, "mode": a.mode, "block": a.block, "launches": a.launches,
+                      "accepted": int(res["nacc"].sum()), "rejected": int(res["nrej"].sum()),
+                      "status_max": int(res["status"].max()), "wall_s_last": times[-1]}))
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(_main())

@@ -1,0 +1,44 @@
+// CPU check of the double-float arithmetic in csrc/perthread/dfloat.cuh
+// (compiled for the host by tests/test_dfloat_cpu.py with -ffp-contract=off).
+// Random operands of mixed sign and magnitude; each operation is compared with
+// the same operation in long double on the exact values hi + lo of the inputs.
+// Prints one line per operation: name, max relative error (to the larger of
+// the result and the operands' magnitude, the bound of a "sloppy" add).
+#include <cmath>
+#include <cstdio>
+#include <random>
+
+#include "dfloat.cuh"
+
+using mpgos::df::dfloat;
+
+static long double val(dfloat a) { return (long double)a.hi + (long double)a.lo; }
+
+int main()
+{
+    std::mt19937_64 rng(12345);
+    std::uniform_real_distribution<double> u(-1.0, 1.0), e(-8.0, 8.0);
+    auto draw = [&]() { return dfloat(u(rng) * std::pow(2.0, std::floor(e(rng)))); };
+    double m_add = 0, m_mul = 0, m_div = 0, m_sqrt = 0, m_cvt = 0, m_cmp = 0, m_norm = 0;
+    for (int n = 0; n < 200000; n++) {
+        const dfloat a = draw(), b = draw();
+        const long double A = val(a), B = val(b);
+        const long double scale_add = std::fabs(A) + std::fabs(B);
+        const dfloat s = a + b, p = a * b, q = a / b, r = mpgos::df::sqrt(mpgos::df::abs(a));
+        m_add = std::fmax(m_add, (double)(std::fabs(val(s) - (A + B)) / scale_add));
+        m_mul = std::fmax(m_mul, (double)(std::fabs(val(p) - A * B) / std::fabs(A * B)));
+        m_div = std::fmax(m_div, (double)(std::fabs(val(q) - A / B) / std::fabs(A / B)));
+        m_sqrt = std::fmax(m_sqrt, (double)(std::fabs(val(r) - std::sqrt(std::fabs(A))) / std::sqrt(std::fabs(A))));
+        // normalisation: |lo| <= ulp(hi) / 2 after every operation
+        for (dfloat z : {s, p, q, r})
+            if (z.hi != 0.0f) m_norm = std::fmax(m_norm, std::fabs(z.lo) / (std::nextafter(std::fabs(z.hi), INFINITY) - std::fabs(z.hi)));
+        // conversion from double keeps 48 bits
+        const double d = u(rng) * std::pow(2.0, std::floor(e(rng)));
+        m_cvt = std::fmax(m_cvt, std::fabs((double)dfloat(d) - d) / std::fabs(d));
+        // comparisons agree with the exact values
+        if (((a < b) != (A < B)) || ((a > b) != (A > B)) || ((a <= b) != (A <= B))) m_cmp = 1;
+    }
+    std::printf("add %.3e\nmul %.3e\ndiv %.3e\nsqrt %.3e\ncvt %.3e\ncmp %.0f\nnorm %.3f\n", m_add, m_mul, m_div, m_sqrt,
+                m_cvt, m_cmp, m_norm);
+    return 0;
+}

@@ -85,9 +85,9 @@ def perturbation_spread(case, rel=0.0, key=None, tol_rel=0.0):
     multiply-adds contracted into fused multiply-adds (the rounding change
     between host and GPU arithmetic, which event refinements and impacts can
     amplify far beyond one ulp); and, with ``tol_rel`` > 0, the tolerances
-    moved by ``tol_rel`` relative (which moves every step size by about
-    tol_rel / 5: the step-grid shift of a step-size factor rounded
-    differently). Returns (|difference| per float output, the largest over
+    moved up and down by ``tol_rel`` relative (which moves every step size by
+    about tol_rel / 5, the step-grid shift of a step-size factor rounded
+    differently, and flips every accept/reject decision within that margin). Returns (|difference| per float output, the largest over
     the variants; mask of instances whose integer outputs no variant changed).
     Cached under ``key``."""
     from oracle import oracle as O
@@ -100,10 +100,11 @@ def perturbation_spread(case, rel=0.0, key=None, tol_rel=0.0):
     pert.arrays["x"] = np.nextafter(x, np.inf) if rel == 0.0 else x * (1.0 + rel) + (x == 0) * rel
     runs = [O.run_oracle(pert), O.run_oracle(case, fma=True)]
     if tol_rel > 0.0:
-        pt = case.copy()
-        pt.rtol = pt.rtol * (1.0 + tol_rel)
-        pt.atol = pt.atol * (1.0 + tol_rel)
-        runs.append(O.run_oracle(pt))
+        for sign in (1.0, -1.0):
+            pt = case.copy()
+            pt.rtol = pt.rtol * (1.0 + sign * tol_rel)
+            pt.atol = pt.atol * (1.0 + sign * tol_rel)
+            runs.append(O.run_oracle(pt))
     spread = {k: np.max([np.abs(np.asarray(m[k], np.float64) - np.asarray(base[k], np.float64)) for m in runs], axis=0)
               for k in END_STATE_KEYS + GRID_KEYS if k in base}
     stable = np.ones(case.nt, bool)
@@ -118,8 +119,33 @@ def perturbation_spread(case, rel=0.0, key=None, tol_rel=0.0):
     return out
 
 
+def assert_ints_equal(res, ref, keys, mask, slack=0.0):
+    """Integer outputs equal on the instances of ``mask``. With ``slack`` > 0
+    (a fraction), up to max(1, slack x #mask) instances may differ, each by
+    one unit at most: a mode whose step-size factor is rounded differently
+    from the reference's (FAST_CONTROL, DF_STAGE) takes one step more or
+    fewer where an error estimate lands within that rounding of the
+    tolerance, which no finite set of perturbations of the CPU reference
+    catches every time."""
+    bad = np.zeros(np.shape(mask), bool)
+    for k in keys:
+        if k not in ref:
+            continue
+        a, b = np.asarray(res[k]), np.asarray(ref[k])
+        d = np.abs(a.astype(np.int64) - b.astype(np.int64))
+        d = d.reshape(-1, d.shape[-1]).max(axis=0) if d.ndim > 1 else d
+        if slack <= 0.0:
+            np.testing.assert_array_equal(a[..., mask], b[..., mask], err_msg=k)
+            continue
+        assert np.all(d[mask] <= 1), f"{k}: integer outputs differ by more than one on stable instances"
+        bad |= (d > 0) & mask
+    if slack > 0.0:
+        limit = max(1, int(slack * int(np.sum(mask))))
+        assert int(bad.sum()) <= limit, f"{int(bad.sum())} stable instances differ in integer outputs (limit {limit})"
+
+
 def assert_cpu_parity(res, ref, case, key, rel=0.0, rtol=1e-9, grid_rtol=1e-4, factor=1e3, min_stable=0.5,
-                      tol_rel=0.0):
+                      tol_rel=0.0, int_slack=0.0):
     """GPU result vs a CPU reference result of the same inputs.
 
     Every float element must agree within the bar of ``scaled_close`` or
@@ -140,9 +166,7 @@ def assert_cpu_parity(res, ref, case, key, rel=0.0, rtol=1e-9, grid_rtol=1e-4, f
             bad = np.argwhere(~ok)[:3]
             raise AssertionError(f"{k}: {int((~ok).sum())} elements outside the bar, e.g. at {bad.tolist()}: "
                                  f"{a[tuple(bad[0])]!r} vs {b[tuple(bad[0])]!r} (spread {spread[k][tuple(bad[0])]!r})")
-    for k in INT_KEYS:
-        if k in ref:
-            np.testing.assert_array_equal(np.asarray(res[k])[..., stable], np.asarray(ref[k])[..., stable], err_msg=k)
+    assert_ints_equal(res, ref, INT_KEYS, stable, int_slack)
 
 
 def sensitive_instances(case, rtol=1e-10):

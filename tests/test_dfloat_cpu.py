@@ -1,0 +1,30 @@
+"""CPU test of the double-float arithmetic of the DF_STAGE mode
+(csrc/perthread/dfloat.cuh), built for the host from the same header."""
+import subprocess
+
+import pytest
+
+from tests.conftest import REPO
+
+HEADER_DIR = REPO / "massively-parallel-gpu-ode-solver_gb300" / "csrc" / "perthread"
+
+
+@pytest.fixture(scope="module")
+def errors(tmp_path_factory):
+    exe = tmp_path_factory.mktemp("dfloat") / "dfloat_check"
+    subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", f"-I{HEADER_DIR}",
+                    str(REPO / "tests" / "dfloat_check.cpp"), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout
+    return {k: float(v) for k, v in (line.split() for line in out.strip().splitlines())}
+
+
+def test_double_float_precision(errors):
+    # ~48 significant bits: 2^-46 = 1.4e-14 covers every operation's bound
+    for op in ("add", "mul", "div", "sqrt"):
+        assert errors[op] < 1.5e-14, (op, errors[op])
+    assert errors["cvt"] < 4e-15          # double -> double-float keeps 48 bits (2^-48)
+
+
+def test_double_float_invariants(errors):
+    assert errors["cmp"] == 0             # comparisons order like the exact values
+    assert errors["norm"] <= 0.5          # |lo| <= ulp(hi) / 2 after every operation
