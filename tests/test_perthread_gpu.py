@@ -197,7 +197,7 @@ def test_lorenz_full_size_df_stage(native_libs, oracle_libs):
     calm = scaled_close(moved["x"], ref["x"], 1e-10).all(axis=0)
     assert calm.mean() > 0.95, calm.mean()
     got = {k: v[..., idx] for k, v in df.items() if np.ndim(v) and np.shape(v)[-1] == case.nt}
-    assert_close(got, ref, mask=calm, keys=("x", "t"))
+    assert_close(got, ref, mask=calm, keys=("x", "t"), ints=False)
     assert_ints_equal(got, ref, ("nacc", "acci"), calm, _int_slack("df"))
 
 
