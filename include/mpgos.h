@@ -353,7 +353,7 @@ enum mpgos_cb_option {
     MPGOS_CB_DENSE_OUTPUT_MINIMUM_TIME_STEP = 11, MPGOS_CB_SHARED_GLOBAL_VARIABLES = 12,
     MPGOS_CB_SHARED_COUPLING_MATRICES = 13,
     /* extensions */
-    MPGOS_CB_KERNEL_MODE = 32,          /* 0 or MPGOS_MODE_PERSISTENT       */
+    MPGOS_CB_KERNEL_MODE = 32,          /* PERSISTENT and/or DF_STAGE bits  */
     MPGOS_CB_MAXIMUM_ATTEMPTS = 33,     /* step attempts per system         */
     MPGOS_CB_WARPS_PER_BLOCK = 34       /* systems per CTA (one per warp)   */
 };

@@ -36,7 +36,10 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 #include "../perthread/numerics.cuh"
+#include "../perthread/dfloat.cuh"
 
 #ifndef MPGOS_CB_MAX_BLOCK
 #define MPGOS_CB_MAX_BLOCK 256
@@ -45,8 +48,22 @@
 namespace mpgos {
 namespace cb {
 
+using df::dfloat;
 using pt::AtLeastOne;
 using pt::Options;
+
+// Compute precision P and the precision of the arrays in HBM: DF_STAGE
+// integrates in double-float (dfloat.cuh) on FP64 arrays.
+template <class P>
+struct StorageOf {
+    using type = P;
+};
+template <>
+struct StorageOf<dfloat> {
+    using type = double;
+};
+template <class P>
+constexpr bool IS_DF = std::is_same<P, dfloat>::value;
 
 template <int UPS_, int UD_, int NC_, int CBW_, int CCI_, int NUP_, int NSP_, int NGP_, int NIGP_, int NUA_,
           int NIUA_, int NSA_, int NISA_, int NE_>
@@ -102,6 +119,7 @@ struct Args {
 template <class S, class P>
 struct WarpSlot {
     P td[2];
+    typename StorageOf<P>::type td_in[2];  // the time domain as loaded from HBM
     P t, dt, newdt, dense_next, evdt, ratio;
     P sp[AtLeastOne<S::NSP>::value];
     P sacc[AtLeastOne<S::NSA>::value];
@@ -119,10 +137,27 @@ __host__ __device__ constexpr size_t block_smem_bytes()
 
 // Coupling value of coupling i for unit `unit`: ComputeCouplingValue of
 // CoupledSystems_PerBlock_ExplicitRungeKutta_Steppers.cuh:2552-2633.
+// Double-float dot product term: s + m * c accumulated as an unnormalised
+// pair (sum of leading floats by two_sum, every rounding error and the
+// cross products into the trailing float); normalised once at the end.
+__device__ __forceinline__ void df_dot_acc(float& sh, float& sl, dfloat m, dfloat c)
+{
+    const dfloat p = df::two_prod(m.hi, c.hi);
+    const dfloat t = df::two_sum(sh, p.hi);
+    sh = t.hi;
+    sl = df::f_add(sl, df::f_add(t.lo, df::f_fma(m.hi, c.lo, df::f_fma(m.lo, c.hi, p.lo))));
+}
+
 template <class S, class P>
 __device__ __forceinline__ P coupling_value(const P* M, const WarpSlot<S, P>& w, int unit, int i)
 {
     constexpr int UPS = S::UPS, CBW = S::CBW, CCI = S::CCI;
+    if constexpr (IS_DF<P> && CCI == 0 && CBW == 0) {
+        const int shift = i * UPS * UPS;
+        float sh = 0.0f, sl = 0.0f;
+        for (int col = 0; col < UPS; col++) df_dot_acc(sh, sl, M[unit + col * UPS + shift], w.cpt[col][i]);
+        return df::two_sum(sh, sl);
+    }
     P v = 0;
     if (CCI == 0 && CBW == 0) {
         const int shift = i * UPS * UPS;
@@ -164,6 +199,21 @@ __device__ __forceinline__ P warp_min(P v)
     for (int off = 16; off > 0; off >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, off));
     return v;
 }
+__device__ __forceinline__ dfloat warp_min(dfloat v)
+{
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        const dfloat o(__shfl_xor_sync(0xffffffffu, v.hi, off), __shfl_xor_sync(0xffffffffu, v.lo, off));
+        v = df::fmin(v, o);
+    }
+    return v;
+}
+__device__ __forceinline__ float warp_minf(float v)
+{
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, off));
+    return v;
+}
 
 template <class S, int ALG, class P, int MODE>
 struct Solver {
@@ -171,6 +221,7 @@ struct Solver {
     static constexpr int NE = S::NE, UPL = S::UPL, NSP = S::NSP, NSA = S::NSA, NISA = S::NISA;
     static constexpr bool PERSISTENT = (MODE & MPGOS_MODE_PERSISTENT) != 0;
     using Slot = WarpSlot<S, P>;
+    using SP   = typename StorageOf<P>::type;  // precision of the arrays in HBM
 
     // Registers of the lane's units.
     struct Units {
@@ -319,19 +370,20 @@ struct Solver {
     // Integrate system s with the calling warp: the body of the reference's
     // MultipleSystems_SingleBlockLaunch kernel for one system
     // (CoupledSystmes_PerBlock_Solver.cuh:1575-2211).
-    __device__ static void system(long long s, int lane, Slot& w, const Args<P>& a, const P* gp, const int* igp,
-                                  const P* M, const int* cidx, const P* rtol, const P* atol, const P* etol,
-                                  const int* edir)
+    __device__ static void system(long long s, int lane, Slot& w, const Args<SP>& a, const Options<P>& o,
+                                  const P* gp, const int* igp, const P* M, const int* cidx, const P* rtol,
+                                  const P* atol, const P* etol, const int* edir)
     {
         const long long ns = a.ns, nu = a.ns * UPS;
-        const Options<P>& o = a.o;
         const int sid = static_cast<int>(s);
         Units u;
         // ---- load: system scope into the slot, unit scope into registers
         if (lane == 0) {
-            w.td[0] = a.td[s];
-            w.td[1] = a.td[s + ns];
-            w.t = a.t[s];
+            w.td_in[0] = a.td[s];
+            w.td_in[1] = a.td[s + ns];
+            w.td[0] = P(w.td_in[0]);
+            w.td[1] = P(w.td_in[1]);
+            w.t = P(a.t[s]);
             w.dt = o.initial_dt;
             w.newdt = o.initial_dt;
             w.didx = a.didx[s];
@@ -339,20 +391,20 @@ struct Solver {
             w.skipped = 0;
             w.dense_next = w.t;
         }
-        for (int k = lane; k < NSP; k += 32) w.sp[k] = a.sp[s + k * ns];
-        for (int k = lane; k < NSA; k += 32) w.sacc[k] = a.sacc[s + k * ns];
+        for (int k = lane; k < NSP; k += 32) w.sp[k] = P(a.sp[s + k * ns]);
+        for (int k = lane; k < NSA; k += 32) w.sacc[k] = P(a.sacc[s + k * ns]);
         for (int k = lane; k < NISA; k += 32) w.isacc[k] = a.isacc[s + k * ns];
-        for (int k = lane; k < NC; k += 32) w.cstr[k] = a.cstr[s + k * ns];
+        for (int k = lane; k < NC; k += 32) w.cstr[k] = P(a.cstr[s + k * ns]);
 #pragma unroll
         for (int j = 0; j < UPL; j++) {
             if (!has(lane, j)) continue;
             const long long g = s * UPS + unit_of(lane, j);
 #pragma unroll
-            for (int d = 0; d < UD; d++) u.x[j][d] = a.x[g + d * nu];
+            for (int d = 0; d < UD; d++) u.x[j][d] = P(a.x[g + d * nu]);
 #pragma unroll
-            for (int k = 0; k < NUP; k++) u.up[j][k] = a.up[g + k * nu];
+            for (int k = 0; k < NUP; k++) u.up[j][k] = P(a.up[g + k * nu]);
 #pragma unroll
-            for (int k = 0; k < NUA; k++) u.uacc[j][k] = a.uacc[g + k * nu];
+            for (int k = 0; k < NUA; k++) u.uacc[j][k] = P(a.uacc[g + k * nu]);
 #pragma unroll
             for (int k = 0; k < NIUA; k++) u.iuacc[j][k] = a.iuacc[g + k * nu];
         }
@@ -376,7 +428,7 @@ struct Solver {
                                                              w.isacc);
             __syncwarp();
         }
-        if (o.ndo > 0) dense_store(s, lane, w, u, a, 1, 1);
+        if (o.ndo > 0) dense_store(s, lane, w, u, a, o, 1, 1);
 
         int status = 0, nacc = 0, nrej = 0, terminate = 0;
         long long attempts = 0;
@@ -418,6 +470,38 @@ struct Solver {
                     status |= MPGOS_INSTANCE_NONFINITE;
                 }
                 newdt = o.initial_dt;
+            } else if constexpr (IS_DF<P>) {
+                // DF_STAGE: exact double-float accept test, step factor
+                // 0.8 * (min tol/err)^(1/5 or 1/4) from FP32 logarithms of the
+                // leading floats (relative error ~1e-7), as in the per-thread
+                // DF_STAGE controller.
+                float lr = INFINITY;
+                int lane_update = 1;
+#pragma unroll
+                for (int j = 0; j < UPL; j++) {
+                    if (!has(lane, j)) continue;
+                    for (int d = 0; d < UD; d++) {
+                        const P tol = fmax(rtol[d] * fmax(fabs(xn[j][d]), fabs(u.x[j][d])), atol[d]);
+                        lane_update = lane_update & (err[j][d] < tol);
+                        lr = fminf(lr, __log2f(tol.hi) - __log2f(err[j][d].hi));
+                    }
+                }
+                update = warp_all(lane_update != 0) ? 1 : 0;
+                lr = warp_minf(lr);
+                float q = 0.8f * exp2f(fminf(fmaxf(lr * ((update == 1) ? 0.2f : 0.25f), -120.0f), 120.0f));
+                if (finite == 0) {
+                    q = o.shrink.hi;
+                    update = 0;
+                    if (dt < o.min_dt_guard) {
+                        terminate = 1;
+                        status |= MPGOS_INSTANCE_NONFINITE;
+                    }
+                } else if (dt < o.min_dt_guard) {
+                    update = 1;
+                    status |= MPGOS_INSTANCE_MINIMUM_STEP;
+                }
+                q = fminf(fmaxf(q, o.shrink.hi), o.grow.hi);
+                newdt = fmax(fmin(df::mul_f(dt, q), o.max_dt), o.min_dt);
             } else {
                 P ratio = 1e30;
                 int lane_update = 1;
@@ -497,7 +581,10 @@ struct Solver {
             // ---- accept (CoupledSystmes_PerBlock_Solver.cuh:1975-2075)
             if (update == 1) {
                 nacc++;
-                if (lane == 0) w.t += dt;
+                if (lane == 0) {
+                    if constexpr (IS_DF<P>) w.t = (end_reached == 1) ? w.td[1] : w.t + dt;
+                    else w.t += dt;
+                }
 #pragma unroll
                 for (int j = 0; j < UPL; j++)
 #pragma unroll
@@ -537,7 +624,7 @@ struct Solver {
             } else {
                 nrej++;
             }
-            if (o.ndo > 0) dense_store(s, lane, w, u, a, update, 0, end_reached);
+            if (o.ndo > 0) dense_store(s, lane, w, u, a, o, update, 0, end_reached);
             __syncwarp();
             if (update == 1 && ((end_reached == 1) || (w.udt == 1))) terminate = 1;
             __syncwarp();
@@ -556,32 +643,34 @@ struct Solver {
             if (!has(lane, j)) continue;
             const long long g = s * UPS + unit_of(lane, j);
 #pragma unroll
-            for (int d = 0; d < UD; d++) a.x[g + d * nu] = u.x[j][d];
+            for (int d = 0; d < UD; d++) a.x[g + d * nu] = static_cast<SP>(u.x[j][d]);
 #pragma unroll
-            for (int k = 0; k < NUA; k++) a.uacc[g + k * nu] = u.uacc[j][k];
+            for (int k = 0; k < NUA; k++) a.uacc[g + k * nu] = static_cast<SP>(u.uacc[j][k]);
 #pragma unroll
             for (int k = 0; k < NIUA; k++) a.iuacc[g + k * nu] = u.iuacc[j][k];
         }
         if (lane == 0) {
-            a.t[s] = w.t;
-            a.td[s] = w.td[0];
-            a.td[s + ns] = w.td[1];
+            // DF_STAGE: values the run left equal to a time-domain bound are
+            // written as the FP64 bound itself (a double-float holds 48 of its
+            // 53 bits, so the round trip alone would move it)
+            a.t[s] = (w.t == P(w.td_in[1])) ? w.td_in[1] : static_cast<SP>(w.t);
+            a.td[s] = (w.td[0] == P(w.td_in[0])) ? w.td_in[0] : static_cast<SP>(w.td[0]);
+            a.td[s + ns] = (w.td[1] == P(w.td_in[1])) ? w.td_in[1] : static_cast<SP>(w.td[1]);
             a.didx[s] = w.didx;
             if (a.status) a.status[s] = status;
             if (a.n_acc) a.n_acc[s] = nacc;
             if (a.n_rej) a.n_rej[s] = nrej;
         }
-        for (int k = lane; k < NSA; k += 32) a.sacc[s + k * ns] = w.sacc[k];
+        for (int k = lane; k < NSA; k += 32) a.sacc[s + k * ns] = static_cast<SP>(w.sacc[k]);
         for (int k = lane; k < NISA; k += 32) a.isacc[s + k * ns] = w.isacc[k];
         __syncwarp();
     }
 
     // Dense output of one system (CoupledSystems_PerBlock_DenseOutput.cuh:210-312).
     // initial = 1: the unconditional store before the loop.
-    __device__ static void dense_store(long long s, int lane, Slot& w, const Units& u, const Args<P>& a, int update,
-                                       int initial, int end_reached = 0)
+    __device__ static void dense_store(long long s, int lane, Slot& w, const Units& u, const Args<SP>& a,
+                                       const Options<P>& o, int update, int initial, int end_reached = 0)
     {
-        const Options<P>& o = a.o;
         int store;
         if (initial) {
             store = 1;
@@ -599,9 +688,9 @@ struct Solver {
                 const long long g = s * UPS + unit_of(lane, j);
 #pragma unroll
                 for (int d = 0; d < UD; d++)
-                    a.dstate[g + d * nu + static_cast<long long>(w.didx) * nu * UD] = u.x[j][d];
+                    a.dstate[g + d * nu + static_cast<long long>(w.didx) * nu * UD] = static_cast<SP>(u.x[j][d]);
             }
-            if (lane == 0) a.dtime[s + static_cast<long long>(w.didx) * a.ns] = w.t;
+            if (lane == 0) a.dtime[s + static_cast<long long>(w.didx) * a.ns] = static_cast<SP>(w.t);
         }
         __syncwarp();
         if (lane == 0) {
@@ -634,7 +723,7 @@ __host__ __device__ constexpr size_t dynamic_smem_bytes(int warps, int shared_gl
 }
 
 template <class S, int ALG, class P, int MODE>
-__global__ void __launch_bounds__(MPGOS_CB_MAX_BLOCK) coupled_kernel(Args<P> a)
+__global__ void __launch_bounds__(MPGOS_CB_MAX_BLOCK) coupled_kernel(Args<typename StorageOf<P>::type> a)
 {
     using Sv = Solver<S, ALG, P, MODE>;
     constexpr int UD = S::UD, NE = S::NE, NC = S::NC, NGP = S::NGP, NIGP = S::NIGP;
@@ -646,7 +735,11 @@ __global__ void __launch_bounds__(MPGOS_CB_MAX_BLOCK) coupled_kernel(Args<P> a)
     __shared__ int s_edir[AtLeastOne<NE>::value];
     __shared__ int s_cidx[AtLeastOne<NC>::value];
 
-    const int sg = a.shared_global, sc = a.shared_coupling;
+    // DF_STAGE converts every FP64 array it reads more than once into shared
+    // memory, so its layout always holds the global parameters and the
+    // coupling matrices (the runtime sizes the allocation accordingly)
+    constexpr bool CONVERT = IS_DF<P>;
+    const int sg = CONVERT ? 1 : a.shared_global, sc = CONVERT ? 1 : a.shared_coupling;
     P* dyn_gp = reinterpret_cast<P*>(mpgos_cb_smem);
     P* dyn_m = dyn_gp + (sg ? NGP : 0);
     int* dyn_igp = reinterpret_cast<int*>(dyn_m + (sc ? NC * S::MAT : 0));
@@ -655,26 +748,46 @@ __global__ void __launch_bounds__(MPGOS_CB_MAX_BLOCK) coupled_kernel(Args<P> a)
 
     for (int k = threadIdx.x; k < UD; k += blockDim.x) {
         if (ADAPTIVE) {
-            s_rtol[k] = a.rtol[k];
-            s_atol[k] = a.atol[k];
+            s_rtol[k] = P(a.rtol[k]);
+            s_atol[k] = P(a.atol[k]);
         }
     }
     for (int k = threadIdx.x; k < NE; k += blockDim.x) {
-        s_etol[k] = a.etol[k];
+        s_etol[k] = P(a.etol[k]);
         s_edir[k] = a.edir[k];
     }
     for (int k = threadIdx.x; k < NC; k += blockDim.x) s_cidx[k] = a.cidx[k];
     if (sg) {
-        for (int k = threadIdx.x; k < NGP; k += blockDim.x) dyn_gp[k] = a.gp[k];
+        for (int k = threadIdx.x; k < NGP; k += blockDim.x) dyn_gp[k] = P(a.gp[k]);
         for (int k = threadIdx.x; k < NIGP; k += blockDim.x) dyn_igp[k] = a.igp[k];
     }
     if (sc)
-        for (int k = threadIdx.x; k < NC * S::MAT; k += blockDim.x) dyn_m[k] = a.cmat[k];
+        for (int k = threadIdx.x; k < NC * S::MAT; k += blockDim.x) dyn_m[k] = P(a.cmat[k]);
     __syncthreads();
 
-    const P* gp = sg ? dyn_gp : a.gp;
-    const int* igp = sg ? dyn_igp : a.igp;
-    const P* M = sc ? dyn_m : a.cmat;
+    const P* gp;
+    const int* igp;
+    const P* M;
+    if constexpr (CONVERT) {
+        gp = dyn_gp;
+        igp = dyn_igp;
+        M = dyn_m;
+    } else {
+        gp = sg ? dyn_gp : reinterpret_cast<const P*>(a.gp);
+        igp = sg ? dyn_igp : a.igp;
+        M = sc ? dyn_m : reinterpret_cast<const P*>(a.cmat);
+    }
+    Options<P> o;
+    o.initial_dt   = P(a.o.initial_dt);
+    o.max_dt       = P(a.o.max_dt);
+    o.min_dt       = P(a.o.min_dt);
+    o.grow         = P(a.o.grow);
+    o.shrink       = P(a.o.shrink);
+    o.dense_min_dt = P(a.o.dense_min_dt);
+    o.min_dt_guard = P(a.o.min_dt_guard);
+    o.dense_freq   = a.o.dense_freq;
+    o.ndo          = a.o.ndo;
+    o.max_attempts = a.o.max_attempts;
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     const int warps = blockDim.x >> 5;
@@ -683,7 +796,7 @@ __global__ void __launch_bounds__(MPGOS_CB_MAX_BLOCK) coupled_kernel(Args<P> a)
     long long s = static_cast<long long>(blockIdx.x) * warps + warp;
     const long long total = static_cast<long long>(gridDim.x) * warps;
     while (s < a.n_active) {
-        Sv::system(s, lane, w, a, gp, igp, M, s_cidx, s_rtol, s_atol, s_etol, s_edir);
+        Sv::system(s, lane, w, a, o, gp, igp, M, s_cidx, s_rtol, s_atol, s_etol, s_edir);
         if (!Sv::PERSISTENT) break;
         unsigned next = 0;
         if (lane == 0) next = atomicAdd(a.work, 1u);
@@ -741,8 +854,16 @@ Args<P> make_args(const mpgos_cb_launch& L)
 
 template <class S, int ALG, class P>
 struct KernelTable {
+    static constexpr bool HAS_DF = std::is_same<P, double>::value;
+
     static void* kernel_for(int mode)
     {
+        if constexpr (HAS_DF) {
+            if (mode & MPGOS_MODE_DF_STAGE)
+                return (mode & MPGOS_MODE_PERSISTENT)
+                           ? reinterpret_cast<void*>(&coupled_kernel<S, ALG, dfloat, MPGOS_MODE_PERSISTENT>)
+                           : reinterpret_cast<void*>(&coupled_kernel<S, ALG, dfloat, 0>);
+        }
         return (mode & MPGOS_MODE_PERSISTENT) ? reinterpret_cast<void*>(&coupled_kernel<S, ALG, P, MPGOS_MODE_PERSISTENT>)
                                               : reinterpret_cast<void*>(&coupled_kernel<S, ALG, P, 0>);
     }

@@ -51,9 +51,18 @@ struct DfInstance {
     int acci[AtLeastOne<S::NIA>::value];
     dfloat ga[AtLeastOne<S::NE>::value];
     dfloat t, dt, new_dt, dense_next;
+    double td64[2];  // the FP64 time domain as loaded (written back unless a hook changed it)
     int didx, skipped, terminate, udt, status, nacc, nrej;
     long long attempts;
 };
+
+// FP64 value of a double-float that started as the FP64 value `orig`: `orig`
+// itself while unchanged (a double-float keeps 48 of its 53 bits, so the round
+// trip alone would move it), else the double-float's value.
+__device__ __forceinline__ double df_to_double(dfloat v, double orig)
+{
+    return (v == dfloat(orig)) ? orig : static_cast<double>(v);
+}
 
 template <class S>
 struct DfStaged {
@@ -134,7 +143,10 @@ struct DfSolver {
         const long long nt = a.nt;
         s.i = i;
 #pragma unroll
-        for (int k = 0; k < 2; k++) s.td[k] = dfloat(a.td[i + k * nt]);
+        for (int k = 0; k < 2; k++) {
+            s.td64[k] = a.td[i + k * nt];
+            s.td[k]   = dfloat(s.td64[k]);
+        }
 #pragma unroll
         for (int k = 0; k < SD; k++) s.x[k] = dfloat(a.x[i + k * nt]);
 #pragma unroll
@@ -227,7 +239,7 @@ struct DfSolver {
         const int ti = static_cast<int>(i), nti = static_cast<int>(nt);
         PerThread_Finalization(ti, nti, s.didx, s.t, s.dt, s.td, s.x, s.cp, g.sp, g.spi, s.acc, s.acci);
 #pragma unroll
-        for (int k = 0; k < 2; k++) a.td[i + k * nt] = static_cast<double>(s.td[k]);
+        for (int k = 0; k < 2; k++) a.td[i + k * nt] = df_to_double(s.td[k], s.td64[k]);
 #pragma unroll
         for (int k = 0; k < SD; k++) a.x[i + k * nt] = static_cast<double>(s.x[k]);
 #pragma unroll
@@ -236,7 +248,7 @@ struct DfSolver {
         for (int k = 0; k < NA; k++) a.acc[i + k * nt] = static_cast<double>(s.acc[k]);
 #pragma unroll
         for (int k = 0; k < NIA; k++) a.acci[i + k * nt] = s.acci[k];
-        a.t[i]    = static_cast<double>(s.t);
+        a.t[i]    = df_to_double(s.t, s.td64[1]);  // ends exactly on the FP64 upper bound
         a.didx[i] = s.didx;
         if (a.status) a.status[i] = s.status;
         if (a.n_acc) a.n_acc[i] = s.nacc;

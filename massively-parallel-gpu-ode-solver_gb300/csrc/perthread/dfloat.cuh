@@ -16,9 +16,9 @@
 //   mul             double-float multiply with FMA (same source)
 //   div             two long-division correction steps on a float quotient
 //   sqrt            Karp & Markstein 1997 (Newton corrections from rsqrt)
-// Transcendental functions (cos, sin, exp, log, pow, sincospi) evaluate in
-// FP64 through CUDA's double functions and round back: hooks call them once
-// per right-hand side, so they cost little next to the stage arithmetic.
+// sin, cos and sincospi run on the FP32 pipe too (Cody-Waite reduction and
+// Taylor series, below); exp, log and pow evaluate in FP64 through CUDA's
+// double functions and round back (one FP64 evaluation per call).
 //
 // Hook code templated on its precision (the reference's
 // `template <class Precision> __device__ void PerThread_OdeFunction(...)`)
@@ -72,6 +72,14 @@ MPGOS_DF_HD float f_fma(float a, float b, float c)
     return __fmaf_rn(a, b, c);
 #else
     return std::fma(a, b, c);
+#endif
+}
+MPGOS_DF_HD float f_rint(float a)
+{
+#if defined(__CUDA_ARCH__)
+    return rintf(a);
+#else
+    return std::nearbyint(a);
 #endif
 }
 MPGOS_DF_HD float f_rcp(float a)
@@ -188,8 +196,84 @@ MPGOS_DF_HD dfloat sqrt(dfloat a)
     return s + dfloat(f_mul((a - s * s).hi, f_mul(x, 0.5f)));
 }
 
-MPGOS_DF_HD dfloat cos(dfloat a) { return dfloat(std::cos(static_cast<double>(a))); }
-MPGOS_DF_HD dfloat sin(dfloat a) { return dfloat(std::sin(static_cast<double>(a))); }
+// ---- sine and cosine on the FP32 pipe --------------------------------------------
+// Cody & Waite (1980) reduction x = k pi/2 + r with pi/2 split into three
+// floats (each k * P_i exact as a double-float; |k| < 2^22), then the Taylor
+// series of sin and cos on |r| <= pi/4: terms through r^9 / r^8 in
+// double-float by Horner's rule, the tail (r^11.. r^17 / r^10.. r^16, below
+// 2e-8 in size) in float. Error: a few 1e-16 plus the double-float rounding of
+// the reduction, ~|x| 2^-48 (the precision the argument itself carries).
+namespace detail {
+constexpr float PIO2_1 = 0x1.921fb6p+0f;
+constexpr float PIO2_2 = -0x1.777a5cp-25f;
+constexpr float PIO2_3 = -0x1.ee59dap-50f;
+
+MPGOS_DF_HD dfloat reduce_pio2(dfloat x, int& quadrant)
+{
+    const float k = f_rint(f_mul(x.hi, 0.63661977236758134f));
+    dfloat r = x - two_prod(k, PIO2_1);
+    r = r - two_prod(k, PIO2_2);
+    r = r - two_prod(k, PIO2_3);
+    quadrant = static_cast<int>(k) & 3;
+    return r;
+}
+
+// sin(r) for |r| <= pi/4
+MPGOS_DF_HD dfloat sin_kernel(dfloat r)
+{
+    const dfloat z = r * r;
+    const float zf = z.hi;
+    float tail = 1.0f / 6402373705728000.0f;                 // 1/17!
+    tail = f_fma(zf, tail, -1.0f / 1307674368000.0f);        // -1/15!
+    tail = f_fma(zf, tail, 1.0f / 6227020800.0f);            // 1/13!
+    tail = f_fma(zf, tail, -1.0f / 39916800.0f);             // -1/11!
+    dfloat p = dfloat(0x1.71de3ap-19f, 0x1.55b1ccp-45f) + mul_f(z, tail);   // 1/9!
+    p = dfloat(-0x1.a01a02p-13f, 0x1.7f97fap-39f) + z * p;                // -1/7!
+    p = dfloat(0x1.111112p-7f, -0x1.dddddep-32f) + z * p;                  // 1/5!
+    p = dfloat(-0x1.555556p-3f, 0x1.555556p-28f) + z * p;                  // -1/3!
+    return r + (r * z) * p;
+}
+
+// cos(r) for |r| <= pi/4
+MPGOS_DF_HD dfloat cos_kernel(dfloat r)
+{
+    const dfloat z = r * r;
+    const float zf = z.hi;
+    float tail = 1.0f / 20922789888000.0f;                   // 1/16!
+    tail = f_fma(zf, tail, -1.0f / 87178291200.0f);          // -1/14!
+    tail = f_fma(zf, tail, 1.0f / 479001600.0f);             // 1/12!
+    tail = f_fma(zf, tail, -1.0f / 3628800.0f);              // -1/10!
+    dfloat p = dfloat(0x1.a01a02p-16f, -0x1.7f97fap-42f) + mul_f(z, tail);  // 1/8!
+    p = dfloat(-0x1.6c16c2p-10f, 0x1.27d27ep-35f) + z * p;                // -1/6!
+    p = dfloat(0x1.555556p-5f, -0x1.555556p-30f) + z * p;                  // 1/4!
+    p = dfloat(-0.5f, 0.0f) + z * p;
+    return dfloat(1.0f) + z * p;
+}
+}  // namespace detail
+
+MPGOS_DF_HD dfloat sin(dfloat a)
+{
+    int q;
+    const dfloat r = detail::reduce_pio2(a, q);
+    switch (q) {
+        case 0: return detail::sin_kernel(r);
+        case 1: return detail::cos_kernel(r);
+        case 2: return -detail::sin_kernel(r);
+        default: return -detail::cos_kernel(r);
+    }
+}
+
+MPGOS_DF_HD dfloat cos(dfloat a)
+{
+    int q;
+    const dfloat r = detail::reduce_pio2(a, q);
+    switch (q) {
+        case 0: return detail::cos_kernel(r);
+        case 1: return -detail::sin_kernel(r);
+        case 2: return -detail::cos_kernel(r);
+        default: return detail::sin_kernel(r);
+    }
+}
 MPGOS_DF_HD dfloat exp(dfloat a) { return dfloat(std::exp(static_cast<double>(a))); }
 MPGOS_DF_HD dfloat log(dfloat a) { return dfloat(std::log(static_cast<double>(a))); }
 MPGOS_DF_HD dfloat pow(dfloat a, dfloat b)
@@ -201,15 +285,13 @@ MPGOS_DF_HD dfloat pow(dfloat a, int n)
 {
     return dfloat(std::pow(static_cast<double>(a), static_cast<double>(n)));
 }
-#if defined(__CUDACC__)
+// sin(pi a) and cos(pi a) with pi a formed in double-float
 MPGOS_DF_HD void sincospi(dfloat a, dfloat* s, dfloat* c)
 {
-    double sd, cd;
-    ::sincospi(static_cast<double>(a), &sd, &cd);
-    *s = dfloat(sd);
-    *c = dfloat(cd);
+    const dfloat x = a * dfloat(0x1.921fb6p+1f, -0x1.777a5cp-24f);   // pi
+    *s = sin(x);
+    *c = cos(x);
 }
-#endif
 
 }  // namespace df
 }  // namespace mpgos

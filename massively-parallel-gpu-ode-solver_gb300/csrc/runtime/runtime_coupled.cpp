@@ -280,7 +280,14 @@ MPGOS_EXPORT int mpgos_cb_set_option(mpgos_cb_solver* s, int32_t option, int32_t
             if ((rc = idx("EventDirection", s->sh.ne))) return rc;
             s->edir[index] = static_cast<int32_t>(value);
             return push_options(s);
-        case MPGOS_CB_KERNEL_MODE: s->mode = static_cast<int32_t>(value) & MPGOS_MODE_PERSISTENT; break;
+        case MPGOS_CB_KERNEL_MODE:
+            if (value < 0 || value != static_cast<int>(value) ||
+                (static_cast<int32_t>(value) & ~(MPGOS_MODE_PERSISTENT | MPGOS_MODE_DF_STAGE | MPGOS_MODE_FAST_CONTROL)))
+                return fail(MPGOS_ERR_ARGUMENT, "coupled kernel mode %g: only PERSISTENT and DF_STAGE apply", value);
+            if ((static_cast<int32_t>(value) & MPGOS_MODE_DF_STAGE) && s->sh.precision_bytes != 8)
+                return fail(MPGOS_ERR_UNSUPPORTED, "DF_STAGE needs a double-precision coupled table");
+            s->mode = static_cast<int32_t>(value) & (MPGOS_MODE_PERSISTENT | MPGOS_MODE_DF_STAGE);
+            break;
         case MPGOS_CB_MAXIMUM_ATTEMPTS:
             if (value < 1) return fail(MPGOS_ERR_ARGUMENT, "MaximumAttempts must be >= 1");
             s->max_attempts = static_cast<int64_t>(value);
@@ -345,12 +352,16 @@ MPGOS_EXPORT int mpgos_cb_solve(mpgos_cb_solver* s)
     if (s->n_active <= 0) return MPGOS_OK;
     CB_CUDA(cudaSetDevice(s->device));
     const int block = 32 * s->warps;
-    int sg = s->shared_global, sc = s->shared_coupling;
+    const bool df = (s->mode & MPGOS_MODE_DF_STAGE) != 0;
+    int sg = df ? 1 : s->shared_global, sc = df ? 1 : s->shared_coupling;
     size_t smem = s->k->dynamic_smem(s->warps, sg, sc);
-    if (smem > 200 * 1024 && sc) {  // coupling matrix too large for shared memory: read it from global
+    if (smem > 200 * 1024 && sc && !df) {  // coupling matrix too large for shared memory: read it from global
         sc = 0;
         smem = s->k->dynamic_smem(s->warps, sg, sc);
     }
+    if (smem > 227 * 1024)
+        return fail(MPGOS_ERR_ARGUMENT, "coupled launch needs %zu bytes of shared memory (DF_STAGE keeps the coupling "
+                    "matrices there); use fewer warps per block", smem);
     int64_t grid = (s->n_active + s->warps - 1) / s->warps;
     if (s->mode & MPGOS_MODE_PERSISTENT) {
         int per_sm = 0;

@@ -202,3 +202,42 @@ def run_coupled_gpu(case: CbCase, mode: int = 0, warps: int | None = None, devic
 def stored_entries(system: str) -> int:
     ups, _, nc, cbw, cci = CB_SHAPES[system][:5]
     return nc * matrix_entries(ups, cbw, cci)
+
+
+def _main(argv=None) -> int:
+    """Integrate one ring ensemble on the GPU and print a summary line:
+    ``python -m mpgos_gb300.coupled_workloads --system ring64 --ns 2048
+    --periods 2 --mode 18 --warps 2 --launches 2`` (the command the coupled
+    kernel profiles are taken with)."""
+    import argparse
+    import json
+    import time
+
+    ap = argparse.ArgumentParser(prog="python -m mpgos_gb300.coupled_workloads")
+    ap.add_argument("--system", default="ring64", choices=sorted(CB_SHAPES))
+    ap.add_argument("--ns", type=int, default=2048)
+    ap.add_argument("--periods", type=float, default=2)
+    ap.add_argument("--mode", type=int, default=0, help="MPGOS_MODE_* bits (PERSISTENT 2, DF_STAGE 16)")
+    ap.add_argument("--warps", type=int, default=4)
+    ap.add_argument("--launches", type=int, default=1)
+    a = ap.parse_args(argv)
+    case = ring_case(a.system, ns=a.ns, periods=a.periods)
+    from .capi import CbVariable as V
+    with load_coupled_solver(case, mode=a.mode, warps=a.warps) as s:
+        s.checkpoint_save()
+        for _ in range(a.launches):
+            s.checkpoint_restore()
+            s.SynchroniseDevice()
+            t0 = time.perf_counter()
+            s.Solve()
+            s.SynchroniseDevice()
+            wall = time.perf_counter() - t0
+        res = read_coupled_results(s)
+    print(json.dumps({"system": a.system, "ns": a.ns, "periods": a.periods, "mode": a.mode, "warps": a.warps,
+                      "accepted": int(res["nacc"].sum()), "rejected": int(res["nrej"].sum()),
+                      "status_max": int(res["status"].max()), "wall_s_last": wall}))
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(_main())

@@ -38,7 +38,21 @@ int main()
         // comparisons agree with the exact values
         if (((a < b) != (A < B)) || ((a > b) != (A > B)) || ((a <= b) != (A <= B))) m_cmp = 1;
     }
-    std::printf("add %.3e\nmul %.3e\ndiv %.3e\nsqrt %.3e\ncvt %.3e\ncmp %.0f\nnorm %.3f\n", m_add, m_mul, m_div, m_sqrt,
-                m_cvt, m_cmp, m_norm);
+    // sin / cos: error relative to |x| 2^-48 + 2^-50 (the argument's own precision)
+    double m_trig = 0, m_trig_small = 0;
+    std::uniform_real_distribution<double> wide(-2000.0, 2000.0), narrow(-1.0, 1.0);
+    for (int n = 0; n < 200000; n++) {
+        const dfloat x = dfloat(n % 2 ? wide(rng) : narrow(rng));
+        const long double X = val(x);
+        const long double bound = std::fabs(X) * std::ldexp(1.0L, -48) + std::ldexp(1.0L, -50);
+        const double es = (double)(std::fabs(val(mpgos::df::sin(x)) - std::sin(X)) / bound);
+        const double ec = (double)(std::fabs(val(mpgos::df::cos(x)) - std::cos(X)) / bound);
+        m_trig = std::fmax(m_trig, std::fmax(es, ec));
+        if (std::fabs(X) < 1.0L)
+            m_trig_small = std::fmax(m_trig_small, (double)std::fmax(std::fabs(val(mpgos::df::sin(x)) - std::sin(X)),
+                                                                     std::fabs(val(mpgos::df::cos(x)) - std::cos(X))));
+    }
+    std::printf("add %.3e\nmul %.3e\ndiv %.3e\nsqrt %.3e\ncvt %.3e\ncmp %.0f\nnorm %.3f\ntrig %.3f\ntrig_small %.3e\n",
+                m_add, m_mul, m_div, m_sqrt, m_cvt, m_cmp, m_norm, m_trig, m_trig_small);
     return 0;
 }

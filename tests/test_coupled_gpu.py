@@ -130,6 +130,42 @@ def test_coupled_matches_oracle(system, native_libs, oracle_libs):
     np.testing.assert_array_equal(res["isacc"][0], res["nacc"])
 
 
+@pytest.mark.parametrize("system", ["ring16_full", "ring64"])
+def test_coupled_df_stage_matches_oracle(system, native_libs, oracle_libs):
+    """DF_STAGE (double-float stages, coupling dot products and sin/cos on the
+    FP32 pipe): end states within 1e-9 of the component scale or the oracle's
+    own perturbation spread; integer outputs equal on the systems the
+    perturbations leave unchanged, with the step-flip allowance."""
+    from tests.parity import assert_ints_equal
+    ns, periods = (128, 1) if system == "ring64" else (256, 2)
+    case = CW.ring_case(system, ns=ns, periods=periods, seed=14)
+    ora, spread, stable = _spread(case)
+    res = CW.run_coupled_gpu(case, mode=capi.MODE_DF_STAGE | capi.MODE_PERSISTENT, warps=4)
+    assert np.all(res["status"] == 0) and np.all(res["t"] == case.arrays["td"][1])
+    mag = np.max(np.abs(case.arrays["x"]), axis=-1)
+    ok = scaled_close(res["x"], ora["x"], 1e-9, mag, floor=1.0) | (np.abs(res["x"] - ora["x"]) <= 1e3 * spread)
+    assert ok.mean() > 0.99, f"{int((~ok).sum())} end-state elements outside the bar"
+    # zero crossings per unit: equal on the stable systems (step-flip allowance)
+    same = np.all(res["iuacc"].reshape(-1, case.ns, case.ups) == ora["iuacc"].reshape(-1, case.ns, case.ups),
+                  axis=(0, 2))
+    assert (~same[stable]).sum() <= max(1, int(0.02 * stable.sum()))
+    # step counts: every event landing must fall inside the +-1e-6 band, and
+    # whether a secant step lands inside it or needs one more refinement turns
+    # on the event value's last bits, so the counts move by a few steps in
+    # ~1000 on most systems; bounded here by 1 %
+    for k in ("nacc", "nrej"):
+        d = np.abs(res[k].astype(np.int64) - ora[k])
+        assert np.all(d[stable] <= np.maximum(3, ora[k][stable] // 100)), k
+    np.testing.assert_array_equal(res["isacc"][0], res["nacc"])
+
+
+def test_coupled_df_stage_mapping_is_invariant(native_libs):
+    case = CW.ring_case("ring64", ns=96, periods=1, seed=12)
+    base = CW.run_coupled_gpu(case, mode=capi.MODE_DF_STAGE, warps=1)
+    for warps in (2, 4, 8):
+        assert_bitwise(base, CW.run_coupled_gpu(case, mode=capi.MODE_DF_STAGE | capi.MODE_PERSISTENT, warps=warps))
+
+
 def test_coupled_full_ensemble_matches_reference_kernel(native_libs):
     """16384 rings of 64 units with the dense coupling matrix (the coupled
     configuration at full ensemble size; two forcing periods): crossing

@@ -25,6 +25,13 @@ def test_double_float_precision(errors):
     assert errors["cvt"] < 4e-15          # double -> double-float keeps 48 bits (2^-48)
 
 
+def test_double_float_sine_cosine(errors):
+    # FP32-pipe sin/cos: within a few times the argument's own double-float
+    # precision (|x| 2^-48 + 2^-50) up to |x| = 2000, ~1e-14 absolute for |x| < 1
+    assert errors["trig"] < 4.0, errors["trig"]
+    assert errors["trig_small"] < 2e-14, errors["trig_small"]
+
+
 def test_double_float_invariants(errors):
     assert errors["cmp"] == 0             # comparisons order like the exact values
     assert errors["norm"] <= 0.5          # |lo| <= ulp(hi) / 2 after every operation
