@@ -14,7 +14,9 @@ Arms:
                     reported beside it: the FP64 FAST_CONTROL form ("fast_fp64"),
                     the PLAIN form (reference arithmetic, static mapping,
                     "plain") and the reference's own kernel built for sm_103a
-                    ("reference_gpu").
+                    ("reference_gpu"); and the coupled configuration (rings of
+                    64 Duffing units) in DF_STAGE and FP64 beside the
+                    reference's coupled kernel ("coupled").
   --impl reference  the reference's CPU implementation of the path: the
                     reference solver compiled for this host where its build
                     exists (oracle/_ref), else the oracle port
@@ -71,6 +73,7 @@ def parse():
     ap.add_argument("--nt", type=int, default=NT, help="instances per GPU (default 2^20)")
     ap.add_argument("--no-plain", action="store_true", help="skip the PLAIN-form measurement")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
+    ap.add_argument("--no-coupled", action="store_true", help="skip the coupled-configuration leg")
     return ap.parse_args()
 
 
@@ -245,6 +248,61 @@ def flush_l2(buf):
     buf.fill_(1)
 
 
+def coupled_leg(local: int, flush) -> dict:
+    """Coupled configuration beside the headline: 16384 rings of 64 Duffing
+    units (dense coupling, RKCK45 1e-9, crossing events), two forcing periods
+    per launch. Times the DF_STAGE and FP64 warp-per-system kernels and the
+    reference's own coupled kernel (sm_103a cubin, TPB 256 / SPB 4) on the same
+    inputs; one warm-up and two timed launches each, L2 flushed before each."""
+    import torch
+    from mpgos_gb300 import capi, coupled_workloads as CW
+    from mpgos_gb300.capi import CbVariable as V
+    case = CW.ring_case("ring64", ns=16384, periods=2, seed=5)
+
+    def run(mode=None, warps=4, ref=None):
+        with CW.load_coupled_solver(case, mode=mode or 0, warps=warps, device=local) as s:
+            s.checkpoint_save()
+            kern = None
+            if ref is not None:
+                from oracle import ref_gpu
+                kern = ref_gpu.CoupledReferenceKernel("ring64", 1, case.ns, ref[0], ref[1], 0)
+                kern.bind(s, case, shared_global=1, shared_coupling=0)
+            launch = kern.launch if kern is not None else s.Solve
+            times = []
+            for i in range(3):
+                flush_l2(flush)
+                torch.cuda.synchronize()
+                s.checkpoint_restore()
+                s.timer_start()
+                launch()
+                ms = s.timer_stop()
+                if i:
+                    times.append(ms)
+            res = CW.read_coupled_results(s)
+            if kern is not None:
+                kern.close()
+        steps = float(res["isacc"][0].sum())  # accepted steps, counted by the systems' own hook
+        return {"ms": statistics.median(times), "value": steps / (statistics.median(times) / 1e3)}, res
+
+    out = {"workload": "ring64_16384x64_dense_rkck45_tol1e-9_2periods", "unit": "accepted system-steps/s"}
+    df, rdf = run(capi.MODE_DF_STAGE | capi.MODE_PERSISTENT, warps=2)
+    fp, rfp = run(capi.MODE_PERSISTENT, warps=4)
+    out["df_stage"], out["fp64"] = df, fp
+    from oracle import ref_gpu as R
+    if R.coupled_available("ring64", 1, case.ns, 256, 4, 0):
+        ref, rref = run(ref=(256, 4))
+        out["reference_gpu"] = ref
+        out["speedup_df_vs_reference_gpu"] = df["value"] / ref["value"]
+        out["fp64_bitwise_equal_to_reference_kernel"] = bool(
+            all(np.array_equal(rfp[k], rref[k]) for k in ("x", "iuacc", "isacc")))
+        mag = np.max(np.abs(rref["x"]), axis=1, keepdims=True)
+        err = (np.abs(rdf["x"] - rref["x"]) / mag).max(axis=0).reshape(case.ns, -1).max(axis=1)
+        out["df_systems_within_1e-9_of_reference"] = float(np.mean(err <= 1e-9))
+        out["df_crossing_counts_equal_fraction"] = float(np.mean(np.all(
+            rdf["iuacc"].reshape(case.ns, -1) == rref["iuacc"].reshape(case.ns, -1), axis=1)))
+    return out
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -369,6 +427,7 @@ def main():
                 "mode": r["mode"]}
 
     fast = summarize(measure(capi.MODE_CHOSEN, max(1, min(args.steps, 3)), 1, tune=True))
+    coupled = None if args.no_coupled else coupled_leg(local, flush)
     plain = ref_gpu = None
     parity = {}
     if not args.no_plain:
@@ -401,9 +460,9 @@ def main():
     kernel_s = statistics.median(chosen["kernel_ms"]) / 1e3
     attempts_per_launch = chosen["attempts"] / args.steps
     prof = load_traffic()
-    fp32_ops = prof.get("lorenz_df_fp32_thread_ops_per_attempt")
+    instr = prof.get("lorenz_df_thread_instr_per_attempt")
     traffic = prof.get("lorenz_df_dram_bytes_per_launch")
-    achieved = (fp32_ops * attempts_per_launch / kernel_s) if fp32_ops else None
+    achieved = (instr * attempts_per_launch / kernel_s) if instr else None
     peaks = load_peaks()
     cpu = None if args.no_cpu else cpu_baseline(args.nt)
     line = {
@@ -417,19 +476,21 @@ def main():
                    "attempts_per_launch": attempts_per_launch},
         "e2e": e2e,
         "fast_fp64": fast,
+        "coupled": coupled,
         "plain": plain,
         "reference_gpu": ref_gpu,
         "speedup_vs_reference_gpu": (value / ref_gpu["value"]) if ref_gpu else None,
         "parity": parity,
-        "roofline": {"bound": "fp32_pipe",
+        "roofline": {"bound": "instruction issue (FP32 pipe)",
                      "achieved": achieved / 1e12 if achieved else None,
-                     "peak": peak_fp32_ops / 1e12, "unit": "T FP32-pipe thread-ops/s",
+                     "peak": peak_fp32_ops / 1e12, "unit": "T thread-instructions/s",
                      "frac": achieved / peak_fp32_ops if achieved else None, "traffic": traffic,
-                     "fp32_thread_ops_per_attempt": fp32_ops,
-                     "ops_source": "FFMA+FADD+FMUL thread instructions per step attempt, ncu capture "
-                                   "(profiles/perthread_df_kernel_lorenz.md)",
+                     "thread_instructions_per_attempt": instr,
+                     "instructions_source": "smsp__inst_executed x thread/inst per step attempt, ncu capture "
+                                            "(profiles/perthread_df_kernel_lorenz_2e18.md)",
                      "kernel_ms": kernel_s * 1e3,
-                     "peak_source": "measured FP32 FMA throughput (mpgos_probe_fma_peak), same GPU, same run",
+                     "peak_source": "measured FFMA instruction rate (mpgos_probe_fma_peak, precision 4), same GPU, "
+                                    "same run: the issue ceiling every instruction shares",
                      "algorithmic_fp64_equivalent_tflops": FLOP_PER_ATTEMPT * attempts_per_launch / kernel_s / 1e12,
                      "fp64_fma_peak_tflops": peak_fp64 / 1e12,
                      "hbm_peak_gbs_measured": peaks.get("hbm_gbs")},
