@@ -16,7 +16,9 @@ Arms:
                     "plain") and the reference's own kernel built for sm_103a
                     ("reference_gpu"); and the coupled configuration (rings of
                     64 Duffing units) in DF_STAGE and FP64 beside the
-                    reference's coupled kernel ("coupled").
+                    reference's coupled kernel ("coupled"), and the
+                    adjoint configuration's adjoint/forward time ratio
+                    ("adjoint").
   --impl reference  the reference's CPU implementation of the path: the
                     reference solver compiled for this host where its build
                     exists (oracle/_ref), else the oracle port
@@ -74,6 +76,7 @@ def parse():
     ap.add_argument("--no-plain", action="store_true", help="skip the PLAIN-form measurement")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--no-coupled", action="store_true", help="skip the coupled-configuration leg")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint-configuration leg")
     return ap.parse_args()
 
 
@@ -246,6 +249,64 @@ def run_reference(args):
 
 def flush_l2(buf):
     buf.fill_(1)
+
+
+def adjoint_leg(local: int, flush) -> dict:
+    """Adjoint configuration: forced Duffing ensemble of 2^18 instances with
+    per-instance (k, B), RKCK45 1e-9 over 64 forcing periods, loss = squared
+    distance of the terminal state to per-instance targets; gradients with
+    respect to (x0, v0, k, B) by the discrete adjoint with a checkpoint every
+    32 accepted steps. Times, on the same inputs: the forward pass alone
+    (FAST_CONTROL + persistent, the FP64 form the adjoint records), the
+    recording forward pass and the reverse pass; the adjoint/forward ratio is
+    (recording + reverse) / forward."""
+    import torch
+    from mpgos_gb300 import capi, workloads as W
+    from mpgos_gb300.solver import Variable
+    nt, max_steps, seg = 1 << 18, 4096, 32
+    case = W.duffing_param_case(nt=nt, periods=64, tol=1e-9)
+    target = torch.tensor(W.duffing_param_targets(nt), device=f"cuda:{local}")
+    mode = capi.MODE_FAST_CONTROL | capi.MODE_PERSISTENT
+    out = {"workload": "duffing_param_2^18_rkck45_tol1e-9_64periods_seg32", "unit": "ms"}
+    with W.load_solver(case, mode=mode, block=128, device=local) as s:
+        s.checkpoint_save()
+        g = torch.empty((2, nt), dtype=torch.float64, device=f"cuda:{local}")
+        gx0, gcp = torch.empty_like(g), torch.empty_like(g)
+        x_dev = torch.empty_like(g)
+        fwd, rec, rev = [], [], []
+        for i in range(3):
+            flush_l2(flush)
+            torch.cuda.synchronize()
+            s.checkpoint_restore()
+            s.timer_start()
+            s.Solve()
+            t_f = s.timer_stop()
+            flush_l2(flush)
+            torch.cuda.synchronize()
+            s.checkpoint_restore()
+            s.timer_start()
+            s.SolveRecord(max_steps, seg)
+            t_r = s.timer_stop()
+            s.SynchroniseFromDeviceToHost(Variable.ActualState)
+            s.SynchroniseDevice()
+            x_dev.copy_(torch.from_numpy(s.host(Variable.ActualState)))
+            g.copy_(2.0 * (x_dev - target))
+            torch.cuda.synchronize()
+            s.timer_start()
+            s.Adjoint(g.data_ptr(), gx0.data_ptr(), gcp.data_ptr())
+            t_b = s.timer_stop()
+            if i:
+                fwd.append(t_f)
+                rec.append(t_r)
+                rev.append(t_b)
+        s.SynchroniseFromDeviceToHost(Variable.Status)
+        s.SynchroniseDevice()
+        overflow = int(np.count_nonzero(s.host(Variable.Status) & capi.INSTANCE_TAPE_OVERFLOW))
+    f, r, b = statistics.median(fwd), statistics.median(rec), statistics.median(rev)
+    out.update({"forward_ms": f, "recording_forward_ms": r, "reverse_ms": b,
+                "adjoint_over_forward": (r + b) / f, "tape_overflow_instances": overflow,
+                "gradients_per_instance": 4})
+    return out
 
 
 def coupled_leg(local: int, flush) -> dict:
@@ -428,6 +489,7 @@ def main():
 
     fast = summarize(measure(capi.MODE_CHOSEN, max(1, min(args.steps, 3)), 1, tune=True))
     coupled = None if args.no_coupled else coupled_leg(local, flush)
+    adjoint = None if args.no_adjoint else adjoint_leg(local, flush)
     plain = ref_gpu = None
     parity = {}
     if not args.no_plain:
@@ -477,6 +539,7 @@ def main():
         "e2e": e2e,
         "fast_fp64": fast,
         "coupled": coupled,
+        "adjoint": adjoint,
         "plain": plain,
         "reference_gpu": ref_gpu,
         "speedup_vs_reference_gpu": (value / ref_gpu["value"]) if ref_gpu else None,

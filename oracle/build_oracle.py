@@ -182,11 +182,16 @@ def build_ref(system: str, force: bool = False) -> Path | None:
 
 # Reference GPU kernels built as cubins: (system, algorithm, NT, NDO). The
 # reference's NT and NDO are template arguments, so every ensemble size the
-# tests and the bench compare against is listed. keller_miksis is absent on
-# purpose: with SD = 2 > NE = 1 the reference kernel indexes its event-option
-# arrays by component (SingleSystem_PerThread_Solver.cuh:60-63), which reads
-# past the NE-entry device array and writes past the NE-entry shared array.
+# tests and the bench compare against is listed. For keller_miksis (SD = 2 >
+# NE = 1) the unmodified reference kernel indexes its event-option arrays by
+# component (SingleSystem_PerThread_Solver.cuh:60: `ltid < SD`), which reads
+# past the NE-entry device array and writes past the NE-entry shared array;
+# it is never built. Systems listed in REF_GPU_EVENT_FIX are built instead
+# from a temporary copy of the reference sources (outside this repository)
+# in which only that condition reads `ltid < NE`.
+REF_GPU_EVENT_FIX = {"keller_miksis"}
 REF_GPU_KERNELS = [
+    ("keller_miksis", 1, 64, 0), ("keller_miksis", 1, 256, 0),
     ("lorenz", 1, 256, 0), ("lorenz", 1, 1000, 0), ("lorenz", 0, 64, 0), ("lorenz", 1, 1 << 20, 0),
     ("duffing", 0, 64, 0), ("duffing", 0, 8192, 0),
     ("duffing_param", 1, 256, 0), ("duffing_param", 1, 1000, 0),
@@ -211,15 +216,47 @@ def build_ref_gpu(system: str, algorithm: int, nt: int, ndo: int, rreg: int | No
     hdr = SYSTEMS_DIR / f"{system}.cuh"
     if not force and _newer(out, [src, hdr, ORACLE_DIR / "ref_types.hpp", Path(__file__)]):
         return out
+    src_dir, tmp = REFERENCE_ROOT / "SourceCodes", None
+    if system in REF_GPU_EVENT_FIX:
+        tmp, src_dir = _event_fixed_sources()
+        if src_dir is None:
+            return None
     cmd = ["nvcc", "-cubin", "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17", "-lineinfo", "-w",
-           f"-I{ORACLE_DIR}", f"-I{SYSTEMS_DIR}", f"-I{REFERENCE_ROOT / 'SourceCodes'}",
+           f"-I{ORACLE_DIR}", f"-I{SYSTEMS_DIR}", f"-I{src_dir}",
            f'-DMPGOS_SYSTEM_HEADER="{system}.cuh"', f"-DREF_NT={nt}", f"-DREF_ALG={'RKCK45' if algorithm else 'RK4'}",
            f"-DREF_NDO={ndo}"]
     if rreg:
         cmd.append(f"-maxrregcount={rreg}")
     cmd += [str(src), "-o", str(out)]
-    _run(cmd, out.name)
+    try:
+        _run(cmd, out.name)
+    finally:
+        if tmp is not None:
+            import shutil
+            shutil.rmtree(tmp, ignore_errors=True)
     return out
+
+
+def _event_fixed_sources():
+    """Copy the reference's SourceCodes to a temporary directory and change the
+    event-option staging condition of SingleSystem_PerThread_Solver.cuh from
+    `ltid < SD` to `ltid < NE` (the only change). Returns (temporary
+    directory, patched SourceCodes path), or (None, None) if the line is not
+    found as expected."""
+    import shutil
+    import tempfile
+    tmp = Path(tempfile.mkdtemp(prefix="mpgos_ref_evfix_"))
+    dst = tmp / "SourceCodes"
+    shutil.copytree(REFERENCE_ROOT / "SourceCodes", dst)
+    f = dst / "SingleSystem_PerThread_Solver.cuh"
+    lines = f.read_text().split("\n")
+    hits = [i for i, l in enumerate(lines) if l.strip() == "if ( ltid < SD)" and "EventTolerance" in "".join(lines[i:i + 4])]
+    if len(hits) != 1:
+        shutil.rmtree(tmp, ignore_errors=True)
+        return None, None
+    lines[hits[0]] = lines[hits[0]].replace("ltid < SD", "ltid < NE")
+    f.write_text("\n".join(lines))
+    return tmp, dst
 
 
 def build_all(force: bool = False) -> dict:
