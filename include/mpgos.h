@@ -403,6 +403,13 @@ typedef struct mpgos_cb_kernels {
     int (*launch)(const mpgos_cb_launch* args, int grid, int block, size_t dynamic_smem, void* stream);
     int (*occupancy)(int32_t mode, int block, size_t dynamic_smem, int* blocks_per_sm);
     size_t (*dynamic_smem)(int warps_per_block, int shared_global, int shared_coupling);
+    /* discrete adjoint (NULL where not compiled): the recording forward launch,
+     * the reverse launch and its dynamic shared memory */
+    int (*launch_record)(const mpgos_cb_launch* args, const mpgos_pt_tape* tape, int grid, int block,
+                         size_t dynamic_smem, void* stream);
+    int (*launch_adjoint)(const mpgos_cb_launch* args, const mpgos_pt_tape* tape, const double* dL_dxT,
+                          double* dL_dx0, double* dL_dsp, int grid, int block, size_t dynamic_smem, void* stream);
+    size_t (*adjoint_smem)(int warps_per_block);
 } mpgos_cb_kernels;
 
 typedef struct mpgos_cb_solver mpgos_cb_solver;
@@ -428,6 +435,19 @@ int mpgos_cb_timer_stop(mpgos_cb_solver* solver, float* milliseconds);
 int mpgos_cb_stream(mpgos_cb_solver* solver, void** stream);
 int mpgos_cb_checkpoint_save(mpgos_cb_solver* solver);
 int mpgos_cb_checkpoint_restore(mpgos_cb_solver* solver);
+/* Discrete adjoint of the coupled solver (extension, no counterpart in the
+ * reference), FP64 tables. mpgos_cb_solve_record: one Solve() that also
+ * records the tape (every accepted step size of every system, the time and
+ * every unit's state every `segment` accepted steps; capacity max_steps per
+ * system; device memory owned by the solver). mpgos_cb_adjoint: reverse pass;
+ * device pointers, FP64: dL_dxT [UD][NS*UPS] in, dL_dx0 [UD][NS*UPS] and
+ * dL_dsp [NSP][NS] (the system parameters) out; the gradient of the discrete
+ * map with the recorded step sequence frozen. Systems whose step count
+ * exceeded the tape get MPGOS_INSTANCE_TAPE_OVERFLOW and no gradient.
+ * Asynchronous on the solver's stream. */
+int mpgos_cb_solve_record(mpgos_cb_solver* solver, int32_t max_steps, int32_t segment);
+int mpgos_cb_adjoint(mpgos_cb_solver* solver, const double* dL_dxT, double* dL_dx0, double* dL_dsp);
+int mpgos_cb_tape_info(const mpgos_cb_solver* solver, mpgos_pt_tape* tape);
 
 /* Coupled kernel table of a coupled-system plugin, or NULL. */
 typedef const mpgos_cb_kernels* (*mpgos_cb_system_fn)(int32_t algorithm, int32_t precision_bytes);

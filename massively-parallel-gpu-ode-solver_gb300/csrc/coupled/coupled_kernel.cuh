@@ -113,7 +113,14 @@ struct Args {
     int shared_global;
     int shared_coupling;
     Options<P> o;
+    // adjoint tape of a recording launch (MODE_RECORD): dt [max_steps][NS],
+    // ckpt_x [max_steps/seg + 1][UD][NS*UPS], ckpt_t [max_steps/seg + 1][NS],
+    // n_steps [NS]
+    pt::Tape tape;
 };
+
+// Kernel-internal mode bit: the forward launch records the adjoint tape.
+constexpr int MODE_RECORD = pt::MODE_RECORD;
 
 // Per-warp (per-system) shared-memory slot.
 template <class S, class P>
@@ -220,6 +227,7 @@ struct Solver {
     static constexpr int UPS = S::UPS, UD = S::UD, NC = S::NC, NUP = S::NUP, NUA = S::NUA, NIUA = S::NIUA;
     static constexpr int NE = S::NE, UPL = S::UPL, NSP = S::NSP, NSA = S::NSA, NISA = S::NISA;
     static constexpr bool PERSISTENT = (MODE & MPGOS_MODE_PERSISTENT) != 0;
+    static constexpr bool RECORD = ((MODE & MODE_RECORD) != 0) && std::is_same<P, double>::value;
     using Slot = WarpSlot<S, P>;
     using SP   = typename StorageOf<P>::type;  // precision of the arrays in HBM
 
@@ -429,6 +437,7 @@ struct Solver {
             __syncwarp();
         }
         if (o.ndo > 0) dense_store(s, lane, w, u, a, o, 1, 1);
+        if constexpr (RECORD) record_checkpoint(s, lane, w, u, a, 0);
 
         int status = 0, nacc = 0, nrej = 0, terminate = 0;
         long long attempts = 0;
@@ -621,6 +630,16 @@ struct Solver {
 #pragma unroll
                         for (int e = 0; e < NE; e++) u.ga[j][e] = gn[j][e];
                 }
+                if constexpr (RECORD) {
+                    // frozen step size of accepted step nacc, checkpoint every seg steps
+                    const int k = nacc - 1;
+                    if (k < a.tape.max_steps) {
+                        if (lane == 0) a.tape.dt[static_cast<long long>(k) * ns + s] = dt;
+                        if (nacc % a.tape.seg == 0) record_checkpoint(s, lane, w, u, a, nacc / a.tape.seg);
+                    } else {
+                        status |= MPGOS_INSTANCE_TAPE_OVERFLOW;
+                    }
+                }
             } else {
                 nrej++;
             }
@@ -660,10 +679,26 @@ struct Solver {
             if (a.status) a.status[s] = status;
             if (a.n_acc) a.n_acc[s] = nacc;
             if (a.n_rej) a.n_rej[s] = nrej;
+            if constexpr (RECORD) a.tape.n_steps[s] = nacc;
         }
         for (int k = lane; k < NSA; k += 32) a.sacc[s + k * ns] = static_cast<SP>(w.sacc[k]);
         for (int k = lane; k < NISA; k += 32) a.isacc[s + k * ns] = w.isacc[k];
         __syncwarp();
+    }
+
+    // Checkpoint c of the adjoint tape: time and every unit's state.
+    __device__ static void record_checkpoint(long long s, int lane, const Slot& w, const Units& u, const Args<SP>& a,
+                                             int c)
+    {
+        const long long ns = a.ns, nu = a.ns * UPS;
+        if (lane == 0) a.tape.ckpt_t[static_cast<long long>(c) * ns + s] = w.t;
+#pragma unroll
+        for (int j = 0; j < UPL; j++) {
+            if (!has(lane, j)) continue;
+            const long long g = s * UPS + unit_of(lane, j);
+#pragma unroll
+            for (int d = 0; d < UD; d++) a.tape.ckpt_x[(static_cast<long long>(c) * UD + d) * nu + g] = u.x[j][d];
+        }
     }
 
     // Dense output of one system (CoupledSystems_PerBlock_DenseOutput.cuh:210-312).
@@ -892,7 +927,13 @@ struct KernelTable {
     {
         return dynamic_smem_bytes<S, P>(warps, shared_global, shared_coupling);
     }
-    static const mpgos_cb_kernels* get(const char* name)
+    using RecordFn  = int (*)(const mpgos_cb_launch*, const mpgos_pt_tape*, int, int, size_t, void*);
+    using AdjointFn = int (*)(const mpgos_cb_launch*, const mpgos_pt_tape*, const double*, double*, double*, int, int,
+                              size_t, void*);
+    using AdjSmemFn = size_t (*)(int);
+
+    static const mpgos_cb_kernels* get(const char* name, RecordFn record = nullptr, AdjointFn adjoint = nullptr,
+                                       AdjSmemFn adjoint_smem = nullptr)
     {
         static mpgos_cb_kernels table = {
             MPGOS_ABI_VERSION,
@@ -901,7 +942,10 @@ struct KernelTable {
             name,
             &launch,
             &occupancy,
-            &smem};
+            &smem,
+            record,
+            adjoint,
+            adjoint_smem};
         return &table;
     }
 };

@@ -2,10 +2,12 @@
 // file (which defines MPGOS_SYS_UPS/UD/NC/NUP/NSP/NGP/NIGP/NUA/NIUA/NSA/NISA/NE)
 // and after defining MPGOS_SYS_NAME, MPGOS_SYS_CBW and MPGOS_SYS_CCI (coupling
 // storage), to export mpgos_cb_system_kernels() of mpgos.h. Instantiated:
-// RKCK45 and RK4 in double.
+// RKCK45 and RK4 in double (with DF_STAGE variants and the discrete adjoint
+// with respect to the system parameters).
 #pragma once
 
 #include "coupled_kernel.cuh"
+#include "coupled_adjoint.cuh"
 
 namespace mpgos_cb_plugin {
 using SysShape = mpgos::cb::Shape<MPGOS_SYS_UPS, MPGOS_SYS_UD, MPGOS_SYS_NC, MPGOS_SYS_CBW, MPGOS_SYS_CCI, MPGOS_SYS_NUP,
@@ -19,8 +21,16 @@ extern "C" __attribute__((visibility("default"))) const mpgos_cb_kernels* mpgos_
     using namespace mpgos::cb;
     using S = mpgos_cb_plugin::SysShape;
     if (precision_bytes == 8) {
-        if (algorithm == MPGOS_RKCK45) return KernelTable<S, MPGOS_RKCK45, double>::get(MPGOS_SYS_NAME);
-        if (algorithm == MPGOS_RK4) return KernelTable<S, MPGOS_RK4, double>::get(MPGOS_SYS_NAME);
+        if (algorithm == MPGOS_RKCK45) {
+            using A = CoupledAdjointTable<S, MPGOS_RKCK45>;
+            return KernelTable<S, MPGOS_RKCK45, double>::get(MPGOS_SYS_NAME, &A::launch_record, &A::launch_adjoint,
+                                                             &A::smem);
+        }
+        if (algorithm == MPGOS_RK4) {
+            using A = CoupledAdjointTable<S, MPGOS_RK4>;
+            return KernelTable<S, MPGOS_RK4, double>::get(MPGOS_SYS_NAME, &A::launch_record, &A::launch_adjoint,
+                                                          &A::smem);
+        }
     }
     return nullptr;
 }

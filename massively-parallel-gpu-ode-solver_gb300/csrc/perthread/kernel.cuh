@@ -43,19 +43,6 @@ struct Shape {
     static constexpr int SD = SD_, NCP = NCP_, NSP = NSP_, NISP = NISP_, NE = NE_, NA = NA_, NIA = NIA_;
 };
 
-// Device-side view of the adjoint tape (mpgos_pt_tape in mpgos.h).
-struct Tape {
-    int seg;
-    int max_steps;
-    double* dt;      // [max_steps][NT]
-    double* ckpt_x;  // [max_steps/seg + 1][SD][NT]
-    double* ckpt_t;  // [max_steps/seg + 1][NT]
-    int* n_steps;    // [NT]
-};
-
-// Kernel-internal mode bit: the forward launch records the adjoint tape.
-constexpr int MODE_RECORD = 8;
-
 // Kernel arguments in the kernel's precision (the reference passes the same
 // information as Struct_ThreadConfiguration / Struct_GlobalVariables /
 // Struct_SharedMemoryUsage / Struct_SolverOptions,

@@ -23,6 +23,19 @@ namespace pt {
 
 template <int N> struct AtLeastOne { static constexpr int value = N > 0 ? N : 1; };
 
+// Device-side view of the adjoint tape (mpgos_pt_tape in mpgos.h).
+struct Tape {
+    int seg;
+    int max_steps;
+    double* dt;      // [max_steps][NT]
+    double* ckpt_x;  // [max_steps/seg + 1][SD][NT]
+    double* ckpt_t;  // [max_steps/seg + 1][NT]
+    int* n_steps;    // [NT]
+};
+
+// Kernel-internal mode bit: the forward launch records the adjoint tape.
+constexpr int MODE_RECORD = 8;
+
 // Solver options in the kernel's precision (Struct_SolverOptions of
 // SingleSystem_PerThread_Interface.cuh:105-115 plus the extensions).
 template <class P>

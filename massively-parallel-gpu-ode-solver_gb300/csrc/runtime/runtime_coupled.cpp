@@ -75,6 +75,7 @@ struct mpgos_cb_solver {
     int32_t dense_freq = 1, shared_global = 1, shared_coupling = 1, mode = 0, warps = 4;
     int64_t max_attempts = 10000000;
     std::vector<void*> ckpt;
+    mpgos_pt_tape tape{};  // discrete-adjoint tape (mpgos_cb_solve_record)
 };
 
 namespace {
@@ -143,6 +144,9 @@ MPGOS_EXPORT int mpgos_cb_destroy(mpgos_cb_solver* s)
     for (void* p : {s->d_rtol, s->d_atol, s->d_etol, static_cast<void*>(s->d_edir), static_cast<void*>(s->d_work)})
         if (p) cudaFree(p);
     for (void* p : s->ckpt)
+        if (p) cudaFree(p);
+    for (void* p : {static_cast<void*>(s->tape.dt), static_cast<void*>(s->tape.ckpt_x),
+                    static_cast<void*>(s->tape.ckpt_t), static_cast<void*>(s->tape.n_steps)})
         if (p) cudaFree(p);
     if (s->t0) cudaEventDestroy(s->t0);
     if (s->t1) cudaEventDestroy(s->t1);
@@ -345,14 +349,36 @@ MPGOS_EXPORT int mpgos_cb_sync_d2h(mpgos_cb_solver* s, int32_t v)
     return MPGOS_OK;
 }
 
+namespace {
+// Launch configuration and arguments of one Solve() (record = the recording
+// forward launch of the discrete adjoint, which uses the FP64 kernels).
+int prepare_launch(mpgos_cb_solver* s, bool record, mpgos_cb_launch& L, int64_t& grid_out, int& block_out,
+                   size_t& smem_out);
+}  // namespace
+
 MPGOS_EXPORT int mpgos_cb_solve(mpgos_cb_solver* s)
 {
     int rc = check(s);
     if (rc) return rc;
     if (s->n_active <= 0) return MPGOS_OK;
     CB_CUDA(cudaSetDevice(s->device));
+    mpgos_cb_launch L;
+    int64_t grid = 0;
+    int block = 0;
+    size_t smem = 0;
+    if ((rc = prepare_launch(s, false, L, grid, block, smem))) return rc;
+    int e = s->k->launch(&L, static_cast<int>(grid), block, smem, s->stream);
+    if (e != 0) return fail(MPGOS_ERR_CUDA, "coupled kernel launch failed: %s", cudaGetErrorString((cudaError_t)e));
+    return MPGOS_OK;
+}
+
+namespace {
+int prepare_launch(mpgos_cb_solver* s, bool record, mpgos_cb_launch& L, int64_t& grid_out, int& block_out,
+                   size_t& smem_out)
+{
+    const int32_t mode = record ? (s->mode & MPGOS_MODE_PERSISTENT) : s->mode;
     const int block = 32 * s->warps;
-    const bool df = (s->mode & MPGOS_MODE_DF_STAGE) != 0;
+    const bool df = (mode & MPGOS_MODE_DF_STAGE) != 0;
     int sg = df ? 1 : s->shared_global, sc = df ? 1 : s->shared_coupling;
     size_t smem = s->k->dynamic_smem(s->warps, sg, sc);
     if (smem > 200 * 1024 && sc && !df) {  // coupling matrix too large for shared memory: read it from global
@@ -363,19 +389,18 @@ MPGOS_EXPORT int mpgos_cb_solve(mpgos_cb_solver* s)
         return fail(MPGOS_ERR_ARGUMENT, "coupled launch needs %zu bytes of shared memory (DF_STAGE keeps the coupling "
                     "matrices there); use fewer warps per block", smem);
     int64_t grid = (s->n_active + s->warps - 1) / s->warps;
-    if (s->mode & MPGOS_MODE_PERSISTENT) {
+    if (mode & MPGOS_MODE_PERSISTENT) {
         int per_sm = 0;
-        int e = s->k->occupancy(s->mode, block, smem, &per_sm);
+        int e = s->k->occupancy(mode, block, smem, &per_sm);
         if (e != 0) return fail(MPGOS_ERR_CUDA, "coupled occupancy query: %s", cudaGetErrorString((cudaError_t)e));
         grid = std::min<int64_t>(grid, static_cast<int64_t>(std::max(per_sm, 1)) * s->sm_count);
         CB_CUDA(cudaMemsetAsync(s->d_work, 0, 4, s->stream));
     }
-    mpgos_cb_launch L;
     std::memset(&L, 0, sizeof(L));
     L.ns = s->ns;
     L.n_active = s->n_active;
     L.ndo = s->ndo;
-    L.mode = s->mode;
+    L.mode = mode;
     L.shared_global = sg;
     L.shared_coupling = sc;
     L.dense_save_frequency = s->dense_freq;
@@ -416,8 +441,82 @@ MPGOS_EXPORT int mpgos_cb_solve(mpgos_cb_solver* s)
     const int32_t* ci = static_cast<const int32_t*>(s->var[MPGOS_CB_COUPLING_INDEX].host);
     for (int i = 0; i < s->sh.nc; i++)
         if (ci[i] < 0 || ci[i] >= s->sh.ud) return fail(MPGOS_ERR_ARGUMENT, "CouplingIndex[%d] = %d outside 0..%d", i, ci[i], s->sh.ud - 1);
-    int e = s->k->launch(&L, static_cast<int>(grid), block, smem, s->stream);
-    if (e != 0) return fail(MPGOS_ERR_CUDA, "coupled kernel launch failed: %s", cudaGetErrorString((cudaError_t)e));
+    grid_out = grid;
+    block_out = block;
+    smem_out = smem;
+    return MPGOS_OK;
+}
+}  // namespace
+
+MPGOS_EXPORT int mpgos_cb_solve_record(mpgos_cb_solver* s, int32_t max_steps, int32_t segment)
+{
+    int rc = check(s);
+    if (rc) return rc;
+    if (s->k->launch_record == nullptr || s->sh.precision_bytes != 8)
+        return fail(MPGOS_ERR_UNSUPPORTED, "coupled system %s has no adjoint kernels (FP64 only)", s->k->name);
+    if (max_steps < 1 || segment < 1 || segment > 64)
+        return fail(MPGOS_ERR_ARGUMENT, "tape: max_steps %d must be >= 1 and segment %d within 1..64", max_steps, segment);
+    CB_CUDA(cudaSetDevice(s->device));
+    const size_t ns = static_cast<size_t>(s->ns), nu = ns * static_cast<size_t>(s->sh.ups);
+    const size_t ud = static_cast<size_t>(s->sh.ud), nck = static_cast<size_t>(max_steps / segment + 1);
+    if (s->tape.max_steps != max_steps || s->tape.segment != segment || s->tape.dt == nullptr) {
+        CB_CUDA(cudaStreamSynchronize(s->stream));
+        for (void* p : {static_cast<void*>(s->tape.dt), static_cast<void*>(s->tape.ckpt_x),
+                        static_cast<void*>(s->tape.ckpt_t), static_cast<void*>(s->tape.n_steps)})
+            if (p) cudaFree(p);
+        s->tape = mpgos_pt_tape{};
+        const size_t b_dt = static_cast<size_t>(max_steps) * ns * 8, b_cx = nck * ud * nu * 8, b_ct = nck * ns * 8;
+        if (cudaMalloc(reinterpret_cast<void**>(&s->tape.dt), b_dt) != cudaSuccess ||
+            cudaMalloc(reinterpret_cast<void**>(&s->tape.ckpt_x), b_cx) != cudaSuccess ||
+            cudaMalloc(reinterpret_cast<void**>(&s->tape.ckpt_t), b_ct) != cudaSuccess ||
+            cudaMalloc(reinterpret_cast<void**>(&s->tape.n_steps), ns * 4) != cudaSuccess) {
+            s->tape.max_steps = 0;
+            return fail(MPGOS_ERR_MEMORY, "coupled adjoint tape allocation (%zu bytes) failed", b_dt + b_cx + b_ct + ns * 4);
+        }
+        s->tape.max_steps = max_steps;
+        s->tape.segment = segment;
+    }
+    if (s->n_active <= 0) return MPGOS_OK;
+    mpgos_cb_launch L;
+    int64_t grid = 0;
+    int block = 0;
+    size_t smem = 0;
+    if ((rc = prepare_launch(s, true, L, grid, block, smem))) return rc;
+    int e = s->k->launch_record(&L, &s->tape, static_cast<int>(grid), block, smem, s->stream);
+    if (e != 0) return fail(MPGOS_ERR_CUDA, "coupled recording launch failed: %s", cudaGetErrorString((cudaError_t)e));
+    return MPGOS_OK;
+}
+
+MPGOS_EXPORT int mpgos_cb_adjoint(mpgos_cb_solver* s, const double* dLdxT, double* dLdx0, double* dLdsp)
+{
+    int rc = check(s);
+    if (rc) return rc;
+    if (s->k->launch_adjoint == nullptr) return fail(MPGOS_ERR_UNSUPPORTED, "coupled system %s has no adjoint kernels", s->k->name);
+    if (s->tape.dt == nullptr) return fail(MPGOS_ERR_ARGUMENT, "no recorded forward pass (call mpgos_cb_solve_record first)");
+    if (dLdxT == nullptr || dLdx0 == nullptr || (dLdsp == nullptr && s->sh.nsp > 0))
+        return fail(MPGOS_ERR_ARGUMENT, "null gradient buffer");
+    if (s->n_active <= 0) return MPGOS_OK;
+    CB_CUDA(cudaSetDevice(s->device));
+    const int warps = 2, block = 32 * warps;
+    const size_t smem = s->k->adjoint_smem(warps);
+    if (smem > 227 * 1024) return fail(MPGOS_ERR_ARGUMENT, "coupled adjoint needs %zu bytes of shared memory", smem);
+    const int64_t grid = (s->n_active + warps - 1) / warps;
+    mpgos_cb_launch L;
+    int64_t g = 0;
+    int b = 0;
+    size_t sm = 0;
+    if ((rc = prepare_launch(s, true, L, g, b, sm))) return rc;
+    int e = s->k->launch_adjoint(&L, &s->tape, dLdxT, dLdx0, dLdsp, static_cast<int>(grid), block, smem, s->stream);
+    if (e != 0) return fail(MPGOS_ERR_CUDA, "coupled adjoint launch failed: %s", cudaGetErrorString((cudaError_t)e));
+    return MPGOS_OK;
+}
+
+MPGOS_EXPORT int mpgos_cb_tape_info(const mpgos_cb_solver* s, mpgos_pt_tape* tape)
+{
+    int rc = check(s);
+    if (rc) return rc;
+    if (tape == nullptr) return fail(MPGOS_ERR_ARGUMENT, "null tape pointer");
+    *tape = s->tape;
     return MPGOS_OK;
 }
 

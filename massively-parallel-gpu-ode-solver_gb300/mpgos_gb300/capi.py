@@ -143,6 +143,9 @@ class CbKernelTable(C.Structure):
         ("launch", C.c_void_p),
         ("occupancy", C.c_void_p),
         ("dynamic_smem", C.c_void_p),
+        ("launch_record", C.c_void_p),
+        ("launch_adjoint", C.c_void_p),
+        ("adjoint_smem", C.c_void_p),
     ]
 
 
@@ -220,6 +223,9 @@ def _declare(lib):
         "mpgos_cb_stream": (C.c_int, [P, C.POINTER(P)]),
         "mpgos_cb_checkpoint_save": (C.c_int, [P]),
         "mpgos_cb_checkpoint_restore": (C.c_int, [P]),
+        "mpgos_cb_solve_record": (C.c_int, [P, i32, i32]),
+        "mpgos_cb_adjoint": (C.c_int, [P, P, P, P]),
+        "mpgos_cb_tape_info": (C.c_int, [P, C.POINTER(Tape)]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(lib, name)
@@ -241,6 +247,7 @@ RUNTIME_SYMBOLS = (
     "mpgos_cb_device_buffer", "mpgos_cb_sync_h2d", "mpgos_cb_sync_d2h", "mpgos_cb_solve",
     "mpgos_cb_insert_sync_point", "mpgos_cb_sync_solver", "mpgos_cb_timer_start", "mpgos_cb_timer_stop",
     "mpgos_cb_stream", "mpgos_cb_checkpoint_save", "mpgos_cb_checkpoint_restore",
+    "mpgos_cb_solve_record", "mpgos_cb_adjoint", "mpgos_cb_tape_info",
 )
 # mpgos_pt_system_kernels: per-thread system plugins; mpgos_cb_system_kernels:
 # coupled-system plugins.

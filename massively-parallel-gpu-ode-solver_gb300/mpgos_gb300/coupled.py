@@ -306,6 +306,22 @@ class CoupledProblemSolver:
     def checkpoint_restore(self):
         capi.check(self._lib.mpgos_cb_checkpoint_restore(self._h))
 
+    def SolveRecord(self, max_steps: int, segment: int = 32):
+        """One Solve() that records the adjoint tape (frozen step sizes and a
+        checkpoint of every unit every ``segment`` accepted steps)."""
+        capi.check(self._lib.mpgos_cb_solve_record(self._h, int(max_steps), int(segment)))
+
+    def Adjoint(self, dLdxT_ptr: int, dLdx0_ptr: int, dLdsp_ptr: int):
+        """Reverse pass over the recorded tape; device pointers, FP64:
+        [UD][NS*UPS] in, [UD][NS*UPS] and [NSP][NS] out."""
+        capi.check(self._lib.mpgos_cb_adjoint(self._h, C.c_void_p(dLdxT_ptr), C.c_void_p(dLdx0_ptr),
+                                              C.c_void_p(dLdsp_ptr or None)))
+
+    def tape_info(self):
+        t = capi.Tape()
+        capi.check(self._lib.mpgos_cb_tape_info(self._h, C.byref(t)))
+        return t
+
     def set_mode(self, mode: int):
         self.SolverOption(CbOption.KernelMode, int(mode))
 

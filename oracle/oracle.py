@@ -226,6 +226,39 @@ def run_oracle_coupled(case, threads: int = 0, first: int = 0, count: int | None
     return out
 
 
+def replay_coupled(case, dt_tape: np.ndarray, n_steps: np.ndarray, x0=None, sp=None, threads: int = 0) -> np.ndarray:
+    """End states of a ``CbCase`` integrated with a frozen step sequence
+    (``dt_tape`` [max_steps][NS], ``n_steps`` [NS]); optional replacement
+    initial states [UD][NS*UPS] / system parameters [NSP][NS]. Returns x(T)."""
+    lib = _oracle_cb(case.system)
+    if not hasattr(lib.oracle_cb_replay, "_typed"):
+        lib.oracle_cb_replay.restype = C.c_int
+        lib.oracle_cb_replay.argtypes = [C.POINTER(_CbArrays), C.POINTER(_CbOpts), C.c_int, _D, _I, C.c_int,
+                                         C.c_longlong, C.c_longlong, C.c_int]
+        lib.oracle_cb_replay._typed = True
+    a = case.arrays
+    f64 = lambda v: np.ascontiguousarray(np.array(v, dtype=np.float64, copy=True))
+    i32 = lambda v: np.ascontiguousarray(np.array(v, dtype=np.int32, copy=True))
+    st = dict(td=f64(a["td"]), t=f64(a["t"]), sp=f64(a["sp"] if sp is None else sp), sacc=f64(a["sacc"]),
+              cstr=f64(a["cstr"]), dtime=f64(a["dtime"]), x=f64(a["x"] if x0 is None else x0), up=f64(a["up"]),
+              uacc=f64(a["uacc"]), dstate=f64(a["dstate"]), isacc=i32(a["isacc"]), didx=i32(a["didx"]),
+              iuacc=i32(a["iuacc"]), gp=f64(a["gp"]), cmat=f64(case.stored_matrix()), rtol=f64(case.rtol),
+              atol=f64(case.atol), etol=f64(case.etol), igp=i32(a["igp"]), cidx=i32(a["cidx"]), edir=i32(case.edir),
+              status=np.zeros(case.ns, np.int32), nacc=np.zeros(case.ns, np.int32), nrej=np.zeros(case.ns, np.int32))
+    pad = {k: (v if v.size else np.zeros(2, v.dtype)) for k, v in st.items()}
+    arr = _CbArrays(case.ns, *[pad[n].ctypes.data for n, _ in _CbArrays._fields_[1:]])
+    o = case.options
+    opts = _CbOpts(o["initial_dt"], o["max_dt"], o["min_dt"], o["grow"], o["shrink"], o["dense_min_dt"],
+                   int(o["dense_freq"]), int(case.ndo), int(o["max_attempts"]))
+    dt = np.ascontiguousarray(dt_tape, dtype=np.float64)
+    rc = lib.oracle_cb_replay(C.byref(arr), C.byref(opts), int(case.algorithm), dt,
+                              np.ascontiguousarray(n_steps, dtype=np.int32), int(dt.shape[0]), 0, int(case.ns),
+                              int(threads))
+    if rc != 0:
+        raise RuntimeError(f"oracle_cb_replay failed with {rc}")
+    return st["x"]
+
+
 def time_oracle_coupled(case, threads: int = 0, count: int | None = None) -> tuple:
     """Wall time of the coupled oracle on the first ``count`` systems; returns
     (seconds, accepted system-steps)."""

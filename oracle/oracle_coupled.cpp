@@ -416,4 +416,60 @@ __attribute__((visibility("default"))) int oracle_cb_solve(const Arrays* a, cons
     return 0;
 }
 
+// Replay of systems [first, first + count) with a frozen step sequence
+// (dt [max_steps][NS], n_steps [NS]): the stepper only, no controller, events
+// or actions; x, t and sp as given. The discrete map the adjoint
+// differentiates, for finite-difference checks.
+__attribute__((visibility("default"))) int oracle_cb_replay(const Arrays* a, const Opts* o, int algorithm,
+                                                            const double* dt, const int* n_steps, int max_steps,
+                                                            long long first, long long count, int threads)
+{
+    if (!a || !o || !dt || !n_steps || first < 0 || count < 0 || first + count > a->ns) return 1;
+    (void)o;
+#ifdef _OPENMP
+    if (threads > 0) omp_set_num_threads(threads);
+#pragma omp parallel for schedule(dynamic, 1)
+#endif
+    for (long long sidx = first; sidx < first + count; sidx++) {
+        const long long ns = a->ns, nu = ns * UPS;
+        const int sid = static_cast<int>(sidx);
+        System* sp_ = new System();
+        System& sy = *sp_;
+        for (int k = 0; k < NSP; k++) sy.sp[k] = a->sp[sidx + k * ns];
+        for (int k = 0; k < NSA; k++) sy.sacc[k] = a->sacc[sidx + k * ns];
+        for (int k = 0; k < NISA; k++) sy.isacc[k] = a->isacc[sidx + k * ns];
+        for (int k = 0; k < NC; k++) sy.cstr[k] = a->cstr[sidx + k * ns];
+        for (int u = 0; u < UPS; u++) {
+            const long long g = sidx * UPS + u;
+            for (int d = 0; d < UD; d++) sy.x[u][d] = a->x[g + d * nu];
+            for (int k = 0; k < NUP; k++) sy.up[u][k] = a->up[g + k * nu];
+            for (int k = 0; k < NUA; k++) sy.uacc[u][k] = a->uacc[g + k * nu];
+            for (int k = 0; k < NIUA; k++) sy.iuacc[u][k] = a->iuacc[g + k * nu];
+        }
+        double gp[one_at_least<NGP>()];
+        int igp[one_at_least<NIGP>()];
+        for (int k = 0; k < NGP; k++) gp[k] = a->gp[k];
+        for (int k = 0; k < NIGP; k++) igp[k] = a->igp[k];
+        double t = a->t[sidx];
+        const int n = n_steps[sidx] < max_steps ? n_steps[sidx] : max_steps;
+        static thread_local double xn[UPS][UD], err[UPS][UD];
+        for (int k = 0; k < n; k++) {
+            const double h = dt[static_cast<long long>(k) * ns + sidx];
+            int finite = 1;
+            if (algorithm == 0)
+                rk4(sid, sy, gp, igp, a->cmat, a->cidx, t, h, xn, finite);
+            else
+                rkck45(sid, sy, gp, igp, a->cmat, a->cidx, t, h, xn, err, finite);
+            for (int u = 0; u < UPS; u++)
+                for (int d = 0; d < UD; d++) sy.x[u][d] = xn[u][d];
+            t += h;
+        }
+        for (int u = 0; u < UPS; u++)
+            for (int d = 0; d < UD; d++) a->x[sidx * UPS + u + d * nu] = sy.x[u][d];
+        a->t[sidx] = t;
+        delete sp_;
+    }
+    return 0;
+}
+
 }  // extern "C"
