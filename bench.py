@@ -263,13 +263,18 @@ def adjoint_leg(local: int, flush) -> dict:
     import torch
     from mpgos_gb300 import capi, workloads as W
     from mpgos_gb300.solver import Variable
-    nt, max_steps, seg = 1 << 18, 4096, 32
+    nt, seg = 1 << 18, 32
     case = W.duffing_param_case(nt=nt, periods=64, tol=1e-9)
     target = torch.tensor(W.duffing_param_targets(nt), device=f"cuda:{local}")
     mode = capi.MODE_FAST_CONTROL | capi.MODE_PERSISTENT
     out = {"workload": "duffing_param_2^18_rkck45_tol1e-9_64periods_seg32", "unit": "ms"}
     with W.load_solver(case, mode=mode, block=128, device=local) as s:
         s.checkpoint_save()
+        # tape capacity: the largest accepted-step count of a plain forward pass
+        s.Solve()
+        s.SynchroniseFromDeviceToHost(Variable.AcceptedSteps)
+        s.SynchroniseDevice()
+        max_steps = int(s.host(Variable.AcceptedSteps).max()) + 64
         g = torch.empty((2, nt), dtype=torch.float64, device=f"cuda:{local}")
         gx0, gcp = torch.empty_like(g), torch.empty_like(g)
         x_dev = torch.empty_like(g)
@@ -305,7 +310,7 @@ def adjoint_leg(local: int, flush) -> dict:
     f, r, b = statistics.median(fwd), statistics.median(rec), statistics.median(rev)
     out.update({"forward_ms": f, "recording_forward_ms": r, "reverse_ms": b,
                 "adjoint_over_forward": (r + b) / f, "tape_overflow_instances": overflow,
-                "gradients_per_instance": 4})
+                "tape_steps": max_steps, "gradients_per_instance": 4})
     return out
 
 
