@@ -285,6 +285,20 @@ MPGOS_DF_HD dfloat pow(dfloat a, int n)
 {
     return dfloat(std::pow(static_cast<double>(a), static_cast<double>(n)));
 }
+// sin and cos of one argument with one reduction
+MPGOS_DF_HD void sincos(dfloat a, dfloat* s, dfloat* c)
+{
+    int q;
+    const dfloat r = detail::reduce_pio2(a, q);
+    const dfloat sk = detail::sin_kernel(r), ck = detail::cos_kernel(r);
+    switch (q) {
+        case 0: *s = sk; *c = ck; break;
+        case 1: *s = ck; *c = -sk; break;
+        case 2: *s = -sk; *c = -ck; break;
+        default: *s = -ck; *c = sk; break;
+    }
+}
+
 // sin(pi a) and cos(pi a) with pi a formed in double-float
 MPGOS_DF_HD void sincospi(dfloat a, dfloat* s, dfloat* c)
 {

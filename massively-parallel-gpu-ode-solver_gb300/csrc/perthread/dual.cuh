@@ -10,14 +10,17 @@
 //
 // Arithmetic, comparisons and the math functions the hooks use (cos, sin,
 // pow, sqrt, exp, log, fabs/abs, sincospi) are overloaded and found by
-// argument-dependent lookup. The value part always calls CUDA's own function;
-// derivative parts use the analytic derivative identities. A dual whose
+// argument-dependent lookup. Values come from CUDA's own functions, except
+// sin/cos (double-float on the FP32 pipe, see below); derivative parts use
+// the analytic derivative identities. A dual whose
 // derivative part is identically zero (the time argument, shared parameters)
 // skips the derivative evaluation of transcendental functions.
 #pragma once
 
 #include <cuda_runtime.h>
 #include <math.h>
+
+#include "dfloat.cuh"
 
 namespace mpgos {
 namespace ad {
@@ -97,16 +100,26 @@ struct Dual {
     friend __device__ bool operator!=(const Dual& a, const Dual& b) { return a.v != b.v; }
 
     // ---- math functions (found by ADL from the hooks) ----
+    // sin and cos run on the FP32 pipe in double-float (dfloat.cuh: error
+    // ~1e-15 + |x| 2^-48): a dual evaluation only feeds Jacobians and
+    // replayed stage values, where that is far below the tolerance, and an
+    // FP64 sin/cos would cost more FP64-pipe time than the rest of a stage.
+    __device__ static void sincos_value(double x, double* s, double* c) {
+        df::dfloat sd, cd;
+        df::sincos(df::dfloat(x), &sd, &cd);
+        *s = static_cast<double>(sd);
+        *c = static_cast<double>(cd);
+    }
     friend __device__ Dual cos(const Dual& a) {
-        if (a.constant()) return Dual(::cos(a.v));
         double s, c;
-        ::sincos(a.v, &s, &c);
+        sincos_value(a.v, &s, &c);
+        if (a.constant()) return Dual(c);
         return a.chain(c, -s);
     }
     friend __device__ Dual sin(const Dual& a) {
-        if (a.constant()) return Dual(::sin(a.v));
         double s, c;
-        ::sincos(a.v, &s, &c);
+        sincos_value(a.v, &s, &c);
+        if (a.constant()) return Dual(s);
         return a.chain(s, c);
     }
     friend __device__ Dual exp(const Dual& a) { const double e = ::exp(a.v); return a.chain(e, e); }

@@ -383,6 +383,9 @@ def _main(argv=None) -> int:
     ap.add_argument("--mode", type=int, default=0, help="MPGOS_MODE_* bits")
     ap.add_argument("--block", type=int, default=128)
     ap.add_argument("--launches", type=int, default=1)
+    ap.add_argument("--periods", type=int, default=None, help="forcing periods (duffing_param, duffing_rk4)")
+    ap.add_argument("--adjoint", type=int, default=0, metavar="SEG",
+                    help="after the launches: one recording pass and one reverse pass with checkpoints every SEG steps")
     a = ap.parse_args(argv)
     if a.case == "lorenz":
         case = lorenz_case(nt=a.nt)
@@ -390,9 +393,9 @@ def _main(argv=None) -> int:
         side = max(1, int(round(math.sqrt(a.nt))))
         case = keller_miksis_case(n_amp=side, n_freq=max(1, a.nt // side))
     elif a.case == "duffing_param":
-        case = duffing_param_case(nt=a.nt)
+        case = duffing_param_case(nt=a.nt, **({"periods": a.periods} if a.periods else {}))
     else:
-        case = duffing_rk4_case(nt=a.nt)
+        case = duffing_rk4_case(nt=a.nt, **({"periods": a.periods} if a.periods else {}))
     from .solver import Variable
     with load_solver(case, mode=a.mode, block=a.block) as s:
         s.checkpoint_save()
@@ -405,9 +408,21 @@ def _main(argv=None) -> int:
             s.SynchroniseDevice()
             times.append(time.perf_counter() - t0)
         res = read_results(s)
+        adj = None
+        if a.adjoint:
+            import torch
+            s.checkpoint_restore()
+            s.SolveRecord(int(res["nacc"].max()) + 64, a.adjoint)
+            g = torch.ones((s.SD, case.nt), dtype=torch.float64, device="cuda")
+            gx0, gp = torch.empty_like(g), torch.empty((max(s.NCP, 1), case.nt), dtype=torch.float64, device="cuda")
+            s.SynchroniseDevice()
+            t0 = time.perf_counter()
+            s.Adjoint(g.data_ptr(), gx0.data_ptr(), gp.data_ptr())
+            s.SynchroniseDevice()
+            adj = time.perf_counter() - t0
     print(json.dumps({"case": a.case, "nt": case.nt, "mode": a.mode, "block": a.block, "launches": a.launches,
                       "accepted": int(res["nacc"].sum()), "rejected": int(res["nrej"].sum()),
-                      "status_max": int(res["status"].max()), "wall_s_last": times[-1]}))
+                      "status_max": int(res["status"].max()), "wall_s_last": times[-1], "adjoint_wall_s": adj}))
     return 0
 
 
