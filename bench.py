@@ -256,61 +256,72 @@ def adjoint_leg(local: int, flush) -> dict:
     per-instance (k, B), RKCK45 1e-9 over 64 forcing periods, loss = squared
     distance of the terminal state to per-instance targets; gradients with
     respect to (x0, v0, k, B) by the discrete adjoint with a checkpoint every
-    32 accepted steps. Times, on the same inputs: the forward pass alone
-    (FAST_CONTROL + persistent, the FP64 form the adjoint records), the
-    recording forward pass and the reverse pass; the adjoint/forward ratio is
-    (recording + reverse) / forward."""
+    32 accepted steps. For each arithmetic (FP64 with FAST_CONTROL, and
+    DF_STAGE double-float), persistent mapping, on the same inputs: the
+    forward pass alone, the recording forward pass and the reverse pass; the
+    adjoint/forward ratio is (recording + reverse) / forward of the same
+    arithmetic. The headline ratio is the DF_STAGE one."""
     import torch
     from mpgos_gb300 import capi, workloads as W
     from mpgos_gb300.solver import Variable
     nt, seg = 1 << 18, 32
     case = W.duffing_param_case(nt=nt, periods=64, tol=1e-9)
     target = torch.tensor(W.duffing_param_targets(nt), device=f"cuda:{local}")
-    mode = capi.MODE_FAST_CONTROL | capi.MODE_PERSISTENT
-    out = {"workload": "duffing_param_2^18_rkck45_tol1e-9_64periods_seg32", "unit": "ms"}
-    with W.load_solver(case, mode=mode, block=128, device=local) as s:
-        s.checkpoint_save()
-        # tape capacity: the largest accepted-step count of a plain forward pass
-        s.Solve()
-        s.SynchroniseFromDeviceToHost(Variable.AcceptedSteps)
-        s.SynchroniseDevice()
-        max_steps = int(s.host(Variable.AcceptedSteps).max()) + 64
-        g = torch.empty((2, nt), dtype=torch.float64, device=f"cuda:{local}")
-        gx0, gcp = torch.empty_like(g), torch.empty_like(g)
-        x_dev = torch.empty_like(g)
-        fwd, rec, rev = [], [], []
-        for i in range(3):
-            flush_l2(flush)
-            torch.cuda.synchronize()
-            s.checkpoint_restore()
-            s.timer_start()
+    out = {"workload": "duffing_param_2^18_rkck45_tol1e-9_64periods_seg32", "unit": "ms",
+           "gradients_per_instance": 4}
+
+    def run(mode):
+        with W.load_solver(case, mode=mode, block=128, device=local) as s:
+            s.checkpoint_save()
+            # tape capacity: the largest accepted-step count of a plain forward pass
             s.Solve()
-            t_f = s.timer_stop()
-            flush_l2(flush)
-            torch.cuda.synchronize()
-            s.checkpoint_restore()
-            s.timer_start()
-            s.SolveRecord(max_steps, seg)
-            t_r = s.timer_stop()
-            s.SynchroniseFromDeviceToHost(Variable.ActualState)
+            s.SynchroniseFromDeviceToHost(Variable.AcceptedSteps)
             s.SynchroniseDevice()
-            x_dev.copy_(torch.from_numpy(s.host(Variable.ActualState)))
-            g.copy_(2.0 * (x_dev - target))
-            torch.cuda.synchronize()
-            s.timer_start()
-            s.Adjoint(g.data_ptr(), gx0.data_ptr(), gcp.data_ptr())
-            t_b = s.timer_stop()
-            if i:
-                fwd.append(t_f)
-                rec.append(t_r)
-                rev.append(t_b)
-        s.SynchroniseFromDeviceToHost(Variable.Status)
-        s.SynchroniseDevice()
-        overflow = int(np.count_nonzero(s.host(Variable.Status) & capi.INSTANCE_TAPE_OVERFLOW))
-    f, r, b = statistics.median(fwd), statistics.median(rec), statistics.median(rev)
-    out.update({"forward_ms": f, "recording_forward_ms": r, "reverse_ms": b,
-                "adjoint_over_forward": (r + b) / f, "tape_overflow_instances": overflow,
-                "tape_steps": max_steps, "gradients_per_instance": 4})
+            max_steps = int(s.host(Variable.AcceptedSteps).max()) + 64
+            g = torch.empty((2, nt), dtype=torch.float64, device=f"cuda:{local}")
+            gx0, gcp = torch.empty_like(g), torch.empty_like(g)
+            x_dev = torch.empty_like(g)
+            fwd, rec, rev = [], [], []
+            for i in range(3):
+                flush_l2(flush)
+                torch.cuda.synchronize()
+                s.checkpoint_restore()
+                s.timer_start()
+                s.Solve()
+                t_f = s.timer_stop()
+                flush_l2(flush)
+                torch.cuda.synchronize()
+                s.checkpoint_restore()
+                s.timer_start()
+                s.SolveRecord(max_steps, seg)
+                t_r = s.timer_stop()
+                s.SynchroniseFromDeviceToHost(Variable.ActualState)
+                s.SynchroniseDevice()
+                x_dev.copy_(torch.from_numpy(s.host(Variable.ActualState)))
+                g.copy_(2.0 * (x_dev - target))
+                torch.cuda.synchronize()
+                s.timer_start()
+                s.Adjoint(g.data_ptr(), gx0.data_ptr(), gcp.data_ptr())
+                t_b = s.timer_stop()
+                if i:
+                    fwd.append(t_f)
+                    rec.append(t_r)
+                    rev.append(t_b)
+            s.SynchroniseFromDeviceToHost(Variable.Status)
+            s.SynchroniseDevice()
+            overflow = int(np.count_nonzero(s.host(Variable.Status) & capi.INSTANCE_TAPE_OVERFLOW))
+            grad = torch.cat([gx0, gcp]).cpu().numpy()
+        f, r, b = statistics.median(fwd), statistics.median(rec), statistics.median(rev)
+        return {"forward_ms": f, "recording_forward_ms": r, "reverse_ms": b, "adjoint_over_forward": (r + b) / f,
+                "tape_overflow_instances": overflow, "tape_steps": max_steps}, grad
+
+    fp64, g64 = run(capi.MODE_FAST_CONTROL | capi.MODE_PERSISTENT)
+    df, gdf = run(capi.MODE_DF_STAGE | capi.MODE_PERSISTENT)
+    scale = np.maximum(np.max(np.abs(g64), axis=1, keepdims=True), 1e-300)
+    out.update({"fp64": fp64, "df_stage": df, "adjoint_over_forward": df["adjoint_over_forward"],
+                "df_adjoint_over_fp64_forward": (df["recording_forward_ms"] + df["reverse_ms"]) / fp64["forward_ms"],
+                # the two forms take different (both 1e-9-controlled) step sequences
+                "gradient_max_rel_diff_df_vs_fp64": float(np.max(np.abs(gdf - g64) / scale))})
     return out
 
 

@@ -285,6 +285,8 @@ int mpgos_pt_checkpoint_restore(mpgos_pt_solver* solver);
  * mpgos_pt_adjoint: reverse pass over the recorded tape. Device pointers,
  * FP64: dL_dxT [SD][NT] in, dL_dx0 [SD][NT] and dL_dp [NCP][NT] out; the
  * gradient of the discrete map with the recorded step sequence frozen.
+ * Under MPGOS_MODE_DF_STAGE both passes compute in double-float (the tape
+ * stays FP64: a double-float value is a double exactly); otherwise in FP64.
  * Instances whose step count exceeded the tape get MPGOS_INSTANCE_TAPE_OVERFLOW
  * in MPGOS_STATUS and no gradient. Asynchronous on the solver's stream. */
 int mpgos_pt_solve_record(mpgos_pt_solver* solver, int32_t max_steps, int32_t segment);

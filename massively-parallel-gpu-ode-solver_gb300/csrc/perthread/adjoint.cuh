@@ -69,6 +69,50 @@ template <> struct Tableau<MPGOS_RK4> {
     }
 };
 
+// The tableau in the arithmetic type T of a reverse pass (double, or
+// double-float for DF_STAGE), staged once per CTA in shared memory so that no
+// per-use conversion is needed.
+template <class T, int ST>
+struct TableauT {
+    T a[ST][ST];
+    T b[ST];
+    T c[ST];
+};
+
+// Coefficient access: FP64 passes use the compile-time constants directly
+// (immediate operands after unrolling), double-float passes the staged pairs.
+template <class TB, class T>
+__device__ __forceinline__ T tab_a(const TableauT<T, TB::S>& tb, int i, int j)
+{
+    if constexpr (std::is_same<T, double>::value) return TB::a(i, j);
+    else return tb.a[i][j];
+}
+template <class TB, class T>
+__device__ __forceinline__ T tab_b(const TableauT<T, TB::S>& tb, int i)
+{
+    if constexpr (std::is_same<T, double>::value) return TB::b(i);
+    else return tb.b[i];
+}
+template <class TB, class T>
+__device__ __forceinline__ T tab_c(const TableauT<T, TB::S>& tb, int i)
+{
+    if constexpr (std::is_same<T, double>::value) return TB::c(i);
+    else return tb.c[i];
+}
+
+template <class TB, class T>
+__device__ void stage_tableau(TableauT<T, TB::S>& tb)
+{
+    for (int k = threadIdx.x; k < TB::S * TB::S; k += blockDim.x) {
+        const int i = k / TB::S, j = k % TB::S;
+        tb.a[i][j] = T(j < i ? TB::a(i, j) : 0.0);
+    }
+    for (int k = threadIdx.x; k < TB::S; k += blockDim.x) {
+        tb.b[k] = T(TB::b(k));
+        tb.c[k] = T(TB::c(k));
+    }
+}
+
 // Maximum segment length compiled into the reverse kernel (local-memory
 // buffer of the replayed states).
 constexpr int MAX_SEG = 64;
@@ -79,22 +123,22 @@ constexpr int JBUF_DOUBLES = 4096;
 // Stage values K and Jacobians J = [df/dx | df/dp] of one step from (x, t)
 // with step dt, by dual-number evaluation of the user's right-hand side at
 // the stage points X_st = x + dt * sum_j a_st,j K_j.
-template <class TB, int ST, int SD, int N, class D>
-__device__ __forceinline__ void dual_stages(int ti, int nti, const double* x, double t, double dt, D* cpd, D* spd,
-                                            int* spi, D* accd, int* acci, double (&K)[ST][SD],
-                                            double (&J)[ST][SD][N])
+template <class TB, int ST, int SD, int N, class D, class T>
+__device__ __forceinline__ void dual_stages(const TableauT<T, ST>& tb, int ti, int nti, const T* x, T t, T dt, D* cpd,
+                                            D* spd, int* spi, D* accd, int* acci, T (&K)[ST][SD],
+                                            T (&J)[ST][SD][N])
 {
     for (int st = 0; st < ST; st++) {
         D Xd[SD];
         D Fd[SD];
 #pragma unroll
         for (int d = 0; d < SD; d++) {
-            double sum = 0.0;
-            for (int j = 0; j < st; j++) sum += TB::a(st, j) * K[j][d];
+            T sum(0.0);
+            for (int j = 0; j < st; j++) sum += tab_a<TB>(tb, st, j) * K[j][d];
             Xd[d] = D(x[d] + dt * sum);
-            Xd[d].d[d] = 1.0;
+            Xd[d].d[d] = T(1.0);
         }
-        const D Td(t + TB::c(st) * dt);
+        const D Td(t + tab_c<TB>(tb, st) * dt);
         PerThread_OdeFunction(ti, nti, Fd, Xd, Td, cpd, spd, spi, accd, acci);
 #pragma unroll
         for (int d = 0; d < SD; d++) {
@@ -107,35 +151,35 @@ __device__ __forceinline__ void dual_stages(int ti, int nti, const double* x, do
 
 // Adjoint of one Runge-Kutta step with frozen dt: lambda <- lambda + sum_i xi_i,
 // mu += sum_i J_p,i^T kappa_i (see the header comment).
-template <class TB, int ST, int SD, int N, int NCP>
-__device__ __forceinline__ void reverse_step(const double (&J)[ST][SD][N], double dt, double* lam, double* mu)
+template <class TB, int ST, int SD, int N, int NCP, class T>
+__device__ __forceinline__ void reverse_step(const TableauT<T, ST>& tb, const T (&J)[ST][SD][N], T dt, T* lam, T* mu)
 {
-    double kap[ST][SD];
+    T kap[ST][SD];
     for (int st = 0; st < ST; st++)
 #pragma unroll
-        for (int d = 0; d < SD; d++) kap[st][d] = dt * TB::b(st) * lam[d];
-    double dlam[SD];
+        for (int d = 0; d < SD; d++) kap[st][d] = dt * tab_b<TB>(tb, st) * lam[d];
+    T dlam[SD];
 #pragma unroll
-    for (int d = 0; d < SD; d++) dlam[d] = 0.0;
+    for (int d = 0; d < SD; d++) dlam[d] = T(0.0);
     for (int st = ST - 1; st >= 0; st--) {
-        double xi[SD];
+        T xi[SD];
 #pragma unroll
         for (int r = 0; r < SD; r++) {
-            double v = 0.0;
+            T v(0.0);
 #pragma unroll
             for (int d = 0; d < SD; d++) v += J[st][d][r] * kap[st][d];
             xi[r] = v;
         }
 #pragma unroll
         for (int q = 0; q < NCP; q++) {
-            double v = 0.0;
+            T v(0.0);
 #pragma unroll
             for (int d = 0; d < SD; d++) v += J[st][d][SD + q] * kap[st][d];
             mu[q] += v;
         }
         for (int j = 0; j < st; j++) {
-            const double w = dt * TB::a(st, j);
-            if (w != 0.0) {
+            if (TB::a(st, j) != 0.0) {
+                const T w = dt * tab_a<TB>(tb, st, j);
 #pragma unroll
                 for (int d = 0; d < SD; d++) kap[j][d] += w * xi[d];
             }
@@ -147,24 +191,31 @@ __device__ __forceinline__ void reverse_step(const double (&J)[ST][SD][N], doubl
     for (int d = 0; d < SD; d++) lam[d] += dlam[d];
 }
 
-template <class S, int ALG>
+// T is the arithmetic type of the reverse pass: double, or double-float
+// (dfloat, ~48-bit significand on the FP32 pipe) for DF_STAGE solvers. The
+// tape is FP64 either way; a DF forward pass records its double-float steps
+// and checkpoints exactly (hi + lo of a normalised pair fits a double).
+template <class S, int ALG, class T>
 __global__ void __launch_bounds__(MPGOS_MAX_BLOCK) adjoint_kernel(Args<double> a, Tape tp, const double* dLdxT,
                                                                   double* dLdx0, double* dLdp)
 {
     constexpr int SD = S::SD, NCP = S::NCP, NSP = S::NSP, NISP = S::NISP, NA = S::NA, NIA = S::NIA;
     constexpr int N = SD + NCP;  // dual directions: state, then control parameters
-    using D = ad::Dual<N>;
+    using D = ad::Dual<N, T>;
     using TB = Tableau<ALG>;
     constexpr int ST = TB::S;
+    static_assert(sizeof(T) == sizeof(double), "shared parameter layout assumes 8-byte values");
     // Keep a segment's stage Jacobians when they fit the local-memory budget;
     // otherwise replay the states and re-evaluate the dual stages per step.
     constexpr bool STORE_J = MAX_SEG * ST * SD * N <= JBUF_DOUBLES;
 
     extern __shared__ __align__(16) unsigned char mpgos_dyn_smem[];
-    double* sp = reinterpret_cast<double*>(mpgos_dyn_smem);
-    int* spi   = reinterpret_cast<int*>(mpgos_dyn_smem + sizeof(double) * NSP);
-    for (int k = threadIdx.x; k < NSP; k += blockDim.x) sp[k] = a.sp[k];
+    __shared__ TableauT<T, ST> tb;
+    T* sp    = reinterpret_cast<T*>(mpgos_dyn_smem);
+    int* spi = reinterpret_cast<int*>(mpgos_dyn_smem + sizeof(T) * NSP);
+    for (int k = threadIdx.x; k < NSP; k += blockDim.x) sp[k] = T(a.sp[k]);
     for (int k = threadIdx.x; k < NISP; k += blockDim.x) spi[k] = a.spi[k];
+    stage_tableau<TB>(tb);
     __syncthreads();
 
     const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -172,13 +223,13 @@ __global__ void __launch_bounds__(MPGOS_MAX_BLOCK) adjoint_kernel(Args<double> a
     const long long nt = a.nt;
     const int ti = static_cast<int>(i), nti = static_cast<int>(nt);
 
-    double cp[AtLeastOne<NCP>::value];
-    double acc[AtLeastOne<NA>::value];
+    T cp[AtLeastOne<NCP>::value];
+    T acc[AtLeastOne<NA>::value];
     int acci[AtLeastOne<NIA>::value];
 #pragma unroll
-    for (int k = 0; k < NCP; k++) cp[k] = a.cp[i + k * nt];
+    for (int k = 0; k < NCP; k++) cp[k] = T(a.cp[i + k * nt]);
 #pragma unroll
-    for (int k = 0; k < NA; k++) acc[k] = a.acc[i + k * nt];
+    for (int k = 0; k < NA; k++) acc[k] = T(a.acc[i + k * nt]);
 #pragma unroll
     for (int k = 0; k < NIA; k++) acci[k] = a.acci[i + k * nt];
 
@@ -189,18 +240,18 @@ __global__ void __launch_bounds__(MPGOS_MAX_BLOCK) adjoint_kernel(Args<double> a
 #pragma unroll
     for (int k = 0; k < NCP; k++) {
         cpd[k] = D(cp[k]);
-        cpd[k].d[SD + k] = 1.0;
+        cpd[k].d[SD + k] = T(1.0);
     }
     for (int k = 0; k < NSP; k++) spd[k] = D(sp[k]);
 #pragma unroll
     for (int k = 0; k < NA; k++) accd[k] = D(acc[k]);
 
-    double lam[SD];
-    double mu[AtLeastOne<NCP>::value];
+    T lam[SD];
+    T mu[AtLeastOne<NCP>::value];
 #pragma unroll
-    for (int d = 0; d < SD; d++) lam[d] = dLdxT[d * nt + i];
+    for (int d = 0; d < SD; d++) lam[d] = T(dLdxT[d * nt + i]);
 #pragma unroll
-    for (int k = 0; k < NCP; k++) mu[k] = 0.0;
+    for (int k = 0; k < NCP; k++) mu[k] = T(0.0);
 
     const int n = tp.n_steps[i];
     int status = a.status ? a.status[i] : 0;
@@ -214,57 +265,58 @@ __global__ void __launch_bounds__(MPGOS_MAX_BLOCK) adjoint_kernel(Args<double> a
         // Jacobians are kept in local memory, then the segment is swept
         // backwards with algebra only. One right-hand-side evaluation per
         // stage and step in the whole reverse pass.
-        double Jseg[MAX_SEG][ST][SD][N];
+        T Jseg[MAX_SEG][ST][SD][N];
         if (!(status & MPGOS_INSTANCE_TAPE_OVERFLOW) && n > 0) {
             for (int sgm = (n - 1) / seg; sgm >= 0; sgm--) {
                 const int k0 = sgm * seg;
                 const int k1 = min(n, k0 + seg);
-                double x[SD];
-                double t = tp.ckpt_t[static_cast<long long>(sgm) * nt + i];
+                T x[SD];
+                T t(tp.ckpt_t[static_cast<long long>(sgm) * nt + i]);
 #pragma unroll
-                for (int d = 0; d < SD; d++) x[d] = tp.ckpt_x[(static_cast<long long>(sgm) * SD + d) * nt + i];
+                for (int d = 0; d < SD; d++) x[d] = T(tp.ckpt_x[(static_cast<long long>(sgm) * SD + d) * nt + i]);
                 for (int k = k0; k < k1; k++) {
-                    const double dt = tp.dt[static_cast<long long>(k) * nt + i];
-                    double K[ST][SD];
-                    dual_stages<TB, ST, SD, N>(ti, nti, x, t, dt, cpd, spd, spi, accd, acci, K, Jseg[k - k0]);
+                    const T dt(tp.dt[static_cast<long long>(k) * nt + i]);
+                    T K[ST][SD];
+                    dual_stages<TB, ST, SD, N>(tb, ti, nti, x, t, dt, cpd, spd, spi, accd, acci, K, Jseg[k - k0]);
                     if (k + 1 < k1) {
 #pragma unroll
                         for (int d = 0; d < SD; d++) {
-                            double sum = 0.0;
-                            for (int st = 0; st < ST; st++) sum += TB::b(st) * K[st][d];
+                            T sum(0.0);
+                            for (int st = 0; st < ST; st++) sum += tab_b<TB>(tb, st) * K[st][d];
                             x[d] = x[d] + dt * sum;
                         }
                         t += dt;
                     }
                 }
                 for (int k = k1 - 1; k >= k0; k--)
-                    reverse_step<TB, ST, SD, N, NCP>(Jseg[k - k0], tp.dt[static_cast<long long>(k) * nt + i], lam, mu);
+                    reverse_step<TB, ST, SD, N, NCP>(tb, Jseg[k - k0], T(tp.dt[static_cast<long long>(k) * nt + i]),
+                                                     lam, mu);
             }
         }
     } else {
-    double xs[MAX_SEG][SD];
-    double ts[MAX_SEG];
+    T xs[MAX_SEG][SD];
+    T ts[MAX_SEG];
     if (!(status & MPGOS_INSTANCE_TAPE_OVERFLOW) && n > 0) {
         for (int sgm = (n - 1) / seg; sgm >= 0; sgm--) {
             const int k0 = sgm * seg;
             const int k1 = min(n, k0 + seg);
             // replay the segment with the recorded steps
-            double x[SD];
-            double t = tp.ckpt_t[static_cast<long long>(sgm) * nt + i];
+            T x[SD];
+            T t(tp.ckpt_t[static_cast<long long>(sgm) * nt + i]);
 #pragma unroll
-            for (int d = 0; d < SD; d++) x[d] = tp.ckpt_x[(static_cast<long long>(sgm) * SD + d) * nt + i];
+            for (int d = 0; d < SD; d++) x[d] = T(tp.ckpt_x[(static_cast<long long>(sgm) * SD + d) * nt + i]);
             for (int k = k0; k < k1; k++) {
-                const double dt = tp.dt[static_cast<long long>(k) * nt + i];
+                const T dt(tp.dt[static_cast<long long>(k) * nt + i]);
 #pragma unroll
                 for (int d = 0; d < SD; d++) xs[k - k0][d] = x[d];
                 ts[k - k0] = t;
                 if (k + 1 < k1) {
-                    double xn[SD], err[SD];
+                    T xn[SD], err[SD];
                     int finite = 1;
                     if (ALG == MPGOS_RK4)
-                        step_rk4<SD, double>(ti, nti, t, dt, x, xn, finite, cp, sp, spi, acc, acci);
+                        step_rk4<SD, T>(ti, nti, t, dt, x, xn, finite, cp, sp, spi, acc, acci);
                     else
-                        step_rkck45<SD, double, true>(ti, nti, t, dt, x, xn, err, finite, cp, sp, spi, acc, acci);
+                        step_rkck45<SD, T, false>(ti, nti, t, dt, x, xn, err, finite, cp, sp, spi, acc, acci);
 #pragma unroll
                     for (int d = 0; d < SD; d++) x[d] = xn[d];
                     t += dt;
@@ -272,19 +324,19 @@ __global__ void __launch_bounds__(MPGOS_MAX_BLOCK) adjoint_kernel(Args<double> a
             }
             // reverse through the segment, re-evaluating the dual stages
             for (int k = k1 - 1; k >= k0; k--) {
-                const double dt = tp.dt[static_cast<long long>(k) * nt + i];
-                double K[ST][SD];
-                double J[ST][SD][N];
-                dual_stages<TB, ST, SD, N>(ti, nti, xs[k - k0], ts[k - k0], dt, cpd, spd, spi, accd, acci, K, J);
-                reverse_step<TB, ST, SD, N, NCP>(J, dt, lam, mu);
+                const T dt(tp.dt[static_cast<long long>(k) * nt + i]);
+                T K[ST][SD];
+                T J[ST][SD][N];
+                dual_stages<TB, ST, SD, N>(tb, ti, nti, xs[k - k0], ts[k - k0], dt, cpd, spd, spi, accd, acci, K, J);
+                reverse_step<TB, ST, SD, N, NCP>(tb, J, dt, lam, mu);
             }
         }
     }
     }
 #pragma unroll
-    for (int d = 0; d < SD; d++) dLdx0[d * nt + i] = lam[d];
+    for (int d = 0; d < SD; d++) dLdx0[d * nt + i] = static_cast<double>(lam[d]);
 #pragma unroll
-    for (int q = 0; q < NCP; q++) dLdp[q * nt + i] = mu[q];
+    for (int q = 0; q < NCP; q++) dLdp[q * nt + i] = static_cast<double>(mu[q]);
     if (a.status) a.status[i] = status;
 }
 
@@ -307,11 +359,22 @@ struct AdjointTable {
     {
         if (tape == nullptr || tape->segment < 1 || tape->segment > MAX_SEG) return static_cast<int>(cudaErrorInvalidValue);
         void* fn = nullptr;
-        switch (L->mode & (MPGOS_MODE_FAST_CONTROL | MPGOS_MODE_PERSISTENT)) {
-            case 0: fn = reinterpret_cast<void*>(&perthread_kernel<S, ALG, double, MODE_RECORD>); break;
-            case 1: fn = reinterpret_cast<void*>(&perthread_kernel<S, ALG, double, MODE_RECORD | 1>); break;
-            case 2: fn = reinterpret_cast<void*>(&perthread_kernel<S, ALG, double, MODE_RECORD | 2>); break;
-            default: fn = reinterpret_cast<void*>(&perthread_kernel<S, ALG, double, MODE_RECORD | 3>); break;
+        if (L->mode & MPGOS_MODE_DF_STAGE) {
+            if constexpr (ALG == MPGOS_RKCK45) {
+                if (L->mode & MPGOS_MODE_PERSISTENT)
+                    fn = reinterpret_cast<void*>(&perthread_df_kernel<S, MODE_RECORD | MPGOS_MODE_DF_STAGE | 2>);
+                else
+                    fn = reinterpret_cast<void*>(&perthread_df_kernel<S, MODE_RECORD | MPGOS_MODE_DF_STAGE>);
+            } else {
+                return static_cast<int>(cudaErrorInvalidValue);
+            }
+        } else {
+            switch (L->mode & (MPGOS_MODE_FAST_CONTROL | MPGOS_MODE_PERSISTENT)) {
+                case 0: fn = reinterpret_cast<void*>(&perthread_kernel<S, ALG, double, MODE_RECORD>); break;
+                case 1: fn = reinterpret_cast<void*>(&perthread_kernel<S, ALG, double, MODE_RECORD | 1>); break;
+                case 2: fn = reinterpret_cast<void*>(&perthread_kernel<S, ALG, double, MODE_RECORD | 2>); break;
+                default: fn = reinterpret_cast<void*>(&perthread_kernel<S, ALG, double, MODE_RECORD | 3>); break;
+            }
         }
         Args<double> a = make_args<double>(*L);
         a.tape = tape_of(*tape);
@@ -327,8 +390,16 @@ struct AdjointTable {
         Args<double> a = make_args<double>(*L);
         Tape t = tape_of(*tape);
         void* params[] = {&a, &t, &dLdxT, &dLdx0, &dLdp};
-        return static_cast<int>(cudaLaunchKernel(reinterpret_cast<void*>(&adjoint_kernel<S, ALG>), dim3(grid),
-                                                 dim3(block), params, smem, static_cast<cudaStream_t>(stream)));
+        // a DF_STAGE solver differentiates in double-float as well
+        void* fn = reinterpret_cast<void*>(&adjoint_kernel<S, ALG, double>);
+        if (L->mode & MPGOS_MODE_DF_STAGE) {
+            if constexpr (ALG == MPGOS_RKCK45)
+                fn = reinterpret_cast<void*>(&adjoint_kernel<S, ALG, dfloat>);
+            else
+                return static_cast<int>(cudaErrorInvalidValue);
+        }
+        return static_cast<int>(cudaLaunchKernel(fn, dim3(grid), dim3(block), params, smem,
+                                                 static_cast<cudaStream_t>(stream)));
     }
 };
 

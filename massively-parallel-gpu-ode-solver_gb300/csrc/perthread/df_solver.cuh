@@ -135,6 +135,7 @@ template <class S, int MODE>
 struct DfSolver {
     static constexpr int SD = S::SD, NCP = S::NCP, NE = S::NE, NA = S::NA, NIA = S::NIA;
     static constexpr bool PERSISTENT = (MODE & MPGOS_MODE_PERSISTENT) != 0;
+    static constexpr bool RECORD = (MODE & MODE_RECORD) != 0;
     using Inst = DfInstance<S>;
 
     __device__ static void begin(Inst& s, long long i, const Args<double>& a, const DfStaged<S>& g,
@@ -174,6 +175,12 @@ struct DfSolver {
         if (o.ndo > 0)
             dense_store_df<SD>(i, nt, 1, s.didx, o.ndo, a.dtime, a.dstate, s.t, s.x, s.skipped, s.dense_next,
                                o.dense_min_dt, s.td[1]);
+        if constexpr (RECORD) {
+            // checkpoint 0: the state the first step starts from
+            a.tape.ckpt_t[i] = static_cast<double>(s.t);
+#pragma unroll
+            for (int d = 0; d < SD; d++) a.tape.ckpt_x[d * nt + i] = static_cast<double>(s.x[d]);
+        }
     }
 
     __device__ static void attempt(Inst& s, const Args<double>& a, const DfStaged<S>& g, const DfOptions& o)
@@ -227,6 +234,22 @@ struct DfSolver {
                 dense_store_df<SD>(s.i, a.nt, store, s.didx, o.ndo, a.dtime, a.dstate, s.t, s.x, s.skipped,
                                    s.dense_next, o.dense_min_dt, s.td[1]);
             }
+            if constexpr (RECORD) {
+                // frozen step size of accepted step nacc, checkpoint every seg steps
+                const int k = s.nacc - 1;
+                if (k < a.tape.max_steps) {
+                    a.tape.dt[static_cast<long long>(k) * a.nt + s.i] = static_cast<double>(s.dt);
+                    if (s.nacc % a.tape.seg == 0) {
+                        const long long c = s.nacc / a.tape.seg;
+                        a.tape.ckpt_t[c * a.nt + s.i] = static_cast<double>(s.t);
+#pragma unroll
+                        for (int d = 0; d < SD; d++)
+                            a.tape.ckpt_x[(c * SD + d) * a.nt + s.i] = static_cast<double>(s.x[d]);
+                    }
+                } else {
+                    s.status |= MPGOS_INSTANCE_TAPE_OVERFLOW;
+                }
+            }
             if ((end_reached == 1) || (s.udt == 1)) s.terminate = 1;
         } else {
             s.nrej++;
@@ -253,6 +276,7 @@ struct DfSolver {
         if (a.status) a.status[i] = s.status;
         if (a.n_acc) a.n_acc[i] = s.nacc;
         if (a.n_rej) a.n_rej[i] = s.nrej;
+        if constexpr (RECORD) a.tape.n_steps[i] = s.nacc;
     }
 };
 

@@ -20,43 +20,54 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include <type_traits>
+
 #include "dfloat.cuh"
 
 namespace mpgos {
 namespace ad {
 
-template <int N>
+template <int N, class T = double>
 struct Dual {
-    double v;
-    double d[N];
+    T v;
+    T d[N];
 
     __host__ __device__ Dual() : v(0.0) {
 #pragma unroll
-        for (int i = 0; i < N; i++) d[i] = 0.0;
+        for (int i = 0; i < N; i++) d[i] = T(0.0);
     }
-    __host__ __device__ Dual(double x) : v(x) {  // NOLINT: implicit, hooks write static_cast<Precision>(c)
+    __host__ __device__ Dual(T x) : v(x) {  // NOLINT: implicit, hooks write static_cast<Precision>(c)
 #pragma unroll
-        for (int i = 0; i < N; i++) d[i] = 0.0;
+        for (int i = 0; i < N; i++) d[i] = T(0.0);
     }
-    __host__ __device__ explicit operator double() const { return v; }
+    template <class U = T, class = typename std::enable_if<!std::is_same<U, double>::value>::type>
+    __host__ __device__ Dual(double x) : Dual(T(x)) {}  // NOLINT: literals and FP64 values for a double-float T
+    __host__ __device__ explicit operator double() const { return static_cast<double>(v); }
 
     // True when every derivative is +-0 (tested on the bit patterns, which
-    // keeps the FP64 pipe free).
+    // keeps the floating-point pipes free).
     __device__ bool constant() const {
-        long long z = 0;
+        if constexpr (std::is_same<T, double>::value) {
+            long long z = 0;
 #pragma unroll
-        for (int i = 0; i < N; i++) z |= (__double_as_longlong(d[i]) << 1);
-        return z == 0;
+            for (int i = 0; i < N; i++) z |= (__double_as_longlong(d[i]) << 1);
+            return z == 0;
+        } else {
+            int z = 0;
+#pragma unroll
+            for (int i = 0; i < N; i++) z |= (__float_as_int(d[i].hi) << 1);  // a zero double-float has lo == 0
+            return z == 0;
+        }
     }
 
     __device__ Dual& operator+=(const Dual& b) { v += b.v; for (int i = 0; i < N; i++) d[i] += b.d[i]; return *this; }
     __device__ Dual& operator-=(const Dual& b) { v -= b.v; for (int i = 0; i < N; i++) d[i] -= b.d[i]; return *this; }
     __device__ Dual& operator*=(const Dual& b) { *this = *this * b; return *this; }
     __device__ Dual& operator/=(const Dual& b) { *this = *this / b; return *this; }
-    __device__ Dual& operator++() { v += 1.0; return *this; }
+    __device__ Dual& operator++() { v += T(1.0); return *this; }
 
     // chain rule helper: f(v) with derivative f'(v)
-    __device__ Dual chain(double fv, double dfv) const {
+    __device__ Dual chain(T fv, T dfv) const {
         Dual r;
         r.v = fv;
 #pragma unroll
@@ -77,20 +88,20 @@ struct Dual {
     }
     friend __device__ Dual operator/(const Dual& a, const Dual& b) {
         Dual r;
-        const double inv = 1.0 / b.v;
+        const T inv = T(1.0) / b.v;
         r.v = a.v * inv;
 #pragma unroll
         for (int i = 0; i < N; i++) r.d[i] = (a.d[i] - r.v * b.d[i]) * inv;
         return r;
     }
-    friend __device__ Dual operator+(const Dual& a, double b) { Dual r = a; r.v += b; return r; }
-    friend __device__ Dual operator+(double a, const Dual& b) { Dual r = b; r.v += a; return r; }
-    friend __device__ Dual operator-(const Dual& a, double b) { Dual r = a; r.v -= b; return r; }
-    friend __device__ Dual operator-(double a, const Dual& b) { Dual r = -b; r.v += a; return r; }
-    friend __device__ Dual operator*(const Dual& a, double b) { Dual r; r.v = a.v * b; for (int i = 0; i < N; i++) r.d[i] = a.d[i] * b; return r; }
+    friend __device__ Dual operator+(const Dual& a, double b) { Dual r = a; r.v += T(b); return r; }
+    friend __device__ Dual operator+(double a, const Dual& b) { Dual r = b; r.v += T(a); return r; }
+    friend __device__ Dual operator-(const Dual& a, double b) { Dual r = a; r.v -= T(b); return r; }
+    friend __device__ Dual operator-(double a, const Dual& b) { Dual r = -b; r.v += T(a); return r; }
+    friend __device__ Dual operator*(const Dual& a, double b) { const T bb(b); Dual r; r.v = a.v * bb; for (int i = 0; i < N; i++) r.d[i] = a.d[i] * bb; return r; }
     friend __device__ Dual operator*(double a, const Dual& b) { return b * a; }
     friend __device__ Dual operator/(const Dual& a, double b) { return a * (1.0 / b); }
-    friend __device__ Dual operator/(double a, const Dual& b) { return Dual(a) / b; }
+    friend __device__ Dual operator/(double a, const Dual& b) { return Dual(T(a)) / b; }
 
     friend __device__ bool operator<(const Dual& a, const Dual& b) { return a.v < b.v; }
     friend __device__ bool operator>(const Dual& a, const Dual& b) { return a.v > b.v; }
@@ -110,43 +121,44 @@ struct Dual {
         *s = static_cast<double>(sd);
         *c = static_cast<double>(cd);
     }
+    __device__ static void sincos_value(df::dfloat x, df::dfloat* s, df::dfloat* c) { df::sincos(x, s, c); }
     friend __device__ Dual cos(const Dual& a) {
-        double s, c;
+        T s, c;
         sincos_value(a.v, &s, &c);
         if (a.constant()) return Dual(c);
         return a.chain(c, -s);
     }
     friend __device__ Dual sin(const Dual& a) {
-        double s, c;
+        T s, c;
         sincos_value(a.v, &s, &c);
         if (a.constant()) return Dual(s);
         return a.chain(s, c);
     }
-    friend __device__ Dual exp(const Dual& a) { const double e = ::exp(a.v); return a.chain(e, e); }
-    friend __device__ Dual log(const Dual& a) { return a.chain(::log(a.v), 1.0 / a.v); }
-    friend __device__ Dual sqrt(const Dual& a) { const double s = ::sqrt(a.v); return a.chain(s, 0.5 / s); }
-    friend __device__ Dual fabs(const Dual& a) { return a.v < 0.0 ? -a : a; }
-    friend __device__ Dual abs(const Dual& a) { return a.v < 0.0 ? -a : a; }
+    friend __device__ Dual exp(const Dual& a) { const T e = exp(a.v); return a.chain(e, e); }
+    friend __device__ Dual log(const Dual& a) { return a.chain(log(a.v), T(1.0) / a.v); }
+    friend __device__ Dual sqrt(const Dual& a) { const T s = sqrt(a.v); return a.chain(s, T(0.5) / s); }
+    friend __device__ Dual fabs(const Dual& a) { return a.v < T(0.0) ? -a : a; }
+    friend __device__ Dual abs(const Dual& a) { return a.v < T(0.0) ? -a : a; }
     friend __device__ Dual pow(const Dual& a, double e) {
-        const double p = ::pow(a.v, e);
-        return a.chain(p, e * ::pow(a.v, e - 1.0));
+        const T p = pow(a.v, e);
+        return a.chain(p, T(e) * pow(a.v, e - 1.0));
     }
     friend __device__ Dual pow(const Dual& a, const Dual& b) {
         // d(a^b) = b a^(b-1) da + a^b ln(a) db
-        const double p = ::pow(a.v, b.v);
+        const T p = pow(a.v, b.v);
         Dual r;
         r.v = p;
-        const double da = b.v * ::pow(a.v, b.v - 1.0);
+        const T da = b.v * pow(a.v, b.v - T(1.0));
         const bool bconst = b.constant();
-        const double db = bconst ? 0.0 : p * ::log(a.v);
+        const T db = bconst ? T(0.0) : p * log(a.v);
 #pragma unroll
         for (int i = 0; i < N; i++) r.d[i] = da * a.d[i] + db * b.d[i];
         return r;
     }
     friend __device__ void sincospi(const Dual& a, Dual* s, Dual* c) {
-        double sv, cv;
-        ::sincospi(a.v, &sv, &cv);
-        const double w = 3.14159265358979323846;
+        T sv, cv;
+        sincos_value(a.v * T(3.14159265358979323846), &sv, &cv);
+        const T w(3.14159265358979323846);
         *s = a.chain(sv, w * cv);
         *c = a.chain(cv, -w * sv);
     }

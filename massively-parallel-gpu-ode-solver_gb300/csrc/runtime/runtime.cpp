@@ -930,7 +930,7 @@ MPGOS_EXPORT int mpgos_pt_solve_record(mpgos_pt_solver* s, int32_t max_steps, in
         s->tape_bytes = b_dt + b_cx + b_ct + nt * 4;
     }
     if (s->n_active <= 0) return MPGOS_OK;
-    const int32_t m = effective_mode(s, s->mode) & (MPGOS_MODE_FAST_CONTROL | MPGOS_MODE_PERSISTENT);
+    const int32_t m = effective_mode(s, s->mode) & (MPGOS_MODE_FAST_CONTROL | MPGOS_MODE_PERSISTENT | MPGOS_MODE_DF_STAGE);
     int grid = 0;
     if ((rc = grid_for(s, m, s->block, &grid))) return rc;
     if (m & MPGOS_MODE_PERSISTENT) MPGOS_CUDA(cudaMemsetAsync(s->d_work, 0, sizeof(uint32_t), s->stream));
@@ -956,7 +956,8 @@ MPGOS_EXPORT int mpgos_pt_adjoint(mpgos_pt_solver* s, const double* dLdxT, doubl
     const int block = 64;
     const int64_t grid = (s->n_active + block - 1) / block;
     mpgos_pt_launch L;
-    fill_launch(s, L, 0);
+    // the reverse pass computes in double-float when the solver does
+    fill_launch(s, L, effective_mode(s, s->mode) & MPGOS_MODE_DF_STAGE);
     rc = s->k->launch_adjoint(&L, &tape, dLdxT, dLdx0, dLdp, static_cast<int>(grid), block, dynamic_smem(s), s->stream);
     if (rc != 0) return fail(MPGOS_ERR_CUDA, "adjoint launch failed: %s", cudaGetErrorString((cudaError_t)rc));
     return MPGOS_OK;
@@ -1036,7 +1037,7 @@ MPGOS_EXPORT int mpgos_pt_solve_record_static(mpgos_pt_solver* s, int32_t max_st
     // step counts of instances this launch does not integrate read as zero
     MPGOS_CUDA(cudaMemsetAsync(t.n_steps, 0, nt * 4, s->stream));
     if (s->n_active <= 0) return MPGOS_OK;
-    const int32_t m = effective_mode(s, s->mode) & (MPGOS_MODE_FAST_CONTROL | MPGOS_MODE_PERSISTENT);
+    const int32_t m = effective_mode(s, s->mode) & (MPGOS_MODE_FAST_CONTROL | MPGOS_MODE_PERSISTENT | MPGOS_MODE_DF_STAGE);
     int grid = 0;
     if ((rc = grid_for(s, m, s->block, &grid))) return rc;
     if (m & MPGOS_MODE_PERSISTENT) MPGOS_CUDA(cudaMemsetAsync(s->d_work, 0, sizeof(uint32_t), s->stream));

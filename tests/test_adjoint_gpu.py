@@ -80,6 +80,58 @@ def test_adjoint_matches_central_differences_of_the_discrete_map(duffing_case, n
     assert np.max(rel) < 1e-6, np.max(rel)
 
 
+DF_PERSISTENT = capi.MODE_DF_STAGE | capi.MODE_PERSISTENT
+
+
+def test_df_adjoint_matches_central_differences_of_the_discrete_map(duffing_case, native_libs, oracle_libs):
+    """DF_STAGE records its double-float step sequence and differentiates in
+    double-float: same 1e-6 bar against FP64 central differences of the
+    replayed map."""
+    case, target = duffing_case
+    xT, gx0, gcp, (dt, n) = forward_adjoint(case, target, mode=DF_PERSISTENT, want_tape=True)
+    assert np.all(n > 0) and np.all(n <= MAX_STEPS)
+    # the FP64 replay of the double-float forward pass: same map, ~48-bit stages
+    base = O.replay(case, dt, n)
+    assert np.max(np.abs(base - xT) / (np.abs(xT) + 1e-3)) < 1e-9
+    grad = np.concatenate([gx0, gcp], axis=0)
+    fd = np.zeros_like(grad)
+    for j in range(4):
+        x0, cp = case.arrays["x"].copy(), case.arrays["cp"].copy()
+        arr = x0 if j < 2 else cp
+        row = j % 2
+        h = 1e-6 * np.maximum(np.abs(arr[row]), 1.0)
+        out = []
+        for sgn in (+1, -1):
+            x0s, cps = x0.copy(), cp.copy()
+            (x0s if j < 2 else cps)[row] += sgn * h
+            out.append(np.sum((O.replay(case, dt, n, x0=x0s, cp=cps) - target) ** 2, axis=0))
+        fd[j] = (out[0] - out[1]) / (2.0 * h)
+    rel = rel_err(grad, fd)
+    assert np.max(rel) < 1e-6, np.max(rel)
+
+
+def test_df_and_fp64_reverse_passes_agree_on_one_tape(duffing_case, native_libs):
+    """One double-float recorded tape, reversed once in double-float and once
+    in FP64 (mode switched between the calls): the two gradients differ only
+    by the double-float rounding of the reverse pass."""
+    import torch
+    from mpgos_gb300.autograd import AdjointRunner
+    case, target = duffing_case
+    runner = AdjointRunner(case, mode=DF_PERSISTENT, max_steps=MAX_STEPS)
+    x0 = torch.tensor(case.arrays["x"], dtype=torch.float64, device="cuda")
+    cp = torch.tensor(case.arrays["cp"], dtype=torch.float64, device="cuda")
+    xT = runner.forward(x0, cp)
+    g = 2.0 * (xT - torch.tensor(target, device="cuda"))
+    gx_df, gc_df = runner.backward(g)
+    runner.solver.set_mode(capi.MODE_PERSISTENT)
+    gx_64, gc_64 = runner.backward(g)
+    runner.close()
+    a = np.concatenate([gx_df.cpu().numpy(), gc_df.cpu().numpy()])
+    b = np.concatenate([gx_64.cpu().numpy(), gc_64.cpu().numpy()])
+    assert not np.array_equal(a, b)       # two different reverse kernels ran
+    assert np.max(rel_err(a, b)) < 1e-9, np.max(rel_err(a, b))
+
+
 def test_adjoint_matches_forward_sensitivities(duffing_case, native_libs, oracle_libs):
     case, target = duffing_case
     xT, gx0, gcp, _ = forward_adjoint(case, target)
