@@ -256,11 +256,16 @@ def adjoint_leg(local: int, flush) -> dict:
     per-instance (k, B), RKCK45 1e-9 over 64 forcing periods, loss = squared
     distance of the terminal state to per-instance targets; gradients with
     respect to (x0, v0, k, B) by the discrete adjoint with a checkpoint every
-    32 accepted steps. For each arithmetic (FP64 with FAST_CONTROL, and
-    DF_STAGE double-float), persistent mapping, on the same inputs: the
-    forward pass alone, the recording forward pass and the reverse pass; the
-    adjoint/forward ratio is (recording + reverse) / forward of the same
-    arithmetic. The headline ratio is the DF_STAGE one."""
+    32 accepted steps. On the same inputs, persistent mapping, three forms:
+      fp64                 FP64 (FAST_CONTROL) forward, recording and reverse;
+      fp64_fwd_df_reverse  the same FP64 forward and recording, reverse pass
+                           in double-float (KERNEL_MODE switched to DF_STAGE
+                           between SolveRecord and Adjoint);
+      df_stage             double-float forward, recording and reverse.
+    Each times the forward pass alone, the recording forward pass and the
+    reverse pass; adjoint/forward = (recording + reverse) / forward of the
+    same forward arithmetic. The headline is the FP64-forward form with the
+    double-float reverse pass (the configuration integrates in FP64)."""
     import torch
     from mpgos_gb300 import capi, workloads as W
     from mpgos_gb300.solver import Variable
@@ -269,8 +274,12 @@ def adjoint_leg(local: int, flush) -> dict:
     target = torch.tensor(W.duffing_param_targets(nt), device=f"cuda:{local}")
     out = {"workload": "duffing_param_2^18_rkck45_tol1e-9_64periods_seg32", "unit": "ms",
            "gradients_per_instance": 4}
+    FP64 = capi.MODE_FAST_CONTROL | capi.MODE_PERSISTENT
+    DF = capi.MODE_DF_STAGE | capi.MODE_PERSISTENT
 
-    def run(mode):
+    def run(mode, reverse_modes):
+        """Forward and recording in `mode`; one reverse pass per entry of
+        `reverse_modes` on the same tape."""
         with W.load_solver(case, mode=mode, block=128, device=local) as s:
             s.checkpoint_save()
             # tape capacity: the largest accepted-step count of a plain forward pass
@@ -281,8 +290,10 @@ def adjoint_leg(local: int, flush) -> dict:
             g = torch.empty((2, nt), dtype=torch.float64, device=f"cuda:{local}")
             gx0, gcp = torch.empty_like(g), torch.empty_like(g)
             x_dev = torch.empty_like(g)
-            fwd, rec, rev = [], [], []
+            fwd, rec, rev = [], [], {m: [] for m in reverse_modes}
+            grads = {}
             for i in range(3):
+                s.set_mode(mode)
                 flush_l2(flush)
                 torch.cuda.synchronize()
                 s.checkpoint_restore()
@@ -299,29 +310,43 @@ def adjoint_leg(local: int, flush) -> dict:
                 s.SynchroniseDevice()
                 x_dev.copy_(torch.from_numpy(s.host(Variable.ActualState)))
                 g.copy_(2.0 * (x_dev - target))
-                torch.cuda.synchronize()
-                s.timer_start()
-                s.Adjoint(g.data_ptr(), gx0.data_ptr(), gcp.data_ptr())
-                t_b = s.timer_stop()
+                for m in reverse_modes:
+                    s.set_mode(m)
+                    torch.cuda.synchronize()
+                    s.timer_start()
+                    s.Adjoint(g.data_ptr(), gx0.data_ptr(), gcp.data_ptr())
+                    t_b = s.timer_stop()
+                    grads[m] = torch.cat([gx0, gcp]).cpu().numpy()
+                    if i:
+                        rev[m].append(t_b)
                 if i:
                     fwd.append(t_f)
                     rec.append(t_r)
-                    rev.append(t_b)
             s.SynchroniseFromDeviceToHost(Variable.Status)
             s.SynchroniseDevice()
             overflow = int(np.count_nonzero(s.host(Variable.Status) & capi.INSTANCE_TAPE_OVERFLOW))
-            grad = torch.cat([gx0, gcp]).cpu().numpy()
-        f, r, b = statistics.median(fwd), statistics.median(rec), statistics.median(rev)
-        return {"forward_ms": f, "recording_forward_ms": r, "reverse_ms": b, "adjoint_over_forward": (r + b) / f,
-                "tape_overflow_instances": overflow, "tape_steps": max_steps}, grad
+        f, r = statistics.median(fwd), statistics.median(rec)
+        res = {}
+        for m in reverse_modes:
+            b = statistics.median(rev[m])
+            res[m] = {"forward_ms": f, "recording_forward_ms": r, "reverse_ms": b,
+                      "adjoint_over_forward": (r + b) / f, "tape_overflow_instances": overflow,
+                      "tape_steps": max_steps}
+        return res, grads
 
-    fp64, g64 = run(capi.MODE_FAST_CONTROL | capi.MODE_PERSISTENT)
-    df, gdf = run(capi.MODE_DF_STAGE | capi.MODE_PERSISTENT)
-    scale = np.maximum(np.max(np.abs(g64), axis=1, keepdims=True), 1e-300)
-    out.update({"fp64": fp64, "df_stage": df, "adjoint_over_forward": df["adjoint_over_forward"],
-                "df_adjoint_over_fp64_forward": (df["recording_forward_ms"] + df["reverse_ms"]) / fp64["forward_ms"],
-                # the two forms take different (both 1e-9-controlled) step sequences
-                "gradient_max_rel_diff_df_vs_fp64": float(np.max(np.abs(gdf - g64) / scale))})
+    def rel(a, b):
+        return float(np.max(np.abs(a - b) / np.maximum(np.max(np.abs(b), axis=1, keepdims=True), 1e-300)))
+
+    r64, g64 = run(FP64, (FP64, DF))
+    rdf, gdf = run(DF, (DF,))
+    head = r64[DF]
+    out.update({"fp64": r64[FP64], "fp64_fwd_df_reverse": head, "df_stage": rdf[DF],
+                "adjoint_over_forward": head["adjoint_over_forward"],
+                "headline_form": "FP64 forward + recording, double-float reverse",
+                # one FP64 tape reversed in FP64 and in double-float: the reverse arithmetic's own error
+                "gradient_max_rel_diff_df_vs_fp64_reverse_same_tape": rel(g64[DF], g64[FP64]),
+                # different (both 1e-9-controlled) step sequences
+                "gradient_max_rel_diff_df_stage_vs_fp64": rel(gdf[DF], g64[FP64])})
     return out
 
 

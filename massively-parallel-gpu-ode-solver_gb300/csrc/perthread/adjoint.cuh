@@ -117,8 +117,36 @@ __device__ void stage_tableau(TableauT<T, TB::S>& tb)
 // buffer of the replayed states).
 constexpr int MAX_SEG = 64;
 
-// Local-memory budget (doubles) for keeping a whole segment's stage Jacobians.
-constexpr int JBUF_DOUBLES = 4096;
+// Local-memory budget (8-byte values) for keeping a whole segment's stage
+// Jacobians; 0 always takes the replay-and-re-evaluate form.
+#ifndef MPGOS_ADJOINT_JBUF_VALUES
+#define MPGOS_ADJOINT_JBUF_VALUES 4096
+#endif
+constexpr int JBUF_DOUBLES = MPGOS_ADJOINT_JBUF_VALUES;
+
+// Launch shape of the reverse pass: fixed block, and the resident blocks per
+// SM the register allocation is held to: FP64 passes (FP64-pipe bound, local
+// Jacobian buffer) take occupancy, double-float passes registers (the
+// segment-tangent form keeps every stage's dual values in registers).
+#ifndef MPGOS_ADJOINT_MIN_BLOCKS
+#define MPGOS_ADJOINT_MIN_BLOCKS 12
+#endif
+#ifndef MPGOS_ADJOINT_MIN_BLOCKS_DF
+#define MPGOS_ADJOINT_MIN_BLOCKS_DF 4
+#endif
+constexpr int ADJOINT_BLOCK = 64;
+template <class T>
+struct AdjointMinBlocks {
+    static constexpr int value = std::is_same<T, double>::value ? MPGOS_ADJOINT_MIN_BLOCKS : MPGOS_ADJOINT_MIN_BLOCKS_DF;
+};
+
+// Largest SD x (SD + NCP + 1) (dual values of the state) for which a
+// double-float reverse pass takes the segment-tangent form; 0 disables it.
+#ifndef MPGOS_ADJOINT_TANGENT_MAX
+#define MPGOS_ADJOINT_TANGENT_MAX 16
+#endif
+constexpr int ADJOINT_TANGENT_MAX = MPGOS_ADJOINT_TANGENT_MAX;
+constexpr int ADJOINT_MIN_BLOCKS = MPGOS_ADJOINT_MIN_BLOCKS;
 
 // Stage values K and Jacobians J = [df/dx | df/dp] of one step from (x, t)
 // with step dt, by dual-number evaluation of the user's right-hand side at
@@ -191,12 +219,55 @@ __device__ __forceinline__ void reverse_step(const TableauT<T, ST>& tb, const T 
     for (int d = 0; d < SD; d++) lam[d] += dlam[d];
 }
 
+// y += a x for dual numbers and a plain coefficient a.
+template <int N, class T>
+__device__ __forceinline__ void dual_axpy(ad::Dual<N, T>& y, T a, const ad::Dual<N, T>& x)
+{
+    y.v = ad::mad(a, x.v, y.v);
+#pragma unroll
+    for (int q = 0; q < N; q++) y.d[q] = ad::mad(a, x.d[q], y.d[q]);
+}
+// One Runge-Kutta step with frozen dt carried out entirely in dual numbers:
+// x holds the state and its tangents d x / d (segment start state, control
+// parameters); on return, the state and tangents one step later.
+template <class TB, int ST, int SD, int N, class D, class T>
+__device__ __forceinline__ void tangent_step(const TableauT<T, ST>& tb, int ti, int nti, D* x, T t, T dt, D* cpd,
+                                             D* spd, int* spi, D* accd, int* acci)
+{
+    // stage sums with the step folded into the coefficients: X_st = x + sum_j (dt a_st,j) K_j
+    D K[ST][SD];
+#pragma unroll
+    for (int st = 0; st < ST; st++) {
+        D Xd[SD];
+#pragma unroll
+        for (int d = 0; d < SD; d++) Xd[d] = x[d];
+#pragma unroll
+        for (int j = 0; j < st; j++) {
+            if (TB::a(st, j) != 0.0) {
+                const T h = dt * tab_a<TB>(tb, st, j);
+#pragma unroll
+                for (int d = 0; d < SD; d++) dual_axpy(Xd[d], h, K[j][d]);
+            }
+        }
+        const D Td(ad::mad(tab_c<TB>(tb, st), dt, t));
+        PerThread_OdeFunction(ti, nti, K[st], Xd, Td, cpd, spd, spi, accd, acci);
+    }
+#pragma unroll
+    for (int st = 0; st < ST; st++) {
+        if (TB::b(st) != 0.0) {
+            const T h = dt * tab_b<TB>(tb, st);
+#pragma unroll
+            for (int d = 0; d < SD; d++) dual_axpy(x[d], h, K[st][d]);
+        }
+    }
+}
+
 // T is the arithmetic type of the reverse pass: double, or double-float
 // (dfloat, ~48-bit significand on the FP32 pipe) for DF_STAGE solvers. The
 // tape is FP64 either way; a DF forward pass records its double-float steps
 // and checkpoints exactly (hi + lo of a normalised pair fits a double).
 template <class S, int ALG, class T>
-__global__ void __launch_bounds__(MPGOS_MAX_BLOCK) adjoint_kernel(Args<double> a, Tape tp, const double* dLdxT,
+__global__ void __launch_bounds__(ADJOINT_BLOCK, AdjointMinBlocks<T>::value) adjoint_kernel(Args<double> a, Tape tp, const double* dLdxT,
                                                                   double* dLdx0, double* dLdp)
 {
     constexpr int SD = S::SD, NCP = S::NCP, NSP = S::NSP, NISP = S::NISP, NA = S::NA, NIA = S::NIA;
@@ -208,6 +279,9 @@ __global__ void __launch_bounds__(MPGOS_MAX_BLOCK) adjoint_kernel(Args<double> a
     // Keep a segment's stage Jacobians when they fit the local-memory budget;
     // otherwise replay the states and re-evaluate the dual stages per step.
     constexpr bool STORE_J = MAX_SEG * ST * SD * N <= JBUF_DOUBLES;
+    // Double-float reverse passes of small systems propagate tangents through
+    // each segment instead (no per-step storage; see below).
+    constexpr bool TANGENT = !std::is_same<T, double>::value && SD * (N + 1) <= ADJOINT_TANGENT_MAX;
 
     extern __shared__ __align__(16) unsigned char mpgos_dyn_smem[];
     __shared__ TableauT<T, ST> tb;
@@ -259,7 +333,52 @@ __global__ void __launch_bounds__(MPGOS_MAX_BLOCK) adjoint_kernel(Args<double> a
 
     const int seg = tp.seg;
 
-    if constexpr (STORE_J) {
+    if constexpr (TANGENT) {
+        // Segment by segment, last first: replay the segment from its
+        // checkpoint with every value a dual number seeded with the identity
+        // on the state (the control parameters are seeded in cpd), so that
+        // at the segment end the duals hold the segment's Jacobians
+        // Phi = d x_end / d x_start and Psi = d x_end / d cPAR. Then
+        //     mu += Psi^T lambda,   lambda <- Phi^T lambda.
+        // This is the same discrete gradient as the per-step reverse sweep
+        // (the chain rule through the same frozen steps, multiplied in another
+        // order); it trades the stored stage Jacobians for SD x N more
+        // arithmetic per stage sum, which pays where the Jacobian buffer would
+        // go to DRAM and the arithmetic runs on the FP32 pipe.
+        if (!(status & MPGOS_INSTANCE_TAPE_OVERFLOW) && n > 0) {
+            for (int sgm = (n - 1) / seg; sgm >= 0; sgm--) {
+                const int k0 = sgm * seg;
+                const int k1 = min(n, k0 + seg);
+                D xd[SD];
+                T t(tp.ckpt_t[static_cast<long long>(sgm) * nt + i]);
+#pragma unroll
+                for (int d = 0; d < SD; d++) {
+                    xd[d] = D(T(tp.ckpt_x[(static_cast<long long>(sgm) * SD + d) * nt + i]));
+                    xd[d].d[d] = T(1.0);
+                }
+                for (int k = k0; k < k1; k++) {
+                    const T dt(tp.dt[static_cast<long long>(k) * nt + i]);
+                    tangent_step<TB, ST, SD, N>(tb, ti, nti, xd, t, dt, cpd, spd, spi, accd, acci);
+                    t += dt;
+                }
+#pragma unroll
+                for (int q = 0; q < NCP; q++) {
+#pragma unroll
+                    for (int d = 0; d < SD; d++) mu[q] += xd[d].d[SD + q] * lam[d];
+                }
+                T ln[SD];
+#pragma unroll
+                for (int r = 0; r < SD; r++) {
+                    T v(0.0);
+#pragma unroll
+                    for (int d = 0; d < SD; d++) v += xd[d].d[r] * lam[d];
+                    ln[r] = v;
+                }
+#pragma unroll
+                for (int d = 0; d < SD; d++) lam[d] = ln[d];
+            }
+        }
+    } else if constexpr (STORE_J) {
         // One forward pass per segment with dual-number stages: the stage
         // values advance the state (tableau form of the step), the stage
         // Jacobians are kept in local memory, then the segment is swept

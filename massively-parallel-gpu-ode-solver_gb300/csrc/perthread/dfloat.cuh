@@ -14,6 +14,9 @@
 //   add             "sloppy" double-float add of Hida, Li & Bailey (QD
 //                   library, 2001): error <= ~2^-46 (|a| + |b|)
 //   mul             double-float multiply with FMA (same source)
+//   fma, dot2       a*b + c and a*b + c*d: the exact leading products summed
+//                   by two_sum, all low-order terms folded into one tail
+//                   (the same error class as add)
 //   div             two long-division correction steps on a float quotient
 //   sqrt            Karp & Markstein 1997 (Newton corrections from rsqrt)
 // sin, cos and sincospi run on the FP32 pipe too (Cody-Waite reduction and
@@ -148,6 +151,35 @@ MPGOS_DF_HD dfloat operator*(dfloat a, dfloat b)
     float e = f_fma(a.hi, b.lo, p.lo);
     e = f_fma(a.lo, b.hi, e);
     return quick_two_sum(p.hi, e);
+}
+
+// a * b + c with one renormalisation (the sloppy add of the exact leading
+// product and c, the product's and c's low parts folded into the tail):
+// 15 FP32 operations instead of 18 for a multiply then an add.
+MPGOS_DF_HD dfloat fma(dfloat a, dfloat b, dfloat c)
+{
+    const dfloat p = two_prod(a.hi, b.hi);
+    const dfloat s = two_sum(p.hi, c.hi);
+    float e = f_add(p.lo, c.lo);
+    e = f_fma(a.hi, b.lo, e);
+    e = f_fma(a.lo, b.hi, e);
+    e = f_add(e, s.lo);
+    return quick_two_sum(s.hi, e);
+}
+
+// a * b + c * d the same way (19 operations instead of 25).
+MPGOS_DF_HD dfloat dot2(dfloat a, dfloat b, dfloat c, dfloat d)
+{
+    const dfloat p = two_prod(a.hi, b.hi);
+    const dfloat q = two_prod(c.hi, d.hi);
+    const dfloat s = two_sum(p.hi, q.hi);
+    float e = f_add(p.lo, q.lo);
+    e = f_fma(a.hi, b.lo, e);
+    e = f_fma(a.lo, b.hi, e);
+    e = f_fma(c.hi, d.lo, e);
+    e = f_fma(c.lo, d.hi, e);
+    e = f_add(e, s.lo);
+    return quick_two_sum(s.hi, e);
 }
 
 // a * f for a float f (one product term fewer)

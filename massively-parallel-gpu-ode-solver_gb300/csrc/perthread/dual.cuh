@@ -27,6 +27,16 @@
 namespace mpgos {
 namespace ad {
 
+// a*b + c and a*b + c*d in the value type: contracted FP64 expressions, or
+// the fused double-float forms (fewer FP32 operations than separate ops).
+__host__ __device__ __forceinline__ double mad(double a, double b, double c) { return a * b + c; }
+__host__ __device__ __forceinline__ double mad2(double a, double b, double c, double d) { return a * b + c * d; }
+__device__ __forceinline__ df::dfloat mad(df::dfloat a, df::dfloat b, df::dfloat c) { return df::fma(a, b, c); }
+__device__ __forceinline__ df::dfloat mad2(df::dfloat a, df::dfloat b, df::dfloat c, df::dfloat d)
+{
+    return df::dot2(a, b, c, d);
+}
+
 template <int N, class T = double>
 struct Dual {
     T v;
@@ -83,7 +93,7 @@ struct Dual {
         Dual r;
         r.v = a.v * b.v;
 #pragma unroll
-        for (int i = 0; i < N; i++) r.d[i] = a.d[i] * b.v + a.v * b.d[i];
+        for (int i = 0; i < N; i++) r.d[i] = mad2(a.d[i], b.v, a.v, b.d[i]);
         return r;
     }
     friend __device__ Dual operator/(const Dual& a, const Dual& b) {

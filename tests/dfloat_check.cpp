@@ -19,7 +19,7 @@ int main()
     std::mt19937_64 rng(12345);
     std::uniform_real_distribution<double> u(-1.0, 1.0), e(-8.0, 8.0);
     auto draw = [&]() { return dfloat(u(rng) * std::pow(2.0, std::floor(e(rng)))); };
-    double m_add = 0, m_mul = 0, m_div = 0, m_sqrt = 0, m_cvt = 0, m_cmp = 0, m_norm = 0;
+    double m_add = 0, m_mul = 0, m_div = 0, m_sqrt = 0, m_cvt = 0, m_cmp = 0, m_norm = 0, m_fma = 0, m_dot = 0;
     for (int n = 0; n < 200000; n++) {
         const dfloat a = draw(), b = draw();
         const long double A = val(a), B = val(b);
@@ -29,8 +29,14 @@ int main()
         m_mul = std::fmax(m_mul, (double)(std::fabs(val(p) - A * B) / std::fabs(A * B)));
         m_div = std::fmax(m_div, (double)(std::fabs(val(q) - A / B) / std::fabs(A / B)));
         m_sqrt = std::fmax(m_sqrt, (double)(std::fabs(val(r) - std::sqrt(std::fabs(A))) / std::sqrt(std::fabs(A))));
+        // fused forms, error relative to the sum of the terms' magnitudes
+        const dfloat c = draw(), dd = draw();
+        const long double C = val(c), D = val(dd);
+        const dfloat f = mpgos::df::fma(a, b, c), g = mpgos::df::dot2(a, b, c, dd);
+        m_fma = std::fmax(m_fma, (double)(std::fabs(val(f) - (A * B + C)) / (std::fabs(A * B) + std::fabs(C))));
+        m_dot = std::fmax(m_dot, (double)(std::fabs(val(g) - (A * B + C * D)) / (std::fabs(A * B) + std::fabs(C * D))));
         // normalisation: |lo| <= ulp(hi) / 2 after every operation
-        for (dfloat z : {s, p, q, r})
+        for (dfloat z : {s, p, q, r, f, g})
             if (z.hi != 0.0f) m_norm = std::fmax(m_norm, std::fabs(z.lo) / (std::nextafter(std::fabs(z.hi), INFINITY) - std::fabs(z.hi)));
         // conversion from double keeps 48 bits
         const double d = u(rng) * std::pow(2.0, std::floor(e(rng)));
@@ -52,7 +58,8 @@ int main()
             m_trig_small = std::fmax(m_trig_small, (double)std::fmax(std::fabs(val(mpgos::df::sin(x)) - std::sin(X)),
                                                                      std::fabs(val(mpgos::df::cos(x)) - std::cos(X))));
     }
-    std::printf("add %.3e\nmul %.3e\ndiv %.3e\nsqrt %.3e\ncvt %.3e\ncmp %.0f\nnorm %.3f\ntrig %.3f\ntrig_small %.3e\n",
-                m_add, m_mul, m_div, m_sqrt, m_cvt, m_cmp, m_norm, m_trig, m_trig_small);
+    std::printf("add %.3e\nmul %.3e\ndiv %.3e\nsqrt %.3e\ncvt %.3e\ncmp %.0f\nnorm %.3f\ntrig %.3f\ntrig_small %.3e\n"
+                "fma %.3e\ndot2 %.3e\n",
+                m_add, m_mul, m_div, m_sqrt, m_cvt, m_cmp, m_norm, m_trig, m_trig_small, m_fma, m_dot);
     return 0;
 }

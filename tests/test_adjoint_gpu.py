@@ -110,18 +110,21 @@ def test_df_adjoint_matches_central_differences_of_the_discrete_map(duffing_case
     assert np.max(rel) < 1e-6, np.max(rel)
 
 
-def test_df_and_fp64_reverse_passes_agree_on_one_tape(duffing_case, native_libs):
-    """One double-float recorded tape, reversed once in double-float and once
-    in FP64 (mode switched between the calls): the two gradients differ only
-    by the double-float rounding of the reverse pass."""
+@pytest.mark.parametrize("record_mode", [DF_PERSISTENT, capi.MODE_CHOSEN])
+def test_df_and_fp64_reverse_passes_agree_on_one_tape(record_mode, duffing_case, native_libs):
+    """One recorded tape (double-float or FP64 forward), reversed once in
+    double-float and once in FP64 (KERNEL_MODE switched between the calls):
+    the two gradients differ only by the double-float rounding of the
+    reverse pass."""
     import torch
     from mpgos_gb300.autograd import AdjointRunner
     case, target = duffing_case
-    runner = AdjointRunner(case, mode=DF_PERSISTENT, max_steps=MAX_STEPS)
+    runner = AdjointRunner(case, mode=record_mode, max_steps=MAX_STEPS)
     x0 = torch.tensor(case.arrays["x"], dtype=torch.float64, device="cuda")
     cp = torch.tensor(case.arrays["cp"], dtype=torch.float64, device="cuda")
     xT = runner.forward(x0, cp)
     g = 2.0 * (xT - torch.tensor(target, device="cuda"))
+    runner.solver.set_mode(DF_PERSISTENT)
     gx_df, gc_df = runner.backward(g)
     runner.solver.set_mode(capi.MODE_PERSISTENT)
     gx_64, gc_64 = runner.backward(g)

@@ -20,8 +20,9 @@ def errors(tmp_path_factory):
 
 def test_double_float_precision(errors):
     # ~48 significant bits: 2^-46 = 1.4e-14 covers every operation's bound
-    for op in ("add", "mul", "div", "sqrt"):
+    for op in ("add", "mul", "div", "sqrt", "fma"):
         assert errors[op] < 1.5e-14, (op, errors[op])
+    assert errors["dot2"] < 2.5e-14, errors["dot2"]   # two products' tails, relative to |ab| + |cd|
     assert errors["cvt"] < 4e-15          # double -> double-float keeps 48 bits (2^-48)
 
 
