@@ -386,10 +386,68 @@ def coupled_leg(local: int, flush) -> dict:
         steps = float(res["isacc"][0].sum())  # accepted steps, counted by the systems' own hook
         return {"ms": statistics.median(times), "value": steps / (statistics.median(times) / 1e3)}, res
 
+    def adjoint(mode, reverse_modes, warps, seg=32):
+        """Recording forward pass in `mode` and one reverse pass per entry of
+        `reverse_modes` on that tape, for the gradient of the summed terminal
+        energy E = sum_i (v_i^2/2 + x_i^2/2 + x_i^4/4) with respect to B (and
+        the initial states); median of two timed rounds after one warm-up,
+        L2 flushed before each pass."""
+        with CW.load_coupled_solver(case, mode=mode, warps=warps, device=local) as s:
+            s.checkpoint_save()
+            s.Solve()
+            res = CW.read_coupled_results(s)
+            max_steps = int(max(res["nacc"].max(), res["isacc"][0].max() if len(res["isacc"]) else 0)) + 64
+            nu = case.ns * case.ups
+            dev = f"cuda:{local}"
+            gx0 = torch.empty((2, nu), dtype=torch.float64, device=dev)
+            gsp = torch.empty((max(s.NSP, 1), case.ns), dtype=torch.float64, device=dev)
+            rec, rev = [], {m: [] for m in reverse_modes}
+            for i in range(3):
+                s.set_mode(mode)
+                flush_l2(flush)
+                torch.cuda.synchronize()
+                s.checkpoint_restore()
+                s.timer_start()
+                s.SolveRecord(max_steps, seg)
+                t_r = s.timer_stop()
+                s.SynchroniseFromDeviceToHost(V.ActualState)
+                s.SynchroniseDevice()
+                xT = s.host(V.ActualState)
+                gT = torch.tensor(np.stack([xT[0] + xT[0] ** 3, xT[1]]), device=dev)
+                for m in reverse_modes:
+                    s.set_mode(m)
+                    flush_l2(flush)
+                    torch.cuda.synchronize()
+                    s.timer_start()
+                    s.Adjoint(gT.data_ptr(), gx0.data_ptr(), gsp.data_ptr())
+                    t_b = s.timer_stop()
+                    if i:
+                        rev[m].append(t_b)
+                if i:
+                    rec.append(t_r)
+            s.SynchroniseFromDeviceToHost(V.Status)
+            s.SynchroniseDevice()
+            overflow = int(np.count_nonzero(s.host(V.Status) & capi.INSTANCE_TAPE_OVERFLOW))
+        return {m: {"recording_forward_ms": statistics.median(rec), "reverse_ms": statistics.median(rev[m]),
+                    "tape_steps": max_steps, "segment": seg, "tape_overflow_systems": overflow}
+                for m in reverse_modes}
+
     out = {"workload": "ring64_16384x64_dense_rkck45_tol1e-9_2periods", "unit": "accepted system-steps/s"}
     df, rdf = run(capi.MODE_DF_STAGE | capi.MODE_PERSISTENT, warps=2)
     fp, rfp = run(capi.MODE_PERSISTENT, warps=4)
     out["df_stage"], out["fp64"] = df, fp
+    FP, DFM = capi.MODE_PERSISTENT, capi.MODE_DF_STAGE | capi.MODE_PERSISTENT
+    a64 = adjoint(FP, (FP, DFM), warps=4)
+    adf = adjoint(DFM, (DFM,), warps=2)
+    forms = {"fp64": (a64[FP], fp), "fp64_fwd_df_reverse": (a64[DFM], fp), "df_stage": (adf[DFM], df)}
+    adj = {}
+    for name, (r, f) in forms.items():
+        r["forward_ms"] = f["ms"]
+        r["adjoint_over_forward"] = (r["recording_forward_ms"] + r["reverse_ms"]) / f["ms"]
+        adj[name] = r
+    adj["adjoint_over_forward"] = adj["fp64_fwd_df_reverse"]["adjoint_over_forward"]
+    adj["headline_form"] = "FP64 forward + recording, double-float reverse"
+    out["adjoint_wrt_B"] = adj
     from oracle import ref_gpu as R
     if R.coupled_available("ring64", 1, case.ns, 256, 4, 0):
         ref, rref = run(ref=(256, 4))

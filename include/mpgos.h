@@ -406,12 +406,13 @@ typedef struct mpgos_cb_kernels {
     int (*occupancy)(int32_t mode, int block, size_t dynamic_smem, int* blocks_per_sm);
     size_t (*dynamic_smem)(int warps_per_block, int shared_global, int shared_coupling);
     /* discrete adjoint (NULL where not compiled): the recording forward launch,
-     * the reverse launch and its dynamic shared memory */
+     * the reverse launch and its dynamic shared memory (FP64, or double-float
+     * when `mode` has MPGOS_MODE_DF_STAGE) */
     int (*launch_record)(const mpgos_cb_launch* args, const mpgos_pt_tape* tape, int grid, int block,
                          size_t dynamic_smem, void* stream);
     int (*launch_adjoint)(const mpgos_cb_launch* args, const mpgos_pt_tape* tape, const double* dL_dxT,
                           double* dL_dx0, double* dL_dsp, int grid, int block, size_t dynamic_smem, void* stream);
-    size_t (*adjoint_smem)(int warps_per_block);
+    size_t (*adjoint_smem)(int warps_per_block, int32_t mode);
 } mpgos_cb_kernels;
 
 typedef struct mpgos_cb_solver mpgos_cb_solver;

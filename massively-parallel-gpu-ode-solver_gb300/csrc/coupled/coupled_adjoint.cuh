@@ -1,5 +1,6 @@
 // Discrete adjoint of the coupled per-block integration (extension: the
-// reference has no differentiation). One warp per system, FP64.
+// reference has no differentiation). One warp per system, in FP64 or, for
+// DF_STAGE solvers, in double-float (T = dfloat; the tape stays FP64).
 //
 // Forward (recording) pass: the coupled kernel compiled with MODE_RECORD
 // (coupled_kernel.cuh) stores, per system, every accepted step size and a
@@ -40,39 +41,45 @@ namespace cb {
 
 // Per-warp shared slot of the reverse pass: the forward slot (system scope,
 // coupling terms) plus the transposed-product inputs z.
-template <class S>
+template <class S, class T>
 struct AdjSlot {
-    WarpSlot<S, double> w;
-    double z[S::UPS][AtLeastOne<S::NC>::value];
+    WarpSlot<S, T> w;
+    T z[S::UPS][AtLeastOne<S::NC>::value];
 };
 
 // Dynamic shared memory of the reverse kernel: [global parameters NGP]
 // [coupling matrices NC*MAT][transposed full matrices NC*UPS*UPS if full
 // storage][integer global parameters NIGP], padded to 16 bytes, then one
 // AdjSlot per warp.
-template <class S>
+template <class S, class T>
 __host__ __device__ constexpr size_t adjoint_block_part_bytes()
 {
     constexpr bool FULL = (S::CCI == 0 && S::CBW == 0);
-    const size_t b = sizeof(double) * (S::NGP + S::NC * S::MAT + (FULL ? S::NC * S::UPS * S::UPS : 0)) +
+    const size_t b = sizeof(T) * (S::NGP + S::NC * S::MAT + (FULL ? S::NC * S::UPS * S::UPS : 0)) +
                      sizeof(int) * S::NIGP;
     return (b + 15) / 16 * 16;
 }
 
-template <class S>
+template <class S, class T>
 __host__ __device__ constexpr size_t adjoint_smem_bytes(int warps)
 {
-    return adjoint_block_part_bytes<S>() + static_cast<size_t>(warps) * sizeof(AdjSlot<S>);
+    return adjoint_block_part_bytes<S, T>() + static_cast<size_t>(warps) * sizeof(AdjSlot<S, T>);
 }
 
 // w_{j,c} = sum_u C_c[u][j] z_{u,c} for unit j, in each of the four storages
 // of the coupling matrix (the transposes of coupling_value).
-template <class S>
-__device__ __forceinline__ double transposed_coupling_value(const double* M, const double* MT, const AdjSlot<S>& sl,
-                                                            int j, int c)
+template <class S, class T>
+__device__ __forceinline__ T transposed_coupling_value(const T* M, const T* MT, const AdjSlot<S, T>& sl, int j, int c)
 {
     constexpr int UPS = S::UPS, CBW = S::CBW, CCI = S::CCI;
-    double v = 0.0;
+    if constexpr (IS_DF<T> && CCI == 0 && CBW == 0) {
+        // compensated double-float dot product, as in the forward product
+        const int shift = c * UPS * UPS;
+        float sh = 0.0f, sl_ = 0.0f;
+        for (int u = 0; u < UPS; u++) df_dot_acc(sh, sl_, MT[j + u * UPS + shift], sl.z[u][c]);
+        return df::two_sum(sh, sl_);
+    }
+    T v(0.0);
     if (CCI == 0 && CBW == 0) {
         const int shift = c * UPS * UPS;
         for (int u = 0; u < UPS; u++) v += MT[j + u * UPS + shift] * sl.z[u][c];
@@ -89,43 +96,44 @@ __device__ __forceinline__ double transposed_coupling_value(const double* M, con
     return v;
 }
 
-template <class S, int ALG>
+template <class S, int ALG, class T>
 struct CoupledAdjoint {
     static constexpr int UPS = S::UPS, UD = S::UD, NC = S::NC, NUP = S::NUP, NSP = S::NSP, NUA = S::NUA;
     static constexpr int NIUA = S::NIUA, NSA = S::NSA, NISA = S::NISA, UPL = S::UPL;
     static constexpr int N = UD + NSP;  // dual directions: the unit's state, then the system parameters
-    using D = ad::Dual<N>;
+    using D = ad::Dual<N, T>;
     using TB = pt::Tableau<ALG>;
     static constexpr int ST = TB::S;
-    using Fwd = Solver<S, ALG, double, 0>;
+    using Tab = pt::TableauT<T, ST>;
+    using Fwd = Solver<S, ALG, T, 0>;
     using Units = typename Fwd::Units;
     static constexpr int NCP1 = AtLeastOne<NC>::value;
 
     // Stage data of one step, per unit of the lane.
     struct StepData {
-        double K[ST][UPL][UD];         // stage derivatives (with coupling)
-        double L[ST][UPL][UD][N];      // d(uncoupled F)/d(X_u, sPAR)
-        double G[ST][UPL][NCP1][N];    // d(CPT)/d(X_u, sPAR)
-        double CF[ST][UPL][NCP1];      // CPF value
-        double CFD[ST][UPL][NCP1][N];  // d(CPF)/d(X_u, sPAR)
-        double V[ST][UPL][NCP1];       // coupling value sum_j C[u][j] CPT_j
+        T K[ST][UPL][UD];         // stage derivatives (with coupling)
+        T L[ST][UPL][UD][N];      // d(uncoupled F)/d(X_u, sPAR)
+        T G[ST][UPL][NCP1][N];    // d(CPT)/d(X_u, sPAR)
+        T CF[ST][UPL][NCP1];      // CPF value
+        T CFD[ST][UPL][NCP1][N];  // d(CPF)/d(X_u, sPAR)
+        T V[ST][UPL][NCP1];       // coupling value sum_j C[u][j] CPT_j
     };
 
     __device__ static bool has(int lane, int j) { return lane + 32 * j < UPS; }
     __device__ static int unit_of(int lane, int j) { return lane + 32 * j; }
 
     // Stages of one step from (x, t) with step dt, dual-evaluated.
-    __device__ static void stages(long long s, int lane, AdjSlot<S>& sl, const Units& u, const double* gp,
-                                  const int* igp, const double* M, const int* cidx, const double (&x)[UPL][UD],
-                                  double t, double dt, StepData& sd)
+    __device__ static void stages(const Tab& tb, long long s, int lane, AdjSlot<S, T>& sl, const Units& u,
+                                  const T* gp, const int* igp, const T* M, const int* cidx, const T (&x)[UPL][UD],
+                                  T t, T dt, StepData& sd)
     {
-        WarpSlot<S, double>& w = sl.w;
+        WarpSlot<S, T>& w = sl.w;
         const int sid = static_cast<int>(s);
         D spd[AtLeastOne<NSP>::value];
 #pragma unroll
         for (int k = 0; k < NSP; k++) {
             spd[k] = D(w.sp[k]);
-            spd[k].d[UD + k] = 1.0;
+            spd[k].d[UD + k] = T(1.0);
         }
         D gpd[AtLeastOne<S::NGP>::value];
 #pragma unroll
@@ -138,7 +146,7 @@ struct CoupledAdjoint {
         for (int k = 0; k < NISA; k++) isacc[k] = w.isacc[k];
 
         for (int st = 0; st < ST; st++) {
-            const D Td(t + TB::c(st) * dt);
+            const D Td(t + pt::tab_c<TB>(tb, st) * dt);
 #pragma unroll
             for (int j = 0; j < UPL; j++) {
                 if (!has(lane, j)) continue;
@@ -146,10 +154,10 @@ struct CoupledAdjoint {
                 D Xd[UD], Fd[UD], cptd[NCP1], cpfd[NCP1];
 #pragma unroll
                 for (int d = 0; d < UD; d++) {
-                    double sum = 0.0;
-                    for (int q = 0; q < st; q++) sum += TB::a(st, q) * sd.K[q][j][d];
-                    Xd[d] = D(x[j][d] + dt * sum);
-                    Xd[d].d[d] = 1.0;
+                    T sum(0.0);
+                    for (int q = 0; q < st; q++) sum = ad::mad(pt::tab_a<TB>(tb, st, q), sd.K[q][j][d], sum);
+                    Xd[d] = D(ad::mad(dt, sum, x[j][d]));
+                    Xd[d].d[d] = T(1.0);
                 }
                 D upd[AtLeastOne<NUP>::value], uaccd[AtLeastOne<NUA>::value];
 #pragma unroll
@@ -183,7 +191,7 @@ struct CoupledAdjoint {
                 if (!has(lane, j)) continue;
                 const int uid = unit_of(lane, j);
                 for (int c = 0; c < NC; c++) {
-                    const double v = coupling_value<S, double>(M, w, uid, c);
+                    const T v = coupling_value<S, T>(M, w, uid, c);
                     sd.V[st][j][c] = v;
                     const int ci = cidx[c];
                     if (ci >= 0 && ci < UD) sd.K[st][j][ci] += w.cstr[c] * sd.CF[st][j][c] * v;
@@ -194,40 +202,42 @@ struct CoupledAdjoint {
     }
 
     // Adjoint of one step (see the file comment).
-    __device__ static void reverse_step(int lane, AdjSlot<S>& sl, const double* M, const double* MT, const int* cidx,
-                                        const StepData& sd, double dt, double (&lam)[UPL][UD],
-                                        double (&mu)[AtLeastOne<NSP>::value])
+    __device__ static void reverse_step(const Tab& tb, int lane, AdjSlot<S, T>& sl, const T* M, const T* MT,
+                                        const int* cidx, const StepData& sd, T dt, T (&lam)[UPL][UD],
+                                        T (&mu)[AtLeastOne<NSP>::value])
     {
-        WarpSlot<S, double>& w = sl.w;
-        double kap[ST][UPL][UD];
-        double dlam[UPL][UD];
-        for (int st = 0; st < ST; st++)
+        WarpSlot<S, T>& w = sl.w;
+        T kap[ST][UPL][UD];
+        T dlam[UPL][UD];
+        for (int st = 0; st < ST; st++) {
+            const T hb = dt * pt::tab_b<TB>(tb, st);
 #pragma unroll
             for (int j = 0; j < UPL; j++)
 #pragma unroll
-                for (int d = 0; d < UD; d++) kap[st][j][d] = dt * TB::b(st) * lam[j][d];
+                for (int d = 0; d < UD; d++) kap[st][j][d] = hb * lam[j][d];
+        }
 #pragma unroll
         for (int j = 0; j < UPL; j++)
 #pragma unroll
-            for (int d = 0; d < UD; d++) dlam[j][d] = 0.0;
+            for (int d = 0; d < UD; d++) dlam[j][d] = T(0.0);
 
         for (int st = ST - 1; st >= 0; st--) {
-            double xi[UPL][UD];
+            T xi[UPL][UD];
 #pragma unroll
             for (int j = 0; j < UPL; j++) {
 #pragma unroll
                 for (int r = 0; r < UD; r++) {
-                    double v = 0.0;
+                    T v(0.0);
 #pragma unroll
-                    for (int d = 0; d < UD; d++) v += sd.L[st][j][d][r] * kap[st][j][d];
+                    for (int d = 0; d < UD; d++) v = ad::mad(sd.L[st][j][d][r], kap[st][j][d], v);
                     xi[j][r] = v;
                 }
                 if (!has(lane, j)) continue;
 #pragma unroll
                 for (int q = 0; q < NSP; q++) {
-                    double v = 0.0;
+                    T v(0.0);
 #pragma unroll
-                    for (int d = 0; d < UD; d++) v += sd.L[st][j][d][UD + q] * kap[st][j][d];
+                    for (int d = 0; d < UD; d++) v = ad::mad(sd.L[st][j][d][UD + q], kap[st][j][d], v);
                     mu[q] += v;
                 }
             }
@@ -236,27 +246,28 @@ struct CoupledAdjoint {
                 const bool ok = ci >= 0 && ci < UD;
 #pragma unroll
                 for (int j = 0; j < UPL; j++)
-                    if (has(lane, j)) sl.z[unit_of(lane, j)][c] = ok ? w.cstr[c] * sd.CF[st][j][c] * kap[st][j][ci] : 0.0;
+                    if (has(lane, j)) sl.z[unit_of(lane, j)][c] = ok ? w.cstr[c] * sd.CF[st][j][c] * kap[st][j][ci] : T(0.0);
                 __syncwarp();
 #pragma unroll
                 for (int j = 0; j < UPL; j++) {
                     if (!has(lane, j)) continue;
-                    const double wv = transposed_coupling_value<S>(M, MT, sl, unit_of(lane, j), c);
-                    const double coef = ok ? w.cstr[c] * sd.V[st][j][c] * kap[st][j][ci] : 0.0;
+                    const T wv = transposed_coupling_value<S, T>(M, MT, sl, unit_of(lane, j), c);
+                    const T coef = ok ? w.cstr[c] * sd.V[st][j][c] * kap[st][j][ci] : T(0.0);
 #pragma unroll
-                    for (int r = 0; r < UD; r++) xi[j][r] += wv * sd.G[st][j][c][r] + coef * sd.CFD[st][j][c][r];
+                    for (int r = 0; r < UD; r++) xi[j][r] += ad::mad2(wv, sd.G[st][j][c][r], coef, sd.CFD[st][j][c][r]);
 #pragma unroll
-                    for (int q = 0; q < NSP; q++) mu[q] += wv * sd.G[st][j][c][UD + q] + coef * sd.CFD[st][j][c][UD + q];
+                    for (int q = 0; q < NSP; q++)
+                        mu[q] += ad::mad2(wv, sd.G[st][j][c][UD + q], coef, sd.CFD[st][j][c][UD + q]);
                 }
                 __syncwarp();
             }
             for (int q = 0; q < st; q++) {
-                const double a = dt * TB::a(st, q);
-                if (a != 0.0) {
+                if (TB::a(st, q) != 0.0) {
+                    const T a = dt * pt::tab_a<TB>(tb, st, q);
 #pragma unroll
                     for (int j = 0; j < UPL; j++)
 #pragma unroll
-                        for (int d = 0; d < UD; d++) kap[q][j][d] += a * xi[j][d];
+                        for (int d = 0; d < UD; d++) kap[q][j][d] = ad::mad(a, xi[j][d], kap[q][j][d]);
                 }
             }
 #pragma unroll
@@ -271,74 +282,92 @@ struct CoupledAdjoint {
     }
 };
 
-template <class S, int ALG>
+// Sum over the warp's lanes (all lanes hold a value).
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    return v;
+}
+__device__ __forceinline__ dfloat warp_sum(dfloat v)
+{
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1)
+        v = v + dfloat(__shfl_xor_sync(0xffffffffu, v.hi, off), __shfl_xor_sync(0xffffffffu, v.lo, off));
+    return v;
+}
+
+template <class S, int ALG, class T>
 __global__ void __launch_bounds__(MPGOS_CB_MAX_BLOCK) coupled_adjoint_kernel(Args<double> a, pt::Tape tp,
                                                                             const double* dLdxT, double* dLdx0,
                                                                             double* dLdsp)
 {
-    using Adj = CoupledAdjoint<S, ALG>;
+    using Adj = CoupledAdjoint<S, ALG, T>;
     using Fwd = typename Adj::Fwd;
     using Units = typename Adj::Units;
+    using TB = typename Adj::TB;
     constexpr int UPS = S::UPS, UD = S::UD, NC = S::NC, NSP = S::NSP, NSA = S::NSA, NISA = S::NISA, UPL = S::UPL;
     constexpr int NGP = S::NGP, NIGP = S::NIGP, NUP = S::NUP, NUA = S::NUA, NIUA = S::NIUA;
     constexpr bool FULL = (S::CCI == 0 && S::CBW == 0);
     constexpr int MAXSEG = pt::MAX_SEG;
     extern __shared__ __align__(16) unsigned char mpgos_cb_adj_smem[];
     __shared__ int s_cidx[AtLeastOne<NC>::value];
+    __shared__ typename Adj::Tab tb;
 
-    double* gp = reinterpret_cast<double*>(mpgos_cb_adj_smem);
-    double* M = gp + NGP;
-    double* MT = M + NC * S::MAT;
+    T* gp = reinterpret_cast<T*>(mpgos_cb_adj_smem);
+    T* M = gp + NGP;
+    T* MT = M + NC * S::MAT;
     int* igp = reinterpret_cast<int*>(MT + (FULL ? NC * UPS * UPS : 0));
-    AdjSlot<S>* slots = reinterpret_cast<AdjSlot<S>*>(mpgos_cb_adj_smem + adjoint_block_part_bytes<S>());
+    AdjSlot<S, T>* slots = reinterpret_cast<AdjSlot<S, T>*>(mpgos_cb_adj_smem + adjoint_block_part_bytes<S, T>());
 
-    for (int k = threadIdx.x; k < NGP; k += blockDim.x) gp[k] = a.gp[k];
+    for (int k = threadIdx.x; k < NGP; k += blockDim.x) gp[k] = T(a.gp[k]);
     for (int k = threadIdx.x; k < NIGP; k += blockDim.x) igp[k] = a.igp[k];
-    for (int k = threadIdx.x; k < NC * S::MAT; k += blockDim.x) M[k] = a.cmat[k];
+    for (int k = threadIdx.x; k < NC * S::MAT; k += blockDim.x) M[k] = T(a.cmat[k]);
     if (FULL) {
         for (int k = threadIdx.x; k < NC * UPS * UPS; k += blockDim.x) {
             const int c = k / (UPS * UPS), r = k % (UPS * UPS);
             const int jj = r % UPS, u = r / UPS;  // MT[j + u*UPS] = M[u + j*UPS]
-            MT[k] = a.cmat[c * UPS * UPS + u + jj * UPS];
+            MT[k] = T(a.cmat[c * UPS * UPS + u + jj * UPS]);
         }
     }
     for (int k = threadIdx.x; k < NC; k += blockDim.x) s_cidx[k] = a.cidx[k];
+    pt::stage_tableau<TB>(tb);
     __syncthreads();
 
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, warps = blockDim.x >> 5;
     const long long s = static_cast<long long>(blockIdx.x) * warps + warp;
     if (s >= a.n_active) return;
-    AdjSlot<S>& sl = slots[warp];
-    WarpSlot<S, double>& w = sl.w;
+    AdjSlot<S, T>& sl = slots[warp];
+    WarpSlot<S, T>& w = sl.w;
     const long long ns = a.ns, nu = a.ns * UPS;
 
     // system and unit scope inputs the hooks read
-    for (int k = lane; k < NSP; k += 32) w.sp[k] = a.sp[s + k * ns];
-    for (int k = lane; k < NSA; k += 32) w.sacc[k] = a.sacc[s + k * ns];
+    for (int k = lane; k < NSP; k += 32) w.sp[k] = T(a.sp[s + k * ns]);
+    for (int k = lane; k < NSA; k += 32) w.sacc[k] = T(a.sacc[s + k * ns]);
     for (int k = lane; k < NISA; k += 32) w.isacc[k] = a.isacc[s + k * ns];
-    for (int k = lane; k < NC; k += 32) w.cstr[k] = a.cstr[s + k * ns];
+    for (int k = lane; k < NC; k += 32) w.cstr[k] = T(a.cstr[s + k * ns]);
     if (lane == 0) {
-        w.td[0] = a.td[s];
-        w.td[1] = a.td[s + ns];
+        w.td[0] = T(a.td[s]);
+        w.td[1] = T(a.td[s + ns]);
     }
     Units u;
-    double lam[UPL][UD];
+    T lam[UPL][UD];
 #pragma unroll
     for (int j = 0; j < UPL; j++) {
         const bool h = Adj::has(lane, j);
         const long long g = s * UPS + Adj::unit_of(lane, j);
 #pragma unroll
-        for (int k = 0; k < NUP; k++) u.up[j][k] = h ? a.up[g + k * nu] : 0.0;
+        for (int k = 0; k < NUP; k++) u.up[j][k] = h ? T(a.up[g + k * nu]) : T(0.0);
 #pragma unroll
-        for (int k = 0; k < NUA; k++) u.uacc[j][k] = h ? a.uacc[g + k * nu] : 0.0;
+        for (int k = 0; k < NUA; k++) u.uacc[j][k] = h ? T(a.uacc[g + k * nu]) : T(0.0);
 #pragma unroll
         for (int k = 0; k < NIUA; k++) u.iuacc[j][k] = h ? a.iuacc[g + k * nu] : 0;
 #pragma unroll
-        for (int d = 0; d < UD; d++) lam[j][d] = h ? dLdxT[g + d * nu] : 0.0;
+        for (int d = 0; d < UD; d++) lam[j][d] = h ? T(dLdxT[g + d * nu]) : T(0.0);
     }
-    double mu[AtLeastOne<NSP>::value];
+    T mu[AtLeastOne<NSP>::value];
 #pragma unroll
-    for (int q = 0; q < NSP; q++) mu[q] = 0.0;
+    for (int q = 0; q < NSP; q++) mu[q] = T(0.0);
     __syncwarp();
 
     const int n = tp.n_steps[s];
@@ -347,30 +376,31 @@ __global__ void __launch_bounds__(MPGOS_CB_MAX_BLOCK) coupled_adjoint_kernel(Arg
     const int seg = tp.seg;
 
     if (!(status & MPGOS_INSTANCE_TAPE_OVERFLOW) && n > 0) {
-        double xs[MAXSEG][UPL][UD];
-        double ts[MAXSEG];
+        T xs[MAXSEG][UPL][UD];
+        T ts[MAXSEG];
         typename Adj::StepData sd;
         for (int sgm = (n - 1) / seg; sgm >= 0; sgm--) {
             const int k0 = sgm * seg;
             const int k1 = min(n, k0 + seg);
-            double t = tp.ckpt_t[static_cast<long long>(sgm) * ns + s];
+            T t(tp.ckpt_t[static_cast<long long>(sgm) * ns + s]);
 #pragma unroll
             for (int j = 0; j < UPL; j++) {
                 const long long g = s * UPS + Adj::unit_of(lane, j);
 #pragma unroll
                 for (int d = 0; d < UD; d++)
-                    u.x[j][d] = Adj::has(lane, j) ? tp.ckpt_x[(static_cast<long long>(sgm) * UD + d) * nu + g] : 0.0;
+                    u.x[j][d] = Adj::has(lane, j) ? T(tp.ckpt_x[(static_cast<long long>(sgm) * UD + d) * nu + g])
+                                                  : T(0.0);
             }
             // replay the segment with the recorded steps (the forward stepper)
             for (int k = k0; k < k1; k++) {
-                const double dt = tp.dt[static_cast<long long>(k) * ns + s];
+                const T dt(tp.dt[static_cast<long long>(k) * ns + s]);
 #pragma unroll
                 for (int j = 0; j < UPL; j++)
 #pragma unroll
                     for (int d = 0; d < UD; d++) xs[k - k0][j][d] = u.x[j][d];
                 ts[k - k0] = t;
                 if (k + 1 < k1) {
-                    double xn[UPL][UD], err[UPL][UD];
+                    T xn[UPL][UD], err[UPL][UD];
                     int finite = 1;
                     if (ALG == MPGOS_RK4)
                         Fwd::step_rk4(s, lane, w, u, gp, igp, M, s_cidx, t, dt, xn, finite);
@@ -385,9 +415,9 @@ __global__ void __launch_bounds__(MPGOS_CB_MAX_BLOCK) coupled_adjoint_kernel(Arg
             }
             // reverse through the segment
             for (int k = k1 - 1; k >= k0; k--) {
-                const double dt = tp.dt[static_cast<long long>(k) * ns + s];
-                Adj::stages(s, lane, sl, u, gp, igp, M, s_cidx, xs[k - k0], ts[k - k0], dt, sd);
-                Adj::reverse_step(lane, sl, M, MT, s_cidx, sd, dt, lam, mu);
+                const T dt(tp.dt[static_cast<long long>(k) * ns + s]);
+                Adj::stages(tb, s, lane, sl, u, gp, igp, M, s_cidx, xs[k - k0], ts[k - k0], dt, sd);
+                Adj::reverse_step(tb, lane, sl, M, MT, s_cidx, sd, dt, lam, mu);
             }
         }
     }
@@ -396,14 +426,12 @@ __global__ void __launch_bounds__(MPGOS_CB_MAX_BLOCK) coupled_adjoint_kernel(Arg
         if (!Adj::has(lane, j)) continue;
         const long long g = s * UPS + Adj::unit_of(lane, j);
 #pragma unroll
-        for (int d = 0; d < UD; d++) dLdx0[g + d * nu] = lam[j][d];
+        for (int d = 0; d < UD; d++) dLdx0[g + d * nu] = static_cast<double>(lam[j][d]);
     }
 #pragma unroll
     for (int q = 0; q < NSP; q++) {
-        double v = mu[q];
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-        if (lane == 0) dLdsp[s + q * ns] = v;
+        const T v = warp_sum(mu[q]);
+        if (lane == 0) dLdsp[s + q * ns] = static_cast<double>(v);
     }
     if (lane == 0 && a.status) a.status[s] = status;
 }
@@ -421,9 +449,14 @@ struct CoupledAdjointTable {
     {
         if (tape == nullptr || tape->segment < 1 || tape->segment > pt::MAX_SEG)
             return static_cast<int>(cudaErrorInvalidValue);
-        void* fn = (L->mode & MPGOS_MODE_PERSISTENT)
-                       ? reinterpret_cast<void*>(&coupled_kernel<S, ALG, double, MODE_RECORD | MPGOS_MODE_PERSISTENT>)
-                       : reinterpret_cast<void*>(&coupled_kernel<S, ALG, double, MODE_RECORD>);
+        const bool pers = (L->mode & MPGOS_MODE_PERSISTENT) != 0;
+        void* fn = nullptr;
+        if (L->mode & MPGOS_MODE_DF_STAGE)
+            fn = pers ? reinterpret_cast<void*>(&coupled_kernel<S, ALG, dfloat, MODE_RECORD | MPGOS_MODE_PERSISTENT>)
+                      : reinterpret_cast<void*>(&coupled_kernel<S, ALG, dfloat, MODE_RECORD>);
+        else
+            fn = pers ? reinterpret_cast<void*>(&coupled_kernel<S, ALG, double, MODE_RECORD | MPGOS_MODE_PERSISTENT>)
+                      : reinterpret_cast<void*>(&coupled_kernel<S, ALG, double, MODE_RECORD>);
         Args<double> a = make_args<double>(*L);
         a.tape = tape_of(*tape);
         if (smem > 48 * 1024) {
@@ -440,7 +473,9 @@ struct CoupledAdjointTable {
     {
         if (tape == nullptr || tape->segment < 1 || tape->segment > pt::MAX_SEG)
             return static_cast<int>(cudaErrorInvalidValue);
-        void* fn = reinterpret_cast<void*>(&coupled_adjoint_kernel<S, ALG>);
+        // a DF_STAGE solver differentiates in double-float
+        void* fn = (L->mode & MPGOS_MODE_DF_STAGE) ? reinterpret_cast<void*>(&coupled_adjoint_kernel<S, ALG, dfloat>)
+                                                  : reinterpret_cast<void*>(&coupled_adjoint_kernel<S, ALG, double>);
         if (smem > 48 * 1024) {
             cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
             if (e != cudaSuccess) return static_cast<int>(e);
@@ -452,7 +487,10 @@ struct CoupledAdjointTable {
                                                  static_cast<cudaStream_t>(stream)));
     }
 
-    static size_t smem(int warps) { return adjoint_smem_bytes<S>(warps); }
+    static size_t smem(int warps, int32_t mode)
+    {
+        return (mode & MPGOS_MODE_DF_STAGE) ? adjoint_smem_bytes<S, dfloat>(warps) : adjoint_smem_bytes<S, double>(warps);
+    }
 };
 
 }  // namespace cb

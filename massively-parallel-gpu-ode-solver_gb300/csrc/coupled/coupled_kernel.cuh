@@ -227,7 +227,8 @@ struct Solver {
     static constexpr int UPS = S::UPS, UD = S::UD, NC = S::NC, NUP = S::NUP, NUA = S::NUA, NIUA = S::NIUA;
     static constexpr int NE = S::NE, UPL = S::UPL, NSP = S::NSP, NSA = S::NSA, NISA = S::NISA;
     static constexpr bool PERSISTENT = (MODE & MPGOS_MODE_PERSISTENT) != 0;
-    static constexpr bool RECORD = ((MODE & MODE_RECORD) != 0) && std::is_same<P, double>::value;
+    // the tape is FP64 for both arithmetics (a double-float value is a double exactly)
+    static constexpr bool RECORD = (MODE & MODE_RECORD) != 0;
     using Slot = WarpSlot<S, P>;
     using SP   = typename StorageOf<P>::type;  // precision of the arrays in HBM
 
@@ -634,7 +635,7 @@ struct Solver {
                     // frozen step size of accepted step nacc, checkpoint every seg steps
                     const int k = nacc - 1;
                     if (k < a.tape.max_steps) {
-                        if (lane == 0) a.tape.dt[static_cast<long long>(k) * ns + s] = dt;
+                        if (lane == 0) a.tape.dt[static_cast<long long>(k) * ns + s] = static_cast<double>(dt);
                         if (nacc % a.tape.seg == 0) record_checkpoint(s, lane, w, u, a, nacc / a.tape.seg);
                     } else {
                         status |= MPGOS_INSTANCE_TAPE_OVERFLOW;
@@ -691,13 +692,14 @@ struct Solver {
                                              int c)
     {
         const long long ns = a.ns, nu = a.ns * UPS;
-        if (lane == 0) a.tape.ckpt_t[static_cast<long long>(c) * ns + s] = w.t;
+        if (lane == 0) a.tape.ckpt_t[static_cast<long long>(c) * ns + s] = static_cast<double>(w.t);
 #pragma unroll
         for (int j = 0; j < UPL; j++) {
             if (!has(lane, j)) continue;
             const long long g = s * UPS + unit_of(lane, j);
 #pragma unroll
-            for (int d = 0; d < UD; d++) a.tape.ckpt_x[(static_cast<long long>(c) * UD + d) * nu + g] = u.x[j][d];
+            for (int d = 0; d < UD; d++)
+                a.tape.ckpt_x[(static_cast<long long>(c) * UD + d) * nu + g] = static_cast<double>(u.x[j][d]);
         }
     }
 
@@ -930,7 +932,7 @@ struct KernelTable {
     using RecordFn  = int (*)(const mpgos_cb_launch*, const mpgos_pt_tape*, int, int, size_t, void*);
     using AdjointFn = int (*)(const mpgos_cb_launch*, const mpgos_pt_tape*, const double*, double*, double*, int, int,
                               size_t, void*);
-    using AdjSmemFn = size_t (*)(int);
+    using AdjSmemFn = size_t (*)(int, int32_t);
 
     static const mpgos_cb_kernels* get(const char* name, RecordFn record = nullptr, AdjointFn adjoint = nullptr,
                                        AdjSmemFn adjoint_smem = nullptr)

@@ -376,7 +376,7 @@ namespace {
 int prepare_launch(mpgos_cb_solver* s, bool record, mpgos_cb_launch& L, int64_t& grid_out, int& block_out,
                    size_t& smem_out)
 {
-    const int32_t mode = record ? (s->mode & MPGOS_MODE_PERSISTENT) : s->mode;
+    const int32_t mode = record ? (s->mode & (MPGOS_MODE_PERSISTENT | MPGOS_MODE_DF_STAGE)) : s->mode;
     const int block = 32 * s->warps;
     const bool df = (mode & MPGOS_MODE_DF_STAGE) != 0;
     int sg = df ? 1 : s->shared_global, sc = df ? 1 : s->shared_coupling;
@@ -498,7 +498,8 @@ MPGOS_EXPORT int mpgos_cb_adjoint(mpgos_cb_solver* s, const double* dLdxT, doubl
     if (s->n_active <= 0) return MPGOS_OK;
     CB_CUDA(cudaSetDevice(s->device));
     const int warps = 2, block = 32 * warps;
-    const size_t smem = s->k->adjoint_smem(warps);
+    // the reverse pass computes in double-float when the solver does
+    const size_t smem = s->k->adjoint_smem(warps, s->mode & MPGOS_MODE_DF_STAGE);
     if (smem > 227 * 1024) return fail(MPGOS_ERR_ARGUMENT, "coupled adjoint needs %zu bytes of shared memory", smem);
     const int64_t grid = (s->n_active + warps - 1) / warps;
     mpgos_cb_launch L;

@@ -90,6 +90,51 @@ def test_coupled_adjoint_matches_central_differences(system, native_libs, oracle
         assert np.max(relx) < 1e-6, (comp, np.max(relx))
 
 
+DF_PERSISTENT = capi.MODE_DF_STAGE | capi.MODE_PERSISTENT
+
+
+@pytest.mark.parametrize("system", ["ring16_full", "ring16_band", "ring64"])
+def test_coupled_df_adjoint_matches_central_differences(system, native_libs, oracle_libs):
+    """DF_STAGE records its double-float step sequence and reverses in
+    double-float; same 1e-6 bar against FP64 central differences of the
+    replayed map."""
+    ns = 32 if system == "ring64" else 64
+    case = CW.ring_case(system, ns=ns, periods=1, seed=44)
+    xT, status, dt, n, gx0, gsp = forward_adjoint(case, mode=DF_PERSISTENT)
+    assert np.all(status & capi.INSTANCE_TAPE_OVERFLOW == 0)
+    base = O.replay_coupled(case, dt, n)
+    assert np.max(np.abs(base - xT)) < 1e-9
+    fd = fd_wrt_B(case, dt, n)
+    rel = np.abs(gsp[0] - fd) / np.maximum(np.abs(fd), 1e-8)
+    assert np.max(rel) < 1e-6, np.max(rel)
+
+
+def test_coupled_df_and_fp64_reverse_agree_on_one_tape(native_libs):
+    """One FP64 tape reversed in FP64 and in double-float (KERNEL_MODE switched
+    between SolveRecord and Adjoint): the gradients differ by the double-float
+    rounding of the reverse pass only."""
+    import torch
+    case = CW.ring_case("ring16_full", ns=64, periods=1, seed=45)
+    grads = []
+    with CW.load_coupled_solver(case, mode=capi.MODE_PERSISTENT, warps=4) as s:
+        s.SolveRecord(MAX_STEPS, SEG)
+        s.SynchroniseFromDeviceToHost(V.ActualState)
+        s.SynchroniseDevice()
+        xT = s.host(V.ActualState).copy()
+        gT = torch.tensor(np.stack([xT[0] + xT[0] ** 3, xT[1]]), device="cuda")
+        for mode in (capi.MODE_PERSISTENT, DF_PERSISTENT):
+            s.set_mode(mode)
+            gx0 = torch.empty_like(gT)
+            gsp = torch.empty((max(s.NSP, 1), case.ns), dtype=torch.float64, device="cuda")
+            torch.cuda.synchronize()
+            s.Adjoint(gT.data_ptr(), gx0.data_ptr(), gsp.data_ptr())
+            s.SynchroniseDevice()
+            grads.append(np.concatenate([gx0.cpu().numpy().ravel(), gsp.cpu().numpy().ravel()]))
+    a, b = grads
+    assert not np.array_equal(a, b)
+    assert np.max(np.abs(a - b)) / np.max(np.abs(a)) < 1e-10
+
+
 def test_coupled_adjoint_segments_and_mapping_agree(native_libs):
     case = CW.ring_case("ring16_full", ns=64, periods=1, seed=42)
     _, _, _, _, gx_a, gs_a = forward_adjoint(case, segment=32, mode=0)
