@@ -413,6 +413,7 @@ typedef struct mpgos_cb_kernels {
     int (*launch_adjoint)(const mpgos_cb_launch* args, const mpgos_pt_tape* tape, const double* dL_dxT,
                           double* dL_dx0, double* dL_dsp, int grid, int block, size_t dynamic_smem, void* stream);
     size_t (*adjoint_smem)(int warps_per_block, int32_t mode);
+    int (*adjoint_occupancy)(int32_t mode, int block, size_t dynamic_smem, int* blocks_per_sm);
 } mpgos_cb_kernels;
 
 typedef struct mpgos_cb_solver mpgos_cb_solver;

@@ -297,8 +297,16 @@ __device__ __forceinline__ dfloat warp_sum(dfloat v)
     return v;
 }
 
+// Launch shape of the reverse pass: up to CB_ADJOINT_BLOCK threads (one warp
+// per system; the runtime picks the warps per block that keep the most warps
+// resident, shared memory and registers both counted).
+#ifndef MPGOS_CB_ADJOINT_MIN_BLOCKS
+#define MPGOS_CB_ADJOINT_MIN_BLOCKS 1
+#endif
+constexpr int CB_ADJOINT_BLOCK = 256;
+
 template <class S, int ALG, class T>
-__global__ void __launch_bounds__(MPGOS_CB_MAX_BLOCK) coupled_adjoint_kernel(Args<double> a, pt::Tape tp,
+__global__ void __launch_bounds__(CB_ADJOINT_BLOCK, MPGOS_CB_ADJOINT_MIN_BLOCKS) coupled_adjoint_kernel(Args<double> a, pt::Tape tp,
                                                                             const double* dLdxT, double* dLdx0,
                                                                             double* dLdsp)
 {
@@ -474,8 +482,7 @@ struct CoupledAdjointTable {
         if (tape == nullptr || tape->segment < 1 || tape->segment > pt::MAX_SEG)
             return static_cast<int>(cudaErrorInvalidValue);
         // a DF_STAGE solver differentiates in double-float
-        void* fn = (L->mode & MPGOS_MODE_DF_STAGE) ? reinterpret_cast<void*>(&coupled_adjoint_kernel<S, ALG, dfloat>)
-                                                  : reinterpret_cast<void*>(&coupled_adjoint_kernel<S, ALG, double>);
+        void* fn = adjoint_fn(L->mode);
         if (smem > 48 * 1024) {
             cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
             if (e != cudaSuccess) return static_cast<int>(e);
@@ -485,6 +492,22 @@ struct CoupledAdjointTable {
         void* params[] = {&a, &t, &dLdxT, &dLdx0, &dLdsp};
         return static_cast<int>(cudaLaunchKernel(fn, dim3(grid), dim3(block), params, smem,
                                                  static_cast<cudaStream_t>(stream)));
+    }
+
+    static void* adjoint_fn(int32_t mode)
+    {
+        return (mode & MPGOS_MODE_DF_STAGE) ? reinterpret_cast<void*>(&coupled_adjoint_kernel<S, ALG, dfloat>)
+                                            : reinterpret_cast<void*>(&coupled_adjoint_kernel<S, ALG, double>);
+    }
+
+    static int occupancy(int32_t mode, int block, size_t smem, int* blocks)
+    {
+        void* fn = adjoint_fn(mode);
+        if (smem > 48 * 1024) {
+            cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+            if (e != cudaSuccess) return static_cast<int>(e);
+        }
+        return static_cast<int>(cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, fn, block, smem));
     }
 
     static size_t smem(int warps, int32_t mode)

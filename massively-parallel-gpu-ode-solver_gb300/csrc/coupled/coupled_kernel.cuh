@@ -933,9 +933,10 @@ struct KernelTable {
     using AdjointFn = int (*)(const mpgos_cb_launch*, const mpgos_pt_tape*, const double*, double*, double*, int, int,
                               size_t, void*);
     using AdjSmemFn = size_t (*)(int, int32_t);
+    using AdjOccFn  = int (*)(int32_t, int, size_t, int*);
 
     static const mpgos_cb_kernels* get(const char* name, RecordFn record = nullptr, AdjointFn adjoint = nullptr,
-                                       AdjSmemFn adjoint_smem = nullptr)
+                                       AdjSmemFn adjoint_smem = nullptr, AdjOccFn adjoint_occupancy = nullptr)
     {
         static mpgos_cb_kernels table = {
             MPGOS_ABI_VERSION,
@@ -947,7 +948,8 @@ struct KernelTable {
             &smem,
             record,
             adjoint,
-            adjoint_smem};
+            adjoint_smem,
+            adjoint_occupancy};
         return &table;
     }
 };

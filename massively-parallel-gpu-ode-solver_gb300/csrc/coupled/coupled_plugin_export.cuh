@@ -24,12 +24,12 @@ extern "C" __attribute__((visibility("default"))) const mpgos_cb_kernels* mpgos_
         if (algorithm == MPGOS_RKCK45) {
             using A = CoupledAdjointTable<S, MPGOS_RKCK45>;
             return KernelTable<S, MPGOS_RKCK45, double>::get(MPGOS_SYS_NAME, &A::launch_record, &A::launch_adjoint,
-                                                             &A::smem);
+                                                             &A::smem, &A::occupancy);
         }
         if (algorithm == MPGOS_RK4) {
             using A = CoupledAdjointTable<S, MPGOS_RK4>;
             return KernelTable<S, MPGOS_RK4, double>::get(MPGOS_SYS_NAME, &A::launch_record, &A::launch_adjoint,
-                                                          &A::smem);
+                                                          &A::smem, &A::occupancy);
         }
     }
     return nullptr;

@@ -497,10 +497,31 @@ MPGOS_EXPORT int mpgos_cb_adjoint(mpgos_cb_solver* s, const double* dLdxT, doubl
         return fail(MPGOS_ERR_ARGUMENT, "null gradient buffer");
     if (s->n_active <= 0) return MPGOS_OK;
     CB_CUDA(cudaSetDevice(s->device));
-    const int warps = 2, block = 32 * warps;
     // the reverse pass computes in double-float when the solver does
-    const size_t smem = s->k->adjoint_smem(warps, s->mode & MPGOS_MODE_DF_STAGE);
-    if (smem > 227 * 1024) return fail(MPGOS_ERR_ARGUMENT, "coupled adjoint needs %zu bytes of shared memory", smem);
+    const int32_t amode = s->mode & MPGOS_MODE_DF_STAGE;
+    // warps (systems) per block: the most resident warps per SM, the smaller
+    // block on ties (shared memory holds the coupling matrices once per block)
+    int warps = 0, best = -1;
+    for (int w : {1, 2, 4, 8}) {
+        const size_t need = s->k->adjoint_smem(w, amode);
+        if (need > 227 * 1024) break;
+        int per_sm = 0;
+        if (s->k->adjoint_occupancy == nullptr) {
+            per_sm = w == 2 ? 1 : 0;  // no occupancy query: two warps per block
+        } else {
+            const int e = s->k->adjoint_occupancy(amode, 32 * w, need, &per_sm);
+            if (e != 0) return fail(MPGOS_ERR_CUDA, "coupled adjoint occupancy query: %s", cudaGetErrorString((cudaError_t)e));
+        }
+        if (per_sm * w > best) {
+            best = per_sm * w;
+            warps = w;
+        }
+    }
+    if (warps == 0 || best <= 0)
+        return fail(MPGOS_ERR_ARGUMENT, "coupled adjoint needs %zu bytes of shared memory per system",
+                    s->k->adjoint_smem(1, amode));
+    const int block = 32 * warps;
+    const size_t smem = s->k->adjoint_smem(warps, amode);
     const int64_t grid = (s->n_active + warps - 1) / warps;
     mpgos_cb_launch L;
     int64_t g = 0;

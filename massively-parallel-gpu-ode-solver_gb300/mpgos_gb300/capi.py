@@ -146,6 +146,7 @@ class CbKernelTable(C.Structure):
         ("launch_record", C.c_void_p),
         ("launch_adjoint", C.c_void_p),
         ("adjoint_smem", C.c_void_p),
+        ("adjoint_occupancy", C.c_void_p),
     ]
 
 
