@@ -287,6 +287,8 @@ int mpgos_pt_checkpoint_restore(mpgos_pt_solver* solver);
  * gradient of the discrete map with the recorded step sequence frozen.
  * Under MPGOS_MODE_DF_STAGE both passes compute in double-float (the tape
  * stays FP64: a double-float value is a double exactly); otherwise in FP64.
+ * The reverse arithmetic follows the mode set when mpgos_pt_adjoint is
+ * called, so an FP64 tape can be reversed in double-float.
  * Instances whose step count exceeded the tape get MPGOS_INSTANCE_TAPE_OVERFLOW
  * in MPGOS_STATUS and no gradient. Asynchronous on the solver's stream. */
 int mpgos_pt_solve_record(mpgos_pt_solver* solver, int32_t max_steps, int32_t segment);
@@ -440,7 +442,10 @@ int mpgos_cb_stream(mpgos_cb_solver* solver, void** stream);
 int mpgos_cb_checkpoint_save(mpgos_cb_solver* solver);
 int mpgos_cb_checkpoint_restore(mpgos_cb_solver* solver);
 /* Discrete adjoint of the coupled solver (extension, no counterpart in the
- * reference), FP64 tables. mpgos_cb_solve_record: one Solve() that also
+ * reference), FP64 tables; under MPGOS_MODE_DF_STAGE the recording and the
+ * reverse pass compute in double-float (the tape stays FP64), and the reverse
+ * arithmetic follows the mode set when mpgos_cb_adjoint is called.
+ * mpgos_cb_solve_record: one Solve() that also
  * records the tape (every accepted step size of every system, the time and
  * every unit's state every `segment` accepted steps; capacity max_steps per
  * system; device memory owned by the solver). mpgos_cb_adjoint: reverse pass;
