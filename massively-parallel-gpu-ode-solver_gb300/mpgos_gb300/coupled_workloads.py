@@ -220,6 +220,10 @@ def _main(argv=None) -> int:
     ap.add_argument("--mode", type=int, default=0, help="MPGOS_MODE_* bits (PERSISTENT 2, DF_STAGE 16)")
     ap.add_argument("--warps", type=int, default=4)
     ap.add_argument("--launches", type=int, default=1)
+    ap.add_argument("--adjoint", type=int, default=0, metavar="SEG",
+                    help="after the launches: one recording pass and one reverse pass (gradient of the summed "
+                         "terminal energy) with checkpoints every SEG steps, in --adjoint-mode")
+    ap.add_argument("--adjoint-mode", type=int, default=None, help="MPGOS_MODE_* bits of the reverse pass")
     a = ap.parse_args(argv)
     case = ring_case(a.system, ns=a.ns, periods=a.periods)
     from .capi import CbVariable as V
@@ -233,9 +237,28 @@ def _main(argv=None) -> int:
             s.SynchroniseDevice()
             wall = time.perf_counter() - t0
         res = read_coupled_results(s)
+        adj = None
+        if a.adjoint:
+            import numpy as np
+            import torch
+            s.checkpoint_restore()
+            s.SolveRecord(int(res["nacc"].max()) + 64, a.adjoint)
+            s.SynchroniseFromDeviceToHost(V.ActualState)
+            s.SynchroniseDevice()
+            xT = s.host(V.ActualState)
+            g = torch.tensor(np.stack([xT[0] + xT[0] ** 3, xT[1]]), device="cuda")
+            gx0 = torch.empty_like(g)
+            gsp = torch.empty((max(s.NSP, 1), case.ns), dtype=torch.float64, device="cuda")
+            if a.adjoint_mode is not None:
+                s.set_mode(a.adjoint_mode)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            s.Adjoint(g.data_ptr(), gx0.data_ptr(), gsp.data_ptr())
+            s.SynchroniseDevice()
+            adj = time.perf_counter() - t0
     print(json.dumps({"system": a.system, "ns": a.ns, "periods": a.periods, "mode": a.mode, "warps": a.warps,
                       "accepted": int(res["nacc"].sum()), "rejected": int(res["nrej"].sum()),
-                      "status_max": int(res["status"].max()), "wall_s_last": wall}))
+                      "status_max": int(res["status"].max()), "wall_s_last": wall, "adjoint_wall_s": adj}))
     return 0
 
 
