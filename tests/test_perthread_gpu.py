@@ -81,10 +81,14 @@ def _tol_perturbation(mode):
 
 
 def _int_slack(mode):
-    """DF_STAGE's error estimate carries double-float rounding (~1e-14 of the
-    stage derivatives) on top of the FP32 step factor: a step count may
-    differ by one on a few instances (see parity.assert_ints_equal)."""
-    return 0.005 if MODES[mode] & capi.MODE_DF_STAGE else 0.0
+    """DF_STAGE's error estimate carries double-float rounding on top of the
+    FP32 step factor: the estimate dt |sum_j e_j k_j| cancels down to ~tol of
+    terms of size |k| dt, so its ~4e-15 |k| dt rounding is ~1e-6 of the
+    estimate at tol 1e-10 (FP64: ~5e-8). Accept/reject decisions within that
+    band of the threshold flip; over thousands of steps per instance a step
+    count may differ by one on a few percent of the instances (see
+    parity.assert_ints_equal), never by more."""
+    return 0.02 if MODES[mode] & capi.MODE_DF_STAGE else 0.0
 
 
 def _skip_unsupported(case, mode):
