@@ -199,6 +199,10 @@ typedef struct mpgos_pt_kernels {
                          size_t dynamic_smem, void* stream);
     int (*launch_adjoint)(const mpgos_pt_launch* args, const mpgos_pt_tape* tape, const double* dL_dxT,
                           double* dL_dx0, double* dL_dp, int grid, int block, size_t dynamic_smem, void* stream);
+    /* Dense-output interpolation at n_times requested times (device arrays;
+     * out [n_times][SD][NT], FP64), one instance per thread. */
+    int (*dense_interpolate)(const mpgos_pt_launch* args, const double* times, int32_t n_times, double* out,
+                             int grid, int block, size_t dynamic_smem, void* stream);
 } mpgos_pt_kernels;
 
 /* ---- solver object (ProblemSolver, SingleSystem_PerThread_Interface.cuh:117-208) */
@@ -295,6 +299,17 @@ int mpgos_pt_solve_record(mpgos_pt_solver* solver, int32_t max_steps, int32_t se
 int mpgos_pt_adjoint(mpgos_pt_solver* solver, const double* dL_dxT, double* dL_dx0, double* dL_dp);
 /* Device pointers and sizes of the recorded tape (read-only view). */
 int mpgos_pt_tape_info(const mpgos_pt_solver* solver, mpgos_pt_tape* tape);
+
+/* Dense-output interpolation (extension; the reference stores the accepted
+ * points only, SingleSystem_PerThread_DenseOutput.cuh:5-58): for every active
+ * instance and each of the n_times requested times (device array, any order),
+ * the cubic Hermite polynomial through the two stored points that bracket the
+ * time, with the right-hand side at those points as slopes. Reads the device
+ * copy of the dense output (a Solve with NDO > 0 before it); out is a device
+ * array [n_times][SD][NT] in FP64 (instances past ActiveNumberOfThreads are
+ * not written). Times outside an instance's stored range give NaN.
+ * Asynchronous on the solver's stream. */
+int mpgos_pt_dense_interpolate(mpgos_pt_solver* solver, const double* times, int32_t n_times, double* out);
 
 /* mpgos_pt_solve_record without device allocation (no counterpart in the
  * reference): records the same tape as mpgos_pt_solve_record, bit for bit, into

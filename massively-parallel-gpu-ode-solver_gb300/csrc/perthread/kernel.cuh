@@ -450,6 +450,14 @@ using RecordFn  = int (*)(const mpgos_pt_launch*, const mpgos_pt_tape*, int, int
 using AdjointFn = int (*)(const mpgos_pt_launch*, const mpgos_pt_tape*, const double*, double*, double*, int, int,
                           size_t, void*);
 
+}  // namespace pt
+}  // namespace mpgos
+
+#include "dense_interp.cuh"
+
+namespace mpgos {
+namespace pt {
+
 template <class S, int ALG, class P>
 struct KernelTable {
     static constexpr bool DOUBLE_ADAPTIVE = sizeof(P) == 8 && ALG == MPGOS_RKCK45;
@@ -507,7 +515,8 @@ struct KernelTable {
             &launch,
             &occupancy,
             record,
-            adjoint};
+            adjoint,
+            &DenseInterpTable<S, P>::launch};
         return &table;
     }
 };

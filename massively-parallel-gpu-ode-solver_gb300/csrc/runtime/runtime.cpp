@@ -963,6 +963,27 @@ MPGOS_EXPORT int mpgos_pt_adjoint(mpgos_pt_solver* s, const double* dLdxT, doubl
     return MPGOS_OK;
 }
 
+MPGOS_EXPORT int mpgos_pt_dense_interpolate(mpgos_pt_solver* s, const double* times, int32_t n_times, double* out)
+{
+    int rc = check_solver(s);
+    if (rc) return rc;
+    if (s->k->dense_interpolate == nullptr)
+        return fail(MPGOS_ERR_UNSUPPORTED, "system %s has no dense-output interpolation kernel", s->k->name);
+    if (s->ndo < 1) return fail(MPGOS_ERR_ARGUMENT, "dense-output interpolation needs NDO > 0 (this object has 0)");
+    if (n_times < 0 || (n_times > 0 && (times == nullptr || out == nullptr)))
+        return fail(MPGOS_ERR_ARGUMENT, "dense-output interpolation: %d times, times %p, out %p", n_times,
+                    static_cast<const void*>(times), static_cast<void*>(out));
+    if (n_times == 0 || s->n_active <= 0) return MPGOS_OK;
+    MPGOS_CUDA(cudaSetDevice(s->device));
+    const int block = 128;
+    const int64_t grid = (s->n_active + block - 1) / block;
+    mpgos_pt_launch L;
+    fill_launch(s, L, 0);
+    rc = s->k->dense_interpolate(&L, times, n_times, out, static_cast<int>(grid), block, dynamic_smem(s), s->stream);
+    if (rc != 0) return fail(MPGOS_ERR_CUDA, "dense interpolation launch failed: %s", cudaGetErrorString((cudaError_t)rc));
+    return MPGOS_OK;
+}
+
 MPGOS_EXPORT int mpgos_pt_tape_info(const mpgos_pt_solver* s, mpgos_pt_tape* tape)
 {
     int rc = check_solver(s);

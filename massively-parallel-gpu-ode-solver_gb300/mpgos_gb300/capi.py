@@ -169,6 +169,7 @@ class KernelTable(C.Structure):
         ("occupancy", C.c_void_p),
         ("launch_record", C.c_void_p),
         ("launch_adjoint", C.c_void_p),
+        ("dense_interpolate", C.c_void_p),
     ]
 
 
@@ -207,6 +208,7 @@ def _declare(lib):
         "mpgos_pt_solve_record": (C.c_int, [P, i32, i32]),
         "mpgos_pt_adjoint": (C.c_int, [P, P, P, P]),
         "mpgos_pt_tape_info": (C.c_int, [P, C.POINTER(Tape)]),
+        "mpgos_pt_dense_interpolate": (C.c_int, [P, P, C.c_int32, P]),
         "mpgos_pt_solve_record_static": (C.c_int, [P, i32, i32]),
         "mpgos_cb_create": (C.c_int, [P, i64, i32, C.c_int, C.POINTER(P)]),
         "mpgos_cb_destroy": (C.c_int, [P]),
@@ -244,6 +246,7 @@ RUNTIME_SYMBOLS = (
     "mpgos_pt_launch_config", "mpgos_pt_timer_start", "mpgos_pt_timer_stop", "mpgos_pt_autotune",
     "mpgos_pt_checkpoint_save", "mpgos_pt_checkpoint_restore", "mpgos_probe_fma_peak",
     "mpgos_pt_solve_record", "mpgos_pt_adjoint", "mpgos_pt_tape_info", "mpgos_pt_solve_record_static",
+    "mpgos_pt_dense_interpolate",
     "mpgos_cb_create", "mpgos_cb_destroy", "mpgos_cb_get_shape", "mpgos_cb_set_option", "mpgos_cb_host_buffer",
     "mpgos_cb_device_buffer", "mpgos_cb_sync_h2d", "mpgos_cb_sync_d2h", "mpgos_cb_solve",
     "mpgos_cb_insert_sync_point", "mpgos_cb_sync_solver", "mpgos_cb_timer_start", "mpgos_cb_timer_stop",

@@ -274,6 +274,12 @@ class ProblemSolver:
         capi.check(self._lib.mpgos_pt_adjoint(self._h, C.c_void_p(dLdxT_ptr), C.c_void_p(dLdx0_ptr),
                                               C.c_void_p(dLdp_ptr or None)))
 
+    def DenseInterpolate(self, times_ptr: int, n_times: int, out_ptr: int):
+        """Cubic Hermite interpolation of the device dense output at n_times
+        requested times (device pointers, FP64): out [n_times][SD][NT]."""
+        capi.check(self._lib.mpgos_pt_dense_interpolate(self._h, C.c_void_p(times_ptr), int(n_times),
+                                                        C.c_void_p(out_ptr)))
+
     def tape_info(self):
         t = capi.Tape()
         capi.check(self._lib.mpgos_pt_tape_info(self._h, C.byref(t)))

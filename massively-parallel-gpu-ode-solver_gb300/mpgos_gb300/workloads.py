@@ -146,9 +146,10 @@ def duffing_rk4_case(nt: int = 8192, periods: int = 1024, B: float = 0.3) -> Cas
     return c
 
 
-def duffing_param_case(nt: int = 1 << 18, periods: int = 64, tol: float = 1e-9, seed: int = 20261203) -> Case:
+def duffing_param_case(nt: int = 1 << 18, periods: int = 64, tol: float = 1e-9, seed: int = 20261203,
+                       ndo: int = 0) -> Case:
     rng = np.random.default_rng(seed)
-    c = empty_case("duffing_param", 1, nt)
+    c = empty_case("duffing_param", 1, nt, ndo)
     a = c.arrays
     a["td"][1] = 2.0 * math.pi * periods
     a["cp"][0] = rng.uniform(0.2, 0.3, nt)

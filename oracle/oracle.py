@@ -74,6 +74,31 @@ def replay(case, dt_tape: np.ndarray, n_steps: np.ndarray, x0=None, cp=None, thr
     return x
 
 
+def dense_interpolate(case, didx, dtime, dstate, times, acc=None, acci=None) -> np.ndarray:
+    """CPU cubic Hermite interpolation of a dense output (``didx`` [NT],
+    ``dtime`` [NDO][NT], ``dstate`` [NDO][SD][NT], e.g. read back from the GPU)
+    at ``times``, with the right-hand side of ``case``'s hooks as slopes.
+    Returns [n_times][SD][NT]."""
+    lib = _oracle(case.system)
+    if not hasattr(lib.oracle_pt_dense_interpolate, "_typed"):
+        lib.oracle_pt_dense_interpolate.restype = C.c_int
+        lib.oracle_pt_dense_interpolate.argtypes = [C.c_longlong, C.c_int, _I, _D, _D, _D, _D, _I, _D, _I, _D,
+                                                    C.c_int, _D]
+        lib.oracle_pt_dense_interpolate._typed = True
+    a, tol, _ = _prepare(case)
+    times = np.ascontiguousarray(np.asarray(times, np.float64))
+    sd = np.asarray(dstate).shape[1] if np.asarray(dstate).ndim == 3 else a["x"].shape[0]
+    out = np.empty((len(times), sd, case.nt))
+    rc = lib.oracle_pt_dense_interpolate(
+        case.nt, case.ndo, np.ascontiguousarray(didx, dtype=np.int32), np.ascontiguousarray(dtime, dtype=np.float64),
+        np.ascontiguousarray(dstate, dtype=np.float64), a["cp"], tol["sp"], tol["spi"],
+        np.ascontiguousarray(a["acc"] if acc is None else acc, dtype=np.float64),
+        np.ascontiguousarray(a["acci"] if acci is None else acci, dtype=np.int32), times, len(times), out)
+    if rc != 0:
+        raise RuntimeError(f"oracle_pt_dense_interpolate failed with {rc}")
+    return out
+
+
 def max_threads(system: str = "lorenz") -> int:
     return int(_oracle(system).oracle_pt_threads())
 

@@ -26,6 +26,8 @@
 
 #include MPGOS_SYSTEM_HEADER
 
+#include <algorithm>
+#include <cmath>
 #include <cstdint>
 #include <vector>
 #ifdef _OPENMP
@@ -356,6 +358,66 @@ int oracle_pt_replay(int algorithm, long long nt, long long first, long long cou
             }
             for (int k = 0; k < SD; k++) x[i + k * nt] = xi[k];
             t[i] = ti;
+        }
+    }
+    return 0;
+}
+
+// Dense-output interpolation, the CPU statement of the GPU extension
+// (csrc/perthread/dense_interp.cuh): for every instance and requested time
+// tau, the cubic Hermite polynomial through the stored points (t_k, x_k),
+// (t_k+1, x_k+1) bracketing tau, slopes f(t_k, x_k) and f(t_k+1, x_k+1) from
+// the hooks; NaN outside [t_0, t_last]; tau equal to the last stored time or
+// a repeated time stamp gives the later stored state. out [n_times][SD][nt].
+int oracle_pt_dense_interpolate(long long nt, int ndo, const int* didx, const double* dtime, const double* dstate,
+                                const double* cp, const double* sp, const int* spi, const double* acc,
+                                const int* acci, const double* times, int n_times, double* out)
+{
+    if (nt < 1 || ndo < 0 || n_times < 0) return 1;
+    std::vector<double> spc(sp, sp + NSP);
+    std::vector<int> spic(spi, spi + NISP);
+    spc.push_back(0.0);
+    spic.push_back(0);
+    const long long step = nt * SD;
+    for (long long i = 0; i < nt; i++) {
+        double cpi[one_at_least<NCP>()], acci_d[one_at_least<NA>()];
+        int accii[one_at_least<NIA>()];
+        for (int k = 0; k < NCP; k++) cpi[k] = cp[i + k * nt];
+        for (int k = 0; k < NA; k++) acci_d[k] = acc[i + k * nt];
+        for (int k = 0; k < NIA; k++) accii[k] = acci[i + k * nt];
+        const int n = std::min(didx[i], ndo);
+        for (int j = 0; j < n_times; j++) {
+            const double tau = times[j];
+            double* o = out + (long long)j * step + i;
+            int k = -1;
+            for (int m = 0; m < n; m++)
+                if (dtime[i + (long long)m * nt] <= tau) k = m;
+            const bool inside = k >= 0 && (k < n - 1 || dtime[i + (long long)k * nt] == tau);
+            if (!inside) {
+                for (int c = 0; c < SD; c++) o[c * nt] = std::nan("");
+                continue;
+            }
+            if (k == n - 1) {
+                for (int c = 0; c < SD; c++) o[c * nt] = dstate[i + c * nt + k * step];
+                continue;
+            }
+            const double t0 = dtime[i + (long long)k * nt], t1 = dtime[i + (long long)(k + 1) * nt];
+            double x0[SD], x1[SD], f0[SD], f1[SD];
+            for (int c = 0; c < SD; c++) {
+                x0[c] = dstate[i + c * nt + k * step];
+                x1[c] = dstate[i + c * nt + (k + 1) * step];
+            }
+            const double h = t1 - t0;
+            if (!(h > 0.0)) {
+                for (int c = 0; c < SD; c++) o[c * nt] = x1[c];
+                continue;
+            }
+            PerThread_OdeFunction((int)i, (int)nt, f0, x0, t0, cpi, spc.data(), spic.data(), acci_d, accii);
+            PerThread_OdeFunction((int)i, (int)nt, f1, x1, t1, cpi, spc.data(), spic.data(), acci_d, accii);
+            const double s = (tau - t0) / h, r = 1.0 - s;
+            const double h00 = (1.0 + 2.0 * s) * r * r, h10 = s * r * r * h;
+            const double h01 = s * s * (3.0 - 2.0 * s), h11 = s * s * (s - 1.0) * h;
+            for (int c = 0; c < SD; c++) o[c * nt] = h00 * x0[c] + h10 * f0[c] + h01 * x1[c] + h11 * f1[c];
         }
     }
     return 0;
