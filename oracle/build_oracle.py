@@ -19,8 +19,9 @@ TEST INFRASTRUCTURE ONLY.
   (oracle_coupled.cpp) compiled once per coupled-system plugin source
   ``systems/<system>.cu`` (its hook file and coupling storage).
 * ``oracle/_ref/ref_gpu_cb_<system>_<alg>_ns<NS>_tpb<TPB>_spb<SPB>_ndo<NDO>.cubin``
-  - the reference's own coupled kernel (MultipleSystems_SingleBlockLaunch)
-  built for sm_103a (ref_gpu_coupled_entry.cu).
+  - the reference's own coupled kernels (all four variants, picked from
+  SPB, UPS and TPB as its Solve() does) built for sm_103a
+  (ref_gpu_coupled_entry.cu).
 * ``oracle/_ref/libref_cpu_<system>.so`` - the reference's own
   SourceCodes/SingleSystem_PerThread_Solver.cuh compiled for the CPU through
   ref_cpu_entry.cpp, straight from the reference checkout (MPGOS_REFERENCE_ROOT,
@@ -94,6 +95,10 @@ REF_GPU_CB_KERNELS = [
     ("ring16_full", 1, 256, 64, 4, 0), ("ring16_band", 1, 256, 64, 4, 0), ("ring16_circband", 1, 256, 64, 4, 0),
     ("ring16_circ", 1, 256, 64, 4, 0), ("ring16_full", 0, 256, 64, 4, 0), ("ring16_full", 1, 256, 64, 4, 8),
     ("ring64", 1, 512, 128, 2, 0), ("ring64", 1, 16384, 128, 2, 0), ("ring64", 1, 16384, 256, 4, 0),
+    # the reference's three other coupled kernels (variant chosen from SPB, UPS, TPB as its Solve() does):
+    # SingleSystem_SingleBlockLaunch, SingleSystem_MultipleBlockLaunches, MultipleSystems_MultipleBlockLaunches
+    ("ring64", 1, 512, 64, 1, 0), ("ring64", 1, 512, 32, 1, 0), ("ring64", 1, 512, 64, 2, 0),
+    ("ring64", 0, 512, 32, 1, 0),
 ]
 
 

@@ -230,14 +230,17 @@ def coupled_available(system: str, algorithm: int, ns: int, tpb: int, spb: int, 
 
 
 class CoupledReferenceKernel(ReferenceKernel):
-    """The reference's MultipleSystems_SingleBlockLaunch coupled kernel
-    (CoupledSystmes_PerBlock_Solver.cuh:1507-2211) for one (system,
-    algorithm, NS, TPB, SPB, NDO), launched as the reference's Solve() does
+    """The reference's coupled kernel for one (system, algorithm, NS, TPB,
+    SPB, NDO): MultipleSystems_SingleBlockLaunch
+    (CoupledSystmes_PerBlock_Solver.cuh:1507-2211), or the SingleSystem /
+    MultipleBlockLaunches variants (:10, :786, :2214) where SPB and UPS > TPB
+    select them, launched as the reference's Solve() does
     (CoupledSystems_PerBlock_Interface.cuh:1947-1966: grid ceil(NS/SPB),
-    block TPB, dynamic shared memory for the global parameters and, when
-    shared, the coupling matrices, :540-544) on the device buffers of a GB300
-    ``CoupledProblemSolver``. SPB * TPB layouts without thread padding only,
-    where the reference's unit layout is the GB300 one."""
+    block TPB, thread configuration of :385-390, dynamic shared memory for the
+    global parameters and, when shared, the coupling matrices, :540-544) on
+    the device buffers of a GB300 ``CoupledProblemSolver``. Layouts without
+    thread padding only (SPB*UPS a multiple of TPB, or SPB*UPS == TPB), where
+    the reference's unit layout is the GB300 one."""
 
     def __init__(self, system: str, algorithm: int, ns: int, tpb: int, spb: int, ndo: int = 0):
         path = _b.ref_cb_cubin(system, algorithm, ns, tpb, spb, ndo)
@@ -266,8 +269,9 @@ class CoupledReferenceKernel(ReferenceKernel):
         SharedCouplingMatrices off unless circular)."""
         from mpgos_gb300.capi import CbVariable as V
         ups = solver.UPS
-        if solver.NS != self.ns or solver.NDO != self.ndo or self.spb * ups != self.tpb or self.ns % self.spb:
-            raise ValueError("solver shape does not match the compiled reference kernel")
+        logical = self.spb * ups
+        if solver.NS != self.ns or solver.NDO != self.ndo or logical % self.tpb or self.ns % self.spb:
+            raise ValueError("solver shape does not match the compiled reference kernel (or needs thread padding)")
         if solver.CCI == 1:
             shared_coupling = 1  # the reference forces it (CoupledSystems_PerBlock_Interface.cuh:524-527)
         d = solver.device_ptr
@@ -279,7 +283,7 @@ class CoupledReferenceKernel(ReferenceKernel):
             self._upload(np.asarray(case.rtol, np.float64)), self._upload(np.asarray(case.atol, np.float64)),
             self._upload(np.asarray(case.etol, np.float64)), self._upload(np.asarray(case.edir, np.int32)))
         grid = self.ns // self.spb
-        self.tc = CbThreadConfiguration(self.tpb, 1, 0, self.tpb, grid, self.ns * ups)
+        self.tc = CbThreadConfiguration(logical, logical // self.tpb, 0, self.tpb, grid, self.ns * ups)
         self.smu = CbSharedMemoryUsage(bool(shared_global), bool(shared_coupling), solver.MAT,
                                        1 if self.algorithm == 1 else 0)
         o = case.options

@@ -1,5 +1,9 @@
-// sm_103a build of the reference's own coupled per-block solver kernel
-// (MultipleSystems_SingleBlockLaunch), one template instantiation per cubin.
+// sm_103a build of the reference's own coupled per-block solver kernels, one
+// template instantiation per cubin. The variant is the one the reference's
+// Solve() launches for the (SPB, UPS, TPB) of the cubin
+// (CoupledSystems_PerBlock_Interface.cuh:1953-1965): MultipleBlockLaunches
+// when SPB*UPS > TPB, SingleBlockLaunch otherwise; MultipleSystems when
+// SPB > 1, SingleSystem when SPB == 1.
 //
 // TEST INFRASTRUCTURE ONLY. oracle/build_oracle.py compiles this file with
 // nvcc -cubin against the reference's unmodified
@@ -24,7 +28,17 @@
 
 #include "CoupledSystmes_PerBlock_Solver.cuh"
 
-template __global__ void CoupledSystems_PerBlock_MultipleSystems_SingleBlockLaunch<
+#if (REF_SPB > 1) && (REF_SPB * MPGOS_SYS_UPS > REF_TPB)
+#define REF_CB_KERNEL CoupledSystems_PerBlock_MultipleSystems_MultipleBlockLaunches
+#elif (REF_SPB == 1) && (MPGOS_SYS_UPS > REF_TPB)
+#define REF_CB_KERNEL CoupledSystems_PerBlock_SingleSystem_MultipleBlockLaunches
+#elif (REF_SPB > 1)
+#define REF_CB_KERNEL CoupledSystems_PerBlock_MultipleSystems_SingleBlockLaunch
+#else
+#define REF_CB_KERNEL CoupledSystems_PerBlock_SingleSystem_SingleBlockLaunch
+#endif
+
+template __global__ void REF_CB_KERNEL<
     REF_NS, MPGOS_SYS_UPS, MPGOS_SYS_UD, REF_TPB, REF_SPB, MPGOS_SYS_NC, MPGOS_SYS_CBW, MPGOS_SYS_CCI, MPGOS_SYS_NUP,
     MPGOS_SYS_NSP, MPGOS_SYS_NGP, MPGOS_SYS_NIGP, MPGOS_SYS_NUA, MPGOS_SYS_NIUA, MPGOS_SYS_NSA, MPGOS_SYS_NISA,
     MPGOS_SYS_NE, REF_NDO, REF_ALG, double>(Struct_ThreadConfiguration, Struct_GlobalVariables<double>,

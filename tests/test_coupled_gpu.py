@@ -168,6 +168,21 @@ def test_coupled_df_stage_mapping_is_invariant(native_libs):
         assert_bitwise(base, CW.run_coupled_gpu(case, mode=capi.MODE_DF_STAGE | capi.MODE_PERSISTENT, warps=warps))
 
 
+@pytest.mark.parametrize("tpb,spb,alg", [(64, 1, 1), (32, 1, 1), (64, 2, 1), (32, 1, 0)],
+                         ids=["SingleSystem_SingleBlockLaunch", "SingleSystem_MultipleBlockLaunches",
+                              "MultipleSystems_MultipleBlockLaunches", "SingleSystem_MultipleBlockLaunches_rk4"])
+def test_coupled_matches_every_reference_kernel_variant(tpb, spb, alg, native_libs):
+    """The reference picks one of four coupled kernels from SPB, UPS and TPB
+    (one system or several per block; the block's logical threads in one or
+    several passes). One warp per system here covers every shape: the GB300
+    FP64 kernel is bit-identical to each variant on 512 rings of 64 units."""
+    case = CW.ring_case("ring64", ns=512, periods=1, seed=12, algorithm=alg)
+    ref = _ref(case, tpb, spb)
+    res = CW.run_coupled_gpu(case, mode=0, warps=4)
+    assert np.all(res["status"] == 0)
+    assert_bitwise(res, ref, keys=KEYS)
+
+
 def test_coupled_full_ensemble_matches_reference_kernel(native_libs):
     """16384 rings of 64 units with the dense coupling matrix (the coupled
     configuration at full ensemble size; two forcing periods): crossing
