@@ -242,23 +242,27 @@ class ProblemSolver {
         return static_cast<T>(static_cast<Precision*>(host_[DenseState])[dense_state("GetHost", sid, uid, v, comp, slot)]);
     }
 
-    // ---- Print (:1808-1945): same file names and number format --------------------
+    // ---- Print (:1808-1945): same file names and number format; unit-scope
+    // files in the reference's padded logical-thread rows for this TPB/SPB ----
     void Print(ListOfVariables v)
     {
+        namespace pr = mpgos::dropin::print;
+        auto P_ = [&](ListOfVariables x) { return static_cast<Precision*>(host_[x]); };
+        auto I_ = [&](ListOfVariables x) { return static_cast<int*>(host_[x]); };
         switch (v) {
-            case TimeDomain: columns("TimeDomainInSolverObject.txt", NS, 2, static_cast<Precision*>(host_[v])); break;
-            case ActualTime: columns("ActualTimeInSolverObject.txt", NS, 1, static_cast<Precision*>(host_[v])); break;
-            case ActualState: columns("ActualStateInSolverObject.txt", NU, UD, static_cast<Precision*>(host_[v])); break;
-            case UnitParameters: columns("UnitParametersInSolverObject.txt", NU, NUP, static_cast<Precision*>(host_[v])); break;
-            case SystemParameters: columns("SystemParametersInSolverObject.txt", NS, NSP, static_cast<Precision*>(host_[v])); break;
-            case GlobalParameters: columns("GlobalParametersInSolverObject.txt", NGP, 1, static_cast<Precision*>(host_[v])); break;
-            case IntegerGlobalParameters: columns("IntegerGlobalParametersInSolverObject.txt", NiGP, 1, static_cast<int*>(host_[v])); break;
-            case UnitAccessories: columns("UnitAccessoriesInSolverObject.txt", NU, NUA, static_cast<Precision*>(host_[v])); break;
-            case IntegerUnitAccessories: columns("IntegerUnitAccessoriesInSolverObject.txt", NU, NiUA, static_cast<int*>(host_[v])); break;
-            case SystemAccessories: columns("SystemAccessoriesInSolverObject.txt", NS, NSA, static_cast<Precision*>(host_[v])); break;
-            case IntegerSystemAccessories: columns("IntegerSystemAccessoriesInSolverObject.txt", NS, NiSA, static_cast<int*>(host_[v])); break;
-            case CouplingStrength: columns("CouplingStrengthInSolverObject.txt", NS, NC, static_cast<Precision*>(host_[v])); break;
-            case CouplingIndex: columns("CouplingIndexInSolverObject.txt", NC, 1, static_cast<int*>(host_[v])); break;
+            case TimeDomain: pr::system_scope("TimeDomainInSolverObject.txt", NS, 2, P_(v)); break;
+            case ActualTime: pr::system_scope("ActualTimeInSolverObject.txt", NS, 1, P_(v)); break;
+            case ActualState: pr::unit_scope("ActualStateInSolverObject.txt", UD, P_(v), NS, UPS, TPB, SPB); break;
+            case UnitParameters: pr::unit_scope("UnitParametersInSolverObject.txt", NUP, P_(v), NS, UPS, TPB, SPB); break;
+            case SystemParameters: pr::system_scope("SystemParametersInSolverObject.txt", NS, NSP, P_(v)); break;
+            case GlobalParameters: pr::system_scope("GlobalParametersInSolverObject.txt", NGP, 1, P_(v)); break;
+            case IntegerGlobalParameters: pr::system_scope("IntegerGlobalParametersInSolverObject.txt", NiGP, 1, I_(v)); break;
+            case UnitAccessories: pr::unit_scope("UnitAccessoriesInSolverObject.txt", NUA, P_(v), NS, UPS, TPB, SPB); break;
+            case IntegerUnitAccessories: pr::unit_scope("IntegerUnitAccessoriesInSolverObject.txt", NiUA, I_(v), NS, UPS, TPB, SPB); break;
+            case SystemAccessories: pr::system_scope("SystemAccessoriesInSolverObject.txt", NS, NSA, P_(v)); break;
+            case IntegerSystemAccessories: pr::system_scope("IntegerSystemAccessoriesInSolverObject.txt", NS, NiSA, I_(v)); break;
+            case CouplingStrength: pr::system_scope("CouplingStrengthInSolverObject.txt", NS, NC, P_(v)); break;
+            case CouplingIndex: pr::system_scope("CouplingIndexInSolverObject.txt", NC, 1, I_(v)); break;
             default: wrong("Print", v);
         }
     }
@@ -266,11 +270,18 @@ class ProblemSolver {
     {
         if (v == CouplingMatrix) {
             mpgos::dropin::bound("Print", "CouplingMatrix", serial, 0, NC - 1);
-            columns("CouplingMatrixInSolverObject_" + std::to_string(serial) + ".txt", UPS, UPS,
-                    full_.data() + static_cast<size_t>(serial) * UPS * UPS);
+            mpgos::dropin::print::system_scope("CouplingMatrixInSolverObject_" + std::to_string(serial) + ".txt", UPS,
+                                               UPS, full_.data() + static_cast<size_t>(serial) * UPS * UPS);
         } else if (v == DenseOutput) {
             mpgos::dropin::bound("Print", "DenseOutput", serial, 0, NS - 1);
-            dense_output(serial);
+            mpgos::dropin::print::coupled_dense(
+                "DenseOutput_" + std::to_string(serial) + ".txt", serial, NS, UPS, UD, NUP, NUA, NiUA, NSP, NSA, NiSA,
+                NGP, NiGP, NDO, static_cast<Precision*>(host_[UnitParameters]),
+                static_cast<Precision*>(host_[UnitAccessories]), static_cast<int*>(host_[IntegerUnitAccessories]),
+                static_cast<Precision*>(host_[SystemParameters]), static_cast<Precision*>(host_[SystemAccessories]),
+                static_cast<int*>(host_[IntegerSystemAccessories]), static_cast<Precision*>(host_[GlobalParameters]),
+                static_cast<int*>(host_[IntegerGlobalParameters]), static_cast<int*>(host_[DenseIndex]),
+                static_cast<Precision*>(host_[DenseTime]), static_cast<Precision*>(host_[DenseState]));
         } else {
             wrong("Print", v);
         }
@@ -364,61 +375,6 @@ class ProblemSolver {
         mpgos::dropin::bound(fn, "ComponentNumber in dense state", comp, 0, UD - 1);
         mpgos::dropin::bound(fn, "DenseState", slot, 0, NDO - 1);
         return static_cast<size_t>(sid) * UPS + uid + static_cast<size_t>(comp) * NU + static_cast<size_t>(slot) * NU * UD;
-    }
-
-    template <typename T> void columns(const std::string& name, int rows, int cols, const T* data)
-    {
-        std::ofstream f(name);
-        f.precision(10);
-        f.flags(std::ios::scientific);
-        for (int i = 0; i < rows; i++) {
-            for (int j = 0; j < cols; j++) {
-                f.width(18);
-                f << data[static_cast<size_t>(i) + static_cast<size_t>(j) * rows] << ',';
-            }
-            f << '\n';
-        }
-    }
-
-    void dense_output(int sid)
-    {
-        std::ofstream f("DenseOutput_" + std::to_string(sid) + ".txt");
-        f.precision(10);
-        f.flags(std::ios::scientific);
-        const Precision* up = static_cast<Precision*>(host_[UnitParameters]);
-        f << "UnitParameters:\n";
-        f.width(18);
-        f << "Serial No." << ',';
-        for (int u = 0; u < UPS; u++) {
-            f.width(18);
-            f << "U" + std::to_string(u) << (u < UPS - 1 ? "," : "");
-        }
-        f << '\n';
-        for (int k = 0; k < NUP; k++) {
-            f.width(18);
-            f << k << ',';
-            for (int u = 0; u < UPS; u++) {
-                f.width(18);
-                f << up[static_cast<size_t>(sid) * UPS + u + static_cast<size_t>(k) * NU] << (u < UPS - 1 ? "," : "");
-            }
-            f << '\n';
-        }
-        f << "\nTime series:\n";
-        const int n = static_cast<int*>(host_[DenseIndex])[sid];
-        const Precision* tt = static_cast<Precision*>(host_[DenseTime]);
-        const Precision* xs = static_cast<Precision*>(host_[DenseState]);
-        for (int i = 0; i < n && i < NDO; i++) {
-            f.width(18);
-            f << tt[sid + static_cast<size_t>(i) * NS] << ',';
-            for (int u = 0; u < UPS; u++)
-                for (int c = 0; c < UD; c++) {
-                    f.width(18);
-                    f << xs[static_cast<size_t>(sid) * UPS + u + static_cast<size_t>(c) * NU +
-                            static_cast<size_t>(i) * NU * UD]
-                      << ((u < UPS - 1 || c < UD - 1) ? "," : "");
-                }
-            f << '\n';
-        }
     }
 };
 

@@ -213,15 +213,16 @@ class ProblemSolver {
     // Print (:1083-1276): same file names and number format.
     void Print(ListOfVariables v)
     {
+        namespace pr = mpgos::dropin::print;
         switch (v) {
-            case TimeDomain: write_columns("TimeDomainInSolverObject.txt", NT, 2, static_cast<Precision*>(host_[v])); break;
-            case ActualState: write_columns("ActualStateInSolverObject.txt", NT, SD, static_cast<Precision*>(host_[v])); break;
-            case ActualTime: write_columns("ActualTimeInSolverObject.txt", NT, 1, static_cast<Precision*>(host_[v])); break;
-            case ControlParameters: write_columns("ControlParametersInSolverObject.txt", NT, NCP, static_cast<Precision*>(host_[v])); break;
-            case SharedParameters: write_columns("SharedParametersInSolverObject.txt", NSP, 1, static_cast<Precision*>(host_[v])); break;
-            case IntegerSharedParameters: write_columns("IntegerSharedParametersInSolverObject.txt", NISP, 1, static_cast<int*>(host_[v])); break;
-            case Accessories: write_columns("AccessoriesInSolverObject.txt", NT, NA, static_cast<Precision*>(host_[v])); break;
-            case IntegerAccessories: write_columns("IntegerAccessoriesInSolverObject.txt", NT, NIA, static_cast<int*>(host_[v])); break;
+            case TimeDomain: pr::general("TimeDomainInSolverObject.txt", NT, 2, static_cast<Precision*>(host_[v])); break;
+            case ActualState: pr::general("ActualStateInSolverObject.txt", NT, SD, static_cast<Precision*>(host_[v])); break;
+            case ActualTime: pr::general("ActualTimeInSolverObject.txt", NT, 1, static_cast<Precision*>(host_[v])); break;
+            case ControlParameters: pr::general("ControlParametersInSolverObject.txt", NT, NCP, static_cast<Precision*>(host_[v])); break;
+            case SharedParameters: pr::general("SharedParametersInSolverObject.txt", NSP, 1, static_cast<Precision*>(host_[v])); break;
+            case IntegerSharedParameters: pr::general("IntegerSharedParametersInSolverObject.txt", NISP, 1, static_cast<int*>(host_[v])); break;
+            case Accessories: pr::general("AccessoriesInSolverObject.txt", NT, NA, static_cast<Precision*>(host_[v])); break;
+            case IntegerAccessories: pr::general("IntegerAccessoriesInSolverObject.txt", NT, NIA, static_cast<int*>(host_[v])); break;
             default: wrong("Print", v);
         }
     }
@@ -229,35 +230,12 @@ class ProblemSolver {
     {
         mpgos::dropin::bound("Print", "Thread", tid, 0, NT - 1);
         if (v != DenseOutput) wrong("Print", v);
-        std::ofstream f("DenseOutput_" + std::to_string(tid) + ".txt");
-        f.precision(10);
-        f.flags(std::ios::scientific);
-        auto row = [&](const char* title, auto* data, int n, int stride) {
-            f << title << "\n";
-            for (int i = 0; i < n; i++) {
-                f.width(18);
-                f << data[tid * (stride ? 1 : 0) + i * (stride ? stride : 1)];
-                if (i < n - 1) f << ',';
-            }
-            f << '\n';
-        };
-        row("ControlParameters:", static_cast<Precision*>(host_[ControlParameters]), NCP, NT);
-        row("SharedParameters:", static_cast<Precision*>(host_[SharedParameters]), NSP, 0);
-        row("IntegerSharedParameters:", static_cast<int*>(host_[IntegerSharedParameters]), NISP, 0);
-        row("Accessories:", static_cast<Precision*>(host_[Accessories]), NA, NT);
-        row("IntegerAccessories:", static_cast<int*>(host_[IntegerAccessories]), NIA, NT);
-        f << "\nTime series:\n";
-        const int n = static_cast<int*>(host_[DenseIndex])[tid];
-        for (int i = 0; i < n && i < NDO; i++) {
-            f.width(18);
-            f << static_cast<Precision*>(host_[DenseTime])[tid + i * NT] << ',';
-            for (int j = 0; j < SD; j++) {
-                f.width(18);
-                f << static_cast<Precision*>(host_[DenseState])[tid + j * NT + i * NT * SD];
-                if (j < SD - 1) f << ',';
-            }
-            f << '\n';
-        }
+        mpgos::dropin::print::perthread_dense(
+            "DenseOutput_" + std::to_string(tid) + ".txt", tid, NT, SD, NCP, NSP, NISP, NA, NIA, NDO,
+            static_cast<Precision*>(host_[ControlParameters]), static_cast<Precision*>(host_[SharedParameters]),
+            static_cast<int*>(host_[IntegerSharedParameters]), static_cast<Precision*>(host_[Accessories]),
+            static_cast<int*>(host_[IntegerAccessories]), static_cast<int*>(host_[DenseIndex]),
+            static_cast<Precision*>(host_[DenseTime]), static_cast<Precision*>(host_[DenseState]));
     }
 
     void Solve() { mpgos::dropin::check(mpgos_pt_solve(h_), "Solve"); }
@@ -304,20 +282,6 @@ class ProblemSolver {
         mpgos::dropin::bound(fn, "DenseState/TimeStepNumber", step, 0, NDO - 1);
     }
 
-    template <typename T> void write_columns(const std::string& name, int rows, int cols, const T* data)
-    {
-        std::ofstream f(name);
-        f.precision(10);
-        f.flags(std::ios::scientific);
-        for (int i = 0; i < rows; i++) {
-            for (int j = 0; j < cols; j++) {
-                f.width(18);
-                f << data[i + j * rows];
-                if (j < cols - 1) f << ',';
-            }
-            f << '\n';
-        }
-    }
 };
 
 #endif

@@ -14,6 +14,7 @@
 #include <iostream>
 
 #include "../mpgos.h"
+#include "dropin_print.h"
 
 #define gpuErrCHK(call)                                                                           \
     {                                                                                             \

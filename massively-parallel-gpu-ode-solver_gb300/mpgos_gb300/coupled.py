@@ -96,7 +96,11 @@ class CoupledProblemSolver:
     """
 
     def __init__(self, system: str, ns: int, ndo: int = 0, algorithm=Algorithm.RKCK45, precision: str = "double",
-                 device: int = 0):
+                 device: int = 0, tpb: int | None = None, spb: int | None = None):
+        # tpb / spb: the reference's launch shape; used only to lay out the
+        # unit-scope files of Print in its padded rows (one warp integrates
+        # one system here whatever the shape)
+        self.print_tpb, self.print_spb = tpb, spb
         self._lib = capi.runtime()
         pbytes = {"double": 8, "float": 4}[precision]
         self._table = capi.coupled_kernel_table(system, int(algorithm), pbytes)
@@ -325,14 +329,46 @@ class CoupledProblemSolver:
     def set_mode(self, mode: int):
         self.SolverOption(CbOption.KernelMode, int(mode))
 
-    def Print(self, var, serial: int | None = None, path: str | None = None):
-        """Write a variable to a text file as the reference's Print does
-        (one row per system or unit, :1808-1945)."""
-        var = CbVariable(var)
-        if var == CbVariable.CouplingMatrix:
-            data = self._full_matrix[serial or 0]
+    def Print(self, var, serial: int | None = None, directory: str = "."):
+        """Write a variable to the reference's file (CoupledSystems_PerBlock_Interface.cuh:1808-1945):
+        <Variable>InSolverObject.txt for the unit, system and global scope,
+        CouplingMatrixInSolverObject_<serial>.txt, DenseOutput_<serial>.txt."""
+        import os
+        from . import textout as T
+        V = CbVariable
+        var = V(var)
+        path = lambda name: os.path.join(directory, name)
+        if serial is not None:
+            if var == V.CouplingMatrix:
+                self._bound("Print", "CouplingMatrix", serial, 0, self.NC - 1)
+                T.system_scope(path(f"CouplingMatrixInSolverObject_{serial}.txt"), self._full_matrix[serial].T)
+            elif var == V.DenseOutput:
+                self._bound("Print", "DenseOutput", serial, 0, self.NS - 1)
+                h = lambda x, n: self.host(x) if n else np.zeros((0, self.NS * self.UPS))
+                hs = lambda x, n: self.host(x) if n else np.zeros((0, self.NS))
+                T.coupled_dense(path(f"DenseOutput_{serial}.txt"), serial, self.UPS, h(V.UnitParameters, self.NUP),
+                                h(V.UnitAccessories, self.NUA), h(V.IntegerUnitAccessories, self.NiUA),
+                                hs(V.SystemParameters, self.NSP), hs(V.SystemAccessories, self.NSA),
+                                hs(V.IntegerSystemAccessories, self.NiSA),
+                                self.host(V.GlobalParameters) if self.NGP else [],
+                                self.host(V.IntegerGlobalParameters) if self.NiGP else [],
+                                int(self.host(V.DenseIndex)[serial]) if self.NDO else 0,
+                                self.host(V.DenseTime) if self.NDO else np.zeros((0, self.NS)),
+                                self.host(V.DenseState) if self.NDO else np.zeros((0, self.UD, self.NS * self.UPS)))
+            else:
+                raise MpgosError(1, f"Print: variable {var.name} needs a different argument configuration")
+            return
+        names = {V.TimeDomain: "TimeDomain", V.ActualTime: "ActualTime", V.ActualState: "ActualState",
+                 V.UnitParameters: "UnitParameters", V.SystemParameters: "SystemParameters",
+                 V.GlobalParameters: "GlobalParameters", V.IntegerGlobalParameters: "IntegerGlobalParameters",
+                 V.UnitAccessories: "UnitAccessories", V.IntegerUnitAccessories: "IntegerUnitAccessories",
+                 V.SystemAccessories: "SystemAccessories", V.IntegerSystemAccessories: "IntegerSystemAccessories",
+                 V.CouplingStrength: "CouplingStrength", V.CouplingIndex: "CouplingIndex"}
+        if var not in names:
+            raise MpgosError(1, f"Print: variable {var.name} needs a different argument configuration")
+        f = path(f"{names[var]}InSolverObject.txt")
+        data = np.atleast_2d(self.host(var))
+        if var in _UNIT:
+            T.unit_scope(f, data, self.NS, self.UPS, self.print_tpb, self.print_spb)
         else:
-            data = np.atleast_2d(self.host(var)).T
-        path = path or f"{var.name}.txt"
-        np.savetxt(path, data, fmt="%+.6e" if data.dtype.kind == "f" else "%d")
-        return path
+            T.system_scope(f, data)

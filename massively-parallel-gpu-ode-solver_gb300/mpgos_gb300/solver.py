@@ -290,9 +290,11 @@ class ProblemSolver:
 
     # ---- Print (:1083-1276): same file names and number format ---------------
     def Print(self, var, thread_id: int | None = None, directory: str = "."):
+        """Write a variable to the reference's file (SingleSystem_PerThread_Interface.cuh:1083-1276):
+        <Variable>InSolverObject.txt, or DenseOutput_<thread>.txt."""
         import os
+        from . import textout as T
         var = Variable(var)
-        fmt = lambda v: f"{v:18.10e}" if not isinstance(v, (int, np.integer)) else f"{v:18d}"
         if thread_id is None:
             names = {Variable.TimeDomain: "TimeDomain", Variable.ActualState: "ActualState",
                      Variable.ActualTime: "ActualTime", Variable.ControlParameters: "ControlParameters",
@@ -301,26 +303,17 @@ class ProblemSolver:
                      Variable.Accessories: "Accessories", Variable.IntegerAccessories: "IntegerAccessories"}
             if var not in names:
                 raise MpgosError(1, f"Print: variable {var.name} needs a different argument configuration")
-            data = self.host(var)
-            data = data.reshape(-1, 1) if data.ndim == 1 else data.T
-            with open(os.path.join(directory, f"{names[var]}InSolverObject.txt"), "w") as f:
-                for row in data:
-                    f.write(",".join(fmt(v) for v in row) + "\n")
+            T.general(os.path.join(directory, f"{names[var]}InSolverObject.txt"), np.atleast_2d(self.host(var)))
             return
         if var != Variable.DenseOutput:
             raise MpgosError(1, f"Print: variable {var.name} needs a different argument configuration")
         self._bound("Print", "Thread", thread_id, 0, self.NT - 1)
         tid = int(thread_id)
-        lines = ["ControlParameters:", ",".join(fmt(v) for v in self.host(ControlParameters)[:, tid]),
-                 "SharedParameters:", ",".join(fmt(v) for v in self.host(SharedParameters)),
-                 "IntegerSharedParameters:", ",".join(fmt(v) for v in self.host(IntegerSharedParameters)),
-                 "Accessories:", ",".join(fmt(v) for v in self.host(Accessories)[:, tid]),
-                 "IntegerAccessories:", ",".join(fmt(v) for v in self.host(IntegerAccessories)[:, tid]), "",
-                 "Time series:"]
-        if self.NDO > 0:
-            n = int(self.host(DenseIndex)[0, tid])
-            dt, ds = self.host(DenseTime), self.host(DenseState)
-            for i in range(min(n, self.NDO)):
-                lines.append(fmt(dt[i, tid]) + "," + ",".join(fmt(ds[i, c, tid]) for c in range(self.SD)))
-        with open(os.path.join(directory, f"DenseOutput_{tid}.txt"), "w") as f:
-            f.write("\n".join(lines) + "\n")
+        z = lambda n, v: self.host(v) if n else np.zeros((0, self.NT))
+        T.perthread_dense(os.path.join(directory, f"DenseOutput_{tid}.txt"), tid, z(self.NCP, ControlParameters),
+                          self.host(SharedParameters).ravel() if self.NSP else [],
+                          self.host(IntegerSharedParameters).ravel() if self.NISP else [],
+                          z(self.NA, Accessories), z(self.NIA, IntegerAccessories),
+                          int(self.host(DenseIndex)[0, tid]) if self.NDO else 0,
+                          self.host(DenseTime) if self.NDO else np.zeros((0, self.NT)),
+                          self.host(DenseState) if self.NDO else np.zeros((0, self.SD, self.NT)))
