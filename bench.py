@@ -153,24 +153,26 @@ def dist_barrier(world):
         dist.barrier()
 
 
-def dist_max(world, value: float) -> float:
+def _reduce(world, value: float, op: str) -> float:
+    """All-reduce of one scalar over the ranks (timing and step counts only;
+    no data-path collective). The tensor lives where the backend wants it:
+    the GPU for nccl, the host for gloo."""
     if world <= 1:
         return value
     import torch
     import torch.distributed as dist
-    t = torch.tensor([value], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    device = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX if op == "max" else dist.ReduceOp.SUM)
     return float(t.item())
+
+
+def dist_max(world, value: float) -> float:
+    return _reduce(world, value, "max")
 
 
 def dist_sum(world, value: float) -> float:
-    if world <= 1:
-        return value
-    import torch
-    import torch.distributed as dist
-    t = torch.tensor([value], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.SUM)
-    return float(t.item())
+    return _reduce(world, value, "sum")
 
 
 def load_peaks() -> dict:
