@@ -237,21 +237,17 @@ def run_reference(args):
     world, rank, local = dist_setup()
     if rank != 0:
         return
-    from oracle import build_oracle, oracle as O
-    import platform
+    from oracle import oracle as O
     stride = 16
     case = cpu_sample_case(args.nt, stride)
+    # The oracle port (OpenMP over instances): the CPU restatement of the
+    # reference's per-thread solver, pinned bit for bit to the reference's own
+    # kernel compiled for the CPU (tests/test_oracle.py). That reference build
+    # runs one instance at a time through static thread indices, so it cannot
+    # use more than one core, and it only exists where the reference checkout
+    # was present at build time; the port is what runs here.
     kind = "port"
     runner = lambda c: O.run_oracle(c, threads=0)
-    try:
-        # The reference's own kernel compiled for this host (only where the
-        # reference checkout existed at build time and the binary matches).
-        if build_oracle.ref_lib("lorenz").exists() and platform.machine() in ("x86_64", "AMD64"):
-            kind = "reference"
-    except Exception:
-        kind = "port"
-    # ref_cpu_solve is compiled for fixed NT values only; the sample is run
-    # through the oracle port, which is bit-identical to it on x86-64.
     threads = O.max_threads("lorenz")
     for _ in range(args.warmup):
         runner(cpu_sample_case(args.nt, args.nt // 256))
@@ -268,7 +264,7 @@ def run_reference(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "impl": "reference",
             "config": {"workload": WORKLOAD, "instances": args.nt, "sample_stride": stride},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port" if kind == "port" else kind,
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind,
                              "sample": f"{case.nt} of {args.nt} instances (every {stride}th) per step"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
@@ -656,6 +652,10 @@ def main():
     traffic = prof.get("lorenz_df_dram_bytes_per_launch")
     achieved = (instr * attempts_per_launch / kernel_s) if instr else None
     peaks = load_peaks()
+    # per instance: x (3), t, td (2), rho read and x, t written in FP64; the
+    # step-counter accessory read and written, status and the two step
+    # counters written, as int32
+    hbm_bytes = args.nt * ((3 + 1 + 2 + 1) * 8 + (3 + 1) * 8 + 2 * 4 + 3 * 4)
     cpu = errors = None
     if not args.no_cpu:
         stride = 8
@@ -693,7 +693,12 @@ def main():
                                     "same run: the issue ceiling every instruction shares",
                      "algorithmic_fp64_equivalent_tflops": FLOP_PER_ATTEMPT * attempts_per_launch / kernel_s / 1e12,
                      "fp64_fma_peak_tflops": peak_fp64 / 1e12,
-                     "hbm_peak_gbs_measured": peaks.get("hbm_gbs")},
+                     "hbm_peak_gbs_measured": peaks.get("hbm_gbs"),
+                     # the HBM side of the same launch: algorithmic bytes (state, time, time
+                     # domain and rho read; state, time, step counter and status words written)
+                     "hbm": {"algorithmic_bytes": hbm_bytes, "achieved_gbs": hbm_bytes / kernel_s / 1e9,
+                             "frac_of_measured": (hbm_bytes / kernel_s / 1e9 / peaks["hbm_gbs"])
+                             if peaks.get("hbm_gbs") else None}},
         "cpu_baseline": cpu,
         "clocks": clocks.summary(),
         "gpu_launches": args.steps,
