@@ -86,7 +86,8 @@ enum mpgos_option {
     MPGOS_PREFER_SHARED_MEMORY         = 13,
     /* extensions */
     MPGOS_KERNEL_MODE                  = 32, /* MPGOS_MODE_* bit set             */
-    MPGOS_MAXIMUM_ATTEMPTS             = 33  /* step attempts per instance and launch */
+    MPGOS_MAXIMUM_ATTEMPTS             = 33, /* step attempts per instance and launch */
+    MPGOS_INSTANCES_PER_THREAD         = 34  /* static mapping: instances each lane integrates in turn (grid stride) */
 };
 
 /* ---- kernel modes (extensions) -----------------------------------------
@@ -266,7 +267,9 @@ int mpgos_pt_timer_start(mpgos_pt_solver* solver);
 int mpgos_pt_timer_stop(mpgos_pt_solver* solver, float* milliseconds);
 
 /* Autotuner (extension): times one Solve() per candidate (block size x
- * static/persistent mapping) on a scratch copy of the current device state,
+ * mapping: static with 1, 2 or 4 instances per thread, or persistent x
+ * placement of the shared parameters: shared memory or global loads, where the
+ * system has any) on a scratch copy of the current device state,
  * restores the state, keeps the fastest configuration and, if cache_path is
  * not NULL, records it in a JSON cache keyed by system, shape, NT and GPU.
  * `arithmetic` fixes the arithmetic the candidates share: 0 the reference's,

@@ -408,7 +408,7 @@ __global__ void __launch_bounds__(MPGOS_MAX_BLOCK) perthread_df_kernel(Args<doub
     while (true) {
         if (s.terminate) {
             Sv::end(s, a, g);
-            i = Solver<S, MPGOS_RKCK45, double, MODE>::next_index(a, total);
+            i = Solver<S, MPGOS_RKCK45, double, MODE>::next_index(a, total, i);
             if (i >= a.n_active) break;
             Sv::begin(s, i, a, g, o);
         }

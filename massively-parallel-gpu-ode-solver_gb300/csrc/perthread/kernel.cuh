@@ -299,12 +299,15 @@ struct Solver {
         if constexpr (RECORD) a.tape.n_steps[i] = s.nacc;
     }
 
-    // Next instance for a lane whose instance finished: warp-aggregated
-    // atomic on the work counter; the counter counts instances handed out
-    // beyond the first one per lane.
-    __device__ static long long next_index(const Args<P>& a, long long total_threads)
+    // Next instance for a lane whose instance finished. Static mapping: the
+    // grid stride (a grid smaller than the ensemble gives every lane several
+    // instances in sequence, MPGOS_INSTANCES_PER_THREAD; with one lane per
+    // instance the stride ends the lane). Persistent: warp-aggregated atomic
+    // on the work counter, which counts instances handed out beyond the first
+    // one per lane.
+    __device__ static long long next_index(const Args<P>& a, long long total_threads, long long current)
     {
-        if (!PERSISTENT) return a.n_active;
+        if (!PERSISTENT) return current + total_threads;
         const unsigned mask   = __activemask();
         const int lane        = threadIdx.x & 31;
         const int leader      = __ffs(mask) - 1;
@@ -387,7 +390,7 @@ __global__ void __launch_bounds__(MPGOS_MAX_BLOCK) perthread_kernel(Args<P> a)
     while (true) {
         if (s.terminate) {
             Sv::end(s, a, g);
-            i = Sv::next_index(a, total);
+            i = Sv::next_index(a, total, i);
             if (i >= a.n_active) break;
             Sv::begin(s, i, a, g, cpf, accf);
         }

@@ -112,6 +112,7 @@ struct mpgos_pt_solver {
     double initial_dt = 1e-2, max_dt = 1e6, min_dt = 1e-12, grow = 5.0, shrink = 0.1, dense_min_dt = 0.0;
     int32_t dense_freq = 1;
     int32_t prefer_shared = 1;
+    int32_t ipt = 1;  // instances per thread of the static mapping
     int32_t mode = MPGOS_MODE_PLAIN;
     int64_t max_attempts = 10000000;
     uint64_t generation = 1;  // bumped by every change that alters a launch
@@ -226,6 +227,10 @@ int grid_for(const mpgos_pt_solver* s, int32_t mode, int block, int* grid)
 {
     const int64_t blocks_needed = (s->n_active + block - 1) / block;
     int64_t g = blocks_needed;
+    if (!(mode & MPGOS_MODE_PERSISTENT) && s->ipt > 1) {
+        const int64_t per_block = static_cast<int64_t>(block) * s->ipt;
+        g = (s->n_active + per_block - 1) / per_block;
+    }
     if (mode & MPGOS_MODE_PERSISTENT) {
         int per_sm = 0;
         int rc = s->k->occupancy(mode, block, dynamic_smem(s), &per_sm);
@@ -508,6 +513,13 @@ MPGOS_EXPORT int mpgos_pt_set_option(mpgos_pt_solver* s, int32_t option, int32_t
             s->max_attempts = n;
             break;
         }
+        case MPGOS_INSTANCES_PER_THREAD: {
+            const int32_t n = static_cast<int32_t>(value);
+            if (n < 1 || n > 64 || n != value)
+                return fail(MPGOS_ERR_ARGUMENT, "InstancesPerThread %g must be an integer in 1..64", value);
+            s->ipt = n;
+            break;
+        }
         default:
             return fail(MPGOS_ERR_ARGUMENT, "unknown solver option %d", option);
     }
@@ -546,6 +558,7 @@ MPGOS_EXPORT int mpgos_pt_get_option(const mpgos_pt_solver* s, int32_t option, i
         }
         case MPGOS_KERNEL_MODE: *value = s->mode; break;
         case MPGOS_MAXIMUM_ATTEMPTS: *value = (double)s->max_attempts; break;
+        case MPGOS_INSTANCES_PER_THREAD: *value = s->ipt; break;
         default: return fail(MPGOS_ERR_ARGUMENT, "unknown solver option %d", option);
     }
     return MPGOS_OK;
@@ -776,13 +789,19 @@ MPGOS_EXPORT int mpgos_pt_autotune(mpgos_pt_solver* s, int32_t arithmetic, const
             const std::string tag = "\"" + json_escape(k) + "\"";
             size_t pos = line.find(tag);
             if (pos == std::string::npos) continue;
-            int b = 0, m = 0;
+            int b = 0, m = 0, n = 1, ps = s->prefer_shared;
             const char* bp = std::strstr(line.c_str() + pos, "\"block\":");
             const char* mp = std::strstr(line.c_str() + pos, "\"mode\":");
+            const char* np = std::strstr(line.c_str() + pos, "\"instances_per_thread\":");
+            const char* pp = std::strstr(line.c_str() + pos, "\"prefer_shared\":");
+            if (np) sscanf(np, "\"instances_per_thread\": %d", &n);
+            if (pp) sscanf(pp, "\"prefer_shared\": %d", &ps);
             if (bp && mp && sscanf(bp, "\"block\": %d", &b) == 1 && sscanf(mp, "\"mode\": %d", &m) == 1 && b >= 1 &&
-                b <= 256) {
+                b <= 256 && n >= 1 && n <= 64) {
                 s->block = b;
                 s->mode = m;
+                s->ipt = n;
+                s->prefer_shared = ps ? 1 : 0;
                 s->generation++;
                 return MPGOS_OK;
             }
@@ -820,26 +839,48 @@ MPGOS_EXPORT int mpgos_pt_autotune(mpgos_pt_solver* s, int32_t arithmetic, const
         return MPGOS_OK;
     };
 
+    // Candidates: block size x mapping (static with 1, 2 or 4 instances per
+    // thread, or persistent) x placement of the shared parameters (shared
+    // memory or global loads; only where the system has any).
     float best = 1e30f;
-    int best_block = s->block;
+    int best_block = s->block, best_ipt = s->ipt, best_ps = s->prefer_shared;
     int32_t best_mode = s->mode;
+    const int keep_ipt = s->ipt, keep_ps = s->prefer_shared;
     const int blocks[] = {32, 64, 96, 128, 192, 256};
-    for (int pers = 0; pers < 2; pers++) {
-        for (int b : blocks) {
-            const int32_t m = base | (pers ? MPGOS_MODE_PERSISTENT : 0);
-            if ((rc = restore())) { release(); return rc; }
-            MPGOS_CUDA(cudaEventRecord(s->timer_begin, s->stream));
-            if ((rc = enqueue_solve(s, m, b))) { release(); return rc; }
-            MPGOS_CUDA(cudaEventRecord(s->timer_end, s->stream));
-            MPGOS_CUDA(cudaEventSynchronize(s->timer_end));
-            float t = 0.f;
-            MPGOS_CUDA(cudaEventElapsedTime(&t, s->timer_begin, s->timer_end));
-            if (t < best) {
-                best = t;
-                best_block = b;
-                best_mode = m;
+    const int ipts[] = {1, 2, 4, 0};  // 0: persistent
+    const bool has_shared = (s->shape.nsp + s->shape.nisp) > 0;
+    for (int ps = has_shared ? 0 : keep_ps; ps <= (has_shared ? 1 : keep_ps); ps++) {
+        for (int n : ipts) {
+            for (int b : blocks) {
+                const int32_t m = base | (n == 0 ? MPGOS_MODE_PERSISTENT : 0);
+                s->ipt = n == 0 ? 1 : n;
+                s->prefer_shared = ps;
+                if ((rc = restore())) break;
+                MPGOS_CUDA(cudaEventRecord(s->timer_begin, s->stream));
+                if ((rc = enqueue_solve(s, m, b))) break;
+                MPGOS_CUDA(cudaEventRecord(s->timer_end, s->stream));
+                MPGOS_CUDA(cudaEventSynchronize(s->timer_end));
+                float t = 0.f;
+                MPGOS_CUDA(cudaEventElapsedTime(&t, s->timer_begin, s->timer_end));
+                if (t < best) {
+                    best = t;
+                    best_block = b;
+                    best_mode = m;
+                    best_ipt = s->ipt;
+                    best_ps = ps;
+                }
             }
+            if (rc) break;
         }
+        if (rc) break;
+    }
+    s->ipt = keep_ipt;
+    s->prefer_shared = keep_ps;
+    if (rc) {
+        restore();
+        cudaStreamSynchronize(s->stream);
+        release();
+        return rc;
     }
     rc = restore();
     cudaStreamSynchronize(s->stream);
@@ -847,11 +888,14 @@ MPGOS_EXPORT int mpgos_pt_autotune(mpgos_pt_solver* s, int32_t arithmetic, const
     if (rc) return rc;
     s->block = best_block;
     s->mode = best_mode;
+    s->ipt = best_ipt;
+    s->prefer_shared = best_ps;
     s->generation++;
 
     if (cache_path != nullptr) {
         std::ofstream outf(cache_path, std::ios::app);
         if (outf) outf << "{\"" << json_escape(k) << "\": {\"block\": " << best_block << ", \"mode\": " << best_mode
+                       << ", \"instances_per_thread\": " << best_ipt << ", \"prefer_shared\": " << best_ps
                        << ", \"ms\": " << best << "}}\n";
     }
     return MPGOS_OK;

@@ -63,6 +63,7 @@ class Option(IntEnum):
     PreferSharedMemory = 13
     KernelMode = 32
     MaximumAttempts = 33
+    InstancesPerThread = 34
 
 
 MODE_PLAIN = 0

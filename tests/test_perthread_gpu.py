@@ -319,3 +319,48 @@ def test_host_api_bounds_and_scalar_access(native_libs):
             s.SolverOption(Option.ThreadsPerBlock, 1024)
         s.SetHost(0, TimeDomain, 1, math.pi)
         assert s.host(Variable.TimeDomain)[1, 0] == math.pi
+
+
+@pytest.mark.parametrize("ipt", [2, 3])
+def test_instances_per_thread_is_a_mapping_only(ipt, native_libs):
+    """InstancesPerThread > 1 shrinks the static grid; each lane integrates
+    its instances in turn (grid stride). Results are bit-identical to one
+    instance per lane, for the reference arithmetic and for DF_STAGE."""
+    from mpgos_gb300.capi import Option
+    case = W.keller_miksis_case(n_amp=8, n_freq=16, periods=2)
+    for mode in (capi.MODE_PLAIN, capi.MODE_DF_STAGE):
+        a = W.run_gpu(case, mode=mode, block=32)
+        with W.load_solver(case, mode=mode, block=32) as s:
+            s.SolverOption(Option.InstancesPerThread, ipt)
+            grid, block, _ = s.launch_config()
+            assert grid == -(-case.nt // (32 * ipt))
+            s.Solve()
+            b = W.read_results(s)
+        assert_bitwise(a, b)
+
+
+def test_autotuner_explores_mapping_and_placement(native_libs, tmp_path):
+    from mpgos_gb300.capi import Option
+    case = W.duffing_rk4_case(nt=4096, periods=2)
+    cache = tmp_path / "tune.json"
+    with W.load_solver(case, mode=0) as s:
+        s.autotune(fast_control=False, cache_path=str(cache))
+        n = int(s.GetOption(Option.InstancesPerThread))
+        ps = int(s.GetOption(Option.PreferSharedMemory))
+        assert n in (1, 2, 4) and ps in (0, 1)
+        ref = W.read_results(s)
+    line = cache.read_text()
+    assert '"instances_per_thread"' in line and '"prefer_shared"' in line
+    with W.load_solver(case, mode=0) as s:   # cached choice restored
+        s.autotune(fast_control=False, cache_path=str(cache))
+        assert int(s.GetOption(Option.InstancesPerThread)) == n
+        assert int(s.GetOption(Option.PreferSharedMemory)) == ps
+    # the tuned launch integrates the same ensemble bit for bit
+    res = W.run_gpu(case, mode=0)
+    with W.load_solver(case, mode=0) as s:
+        s.SolverOption(Option.InstancesPerThread, n)
+        s.SolverOption(Option.PreferSharedMemory, ps)
+        for _ in range(case.phases):
+            s.Solve()
+        tuned = W.read_results(s)
+    assert_bitwise(res, tuned)
