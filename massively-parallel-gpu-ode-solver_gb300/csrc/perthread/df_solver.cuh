@@ -77,72 +77,79 @@ struct DfStaged {
 // Controller of DF_STAGE (see the file comment).
 // Cash-Karp 4(5) step in double-float: the scheme of step_rkck45
 // (SingleSystem_PerThread_ExplicitRungeKutta_Steppers.cuh:121-289, same
-// coefficients and stage order), each stage sum accumulated with the fused
-// double-float multiply-add (df::fma: 15 FP32 operations per term instead of
-// a multiply and an add, 18), X = fma(dt, sum, x).
+// coefficients and stage order). Each stage sum sum_j a_j k_j is accumulated
+// unnormalised (df::prod_sum: 12 FP32 operations per term after the first)
+// and applied as X = x + dt * sum in one renormalising step.
 template <int SD>
 __device__ __forceinline__ void step_rkck45_df(int tid, int nt, dfloat t, dfloat dt, dfloat* x, dfloat* xn,
                                                dfloat* err, int& finite, dfloat* cp, dfloat* sp, int* spi,
                                                dfloat* acc, int* acci)
 {
     using df::fma;
+    using df::prod_sum;
+    using df::prod_sum_add;
+    using df::prod_sum_axpy;
+    using df::prod_sum_start;
     dfloat X[SD];
     dfloat k1[SD], k2[SD], k3[SD], k4[SD], k5[SD], k6[SD];
 
     PerThread_OdeFunction(tid, nt, k1, x, t, cp, sp, spi, acc, acci);
 
 #pragma unroll
-    for (int i = 0; i < SD; i++) X[i] = fma(dt, dfloat(1.0 / 5.0) * k1[i], x[i]);
+    for (int i = 0; i < SD; i++) X[i] = prod_sum_axpy(dt, prod_sum_start(dfloat(1.0 / 5.0), k1[i]), x[i]);
     PerThread_OdeFunction(tid, nt, k2, X, fma(dt, dfloat(1.0 / 5.0), t), cp, sp, spi, acc, acci);
 
 #pragma unroll
-    for (int i = 0; i < SD; i++)
-        X[i] = fma(dt, fma(dfloat(9.0 / 40.0), k2[i], dfloat(3.0 / 40.0) * k1[i]), x[i]);
+    for (int i = 0; i < SD; i++) {
+        prod_sum s = prod_sum_start(dfloat(3.0 / 40.0), k1[i]);
+        prod_sum_add(s, dfloat(9.0 / 40.0), k2[i]);
+        X[i] = prod_sum_axpy(dt, s, x[i]);
+    }
     PerThread_OdeFunction(tid, nt, k3, X, fma(dt, dfloat(3.0 / 10.0), t), cp, sp, spi, acc, acci);
 
 #pragma unroll
     for (int i = 0; i < SD; i++) {
-        dfloat s = dfloat(3.0 / 10.0) * k1[i];
-        s = fma(dfloat(-9.0 / 10.0), k2[i], s);
-        s = fma(dfloat(6.0 / 5.0), k3[i], s);
-        X[i] = fma(dt, s, x[i]);
+        prod_sum s = prod_sum_start(dfloat(3.0 / 10.0), k1[i]);
+        prod_sum_add(s, dfloat(-9.0 / 10.0), k2[i]);
+        prod_sum_add(s, dfloat(6.0 / 5.0), k3[i]);
+        X[i] = prod_sum_axpy(dt, s, x[i]);
     }
     PerThread_OdeFunction(tid, nt, k4, X, fma(dt, dfloat(3.0 / 5.0), t), cp, sp, spi, acc, acci);
 
 #pragma unroll
     for (int i = 0; i < SD; i++) {
-        dfloat s = dfloat(-11.0 / 54.0) * k1[i];
-        s = fma(dfloat(5.0 / 2.0), k2[i], s);
-        s = fma(dfloat(-70.0 / 27.0), k3[i], s);
-        s = fma(dfloat(35.0 / 27.0), k4[i], s);
-        X[i] = fma(dt, s, x[i]);
+        prod_sum s = prod_sum_start(dfloat(-11.0 / 54.0), k1[i]);
+        prod_sum_add(s, dfloat(5.0 / 2.0), k2[i]);
+        prod_sum_add(s, dfloat(-70.0 / 27.0), k3[i]);
+        prod_sum_add(s, dfloat(35.0 / 27.0), k4[i]);
+        X[i] = prod_sum_axpy(dt, s, x[i]);
     }
     PerThread_OdeFunction(tid, nt, k5, X, t + dt, cp, sp, spi, acc, acci);
 
 #pragma unroll
     for (int i = 0; i < SD; i++) {
-        dfloat s = dfloat(1631.0 / 55296.0) * k1[i];
-        s = fma(dfloat(175.0 / 512.0), k2[i], s);
-        s = fma(dfloat(575.0 / 13824.0), k3[i], s);
-        s = fma(dfloat(44275.0 / 110592.0), k4[i], s);
-        s = fma(dfloat(253.0 / 4096.0), k5[i], s);
-        X[i] = fma(dt, s, x[i]);
+        prod_sum s = prod_sum_start(dfloat(1631.0 / 55296.0), k1[i]);
+        prod_sum_add(s, dfloat(175.0 / 512.0), k2[i]);
+        prod_sum_add(s, dfloat(575.0 / 13824.0), k3[i]);
+        prod_sum_add(s, dfloat(44275.0 / 110592.0), k4[i]);
+        prod_sum_add(s, dfloat(253.0 / 4096.0), k5[i]);
+        X[i] = prod_sum_axpy(dt, s, x[i]);
     }
     PerThread_OdeFunction(tid, nt, k6, X, fma(dt, dfloat(7.0 / 8.0), t), cp, sp, spi, acc, acci);
 
 #pragma unroll
     for (int i = 0; i < SD; i++) {
-        dfloat s = dfloat(37.0 / 378.0) * k1[i];
-        s = fma(dfloat(250.0 / 621.0), k3[i], s);
-        s = fma(dfloat(125.0 / 594.0), k4[i], s);
-        s = fma(dfloat(512.0 / 1771.0), k6[i], s);
-        xn[i] = fma(dt, s, x[i]);
-        dfloat e = dfloat(37.0 / 378.0 - 2825.0 / 27648.0) * k1[i];
-        e = fma(dfloat(250.0 / 621.0 - 18575.0 / 48384.0), k3[i], e);
-        e = fma(dfloat(125.0 / 594.0 - 13525.0 / 55296.0), k4[i], e);
-        e = fma(dfloat(0.0 - 277.0 / 14336.0), k5[i], e);
-        e = fma(dfloat(512.0 / 1771.0 - 1.0 / 4.0), k6[i], e);
-        err[i] = fma(dt, abs(e), dfloat(1e-18));
+        prod_sum s = prod_sum_start(dfloat(37.0 / 378.0), k1[i]);
+        prod_sum_add(s, dfloat(250.0 / 621.0), k3[i]);
+        prod_sum_add(s, dfloat(125.0 / 594.0), k4[i]);
+        prod_sum_add(s, dfloat(512.0 / 1771.0), k6[i]);
+        xn[i] = prod_sum_axpy(dt, s, x[i]);
+        prod_sum e = prod_sum_start(dfloat(37.0 / 378.0 - 2825.0 / 27648.0), k1[i]);
+        prod_sum_add(e, dfloat(250.0 / 621.0 - 18575.0 / 48384.0), k3[i]);
+        prod_sum_add(e, dfloat(125.0 / 594.0 - 13525.0 / 55296.0), k4[i]);
+        prod_sum_add(e, dfloat(0.0 - 277.0 / 14336.0), k5[i]);
+        prod_sum_add(e, dfloat(512.0 / 1771.0 - 1.0 / 4.0), k6[i]);
+        err[i] = fma(dt, abs(df::prod_sum_value(e)), dfloat(1e-18));
         if ((isfinite(xn[i]) == 0) || (isfinite(err[i]) == 0)) finite = 0;
     }
 }

@@ -17,6 +17,8 @@
 //   fma, dot2       a*b + c and a*b + c*d: the exact leading products summed
 //                   by two_sum, all low-order terms folded into one tail
 //                   (the same error class as add)
+//   prod_sum        sums of products accumulated as (two_sum of the leading
+//                   floats, one float of tails), normalised once at the end
 //   div             two long-division correction steps on a float quotient
 //   sqrt            Karp & Markstein 1997 (Newton corrections from rsqrt)
 // sin, cos and sincospi run on the FP32 pipe too (Cody-Waite reduction and
@@ -180,6 +182,42 @@ MPGOS_DF_HD dfloat dot2(dfloat a, dfloat b, dfloat c, dfloat d)
     e = f_fma(c.lo, d.hi, e);
     e = f_add(e, s.lo);
     return quick_two_sum(s.hi, e);
+}
+
+// Sum of double-float products kept unnormalised between terms: the leading
+// floats are summed by two_sum, every rounding error and cross product goes
+// into the trailing float, normalised once when the sum is used
+// (prod_sum_start: 4 FP32 operations, prod_sum_add: 12 per further term
+// instead of 15 for a fused multiply-add with renormalisation).
+struct prod_sum {
+    float h, l;
+};
+
+MPGOS_DF_HD prod_sum prod_sum_start(dfloat a, dfloat b)
+{
+    const dfloat p = two_prod(a.hi, b.hi);
+    return prod_sum{p.hi, f_fma(a.hi, b.lo, f_fma(a.lo, b.hi, p.lo))};
+}
+
+MPGOS_DF_HD void prod_sum_add(prod_sum& s, dfloat a, dfloat b)
+{
+    const dfloat p = two_prod(a.hi, b.hi);
+    const dfloat t = two_sum(s.h, p.hi);
+    s.h = t.hi;
+    s.l = f_add(s.l, f_add(t.lo, f_fma(a.hi, b.lo, f_fma(a.lo, b.hi, p.lo))));
+}
+
+MPGOS_DF_HD dfloat prod_sum_value(prod_sum s) { return quick_two_sum(s.h, s.l); }
+
+// c + a * s for an unnormalised product sum s (15 operations, the same as
+// fma(a, value(s), c) without normalising s first).
+MPGOS_DF_HD dfloat prod_sum_axpy(dfloat a, prod_sum s, dfloat c)
+{
+    const dfloat p = two_prod(a.hi, s.h);
+    float e = f_fma(a.hi, s.l, f_fma(a.lo, s.h, p.lo));
+    const dfloat t = two_sum(p.hi, c.hi);
+    e = f_add(e, f_add(c.lo, t.lo));
+    return quick_two_sum(t.hi, e);
 }
 
 // a * f for a float f (one product term fewer)

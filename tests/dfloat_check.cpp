@@ -20,6 +20,7 @@ int main()
     std::uniform_real_distribution<double> u(-1.0, 1.0), e(-8.0, 8.0);
     auto draw = [&]() { return dfloat(u(rng) * std::pow(2.0, std::floor(e(rng)))); };
     double m_add = 0, m_mul = 0, m_div = 0, m_sqrt = 0, m_cvt = 0, m_cmp = 0, m_norm = 0, m_fma = 0, m_dot = 0;
+    double m_psum = 0, m_paxpy = 0;
     for (int n = 0; n < 200000; n++) {
         const dfloat a = draw(), b = draw();
         const long double A = val(a), B = val(b);
@@ -33,6 +34,23 @@ int main()
         const dfloat c = draw(), dd = draw();
         const long double C = val(c), D = val(dd);
         const dfloat f = mpgos::df::fma(a, b, c), g = mpgos::df::dot2(a, b, c, dd);
+        // five-term product sum and c + a * (sum), unnormalised in between
+        {
+            const dfloat e = draw(), h = draw(), q = draw(), w = draw(), z = draw(), y = draw();
+            mpgos::df::prod_sum ps = mpgos::df::prod_sum_start(a, b);
+            mpgos::df::prod_sum_add(ps, c, dd);
+            mpgos::df::prod_sum_add(ps, e, h);
+            mpgos::df::prod_sum_add(ps, q, w);
+            mpgos::df::prod_sum_add(ps, z, y);
+            const long double E = val(e), H = val(h), Q = val(q), W = val(w), Z = val(z), Y = val(y);
+            const long double exact = A * B + C * D + E * H + Q * W + Z * Y;
+            const long double mag = std::fabs(A * B) + std::fabs(C * D) + std::fabs(E * H) + std::fabs(Q * W) +
+                                    std::fabs(Z * Y);
+            m_psum = std::fmax(m_psum, (double)(std::fabs(val(mpgos::df::prod_sum_value(ps)) - exact) / mag));
+            const dfloat ax = mpgos::df::prod_sum_axpy(e, ps, h);
+            const long double ex2 = E * exact + H;
+            m_paxpy = std::fmax(m_paxpy, (double)(std::fabs(val(ax) - ex2) / (std::fabs(E) * mag + std::fabs(H))));
+        }
         m_fma = std::fmax(m_fma, (double)(std::fabs(val(f) - (A * B + C)) / (std::fabs(A * B) + std::fabs(C))));
         m_dot = std::fmax(m_dot, (double)(std::fabs(val(g) - (A * B + C * D)) / (std::fabs(A * B) + std::fabs(C * D))));
         // normalisation: |lo| <= ulp(hi) / 2 after every operation
@@ -59,7 +77,8 @@ int main()
                                                                      std::fabs(val(mpgos::df::cos(x)) - std::cos(X))));
     }
     std::printf("add %.3e\nmul %.3e\ndiv %.3e\nsqrt %.3e\ncvt %.3e\ncmp %.0f\nnorm %.3f\ntrig %.3f\ntrig_small %.3e\n"
-                "fma %.3e\ndot2 %.3e\n",
-                m_add, m_mul, m_div, m_sqrt, m_cvt, m_cmp, m_norm, m_trig, m_trig_small, m_fma, m_dot);
+                "fma %.3e\ndot2 %.3e\nprod_sum %.3e\nprod_sum_axpy %.3e\n",
+                m_add, m_mul, m_div, m_sqrt, m_cvt, m_cmp, m_norm, m_trig, m_trig_small, m_fma, m_dot, m_psum,
+                m_paxpy);
     return 0;
 }

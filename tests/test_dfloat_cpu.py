@@ -23,6 +23,9 @@ def test_double_float_precision(errors):
     for op in ("add", "mul", "div", "sqrt", "fma"):
         assert errors[op] < 1.5e-14, (op, errors[op])
     assert errors["dot2"] < 2.5e-14, errors["dot2"]   # two products' tails, relative to |ab| + |cd|
+    # five-term unnormalised product sums, relative to the sum of the terms' magnitudes
+    assert errors["prod_sum"] < 5e-14, errors["prod_sum"]
+    assert errors["prod_sum_axpy"] < 7e-14, errors["prod_sum_axpy"]
     assert errors["cvt"] < 4e-15          # double -> double-float keeps 48 bits (2^-48)
 
 
