@@ -79,10 +79,14 @@ struct DfStaged {
 // (SingleSystem_PerThread_ExplicitRungeKutta_Steppers.cuh:121-289, same
 // coefficients and stage order). Each stage sum sum_j a_j k_j is accumulated
 // unnormalised (df::prod_sum: 12 FP32 operations per term after the first)
-// and applied as X = x + dt * sum in one renormalising step.
+// and applied as X = x + dt * sum in one renormalising step. The embedded
+// error estimate dt |sum_j e_j k_j| + 1e-18 is accumulated the same way and
+// delivered in FP32: it cancels down to ~tol of terms of size |k| dt, so its
+// double-float rounding is already ~1e-6 of it at tol 1e-10 and the FP32
+// rounding of the result (6e-8) adds nothing the controller could see.
 template <int SD>
 __device__ __forceinline__ void step_rkck45_df(int tid, int nt, dfloat t, dfloat dt, dfloat* x, dfloat* xn,
-                                               dfloat* err, int& finite, dfloat* cp, dfloat* sp, int* spi,
+                                               float* err, int& finite, dfloat* cp, dfloat* sp, int* spi,
                                                dfloat* acc, int* acci)
 {
     using df::fma;
@@ -149,23 +153,28 @@ __device__ __forceinline__ void step_rkck45_df(int tid, int nt, dfloat t, dfloat
         prod_sum_add(e, dfloat(125.0 / 594.0 - 13525.0 / 55296.0), k4[i]);
         prod_sum_add(e, dfloat(0.0 - 277.0 / 14336.0), k5[i]);
         prod_sum_add(e, dfloat(512.0 / 1771.0 - 1.0 / 4.0), k6[i]);
-        err[i] = fma(dt, abs(df::prod_sum_value(e)), dfloat(1e-18));
-        if ((isfinite(xn[i]) == 0) || (isfinite(err[i]) == 0)) finite = 0;
+        err[i] = fmaf(dt.hi, fabsf(e.h + e.l), 1e-18f);
+        if ((isfinite(xn[i]) == 0) || !isfinite(err[i])) finite = 0;
     }
 }
 
+// Step-size control of the double-float solver
+// (SingleSystem_PerThread_ExplicitRungeKutta_ErrorControllers.cuh:23-85 in
+// structure): tolerance max(rtol max(|xn|, |x|), atol) and the accept test in
+// FP32 on the leading floats (their rounding, ~6e-8, is far below the error
+// estimate's own), factor 0.9 (tol/err)^(1/5 or 1/4) through FP32 log2/exp2.
 template <int SD>
 __device__ __forceinline__ void control_rkck45_df(const DfOptions& o, dfloat dt, const dfloat* x, const dfloat* xn,
-                                                  const dfloat* err, const dfloat* rtol, const dfloat* atol,
+                                                  const float* err, const dfloat* rtol, const dfloat* atol,
                                                   int& update, int& finite, int& terminate, dfloat& new_dt,
                                                   int& status)
 {
     float lr = INFINITY;
 #pragma unroll
     for (int i = 0; i < SD; i++) {
-        const dfloat tol = df::fmax(rtol[i] * df::fmax(df::abs(xn[i]), df::abs(x[i])), atol[i]);
+        const float tol = fmaxf(rtol[i].hi * fmaxf(fabsf(xn[i].hi), fabsf(x[i].hi)), atol[i].hi);
         update = update && (err[i] < tol);
-        lr = fminf(lr, __log2f(tol.hi) - __log2f(err[i].hi));
+        lr = fminf(lr, __log2f(tol) - __log2f(err[i]));
     }
     const float expo = (update == 1) ? 0.2f : 0.25f;
     float q = 0.9f * exp2f(fminf(fmaxf(lr * expo, -120.0f), 120.0f));
@@ -272,7 +281,8 @@ struct DfSolver {
         s.attempts++;
         const int ti = static_cast<int>(s.i), nti = static_cast<int>(a.nt);
         int update = 1, finite = 1, end_reached = 0;
-        dfloat xn[SD], err[SD];
+        dfloat xn[SD];
+        float err[SD];
         s.dt = s.new_dt;
         const dfloat rem = s.td[1] - s.t;
         if (s.dt > rem) {
