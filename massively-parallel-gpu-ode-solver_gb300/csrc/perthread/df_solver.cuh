@@ -154,7 +154,10 @@ __device__ __forceinline__ void step_rkck45_df(int tid, int nt, dfloat t, dfloat
         prod_sum_add(e, dfloat(0.0 - 277.0 / 14336.0), k5[i]);
         prod_sum_add(e, dfloat(512.0 / 1771.0 - 1.0 / 4.0), k6[i]);
         err[i] = fmaf(dt.hi, fabsf(e.h + e.l), 1e-18f);
-        if ((isfinite(xn[i]) == 0) || !isfinite(err[i])) finite = 0;
+        // finiteness on the exponent bits (integer pipe; no conversion to double)
+        if ((__float_as_uint(xn[i].hi) & 0x7f800000u) == 0x7f800000u ||
+            (__float_as_uint(err[i]) & 0x7f800000u) == 0x7f800000u)
+            finite = 0;
     }
 }
 
