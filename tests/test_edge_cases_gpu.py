@@ -1,0 +1,60 @@
+"""Edge cases of the launch: no active instance or system (Solve is a
+no-op), a one-instance ensemble, and an empty time domain (t0 == t1): the
+reference's loop takes one accepted step of size 0 and stops, leaving the
+state unchanged, in every mode."""
+import numpy as np
+import pytest
+
+from mpgos_gb300 import capi, coupled_workloads as CW, workloads as W
+from mpgos_gb300.capi import CbOption, CbVariable
+from mpgos_gb300.solver import Option, Variable
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+MODES = [capi.MODE_PLAIN, capi.MODE_CHOSEN, capi.MODE_DF_STAGE | capi.MODE_PERSISTENT]
+
+
+@pytest.mark.parametrize("mode", MODES)
+def test_no_active_instance_is_a_no_op(mode, native_libs):
+    case = W.lorenz_case(nt=256)
+    with W.load_solver(case, mode=mode) as s:
+        before = W.read_results(s)
+        s.SolverOption(Option.ActiveNumberOfThreads, 0)
+        s.Solve()
+        after = W.read_results(s)
+    for k in ("x", "t", "acci", "td"):
+        np.testing.assert_array_equal(before[k], after[k])
+
+
+def test_no_active_system_is_a_no_op(native_libs):
+    case = CW.ring_case("ring16_full", ns=32, periods=1)
+    with CW.load_coupled_solver(case, mode=capi.MODE_PERSISTENT) as s:
+        before = CW.read_coupled_results(s)
+        s.SolverOption(CbOption.ActiveSystems, 0)
+        s.Solve()
+        after = CW.read_coupled_results(s)
+    for k in ("x", "t", "iuacc", "isacc"):
+        np.testing.assert_array_equal(before[k], after[k])
+
+
+@pytest.mark.parametrize("mode", MODES)
+def test_single_instance_ensemble(mode, native_libs, oracle_libs):
+    case = W.lorenz_case(nt=1, rho=(10.0, 10.0))
+    res = W.run_gpu(case, mode=mode, block=32)
+    ref = O.run_oracle(case)
+    assert res["status"][0] == 0 and res["t"][0] == 10.0
+    assert np.max(np.abs(res["x"] - ref["x"]) / np.abs(ref["x"])) < 1e-9
+    assert abs(int(res["nacc"][0]) - int(ref["nacc"][0])) <= 1
+
+
+@pytest.mark.parametrize("mode", MODES)
+def test_empty_time_domain(mode, native_libs, oracle_libs):
+    case = W.lorenz_case(nt=64)
+    case.arrays["td"][1] = case.arrays["td"][0]
+    res = W.run_gpu(case, mode=mode)
+    ref = O.run_oracle(case)
+    np.testing.assert_array_equal(res["x"], case.arrays["x"])
+    np.testing.assert_array_equal(res["t"], case.arrays["td"][0])
+    np.testing.assert_array_equal(res["nacc"], ref["nacc"])
+    assert np.all(res["status"] == 0)
