@@ -1,7 +1,8 @@
 """Edge cases of the launch: no active instance or system (Solve is a
 no-op), a one-instance ensemble, and an empty time domain (t0 == t1): the
-reference's loop takes one accepted step of size 0 and stops, leaving the
-state unchanged, in every mode."""
+reference's loop takes one accepted step of size 0 (below the minimum step:
+accepted with the minimum-step warning, which the oracle reports too) and
+stops, leaving the state unchanged, in every mode."""
 import numpy as np
 import pytest
 
@@ -57,4 +58,5 @@ def test_empty_time_domain(mode, native_libs, oracle_libs):
     np.testing.assert_array_equal(res["x"], case.arrays["x"])
     np.testing.assert_array_equal(res["t"], case.arrays["td"][0])
     np.testing.assert_array_equal(res["nacc"], ref["nacc"])
-    assert np.all(res["status"] == 0)
+    np.testing.assert_array_equal(res["status"], ref["status"])
+    assert np.all(res["status"] == capi.INSTANCE_MINIMUM_STEP)
