@@ -77,6 +77,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--no-coupled", action="store_true", help="skip the coupled-configuration leg")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint-configuration leg")
+    ap.add_argument("--no-uneven", action="store_true", help="skip the uneven (Keller-Miksis) leg")
     return ap.parse_args()
 
 
@@ -373,6 +374,75 @@ def adjoint_leg(local: int, flush) -> dict:
     return out
 
 
+def uneven_leg(local: int, flush) -> dict:
+    """Uneven configuration at reduced size: Keller-Miksis bubbles on a
+    256 x 256 grid of driving amplitude x frequency (2^16 instances; the
+    configuration's 512 x 512 grid and 1024 periods scaled down to keep the
+    bench short), RKCK45 1e-10, 4 acoustic periods as 4 phases captured in
+    one CUDA graph, the per-period maximum radius streamed out after every
+    phase. Step counts per instance differ by two orders of magnitude. Times
+    the static and persistent mappings of the FP64 (FAST_CONTROL) and
+    double-float forms and the reference's kernel (sm_103a cubin, event
+    options fixed, one launch per period) on the same inputs; checks PLAIN
+    against the reference kernel bit for bit."""
+    import torch
+    from mpgos_gb300 import capi, workloads as W
+    from mpgos_gb300.solver import Variable
+    from oracle import ref_gpu as R
+    case = W.keller_miksis_case(n_amp=256, n_freq=256, periods=4)
+    nt, phases = case.nt, case.phases
+    out = {"workload": "keller_miksis_256x256_rkck45_tol1e-10_4periods", "unit": "accepted instance-steps/s",
+           "phases": phases}
+    per_phase = torch.empty((phases, nt), dtype=torch.float64, device=f"cuda:{local}")
+
+    def run(mode, block=128, reference=False):
+        with W.load_solver(case, mode=mode, block=block, device=local) as s:
+            s.checkpoint_save()
+            kern = None
+            if reference:
+                kern = R.ReferenceKernel("keller_miksis", 1, nt, 0)
+                kern.bind(s, case, block=32)
+            times = []
+            for i in range(3):
+                flush_l2(flush)
+                torch.cuda.synchronize()
+                s.checkpoint_restore()
+                s.timer_start()
+                if reference:
+                    for _ in range(phases):
+                        kern.launch()
+                else:
+                    s.SolvePhases(phases, 0, per_phase.data_ptr())
+                ms = s.timer_stop()
+                if i:
+                    times.append(ms)
+            res = W.read_results(s)
+            if kern is not None:
+                kern.close()
+        steps = float(res["acci"][0].sum())  # accepted steps, counted by the system's own hook
+        return {"ms": statistics.median(times), "value": steps / (statistics.median(times) / 1e3)}, res
+
+    FAST, DF, P = capi.MODE_FAST_CONTROL, capi.MODE_DF_STAGE, capi.MODE_PERSISTENT
+    forms = {"fp64_static": FAST, "fp64_persistent": FAST | P, "df_static": DF, "df_persistent": DF | P}
+    results = {}
+    for name, mode in forms.items():
+        out[name], results[name] = run(mode)
+    plain, rplain = run(capi.MODE_PLAIN)
+    out["plain"] = plain
+    n = results["fp64_static"]["nacc"]
+    out["steps_per_instance_min_max"] = [int(n.min()), int(n.max())]
+    out["persistent_over_static_fp64"] = out["fp64_static"]["ms"] / out["fp64_persistent"]["ms"]
+    out["persistent_over_static_df"] = out["df_static"]["ms"] / out["df_persistent"]["ms"]
+    if R.available("keller_miksis", 1, nt, 0):
+        ref, rref = run(capi.MODE_PLAIN, reference=True)
+        out["reference_gpu"] = ref
+        out["speedup_df_persistent_vs_reference_gpu"] = out["df_persistent"]["value"] / ref["value"]
+        out["plain_bitwise_equal_to_reference_kernel"] = bool(all(
+            np.array_equal(np.asarray(rplain[k]).view(np.uint8), np.asarray(rref[k]).view(np.uint8))
+            for k in ("x", "t", "acc", "acci")))
+    return out
+
+
 def coupled_leg(local: int, flush) -> dict:
     """Coupled configuration beside the headline: 16384 rings of 64 Duffing
     units (dense coupling, RKCK45 1e-9, crossing events), two forcing periods
@@ -616,6 +686,7 @@ def main():
     fp32_stage = summarize(f32_r)
     coupled = None if args.no_coupled else coupled_leg(local, flush)
     adjoint = None if args.no_adjoint else adjoint_leg(local, flush)
+    uneven = None if args.no_uneven else uneven_leg(local, flush)
     plain = ref_gpu = p = None
     parity = {}
     if not args.no_plain:
@@ -677,6 +748,7 @@ def main():
         "end_state_error_vs_fp64_oracle": errors,
         "coupled": coupled,
         "adjoint": adjoint,
+        "uneven": uneven,
         "plain": plain,
         "reference_gpu": ref_gpu,
         "speedup_vs_reference_gpu": (value / ref_gpu["value"]) if ref_gpu else None,

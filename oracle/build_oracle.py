@@ -196,7 +196,7 @@ def build_ref(system: str, force: bool = False) -> Path | None:
 # in which only that condition reads `ltid < NE`.
 REF_GPU_EVENT_FIX = {"keller_miksis"}
 REF_GPU_KERNELS = [
-    ("keller_miksis", 1, 64, 0), ("keller_miksis", 1, 256, 0),
+    ("keller_miksis", 1, 64, 0), ("keller_miksis", 1, 256, 0), ("keller_miksis", 1, 65536, 0),
     ("lorenz", 1, 256, 0), ("lorenz", 1, 1000, 0), ("lorenz", 0, 64, 0), ("lorenz", 1, 1 << 20, 0),
     ("duffing", 0, 64, 0), ("duffing", 0, 8192, 0),
     ("duffing_param", 1, 256, 0), ("duffing_param", 1, 1000, 0),
