@@ -421,18 +421,24 @@ __global__ void __launch_bounds__(MPGOS_MAX_BLOCK) perthread_df_kernel(Args<doub
 
     const long long total = static_cast<long long>(gridDim.x) * blockDim.x;
     long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    // one ballot over the integrating lanes per iteration reconverges the
+    // warp once per step attempt (as in perthread_kernel)
+    unsigned live = __ballot_sync(__activemask(), i < a.n_active);
     if (i >= a.n_active) return;
 
     typename Sv::Inst s;
     Sv::begin(s, i, a, g, o);
     while (true) {
+        bool stop = false;
         if (s.terminate) {
             Sv::end(s, a, g);
             i = Solver<S, MPGOS_RKCK45, double, MODE>::next_index(a, total, i);
-            if (i >= a.n_active) break;
-            Sv::begin(s, i, a, g, o);
+            if (i >= a.n_active) stop = true;
+            else Sv::begin(s, i, a, g, o);
         }
-        Sv::attempt(s, a, g, o);
+        if (!stop) Sv::attempt(s, a, g, o);
+        live = __ballot_sync(live, !stop);
+        if (stop) break;
     }
 }
 

@@ -383,18 +383,26 @@ __global__ void __launch_bounds__(MPGOS_MAX_BLOCK) perthread_kernel(Args<P> a)
 
     const long long total = static_cast<long long>(gridDim.x) * blockDim.x;
     long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    // Lanes of this warp that integrate; every iteration ends with a ballot
+    // over them, which reconverges the warp once per step attempt (divergent
+    // accept/reject, event and end-of-instance paths would otherwise leave
+    // lanes running the next attempt's stages in separate groups).
+    unsigned live = __ballot_sync(__activemask(), i < a.n_active);
     if (i >= a.n_active) return;
 
     typename Sv::Inst s;
     Sv::begin(s, i, a, g, cpf, accf);
     while (true) {
+        bool stop = false;
         if (s.terminate) {
             Sv::end(s, a, g);
             i = Sv::next_index(a, total, i);
-            if (i >= a.n_active) break;
-            Sv::begin(s, i, a, g, cpf, accf);
+            if (i >= a.n_active) stop = true;
+            else Sv::begin(s, i, a, g, cpf, accf);
         }
-        Sv::attempt(s, a, g, cpf, s_spf, accf);
+        if (!stop) Sv::attempt(s, a, g, cpf, s_spf, accf);
+        live = __ballot_sync(live, !stop);
+        if (stop) break;
     }
 }
 
