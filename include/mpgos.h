@@ -87,7 +87,11 @@ enum mpgos_option {
     /* extensions */
     MPGOS_KERNEL_MODE                  = 32, /* MPGOS_MODE_* bit set             */
     MPGOS_MAXIMUM_ATTEMPTS             = 33, /* step attempts per instance and launch */
-    MPGOS_INSTANCES_PER_THREAD         = 34  /* static mapping: instances each lane integrates in turn (grid stride) */
+    MPGOS_INSTANCES_PER_THREAD         = 34, /* static mapping: instances each lane integrates in turn (grid stride) */
+    MPGOS_WARP_RECONVERGE              = 35  /* 1: the integrating lanes of a warp reconverge once per step attempt
+                                                (a warp ballot; pays where lanes diverge: events, uneven
+                                                accept/reject); 0: leave it to the compiler. Default 1 for
+                                                systems with events, else 0; the autotuner tries both. */
 };
 
 /* ---- kernel modes (extensions) -----------------------------------------
@@ -172,6 +176,7 @@ typedef struct mpgos_pt_launch {
     int32_t*       accepted_steps;  /* [NT] or NULL */
     int32_t*       rejected_steps;  /* [NT] or NULL */
     uint32_t*      work_counter;    /* PERSISTENT: one zeroed counter */
+    int32_t        reconverge;      /* MPGOS_WARP_RECONVERGE */
 } mpgos_pt_launch;
 
 /* Adjoint tape (extension): frozen step sizes and state checkpoints of a
@@ -269,7 +274,8 @@ int mpgos_pt_timer_stop(mpgos_pt_solver* solver, float* milliseconds);
 /* Autotuner (extension): times one Solve() per candidate (block size x
  * mapping: static with 1, 2 or 4 instances per thread, or persistent x
  * placement of the shared parameters: shared memory or global loads, where the
- * system has any) on a scratch copy of the current device state,
+ * system has any; then the warp reconvergence ballot on and off at the best
+ * of those) on a scratch copy of the current device state,
  * restores the state, keeps the fastest configuration and, if cache_path is
  * not NULL, records it in a JSON cache keyed by system, shape, NT and GPU.
  * `arithmetic` fixes the arithmetic the candidates share: 0 the reference's,

@@ -38,6 +38,7 @@ struct DfOptions {
     float grow, shrink;
     int ndo, dense_freq;
     long long max_attempts;
+    int reconverge;
 };
 
 template <class S>
@@ -418,6 +419,7 @@ __global__ void __launch_bounds__(MPGOS_MAX_BLOCK) perthread_df_kernel(Args<doub
     o.ndo          = a.o.ndo;
     o.dense_freq   = a.o.dense_freq;
     o.max_attempts = a.o.max_attempts;
+    o.reconverge   = a.o.reconverge;
 
     const long long total = static_cast<long long>(gridDim.x) * blockDim.x;
     long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -437,7 +439,7 @@ __global__ void __launch_bounds__(MPGOS_MAX_BLOCK) perthread_df_kernel(Args<doub
             else Sv::begin(s, i, a, g, o);
         }
         if (!stop) Sv::attempt(s, a, g, o);
-        live = __ballot_sync(live, !stop);
+        if (o.reconverge) live = __ballot_sync(live, !stop);
         if (stop) break;
     }
 }

@@ -383,10 +383,11 @@ __global__ void __launch_bounds__(MPGOS_MAX_BLOCK) perthread_kernel(Args<P> a)
 
     const long long total = static_cast<long long>(gridDim.x) * blockDim.x;
     long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
-    // Lanes of this warp that integrate; every iteration ends with a ballot
-    // over them, which reconverges the warp once per step attempt (divergent
-    // accept/reject, event and end-of-instance paths would otherwise leave
-    // lanes running the next attempt's stages in separate groups).
+    // Lanes of this warp that integrate. With reconverge set, every
+    // iteration ends with a ballot over them, which reconverges the warp once
+    // per step attempt (divergent accept/reject, event and end-of-instance
+    // paths can otherwise leave lanes running the next attempt's stages in
+    // separate groups); without it the compiler's reconvergence stands.
     unsigned live = __ballot_sync(__activemask(), i < a.n_active);
     if (i >= a.n_active) return;
 
@@ -401,7 +402,7 @@ __global__ void __launch_bounds__(MPGOS_MAX_BLOCK) perthread_kernel(Args<P> a)
             else Sv::begin(s, i, a, g, cpf, accf);
         }
         if (!stop) Sv::attempt(s, a, g, cpf, s_spf, accf);
-        live = __ballot_sync(live, !stop);
+        if (a.o.reconverge) live = __ballot_sync(live, !stop);
         if (stop) break;
     }
 }
@@ -453,6 +454,7 @@ Args<P> make_args(const mpgos_pt_launch& L)
     a.o.dense_freq   = L.dense_save_frequency;
     a.o.ndo          = L.ndo;
     a.o.max_attempts = L.max_attempts;
+    a.o.reconverge = L.reconverge;
     return a;
 }
 

@@ -45,6 +45,7 @@ struct Options {
     int dense_freq;
     int ndo;
     long long max_attempts;
+    int reconverge;        // per-thread kernels: warp ballot once per step attempt
 };
 
 // ---------------------------------------------------------------------------

@@ -113,6 +113,7 @@ struct mpgos_pt_solver {
     int32_t dense_freq = 1;
     int32_t prefer_shared = 1;
     int32_t ipt = 1;  // instances per thread of the static mapping
+    int32_t reconverge = -1;  // MPGOS_WARP_RECONVERGE; -1: by the system (events: 1)
     int32_t mode = MPGOS_MODE_PLAIN;
     int64_t max_attempts = 10000000;
     uint64_t generation = 1;  // bumped by every change that alters a launch
@@ -208,6 +209,7 @@ void fill_launch(const mpgos_pt_solver* s, mpgos_pt_launch& L, int32_t mode)
     L.accepted_steps            = static_cast<int32_t*>(s->var[MPGOS_ACCEPTED_STEPS].device);
     L.rejected_steps            = static_cast<int32_t*>(s->var[MPGOS_REJECTED_STEPS].device);
     L.work_counter              = s->d_work;
+    L.reconverge                = s->reconverge >= 0 ? s->reconverge : (s->shape.ne > 0 ? 1 : 0);
 }
 
 size_t dynamic_smem(const mpgos_pt_solver* s)
@@ -520,6 +522,10 @@ MPGOS_EXPORT int mpgos_pt_set_option(mpgos_pt_solver* s, int32_t option, int32_t
             s->ipt = n;
             break;
         }
+        case MPGOS_WARP_RECONVERGE:
+            if (value != 0.0 && value != 1.0) return fail(MPGOS_ERR_ARGUMENT, "WarpReconverge %g must be 0 or 1", value);
+            s->reconverge = static_cast<int32_t>(value);
+            break;
         default:
             return fail(MPGOS_ERR_ARGUMENT, "unknown solver option %d", option);
     }
@@ -559,6 +565,7 @@ MPGOS_EXPORT int mpgos_pt_get_option(const mpgos_pt_solver* s, int32_t option, i
         case MPGOS_KERNEL_MODE: *value = s->mode; break;
         case MPGOS_MAXIMUM_ATTEMPTS: *value = (double)s->max_attempts; break;
         case MPGOS_INSTANCES_PER_THREAD: *value = s->ipt; break;
+        case MPGOS_WARP_RECONVERGE: *value = s->reconverge >= 0 ? s->reconverge : (s->shape.ne > 0 ? 1 : 0); break;
         default: return fail(MPGOS_ERR_ARGUMENT, "unknown solver option %d", option);
     }
     return MPGOS_OK;
@@ -789,19 +796,22 @@ MPGOS_EXPORT int mpgos_pt_autotune(mpgos_pt_solver* s, int32_t arithmetic, const
             const std::string tag = "\"" + json_escape(k) + "\"";
             size_t pos = line.find(tag);
             if (pos == std::string::npos) continue;
-            int b = 0, m = 0, n = 1, ps = s->prefer_shared;
+            int b = 0, m = 0, n = 1, ps = s->prefer_shared, rv = s->reconverge;
             const char* bp = std::strstr(line.c_str() + pos, "\"block\":");
             const char* mp = std::strstr(line.c_str() + pos, "\"mode\":");
             const char* np = std::strstr(line.c_str() + pos, "\"instances_per_thread\":");
             const char* pp = std::strstr(line.c_str() + pos, "\"prefer_shared\":");
+            const char* rp = std::strstr(line.c_str() + pos, "\"reconverge\":");
             if (np) sscanf(np, "\"instances_per_thread\": %d", &n);
             if (pp) sscanf(pp, "\"prefer_shared\": %d", &ps);
+            if (rp) sscanf(rp, "\"reconverge\": %d", &rv);
             if (bp && mp && sscanf(bp, "\"block\": %d", &b) == 1 && sscanf(mp, "\"mode\": %d", &m) == 1 && b >= 1 &&
                 b <= 256 && n >= 1 && n <= 64) {
                 s->block = b;
                 s->mode = m;
                 s->ipt = n;
                 s->prefer_shared = ps ? 1 : 0;
+                s->reconverge = (rv == 0 || rv == 1) ? rv : -1;
                 s->generation++;
                 return MPGOS_OK;
             }
@@ -874,6 +884,29 @@ MPGOS_EXPORT int mpgos_pt_autotune(mpgos_pt_solver* s, int32_t arithmetic, const
         }
         if (rc) break;
     }
+    // the warp reconvergence ballot, on and off, at the best configuration
+    const int keep_rv = s->reconverge;
+    const int cur_rv = keep_rv >= 0 ? keep_rv : (s->shape.ne > 0 ? 1 : 0);
+    int best_rv = cur_rv;
+    if (!rc) {
+        s->ipt = best_ipt;
+        s->prefer_shared = best_ps;
+        s->reconverge = 1 - cur_rv;
+        if (!(rc = restore())) {
+            MPGOS_CUDA(cudaEventRecord(s->timer_begin, s->stream));
+            if (!(rc = enqueue_solve(s, best_mode, best_block))) {
+                MPGOS_CUDA(cudaEventRecord(s->timer_end, s->stream));
+                MPGOS_CUDA(cudaEventSynchronize(s->timer_end));
+                float t = 0.f;
+                MPGOS_CUDA(cudaEventElapsedTime(&t, s->timer_begin, s->timer_end));
+                if (t < best) {
+                    best = t;
+                    best_rv = 1 - cur_rv;
+                }
+            }
+        }
+    }
+    s->reconverge = keep_rv;
     s->ipt = keep_ipt;
     s->prefer_shared = keep_ps;
     if (rc) {
@@ -890,13 +923,14 @@ MPGOS_EXPORT int mpgos_pt_autotune(mpgos_pt_solver* s, int32_t arithmetic, const
     s->mode = best_mode;
     s->ipt = best_ipt;
     s->prefer_shared = best_ps;
+    s->reconverge = best_rv;
     s->generation++;
 
     if (cache_path != nullptr) {
         std::ofstream outf(cache_path, std::ios::app);
         if (outf) outf << "{\"" << json_escape(k) << "\": {\"block\": " << best_block << ", \"mode\": " << best_mode
                        << ", \"instances_per_thread\": " << best_ipt << ", \"prefer_shared\": " << best_ps
-                       << ", \"ms\": " << best << "}}\n";
+                       << ", \"reconverge\": " << best_rv << ", \"ms\": " << best << "}}\n";
     }
     return MPGOS_OK;
 }

@@ -64,6 +64,7 @@ class Option(IntEnum):
     KernelMode = 32
     MaximumAttempts = 33
     InstancesPerThread = 34
+    WarpReconverge = 35
 
 
 MODE_PLAIN = 0

@@ -365,3 +365,21 @@ def test_autotuner_explores_mapping_and_placement(native_libs, tmp_path):
             s.Solve()
         tuned = W.read_results(s)
     assert_bitwise(res, tuned)
+
+
+def test_warp_reconvergence_is_scheduling_only(native_libs):
+    """The per-attempt warp ballot only changes how lanes are scheduled:
+    results are bit-identical with it on and off (events make lanes diverge
+    on this system, so both code paths run divergent warps)."""
+    from mpgos_gb300.capi import Option
+    case = W.keller_miksis_case(n_amp=8, n_freq=16, periods=2)
+    for mode in (capi.MODE_PLAIN, capi.MODE_CHOSEN, capi.MODE_DF_STAGE | capi.MODE_PERSISTENT):
+        out = []
+        for rv in (0, 1):
+            with W.load_solver(case, mode=mode, block=64) as s:
+                s.SolverOption(Option.WarpReconverge, rv)
+                assert int(s.GetOption(Option.WarpReconverge)) == rv
+                for _ in range(case.phases):
+                    s.Solve()
+                out.append(W.read_results(s))
+        assert_bitwise(out[0], out[1])
