@@ -176,7 +176,6 @@ typedef struct mpgos_pt_launch {
     int32_t*       accepted_steps;  /* [NT] or NULL */
     int32_t*       rejected_steps;  /* [NT] or NULL */
     uint32_t*      work_counter;    /* PERSISTENT: one zeroed counter */
-    int32_t        reconverge;      /* MPGOS_WARP_RECONVERGE */
 } mpgos_pt_launch;
 
 /* Adjoint tape (extension): frozen step sizes and state checkpoints of a

@@ -38,7 +38,6 @@ struct DfOptions {
     float grow, shrink;
     int ndo, dense_freq;
     long long max_attempts;
-    int reconverge;
 };
 
 template <class S>
@@ -419,28 +418,42 @@ __global__ void __launch_bounds__(MPGOS_MAX_BLOCK) perthread_df_kernel(Args<doub
     o.ndo          = a.o.ndo;
     o.dense_freq   = a.o.dense_freq;
     o.max_attempts = a.o.max_attempts;
-    o.reconverge   = a.o.reconverge;
 
     const long long total = static_cast<long long>(gridDim.x) * blockDim.x;
     long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
-    // one ballot over the integrating lanes per iteration reconverges the
-    // warp once per step attempt (as in perthread_kernel)
-    unsigned live = __ballot_sync(__activemask(), i < a.n_active);
-    if (i >= a.n_active) return;
-
-    typename Sv::Inst s;
-    Sv::begin(s, i, a, g, o);
-    while (true) {
-        bool stop = false;
-        if (s.terminate) {
-            Sv::end(s, a, g);
-            i = Solver<S, MPGOS_RKCK45, double, MODE>::next_index(a, total, i);
-            if (i >= a.n_active) stop = true;
-            else Sv::begin(s, i, a, g, o);
+    using Next = Solver<S, MPGOS_RKCK45, double, MODE & ~MODE_RECONVERGE>;
+    if constexpr ((MODE & MODE_RECONVERGE) != 0) {
+        // one ballot over the integrating lanes per iteration reconverges the
+        // warp once per step attempt (as in perthread_kernel)
+        unsigned live = __ballot_sync(__activemask(), i < a.n_active);
+        if (i >= a.n_active) return;
+        typename Sv::Inst s;
+        Sv::begin(s, i, a, g, o);
+        while (true) {
+            bool stop = false;
+            if (s.terminate) {
+                Sv::end(s, a, g);
+                i = Next::next_index(a, total, i);
+                if (i >= a.n_active) stop = true;
+                else Sv::begin(s, i, a, g, o);
+            }
+            if (!stop) Sv::attempt(s, a, g, o);
+            live = __ballot_sync(live, !stop);
+            if (stop) break;
         }
-        if (!stop) Sv::attempt(s, a, g, o);
-        if (o.reconverge) live = __ballot_sync(live, !stop);
-        if (stop) break;
+    } else {
+        if (i >= a.n_active) return;
+        typename Sv::Inst s;
+        Sv::begin(s, i, a, g, o);
+        while (true) {
+            if (s.terminate) {
+                Sv::end(s, a, g);
+                i = Next::next_index(a, total, i);
+                if (i >= a.n_active) break;
+                Sv::begin(s, i, a, g, o);
+            }
+            Sv::attempt(s, a, g, o);
+        }
     }
 }
 

@@ -383,27 +383,41 @@ __global__ void __launch_bounds__(MPGOS_MAX_BLOCK) perthread_kernel(Args<P> a)
 
     const long long total = static_cast<long long>(gridDim.x) * blockDim.x;
     long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
-    // Lanes of this warp that integrate. With reconverge set, every
-    // iteration ends with a ballot over them, which reconverges the warp once
-    // per step attempt (divergent accept/reject, event and end-of-instance
-    // paths can otherwise leave lanes running the next attempt's stages in
-    // separate groups); without it the compiler's reconvergence stands.
-    unsigned live = __ballot_sync(__activemask(), i < a.n_active);
-    if (i >= a.n_active) return;
-
-    typename Sv::Inst s;
-    Sv::begin(s, i, a, g, cpf, accf);
-    while (true) {
-        bool stop = false;
-        if (s.terminate) {
-            Sv::end(s, a, g);
-            i = Sv::next_index(a, total, i);
-            if (i >= a.n_active) stop = true;
-            else Sv::begin(s, i, a, g, cpf, accf);
+    if constexpr ((MODE & MODE_RECONVERGE) != 0) {
+        // Lanes of this warp that integrate; every iteration ends with a
+        // ballot over them, which reconverges the warp once per step attempt
+        // (divergent accept/reject, event and end-of-instance paths can
+        // otherwise leave lanes running the next attempt's stages in
+        // separate groups).
+        unsigned live = __ballot_sync(__activemask(), i < a.n_active);
+        if (i >= a.n_active) return;
+        typename Sv::Inst s;
+        Sv::begin(s, i, a, g, cpf, accf);
+        while (true) {
+            bool stop = false;
+            if (s.terminate) {
+                Sv::end(s, a, g);
+                i = Sv::next_index(a, total, i);
+                if (i >= a.n_active) stop = true;
+                else Sv::begin(s, i, a, g, cpf, accf);
+            }
+            if (!stop) Sv::attempt(s, a, g, cpf, s_spf, accf);
+            live = __ballot_sync(live, !stop);
+            if (stop) break;
         }
-        if (!stop) Sv::attempt(s, a, g, cpf, s_spf, accf);
-        if (a.o.reconverge) live = __ballot_sync(live, !stop);
-        if (stop) break;
+    } else {
+        if (i >= a.n_active) return;
+        typename Sv::Inst s;
+        Sv::begin(s, i, a, g, cpf, accf);
+        while (true) {
+            if (s.terminate) {
+                Sv::end(s, a, g);
+                i = Sv::next_index(a, total, i);
+                if (i >= a.n_active) break;
+                Sv::begin(s, i, a, g, cpf, accf);
+            }
+            Sv::attempt(s, a, g, cpf, s_spf, accf);
+        }
     }
 }
 
@@ -454,7 +468,6 @@ Args<P> make_args(const mpgos_pt_launch& L)
     a.o.dense_freq   = L.dense_save_frequency;
     a.o.ndo          = L.ndo;
     a.o.max_attempts = L.max_attempts;
-    a.o.reconverge = L.reconverge;
     return a;
 }
 
@@ -478,9 +491,11 @@ struct KernelTable {
         MPGOS_MODE_PERSISTENT |
         (DOUBLE_ADAPTIVE ? (MPGOS_MODE_FAST_CONTROL | MPGOS_MODE_FP32_STAGE | MPGOS_MODE_DF_STAGE) : 0);
 
-    // Modes a table can run; the runtime only asks for these.
+    // Modes a table can run; the runtime only asks for these. MODE_RECONVERGE
+    // selects the twin of each kernel with the per-attempt warp ballot.
     static void* kernel_for(int mode)
     {
+        if (mode & MODE_RECONVERGE) return kernel_for_rc(mode & ~MODE_RECONVERGE);
         switch (mode) {
             case 0: return reinterpret_cast<void*>(&perthread_kernel<S, ALG, P, 0>);
             case 2: return reinterpret_cast<void*>(&perthread_kernel<S, ALG, P, 2>);
@@ -496,6 +511,31 @@ struct KernelTable {
                 case MPGOS_MODE_DF_STAGE | MPGOS_MODE_PERSISTENT:
                     return reinterpret_cast<void*>(
                         &perthread_df_kernel<S, MPGOS_MODE_DF_STAGE | MPGOS_MODE_PERSISTENT>);
+                default: break;
+            }
+        }
+        return nullptr;
+    }
+
+    static void* kernel_for_rc(int mode)
+    {
+        constexpr int R = MODE_RECONVERGE;
+        switch (mode) {
+            case 0: return reinterpret_cast<void*>(&perthread_kernel<S, ALG, P, R>);
+            case 2: return reinterpret_cast<void*>(&perthread_kernel<S, ALG, P, R | 2>);
+            default: break;
+        }
+        if constexpr (DOUBLE_ADAPTIVE) {
+            switch (mode) {
+                case 1: return reinterpret_cast<void*>(&perthread_kernel<S, ALG, P, R | 1>);
+                case 3: return reinterpret_cast<void*>(&perthread_kernel<S, ALG, P, R | 3>);
+                case 5: return reinterpret_cast<void*>(&perthread_kernel<S, ALG, P, R | 5>);
+                case 7: return reinterpret_cast<void*>(&perthread_kernel<S, ALG, P, R | 7>);
+                case MPGOS_MODE_DF_STAGE:
+                    return reinterpret_cast<void*>(&perthread_df_kernel<S, R | MPGOS_MODE_DF_STAGE>);
+                case MPGOS_MODE_DF_STAGE | MPGOS_MODE_PERSISTENT:
+                    return reinterpret_cast<void*>(
+                        &perthread_df_kernel<S, R | MPGOS_MODE_DF_STAGE | MPGOS_MODE_PERSISTENT>);
                 default: break;
             }
         }

@@ -35,6 +35,9 @@ struct Tape {
 
 // Kernel-internal mode bit: the forward launch records the adjoint tape.
 constexpr int MODE_RECORD = 8;
+// Internal mode bit of the per-thread kernels (MPGOS_WARP_RECONVERGE): the
+// integrating lanes of a warp reconverge once per step attempt.
+constexpr int MODE_RECONVERGE = 32;
 
 // Solver options in the kernel's precision (Struct_SolverOptions of
 // SingleSystem_PerThread_Interface.cuh:105-115 plus the extensions).
@@ -45,7 +48,6 @@ struct Options {
     int dense_freq;
     int ndo;
     long long max_attempts;
-    int reconverge;        // per-thread kernels: warp ballot once per step attempt
 };
 
 // ---------------------------------------------------------------------------

@@ -209,7 +209,6 @@ void fill_launch(const mpgos_pt_solver* s, mpgos_pt_launch& L, int32_t mode)
     L.accepted_steps            = static_cast<int32_t*>(s->var[MPGOS_ACCEPTED_STEPS].device);
     L.rejected_steps            = static_cast<int32_t*>(s->var[MPGOS_REJECTED_STEPS].device);
     L.work_counter              = s->d_work;
-    L.reconverge                = s->reconverge >= 0 ? s->reconverge : (s->shape.ne > 0 ? 1 : 0);
 }
 
 size_t dynamic_smem(const mpgos_pt_solver* s)
@@ -217,12 +216,17 @@ size_t dynamic_smem(const mpgos_pt_solver* s)
     return prec(s) * static_cast<size_t>(s->shape.nsp) + sizeof(int32_t) * static_cast<size_t>(s->shape.nisp);
 }
 
+// Bit 32 of a launch mode selects the kernels with the per-attempt warp
+// ballot (MPGOS_WARP_RECONVERGE; plugin side: MODE_RECONVERGE).
+constexpr int32_t kModeReconverge = 32;
+
 int32_t effective_mode(const mpgos_pt_solver* s, int32_t mode)
 {
     int32_t m = mode & (s->shape.modes | MPGOS_MODE_PERSISTENT);
-    if (m & MPGOS_MODE_DF_STAGE) return MPGOS_MODE_DF_STAGE | (m & MPGOS_MODE_PERSISTENT);
-    if (m & MPGOS_MODE_FP32_STAGE) m |= MPGOS_MODE_FAST_CONTROL;  // compiled together
-    return m;
+    if (m & MPGOS_MODE_DF_STAGE) m = MPGOS_MODE_DF_STAGE | (m & MPGOS_MODE_PERSISTENT);
+    else if (m & MPGOS_MODE_FP32_STAGE) m |= MPGOS_MODE_FAST_CONTROL;  // compiled together
+    const bool rc = s->reconverge >= 0 ? s->reconverge != 0 : s->shape.ne > 0;
+    return rc ? (m | kModeReconverge) : m;
 }
 
 int grid_for(const mpgos_pt_solver* s, int32_t mode, int block, int* grid)
