@@ -227,6 +227,40 @@ __device__ __forceinline__ void dual_axpy(ad::Dual<N, T>& y, T a, const ad::Dual
 #pragma unroll
     for (int q = 0; q < N; q++) y.d[q] = ad::mad(a, x.d[q], y.d[q]);
 }
+// x + sum_j h_j K_j for double-float duals, every component accumulated as
+// an unnormalised product sum (df::prod_sum, 12 FP32 operations per term)
+// and normalised once.
+template <int N>
+struct DualSum {
+    df::prod_sum v;
+    df::prod_sum d[N];
+};
+template <int N>
+__device__ __forceinline__ DualSum<N> dual_sum_from(const ad::Dual<N, dfloat>& x)
+{
+    DualSum<N> s;
+    s.v = df::prod_sum{x.v.hi, x.v.lo};
+#pragma unroll
+    for (int q = 0; q < N; q++) s.d[q] = df::prod_sum{x.d[q].hi, x.d[q].lo};
+    return s;
+}
+template <int N>
+__device__ __forceinline__ void dual_sum_add(DualSum<N>& s, dfloat h, const ad::Dual<N, dfloat>& k)
+{
+    df::prod_sum_add(s.v, h, k.v);
+#pragma unroll
+    for (int q = 0; q < N; q++) df::prod_sum_add(s.d[q], h, k.d[q]);
+}
+template <int N>
+__device__ __forceinline__ ad::Dual<N, dfloat> dual_sum_value(const DualSum<N>& s)
+{
+    ad::Dual<N, dfloat> r;
+    r.v = df::prod_sum_value(s.v);
+#pragma unroll
+    for (int q = 0; q < N; q++) r.d[q] = df::prod_sum_value(s.d[q]);
+    return r;
+}
+
 // One Runge-Kutta step with frozen dt carried out entirely in dual numbers:
 // x holds the state and its tangents d x / d (segment start state, control
 // parameters); on return, the state and tangents one step later.
@@ -235,29 +269,52 @@ __device__ __forceinline__ void tangent_step(const TableauT<T, ST>& tb, int ti, 
                                              D* spd, int* spi, D* accd, int* acci)
 {
     // stage sums with the step folded into the coefficients: X_st = x + sum_j (dt a_st,j) K_j
+    constexpr bool DF = std::is_same<T, dfloat>::value;
     D K[ST][SD];
 #pragma unroll
     for (int st = 0; st < ST; st++) {
         D Xd[SD];
+        if constexpr (DF) {
 #pragma unroll
-        for (int d = 0; d < SD; d++) Xd[d] = x[d];
+            for (int d = 0; d < SD; d++) {
+                DualSum<N> acc = dual_sum_from(x[d]);
 #pragma unroll
-        for (int j = 0; j < st; j++) {
-            if (TB::a(st, j) != 0.0) {
-                const T h = dt * tab_a<TB>(tb, st, j);
+                for (int j = 0; j < st; j++)
+                    if (TB::a(st, j) != 0.0) dual_sum_add(acc, dt * tab_a<TB>(tb, st, j), K[j][d]);
+                Xd[d] = dual_sum_value(acc);
+            }
+        } else {
 #pragma unroll
-                for (int d = 0; d < SD; d++) dual_axpy(Xd[d], h, K[j][d]);
+            for (int d = 0; d < SD; d++) Xd[d] = x[d];
+#pragma unroll
+            for (int j = 0; j < st; j++) {
+                if (TB::a(st, j) != 0.0) {
+                    const T h = dt * tab_a<TB>(tb, st, j);
+#pragma unroll
+                    for (int d = 0; d < SD; d++) dual_axpy(Xd[d], h, K[j][d]);
+                }
             }
         }
         const D Td(ad::mad(tab_c<TB>(tb, st), dt, t));
         PerThread_OdeFunction(ti, nti, K[st], Xd, Td, cpd, spd, spi, accd, acci);
     }
+    if constexpr (DF) {
 #pragma unroll
-    for (int st = 0; st < ST; st++) {
-        if (TB::b(st) != 0.0) {
-            const T h = dt * tab_b<TB>(tb, st);
+        for (int d = 0; d < SD; d++) {
+            DualSum<N> acc = dual_sum_from(x[d]);
 #pragma unroll
-            for (int d = 0; d < SD; d++) dual_axpy(x[d], h, K[st][d]);
+            for (int st = 0; st < ST; st++)
+                if (TB::b(st) != 0.0) dual_sum_add(acc, dt * tab_b<TB>(tb, st), K[st][d]);
+            x[d] = dual_sum_value(acc);
+        }
+    } else {
+#pragma unroll
+        for (int st = 0; st < ST; st++) {
+            if (TB::b(st) != 0.0) {
+                const T h = dt * tab_b<TB>(tb, st);
+#pragma unroll
+                for (int d = 0; d < SD; d++) dual_axpy(x[d], h, K[st][d]);
+            }
         }
     }
 }
