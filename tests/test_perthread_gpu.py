@@ -383,3 +383,20 @@ def test_warp_reconvergence_is_scheduling_only(native_libs):
                     s.Solve()
                 out.append(W.read_results(s))
         assert_bitwise(out[0], out[1])
+
+
+def test_config1_duffing_rk4_full_size(native_libs):
+    """The plain small configuration at full size: forced Duffing, 8192
+    instances, fixed-step RK4 with dt = 2 pi / 400 over 1024 forcing periods
+    (1024 phases replayed from one CUDA graph), running maximum of x as an
+    accessory. PLAIN (and the persistent mapping) are bit-identical to the
+    reference's kernel launched once per period; every instance takes
+    1024 x 401 steps (400 plus the clamped end step of each period)."""
+    case = W.duffing_rk4_case(nt=8192, periods=1024)
+    if not R.available(case.system, case.algorithm, case.nt, case.ndo):
+        pytest.skip("reference cubin for Duffing RK4 at 8192 instances not built")
+    ref = R.run_ref_gpu(case)
+    for mode in (capi.MODE_PLAIN, capi.MODE_PERSISTENT):
+        res = W.run_gpu(case, mode=mode, graph=True)
+        assert_bitwise(res, ref, keys=["x", "t", "acc", "acci"])
+    assert np.all(res["acci"][0] == 1024 * 401)
