@@ -91,7 +91,8 @@ class Clocks:
     def __init__(self, device: int):
         self.device = device
         self.proc = None
-        self.path = REPO / "gpurun_out" / f"clocks_{os.getpid()}.csv"
+        import tempfile
+        self.path = Path(tempfile.gettempdir()) / f"mpgos_clocks_{os.getpid()}.csv"
 
     def __enter__(self):
         try:

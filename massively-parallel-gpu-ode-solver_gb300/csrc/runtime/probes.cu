@@ -1,5 +1,5 @@
 // FMA-throughput probe (mpgos_probe_fma_peak in mpgos.h): the measured FP64
-// and FP32 peaks the per-thread kernels are judged against.
+// and FP32 peaks the per-thread kernels are measured against.
 #include "mpgos.h"
 
 #include <cuda_runtime.h>

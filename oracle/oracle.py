@@ -1,7 +1,8 @@
 """Python front end of the CPU oracle (and of the pinned reference CPU build).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() and
-by bench.py's CPU-baseline leg, as the checker. The product never imports it.
+by bench.py's CPU-baseline leg, as the reference results to compare with. The
+product never imports it.
 
 ``run_oracle(case)`` integrates a ``mpgos_gb300.workloads.Case`` with the
 oracle (oracle_perthread.cpp), ``run_ref_cpu(case)`` with the reference's own

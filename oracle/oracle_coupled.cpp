@@ -1,6 +1,6 @@
 // CPU oracle of the coupled per-block ensemble solver.
 //
-// TEST INFRASTRUCTURE ONLY. This is the checker the GPU coupled kernels are
+// TEST INFRASTRUCTURE ONLY. This is the oracle the GPU coupled kernels are
 // compared against (tests, smoke test, the bench's CPU baseline); the product
 // never links or calls it.
 //

@@ -1,6 +1,6 @@
 // CPU oracle of the per-thread ensemble solver.
 //
-// TEST INFRASTRUCTURE ONLY. This is the checker the GPU kernels are compared
+// TEST INFRASTRUCTURE ONLY. This is the oracle the GPU kernels are compared
 // against (tests, smoke test, the bench's CPU baseline); the product never
 // links or calls it.
 //

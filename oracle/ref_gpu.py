@@ -1,6 +1,6 @@
 """Launch the reference's own per-thread kernel (sm_103a cubin) on the GPU.
 
-TEST INFRASTRUCTURE ONLY: the checker for bit-level parity of the GB300
+TEST INFRASTRUCTURE ONLY: the reference kernels for bit-level parity of the GB300
 kernels and the reference-kernel timing in bench.py. Never used by the
 product.
 

@@ -1,6 +1,6 @@
 """GPU parity tests of the per-thread solver (sm_103a kernels through the C-ABI).
 
-Bar (BASELINE the benchmark spec): against the reference's own CUDA solver built for
+Bar: against the reference's own CUDA solver built for
 sm_103a, event counts and integer accessories bit-exact and FP64 end states
 within 1e-9 relative. The PLAIN kernels meet it with margin: they are
 bit-identical to the reference kernel (oracle/_ref cubins, launched on the
