@@ -772,7 +772,7 @@ def main():
                      "frac": achieved / peak_fp32_ops if achieved else None, "traffic": traffic,
                      "thread_instructions_per_attempt": instr,
                      "instructions_source": "smsp__inst_executed x thread/inst per step attempt, ncu capture "
-                                            "(profiles/perthread_df_kernel_lorenz_2e18.md)",
+                                            "of the same kernel on 2^18 instances (profiles/roofline_traffic.json)",
                      "kernel_ms": kernel_s * 1e3,
                      "peak_source": "measured FFMA instruction rate (mpgos_probe_fma_peak, precision 4), same GPU, "
                                     "same run: the issue ceiling every instruction shares",
