@@ -60,3 +60,20 @@ def test_empty_time_domain(mode, native_libs, oracle_libs):
     np.testing.assert_array_equal(res["nacc"], ref["nacc"])
     np.testing.assert_array_equal(res["status"], ref["status"])
     assert np.all(res["status"] == capi.INSTANCE_MINIMUM_STEP)
+
+
+@pytest.mark.parametrize("mode", [0, capi.MODE_PERSISTENT, capi.MODE_DF_STAGE | capi.MODE_PERSISTENT])
+def test_coupled_single_system_and_empty_time_domain(mode, native_libs, oracle_libs):
+    """One coupled system (a warp integrates it alone) against the oracle, and
+    an empty time domain leaving every unit unchanged."""
+    case = CW.ring_case("ring16_full", ns=1, periods=1, seed=3)
+    res = CW.run_coupled_gpu(case, mode=mode, warps=1)
+    ref = O.run_oracle_coupled(case)
+    scale = np.max(np.abs(case.arrays["x"]), axis=1, keepdims=True)
+    assert np.all(np.abs(res["x"] - ref["x"]) <= 1e-9 * (np.abs(ref["x"]) + scale))
+    np.testing.assert_array_equal(res["iuacc"], ref["iuacc"])
+    empty = CW.ring_case("ring16_full", ns=8, periods=1, seed=4)
+    empty.arrays["td"][1] = empty.arrays["td"][0]
+    res = CW.run_coupled_gpu(empty, mode=mode, warps=2)
+    np.testing.assert_array_equal(res["x"], empty.arrays["x"])
+    np.testing.assert_array_equal(res["t"], empty.arrays["td"][0])
