@@ -663,9 +663,9 @@ struct Solver {
             if (!has(lane, j)) continue;
             const long long g = s * UPS + unit_of(lane, j);
 #pragma unroll
-            for (int d = 0; d < UD; d++) a.x[g + d * nu] = static_cast<SP>(u.x[j][d]);
+            for (int d = 0; d < UD; d++) a.x[g + d * nu] = stored(u.x[j][d], a.x[g + d * nu]);
 #pragma unroll
-            for (int k = 0; k < NUA; k++) a.uacc[g + k * nu] = static_cast<SP>(u.uacc[j][k]);
+            for (int k = 0; k < NUA; k++) a.uacc[g + k * nu] = stored(u.uacc[j][k], a.uacc[g + k * nu]);
 #pragma unroll
             for (int k = 0; k < NIUA; k++) a.iuacc[g + k * nu] = u.iuacc[j][k];
         }
@@ -682,9 +682,19 @@ struct Solver {
             if (a.n_rej) a.n_rej[s] = nrej;
             if constexpr (RECORD) a.tape.n_steps[s] = nacc;
         }
-        for (int k = lane; k < NSA; k += 32) a.sacc[s + k * ns] = static_cast<SP>(w.sacc[k]);
+        for (int k = lane; k < NSA; k += 32) a.sacc[s + k * ns] = stored(w.sacc[k], a.sacc[s + k * ns]);
         for (int k = lane; k < NISA; k += 32) a.isacc[s + k * ns] = w.isacc[k];
         __syncwarp();
+    }
+
+    // Value to write back over `orig`, the FP64 value the launch loaded: in
+    // DF_STAGE `orig` itself while the double-float still equals its
+    // conversion (the round trip alone would move the last 5 bits of data the
+    // run never changed), else the double-float's value.
+    __device__ static SP stored(P v, SP orig)
+    {
+        if constexpr (IS_DF<P>) return (v == P(orig)) ? orig : static_cast<SP>(v);
+        else return v;
     }
 
     // Checkpoint c of the adjoint tape: time and every unit's state.

@@ -355,12 +355,13 @@ struct DfSolver {
         PerThread_Finalization(ti, nti, s.didx, s.t, s.dt, s.td, s.x, s.cp, g.sp, g.spi, s.acc, s.acci);
 #pragma unroll
         for (int k = 0; k < 2; k++) a.td[i + k * nt] = df_to_double(s.td[k], s.td64[k]);
+        // values the run left unchanged keep their FP64 bits (df_to_double)
 #pragma unroll
-        for (int k = 0; k < SD; k++) a.x[i + k * nt] = static_cast<double>(s.x[k]);
+        for (int k = 0; k < SD; k++) a.x[i + k * nt] = df_to_double(s.x[k], a.x[i + k * nt]);
 #pragma unroll
-        for (int k = 0; k < NCP; k++) a.cp[i + k * nt] = static_cast<double>(s.cp[k]);
+        for (int k = 0; k < NCP; k++) a.cp[i + k * nt] = df_to_double(s.cp[k], a.cp[i + k * nt]);
 #pragma unroll
-        for (int k = 0; k < NA; k++) a.acc[i + k * nt] = static_cast<double>(s.acc[k]);
+        for (int k = 0; k < NA; k++) a.acc[i + k * nt] = df_to_double(s.acc[k], a.acc[i + k * nt]);
 #pragma unroll
         for (int k = 0; k < NIA; k++) a.acci[i + k * nt] = s.acci[k];
         a.t[i]    = df_to_double(s.t, s.td64[1]);  // ends exactly on the FP64 upper bound

@@ -77,3 +77,13 @@ def test_coupled_single_system_and_empty_time_domain(mode, native_libs, oracle_l
     res = CW.run_coupled_gpu(empty, mode=mode, warps=2)
     np.testing.assert_array_equal(res["x"], empty.arrays["x"])
     np.testing.assert_array_equal(res["t"], empty.arrays["td"][0])
+
+
+def test_df_stage_leaves_untouched_inputs_bit_exact(native_libs):
+    """DF_STAGE holds values as double-floats (48 of 53 bits); data a run does
+    not change (the 21 Keller-Miksis coefficients here) is written back with
+    its original FP64 bits, not as a rounded round trip."""
+    case = W.keller_miksis_case(n_amp=4, n_freq=8, periods=1)
+    res = W.run_gpu(case, mode=capi.MODE_DF_STAGE | capi.MODE_PERSISTENT)
+    np.testing.assert_array_equal(res["cp"], case.arrays["cp"])
+    assert np.all(res["t"] == case.arrays["td"][1])
