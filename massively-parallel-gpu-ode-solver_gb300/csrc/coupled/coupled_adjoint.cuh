@@ -9,15 +9,13 @@
 // Reverse pass (this file): for each segment, last first, the states of every
 // step of the segment are recomputed from the checkpoint with the recorded
 // step sizes by the forward stepper itself (bit-identical to the forward
-// pass). Each step is then differentiated through its Runge-Kutta stages,
-// last first: the step's stage values (K with coupling, coupling values V)
-// are evaluated once in plain arithmetic, and at each stage point, where the
-// reverse recursion needs it, the user's CoupledSystems_PerBlock_OdeFunction
-// is evaluated with dual numbers seeded along the unit's own state components
-// and the system parameters, which gives per unit the local Jacobian of the
-// uncoupled right-hand side, the derivatives of the coupling term CPT and of
-// the coupling factor CPF, and CPF. Only one stage's Jacobians are alive at a
-// time. With K_i = f(X_i) the stage derivatives and
+// pass). Each step is then differentiated through its Runge-Kutta stages:
+// the stage points are re-evaluated with the user's
+// CoupledSystems_PerBlock_OdeFunction instantiated with dual numbers, seeded
+// along the unit's own state components and the system parameters, which
+// gives per unit and stage the local Jacobian of the uncoupled right-hand
+// side, the derivatives of the coupling term CPT and of the coupling factor
+// CPF, and their values. With K_i = f(X_i) the stage derivatives and
 //   f_u = F_u(X_u) + e_{CouplingIndex_c} cstr_c CPF_{u,c}(X_u) sum_j C_c[u][j] CPT_{j,c}(X_j),
 // the stage Jacobian-transpose product J_i^T kappa is, for unit j,
 //   dF_j^T kappa_j                                           (local part)
@@ -111,93 +109,23 @@ struct CoupledAdjoint {
     using Units = typename Fwd::Units;
     static constexpr int NCP1 = AtLeastOne<NC>::value;
 
-    // Stage values of one step, per unit of the lane: the stage derivatives
-    // with coupling and the coupling values sum_j C[u][j] CPT_j.
-    struct StageVals {
-        T K[ST][UPL][UD];
-        T V[ST][UPL][NCP1];
-    };
-    // Local Jacobians of one stage, per unit of the lane.
-    struct StageJac {
-        T L[UPL][UD][N];      // d(uncoupled F)/d(X_u, sPAR)
-        T G[UPL][NCP1][N];    // d(CPT)/d(X_u, sPAR)
-        T CF[UPL][NCP1];      // CPF value
-        T CFD[UPL][NCP1][N];  // d(CPF)/d(X_u, sPAR)
+    // Stage data of one step, per unit of the lane.
+    struct StepData {
+        T K[ST][UPL][UD];         // stage derivatives (with coupling)
+        T L[ST][UPL][UD][N];      // d(uncoupled F)/d(X_u, sPAR)
+        T G[ST][UPL][NCP1][N];    // d(CPT)/d(X_u, sPAR)
+        T CF[ST][UPL][NCP1];      // CPF value
+        T CFD[ST][UPL][NCP1][N];  // d(CPF)/d(X_u, sPAR)
+        T V[ST][UPL][NCP1];       // coupling value sum_j C[u][j] CPT_j
     };
 
     __device__ static bool has(int lane, int j) { return lane + 32 * j < UPS; }
     __device__ static int unit_of(int lane, int j) { return lane + 32 * j; }
 
-    // Stage point of stage st from (x, dt) and the earlier stages' K.
-    __device__ static T stage_point(const Tab& tb, int st, const T (&x)[UPL][UD], T dt, const StageVals& sv, int j,
-                                    int d)
-    {
-        T sum(0.0);
-        for (int q = 0; q < st; q++) sum = ad::mad(pt::tab_a<TB>(tb, st, q), sv.K[q][j][d], sum);
-        return ad::mad(dt, sum, x[j][d]);
-    }
-
-    // All stages of one step from (x, t) with step dt, plain values: K with
-    // the coupling term and the coupling values V (one coupling product per
-    // stage and coupling, over the warp).
-    __device__ static void plain_stages(const Tab& tb, long long s, int lane, AdjSlot<S, T>& sl, const Units& u,
-                                        const T* gp, const int* igp, const T* M, const int* cidx,
-                                        const T (&x)[UPL][UD], T t, T dt, StageVals& sv)
-    {
-        WarpSlot<S, T>& w = sl.w;
-        const int sid = static_cast<int>(s);
-        for (int st = 0; st < ST; st++) {
-            const T Ts = t + pt::tab_c<TB>(tb, st) * dt;
-#pragma unroll
-            for (int j = 0; j < UPL; j++) {
-                if (!has(lane, j)) continue;
-                const int uid = unit_of(lane, j);
-                T X[UD], F[UD], cpt[NCP1], cpf[NCP1];
-#pragma unroll
-                for (int d = 0; d < UD; d++) X[d] = stage_point(tb, st, x, dt, sv, j, d);
-                T up[AtLeastOne<NUP>::value], uacc[AtLeastOne<NUA>::value];
-#pragma unroll
-                for (int k = 0; k < NUP; k++) up[k] = u.up[j][k];
-#pragma unroll
-                for (int k = 0; k < NUA; k++) uacc[k] = u.uacc[j][k];
-                int iuacc[AtLeastOne<NIUA>::value];
-#pragma unroll
-                for (int k = 0; k < NIUA; k++) iuacc[k] = u.iuacc[j][k];
-                T gpc[AtLeastOne<S::NGP>::value];
-#pragma unroll
-                for (int k = 0; k < S::NGP; k++) gpc[k] = gp[k];
-                CoupledSystems_PerBlock_OdeFunction<T>(sid, uid, F, X, Ts, up, w.sp, gpc, const_cast<int*>(igp),
-                                                       uacc, iuacc, w.sacc, w.isacc, cpt, cpf);
-#pragma unroll
-                for (int d = 0; d < UD; d++) sv.K[st][j][d] = F[d];
-                for (int c = 0; c < NC; c++) {
-                    w.cpt[uid][c] = cpt[c];
-                    sv.V[st][j][c] = cpf[c];  // CPF for now; replaced by the coupling value below
-                }
-            }
-            __syncwarp();
-#pragma unroll
-            for (int j = 0; j < UPL; j++) {
-                if (!has(lane, j)) continue;
-                const int uid = unit_of(lane, j);
-                for (int c = 0; c < NC; c++) {
-                    const T cpf = sv.V[st][j][c];
-                    const T v = coupling_value<S, T>(M, w, uid, c);
-                    sv.V[st][j][c] = v;
-                    const int ci = cidx[c];
-                    if (ci >= 0 && ci < UD) sv.K[st][j][ci] += w.cstr[c] * cpf * v;
-                }
-            }
-            __syncwarp();
-        }
-    }
-
-    // Local Jacobians of stage st by one dual-number evaluation of the
-    // user's right-hand side at the stage point, seeded along the unit's own
-    // state and the system parameters.
-    __device__ static void dual_stage(const Tab& tb, int st, long long s, int lane, AdjSlot<S, T>& sl,
-                                      const Units& u, const T* gp, const int* igp, const T (&x)[UPL][UD], T t, T dt,
-                                      const StageVals& sv, StageJac& sj)
+    // Stages of one step from (x, t) with step dt, dual-evaluated.
+    __device__ static void stages(const Tab& tb, long long s, int lane, AdjSlot<S, T>& sl, const Units& u,
+                                  const T* gp, const int* igp, const T* M, const int* cidx, const T (&x)[UPL][UD],
+                                  T t, T dt, StepData& sd)
     {
         WarpSlot<S, T>& w = sl.w;
         const int sid = static_cast<int>(s);
@@ -216,48 +144,66 @@ struct CoupledAdjoint {
         int isacc[AtLeastOne<NISA>::value];
 #pragma unroll
         for (int k = 0; k < NISA; k++) isacc[k] = w.isacc[k];
-        const D Td(t + pt::tab_c<TB>(tb, st) * dt);
+
+        for (int st = 0; st < ST; st++) {
+            const D Td(t + pt::tab_c<TB>(tb, st) * dt);
 #pragma unroll
-        for (int j = 0; j < UPL; j++) {
-            if (!has(lane, j)) continue;
-            const int uid = unit_of(lane, j);
-            D Xd[UD], Fd[UD], cptd[NCP1], cpfd[NCP1];
+            for (int j = 0; j < UPL; j++) {
+                if (!has(lane, j)) continue;
+                const int uid = unit_of(lane, j);
+                D Xd[UD], Fd[UD], cptd[NCP1], cpfd[NCP1];
 #pragma unroll
-            for (int d = 0; d < UD; d++) {
-                Xd[d] = D(stage_point(tb, st, x, dt, sv, j, d));
-                Xd[d].d[d] = T(1.0);
-            }
-            D upd[AtLeastOne<NUP>::value], uaccd[AtLeastOne<NUA>::value];
+                for (int d = 0; d < UD; d++) {
+                    T sum(0.0);
+                    for (int q = 0; q < st; q++) sum = ad::mad(pt::tab_a<TB>(tb, st, q), sd.K[q][j][d], sum);
+                    Xd[d] = D(ad::mad(dt, sum, x[j][d]));
+                    Xd[d].d[d] = T(1.0);
+                }
+                D upd[AtLeastOne<NUP>::value], uaccd[AtLeastOne<NUA>::value];
 #pragma unroll
-            for (int k = 0; k < NUP; k++) upd[k] = D(u.up[j][k]);
+                for (int k = 0; k < NUP; k++) upd[k] = D(u.up[j][k]);
 #pragma unroll
-            for (int k = 0; k < NUA; k++) uaccd[k] = D(u.uacc[j][k]);
-            int iuacc[AtLeastOne<NIUA>::value];
+                for (int k = 0; k < NUA; k++) uaccd[k] = D(u.uacc[j][k]);
+                int iuacc[AtLeastOne<NIUA>::value];
 #pragma unroll
-            for (int k = 0; k < NIUA; k++) iuacc[k] = u.iuacc[j][k];
-            CoupledSystems_PerBlock_OdeFunction<D>(sid, uid, Fd, Xd, Td, upd, spd, gpd, const_cast<int*>(igp), uaccd,
-                                                   iuacc, saccd, isacc, cptd, cpfd);
+                for (int k = 0; k < NIUA; k++) iuacc[k] = u.iuacc[j][k];
+                CoupledSystems_PerBlock_OdeFunction<D>(sid, uid, Fd, Xd, Td, upd, spd, gpd, const_cast<int*>(igp),
+                                                       uaccd, iuacc, saccd, isacc, cptd, cpfd);
 #pragma unroll
-            for (int d = 0; d < UD; d++)
+                for (int d = 0; d < UD; d++) {
+                    sd.K[st][j][d] = Fd[d].v;
 #pragma unroll
-                for (int q = 0; q < N; q++) sj.L[j][d][q] = Fd[d].d[q];
-            for (int c = 0; c < NC; c++) {
-                sj.CF[j][c] = cpfd[c].v;
+                    for (int q = 0; q < N; q++) sd.L[st][j][d][q] = Fd[d].d[q];
+                }
+                for (int c = 0; c < NC; c++) {
+                    w.cpt[uid][c] = cptd[c].v;
+                    sd.CF[st][j][c] = cpfd[c].v;
 #pragma unroll
-                for (int q = 0; q < N; q++) {
-                    sj.G[j][c][q] = cptd[c].d[q];
-                    sj.CFD[j][c][q] = cpfd[c].d[q];
+                    for (int q = 0; q < N; q++) {
+                        sd.G[st][j][c][q] = cptd[c].d[q];
+                        sd.CFD[st][j][c][q] = cpfd[c].d[q];
+                    }
                 }
             }
+            __syncwarp();
+#pragma unroll
+            for (int j = 0; j < UPL; j++) {
+                if (!has(lane, j)) continue;
+                const int uid = unit_of(lane, j);
+                for (int c = 0; c < NC; c++) {
+                    const T v = coupling_value<S, T>(M, w, uid, c);
+                    sd.V[st][j][c] = v;
+                    const int ci = cidx[c];
+                    if (ci >= 0 && ci < UD) sd.K[st][j][ci] += w.cstr[c] * sd.CF[st][j][c] * v;
+                }
+            }
+            __syncwarp();
         }
     }
 
-    // Adjoint of one step (see the file comment): stages last first, each
-    // stage's local Jacobians recomputed where they are used, so only the
-    // step's stage values are kept.
-    __device__ static void reverse_step(const Tab& tb, long long s, int lane, AdjSlot<S, T>& sl, const Units& u,
-                                        const T* gp, const int* igp, const T* M, const T* MT, const int* cidx,
-                                        const T (&x)[UPL][UD], T t, T dt, const StageVals& sv, T (&lam)[UPL][UD],
+    // Adjoint of one step (see the file comment).
+    __device__ static void reverse_step(const Tab& tb, int lane, AdjSlot<S, T>& sl, const T* M, const T* MT,
+                                        const int* cidx, const StepData& sd, T dt, T (&lam)[UPL][UD],
                                         T (&mu)[AtLeastOne<NSP>::value])
     {
         WarpSlot<S, T>& w = sl.w;
@@ -275,9 +221,7 @@ struct CoupledAdjoint {
 #pragma unroll
             for (int d = 0; d < UD; d++) dlam[j][d] = T(0.0);
 
-        StageJac sj;
         for (int st = ST - 1; st >= 0; st--) {
-            dual_stage(tb, st, s, lane, sl, u, gp, igp, x, t, dt, sv, sj);
             T xi[UPL][UD];
 #pragma unroll
             for (int j = 0; j < UPL; j++) {
@@ -285,7 +229,7 @@ struct CoupledAdjoint {
                 for (int r = 0; r < UD; r++) {
                     T v(0.0);
 #pragma unroll
-                    for (int d = 0; d < UD; d++) v = ad::mad(sj.L[j][d][r], kap[st][j][d], v);
+                    for (int d = 0; d < UD; d++) v = ad::mad(sd.L[st][j][d][r], kap[st][j][d], v);
                     xi[j][r] = v;
                 }
                 if (!has(lane, j)) continue;
@@ -293,7 +237,7 @@ struct CoupledAdjoint {
                 for (int q = 0; q < NSP; q++) {
                     T v(0.0);
 #pragma unroll
-                    for (int d = 0; d < UD; d++) v = ad::mad(sj.L[j][d][UD + q], kap[st][j][d], v);
+                    for (int d = 0; d < UD; d++) v = ad::mad(sd.L[st][j][d][UD + q], kap[st][j][d], v);
                     mu[q] += v;
                 }
             }
@@ -302,18 +246,18 @@ struct CoupledAdjoint {
                 const bool ok = ci >= 0 && ci < UD;
 #pragma unroll
                 for (int j = 0; j < UPL; j++)
-                    if (has(lane, j)) sl.z[unit_of(lane, j)][c] = ok ? w.cstr[c] * sj.CF[j][c] * kap[st][j][ci] : T(0.0);
+                    if (has(lane, j)) sl.z[unit_of(lane, j)][c] = ok ? w.cstr[c] * sd.CF[st][j][c] * kap[st][j][ci] : T(0.0);
                 __syncwarp();
 #pragma unroll
                 for (int j = 0; j < UPL; j++) {
                     if (!has(lane, j)) continue;
                     const T wv = transposed_coupling_value<S, T>(M, MT, sl, unit_of(lane, j), c);
-                    const T coef = ok ? w.cstr[c] * sv.V[st][j][c] * kap[st][j][ci] : T(0.0);
+                    const T coef = ok ? w.cstr[c] * sd.V[st][j][c] * kap[st][j][ci] : T(0.0);
 #pragma unroll
-                    for (int r = 0; r < UD; r++) xi[j][r] += ad::mad2(wv, sj.G[j][c][r], coef, sj.CFD[j][c][r]);
+                    for (int r = 0; r < UD; r++) xi[j][r] += ad::mad2(wv, sd.G[st][j][c][r], coef, sd.CFD[st][j][c][r]);
 #pragma unroll
                     for (int q = 0; q < NSP; q++)
-                        mu[q] += ad::mad2(wv, sj.G[j][c][UD + q], coef, sj.CFD[j][c][UD + q]);
+                        mu[q] += ad::mad2(wv, sd.G[st][j][c][UD + q], coef, sd.CFD[st][j][c][UD + q]);
                 }
                 __syncwarp();
             }
@@ -442,7 +386,7 @@ __global__ void __launch_bounds__(CB_ADJOINT_BLOCK, MPGOS_CB_ADJOINT_MIN_BLOCKS)
     if (!(status & MPGOS_INSTANCE_TAPE_OVERFLOW) && n > 0) {
         T xs[MAXSEG][UPL][UD];
         T ts[MAXSEG];
-        typename Adj::StageVals sv;
+        typename Adj::StepData sd;
         for (int sgm = (n - 1) / seg; sgm >= 0; sgm--) {
             const int k0 = sgm * seg;
             const int k1 = min(n, k0 + seg);
@@ -480,9 +424,8 @@ __global__ void __launch_bounds__(CB_ADJOINT_BLOCK, MPGOS_CB_ADJOINT_MIN_BLOCKS)
             // reverse through the segment
             for (int k = k1 - 1; k >= k0; k--) {
                 const T dt(tp.dt[static_cast<long long>(k) * ns + s]);
-                Adj::plain_stages(tb, s, lane, sl, u, gp, igp, M, s_cidx, xs[k - k0], ts[k - k0], dt, sv);
-                Adj::reverse_step(tb, s, lane, sl, u, gp, igp, M, MT, s_cidx, xs[k - k0], ts[k - k0], dt, sv, lam,
-                                  mu);
+                Adj::stages(tb, s, lane, sl, u, gp, igp, M, s_cidx, xs[k - k0], ts[k - k0], dt, sd);
+                Adj::reverse_step(tb, lane, sl, M, MT, s_cidx, sd, dt, lam, mu);
             }
         }
     }
