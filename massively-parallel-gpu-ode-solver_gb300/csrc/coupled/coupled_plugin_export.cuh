@@ -3,11 +3,14 @@
 // and after defining MPGOS_SYS_NAME, MPGOS_SYS_CBW and MPGOS_SYS_CCI (coupling
 // storage), to export mpgos_cb_system_kernels() of mpgos.h. Instantiated:
 // RKCK45 and RK4 in double (with DF_STAGE variants and the discrete adjoint
-// with respect to the system parameters).
+// with respect to the system parameters, unless MPGOS_PLUGIN_NO_ADJOINT is
+// defined: the reverse kernels of large systems dominate the compile time).
 #pragma once
 
 #include "coupled_kernel.cuh"
+#ifndef MPGOS_PLUGIN_NO_ADJOINT
 #include "coupled_adjoint.cuh"
+#endif
 
 namespace mpgos_cb_plugin {
 using SysShape = mpgos::cb::Shape<MPGOS_SYS_UPS, MPGOS_SYS_UD, MPGOS_SYS_NC, MPGOS_SYS_CBW, MPGOS_SYS_CCI, MPGOS_SYS_NUP,
@@ -21,6 +24,10 @@ extern "C" __attribute__((visibility("default"))) const mpgos_cb_kernels* mpgos_
     using namespace mpgos::cb;
     using S = mpgos_cb_plugin::SysShape;
     if (precision_bytes == 8) {
+#ifdef MPGOS_PLUGIN_NO_ADJOINT
+        if (algorithm == MPGOS_RKCK45) return KernelTable<S, MPGOS_RKCK45, double>::get(MPGOS_SYS_NAME);
+        if (algorithm == MPGOS_RK4) return KernelTable<S, MPGOS_RK4, double>::get(MPGOS_SYS_NAME);
+#else
         if (algorithm == MPGOS_RKCK45) {
             using A = CoupledAdjointTable<S, MPGOS_RKCK45>;
             return KernelTable<S, MPGOS_RKCK45, double>::get(MPGOS_SYS_NAME, &A::launch_record, &A::launch_adjoint,
@@ -31,6 +38,7 @@ extern "C" __attribute__((visibility("default"))) const mpgos_cb_kernels* mpgos_
             return KernelTable<S, MPGOS_RK4, double>::get(MPGOS_SYS_NAME, &A::launch_record, &A::launch_adjoint,
                                                           &A::smem, &A::occupancy);
         }
+#endif
     }
     return nullptr;
 }

@@ -34,7 +34,7 @@ SYSTEMS = ["lorenz", "duffing", "duffing_param", "duffing_param_sens", "duffing_
            "keller_miksis"]
 # Coupled-system plugins: the ring of Duffing oscillators with 64 units and,
 # at 16 units, each of the four coupling-matrix storages.
-COUPLED = ["ring64", "ring16_full", "ring16_band", "ring16_circband", "ring16_circ"]
+COUPLED = ["ring64", "ring16_full", "ring16_band", "ring16_circband", "ring16_circ", "ring256"]
 
 
 def nvcc_path() -> str:

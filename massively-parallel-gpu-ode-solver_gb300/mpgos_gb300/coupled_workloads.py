@@ -33,6 +33,7 @@ CB_SHAPES = {  # UPS, UD, NC, CBW, CCI, NUP, NSP, NGP, NIGP, NUA, NIUA, NSA, NIS
     "ring16_band": (16, 2, 1, 1, 0, 0, 1, 1, 0, 0, 1, 0, 1, 1),
     "ring16_circband": (16, 2, 1, 1, 1, 0, 1, 1, 0, 0, 1, 0, 1, 1),
     "ring16_circ": (16, 2, 1, 0, 1, 0, 1, 1, 0, 0, 1, 0, 1, 1),
+    "ring256": (256, 2, 1, 0, 0, 0, 1, 1, 0, 0, 1, 0, 1, 1),
 }
 
 CB_DEFAULT_OPTIONS = dict(initial_dt=1e-2, max_dt=1e6, min_dt=1e-12, grow=5.0, shrink=0.1, dense_min_dt=0.0,

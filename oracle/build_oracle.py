@@ -50,7 +50,7 @@ SYSTEMS = ["lorenz", "duffing", "duffing_param", "duffing_param_sens", "duffing_
 FLAGS = ["-O3", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math"]
 # Coupled-system plugins (the product's build list): the oracle and the
 # reference cubins read hook file, UPS, CBW and CCI from systems/<name>.cu.
-COUPLED = ["ring64", "ring16_full", "ring16_band", "ring16_circband", "ring16_circ"]
+COUPLED = ["ring64", "ring16_full", "ring16_band", "ring16_circband", "ring16_circ", "ring256"]
 
 
 def coupled_defs(system: str) -> dict:
@@ -99,6 +99,9 @@ REF_GPU_CB_KERNELS = [
     # SingleSystem_SingleBlockLaunch, SingleSystem_MultipleBlockLaunches, MultipleSystems_MultipleBlockLaunches
     ("ring64", 1, 512, 64, 1, 0), ("ring64", 1, 512, 32, 1, 0), ("ring64", 1, 512, 64, 2, 0),
     ("ring64", 0, 512, 32, 1, 0),
+    # 256 units per system: more units than threads per block (SingleSystem_MultipleBlockLaunches)
+    # and one 256-thread block per system (SingleSystem_SingleBlockLaunch)
+    ("ring256", 1, 64, 128, 1, 0), ("ring256", 1, 64, 256, 1, 0),
 ]
 
 

@@ -202,3 +202,27 @@ def test_attempt_limit_is_reported(native_libs):
     assert np.all(res["status"] & capi.INSTANCE_ATTEMPT_LIMIT)
     assert np.all(res["nacc"] + res["nrej"] == 50)
     assert np.all(res["t"] < case.arrays["td"][1])
+
+
+@pytest.mark.parametrize("tpb", [128, 256], ids=["SingleSystem_MultipleBlockLaunches", "SingleSystem_SingleBlockLaunch"])
+def test_large_systems_match_reference_kernels(tpb, native_libs):
+    """Rings of 256 units (eight units per lane of the integrating warp; the
+    256x256 FP64 coupling matrix is read from global memory, as it does not fit
+    shared memory): bit-identical to the reference's kernel for one system per
+    block, with the block's 256 logical threads in two passes of 128 or one of
+    256."""
+    case = CW.ring_case("ring256", ns=64, periods=1, seed=13)
+    ref = _ref(case, tpb, 1)
+    for mode, warps in ((0, 2), (capi.MODE_PERSISTENT, 1)):
+        res = CW.run_coupled_gpu(case, mode=mode, warps=warps)
+        assert np.all(res["status"] == 0)
+        assert_bitwise(res, ref, keys=KEYS)
+
+
+def test_large_systems_double_float_needs_shared_matrices(native_libs):
+    """DF_STAGE keeps the coupling matrices in shared memory as double-floats;
+    a 256x256 matrix (512 KB) does not fit, and the launch is refused with an
+    error instead of running out of bounds."""
+    case = CW.ring_case("ring256", ns=8, periods=1, seed=14)
+    with pytest.raises(capi.MpgosError, match="shared memory"):
+        CW.run_coupled_gpu(case, mode=capi.MODE_DF_STAGE, warps=1)
