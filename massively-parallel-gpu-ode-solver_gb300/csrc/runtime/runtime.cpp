@@ -860,6 +860,19 @@ MPGOS_EXPORT int mpgos_pt_autotune(mpgos_pt_solver* s, int32_t arithmetic, const
     int best_block = s->block, best_ipt = s->ipt, best_ps = s->prefer_shared;
     int32_t best_mode = s->mode;
     const int keep_ipt = s->ipt, keep_ps = s->prefer_shared;
+    // one timed Solve() from the backed-up state; errors are returned (not
+    // thrown out of the tuner) so that the state and the backups are restored
+    auto time_one = [&](int32_t m, int b, float* ms) -> int {
+        int r = restore();
+        if (r) return r;
+        cudaError_t e = cudaEventRecord(s->timer_begin, s->stream);
+        if (e == cudaSuccess && (r = enqueue_solve(s, m, b))) return r;
+        if (e == cudaSuccess) e = cudaEventRecord(s->timer_end, s->stream);
+        if (e == cudaSuccess) e = cudaEventSynchronize(s->timer_end);
+        if (e == cudaSuccess) e = cudaEventElapsedTime(ms, s->timer_begin, s->timer_end);
+        if (e != cudaSuccess) return fail(MPGOS_ERR_CUDA, "autotune timing failed: %s", cudaGetErrorString(e));
+        return MPGOS_OK;
+    };
     const int blocks[] = {32, 64, 96, 128, 192, 256};
     const int ipts[] = {1, 2, 4, 0};  // 0: persistent
     const bool has_shared = (s->shape.nsp + s->shape.nisp) > 0;
@@ -869,13 +882,8 @@ MPGOS_EXPORT int mpgos_pt_autotune(mpgos_pt_solver* s, int32_t arithmetic, const
                 const int32_t m = base | (n == 0 ? MPGOS_MODE_PERSISTENT : 0);
                 s->ipt = n == 0 ? 1 : n;
                 s->prefer_shared = ps;
-                if ((rc = restore())) break;
-                MPGOS_CUDA(cudaEventRecord(s->timer_begin, s->stream));
-                if ((rc = enqueue_solve(s, m, b))) break;
-                MPGOS_CUDA(cudaEventRecord(s->timer_end, s->stream));
-                MPGOS_CUDA(cudaEventSynchronize(s->timer_end));
                 float t = 0.f;
-                MPGOS_CUDA(cudaEventElapsedTime(&t, s->timer_begin, s->timer_end));
+                if ((rc = time_one(m, b, &t))) break;
                 if (t < best) {
                     best = t;
                     best_block = b;
@@ -896,18 +904,10 @@ MPGOS_EXPORT int mpgos_pt_autotune(mpgos_pt_solver* s, int32_t arithmetic, const
         s->ipt = best_ipt;
         s->prefer_shared = best_ps;
         s->reconverge = 1 - cur_rv;
-        if (!(rc = restore())) {
-            MPGOS_CUDA(cudaEventRecord(s->timer_begin, s->stream));
-            if (!(rc = enqueue_solve(s, best_mode, best_block))) {
-                MPGOS_CUDA(cudaEventRecord(s->timer_end, s->stream));
-                MPGOS_CUDA(cudaEventSynchronize(s->timer_end));
-                float t = 0.f;
-                MPGOS_CUDA(cudaEventElapsedTime(&t, s->timer_begin, s->timer_end));
-                if (t < best) {
-                    best = t;
-                    best_rv = 1 - cur_rv;
-                }
-            }
+        float t = 0.f;
+        if (!(rc = time_one(best_mode, best_block, &t)) && t < best) {
+            best = t;
+            best_rv = 1 - cur_rv;
         }
     }
     s->reconverge = keep_rv;
