@@ -112,11 +112,12 @@ enum mpgos_option {
 #define MPGOS_MODE_FAST_CONTROL 1
 #define MPGOS_MODE_PERSISTENT   2
 #define MPGOS_MODE_FP32_STAGE   4
-/* DF_STAGE: every per-instance quantity of the adaptive FP64 scheme in
- * double-float arithmetic (pairs of floats, ~48 significant bits) on the FP32
- * pipe, with a log-domain step-size factor; results agree with the FP64
- * kernels to ~1e-13 relative on non-chaotic instances. Exclusive with
- * FP32_STAGE; FAST_CONTROL is implied. */
+/* DF_STAGE: every per-instance quantity of the FP64 scheme in double-float
+ * arithmetic (pairs of floats, ~48 significant bits) on the FP32 pipe: RKCK45
+ * with a log-domain step-size factor, RK4 on the reference's FP64 time grid
+ * (identical step counts); results agree with the FP64 kernels to ~1e-13
+ * relative on non-chaotic instances. Exclusive with FP32_STAGE; FAST_CONTROL
+ * is implied. */
 #define MPGOS_MODE_DF_STAGE     16
 #define MPGOS_MODE_CHOSEN       (MPGOS_MODE_FAST_CONTROL | MPGOS_MODE_PERSISTENT)
 

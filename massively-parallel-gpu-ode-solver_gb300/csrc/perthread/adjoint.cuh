@@ -536,14 +536,10 @@ struct AdjointTable {
         if (tape == nullptr || tape->segment < 1 || tape->segment > MAX_SEG) return static_cast<int>(cudaErrorInvalidValue);
         void* fn = nullptr;
         if (L->mode & MPGOS_MODE_DF_STAGE) {
-            if constexpr (ALG == MPGOS_RKCK45) {
-                if (L->mode & MPGOS_MODE_PERSISTENT)
-                    fn = reinterpret_cast<void*>(&perthread_df_kernel<S, MODE_RECORD | MPGOS_MODE_DF_STAGE | 2>);
-                else
-                    fn = reinterpret_cast<void*>(&perthread_df_kernel<S, MODE_RECORD | MPGOS_MODE_DF_STAGE>);
-            } else {
-                return static_cast<int>(cudaErrorInvalidValue);
-            }
+            if (L->mode & MPGOS_MODE_PERSISTENT)
+                fn = reinterpret_cast<void*>(&perthread_df_kernel<S, MODE_RECORD | MPGOS_MODE_DF_STAGE | 2, ALG>);
+            else
+                fn = reinterpret_cast<void*>(&perthread_df_kernel<S, MODE_RECORD | MPGOS_MODE_DF_STAGE, ALG>);
         } else {
             switch (L->mode & (MPGOS_MODE_FAST_CONTROL | MPGOS_MODE_PERSISTENT)) {
                 case 0: fn = reinterpret_cast<void*>(&perthread_kernel<S, ALG, double, MODE_RECORD>); break;
@@ -567,13 +563,8 @@ struct AdjointTable {
         Tape t = tape_of(*tape);
         void* params[] = {&a, &t, &dLdxT, &dLdx0, &dLdp};
         // a DF_STAGE solver differentiates in double-float as well
-        void* fn = reinterpret_cast<void*>(&adjoint_kernel<S, ALG, double>);
-        if (L->mode & MPGOS_MODE_DF_STAGE) {
-            if constexpr (ALG == MPGOS_RKCK45)
-                fn = reinterpret_cast<void*>(&adjoint_kernel<S, ALG, dfloat>);
-            else
-                return static_cast<int>(cudaErrorInvalidValue);
-        }
+        void* fn = (L->mode & MPGOS_MODE_DF_STAGE) ? reinterpret_cast<void*>(&adjoint_kernel<S, ALG, dfloat>)
+                                                  : reinterpret_cast<void*>(&adjoint_kernel<S, ALG, double>);
         return static_cast<int>(cudaLaunchKernel(fn, dim3(grid), dim3(block), params, smem,
                                                  static_cast<cudaStream_t>(stream)));
     }

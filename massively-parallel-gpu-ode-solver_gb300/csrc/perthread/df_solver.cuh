@@ -35,6 +35,7 @@ using df::dfloat;
 
 struct DfOptions {
     dfloat initial_dt, max_dt, min_dt, min_dt_guard, dense_min_dt;
+    double initial_dt64;
     float grow, shrink;
     int ndo, dense_freq;
     long long max_attempts;
@@ -52,6 +53,7 @@ struct DfInstance {
     dfloat ga[AtLeastOne<S::NE>::value];
     dfloat t, dt, new_dt, dense_next;
     double td64[2];  // the FP64 time domain as loaded (written back unless a hook changed it)
+    double t64;      // RK4: the time in FP64 (the reference's fixed-step time grid, step for step)
     int didx, skipped, terminate, udt, status, nacc, nrej;
     long long attempts;
 };
@@ -166,6 +168,40 @@ __device__ __forceinline__ void step_rkck45_df(int tid, int nt, dfloat t, dfloat
 // structure): tolerance max(rtol max(|xn|, |x|), atol) and the accept test in
 // FP32 on the leading floats (their rounding, ~6e-8, is far below the error
 // estimate's own), factor 0.9 (tol/err)^(1/5 or 1/4) through FP32 log2/exp2.
+// Classic RK4 step in double-float (SingleSystem_PerThread_ExplicitRungeKutta_Steppers.cuh:6-117:
+// x + dt (k1 + 2 k2 + 2 k3 + k4) / 6), stage sums as unnormalised product sums.
+template <int SD>
+__device__ __forceinline__ void step_rk4_df(int tid, int nt, dfloat t, dfloat dt, dfloat* x, dfloat* xn, int& finite,
+                                            dfloat* cp, dfloat* sp, int* spi, dfloat* acc, int* acci)
+{
+    using df::prod_sum;
+    using df::prod_sum_add;
+    using df::prod_sum_axpy;
+    using df::prod_sum_start;
+    dfloat X[SD], k1[SD], k2[SD], k3[SD], k4[SD];
+    const dfloat half(0.5);
+    const dfloat th = df::fma(dt, half, t);
+    PerThread_OdeFunction(tid, nt, k1, x, t, cp, sp, spi, acc, acci);
+#pragma unroll
+    for (int i = 0; i < SD; i++) X[i] = prod_sum_axpy(dt, prod_sum_start(half, k1[i]), x[i]);
+    PerThread_OdeFunction(tid, nt, k2, X, th, cp, sp, spi, acc, acci);
+#pragma unroll
+    for (int i = 0; i < SD; i++) X[i] = prod_sum_axpy(dt, prod_sum_start(half, k2[i]), x[i]);
+    PerThread_OdeFunction(tid, nt, k3, X, th, cp, sp, spi, acc, acci);
+#pragma unroll
+    for (int i = 0; i < SD; i++) X[i] = prod_sum_axpy(dt, prod_sum{k3[i].hi, k3[i].lo}, x[i]);
+    PerThread_OdeFunction(tid, nt, k4, X, t + dt, cp, sp, spi, acc, acci);
+#pragma unroll
+    for (int i = 0; i < SD; i++) {
+        prod_sum s = prod_sum_start(dfloat(1.0 / 6.0), k1[i]);
+        prod_sum_add(s, dfloat(1.0 / 3.0), k2[i]);
+        prod_sum_add(s, dfloat(1.0 / 3.0), k3[i]);
+        prod_sum_add(s, dfloat(1.0 / 6.0), k4[i]);
+        xn[i] = prod_sum_axpy(dt, s, x[i]);
+        if ((__float_as_uint(xn[i].hi) & 0x7f800000u) == 0x7f800000u) finite = 0;
+    }
+}
+
 template <int SD>
 __device__ __forceinline__ void control_rkck45_df(const DfOptions& o, dfloat dt, const dfloat* x, const dfloat* xn,
                                                   const float* err, const dfloat* rtol, const dfloat* atol,
@@ -222,9 +258,10 @@ __device__ __forceinline__ void dense_store_df(long long i, long long nt, int st
     }
 }
 
-template <class S, int MODE>
+template <class S, int MODE, int ALG = MPGOS_RKCK45>
 struct DfSolver {
     static constexpr int SD = S::SD, NCP = S::NCP, NE = S::NE, NA = S::NA, NIA = S::NIA;
+    static constexpr bool RK4 = (ALG == MPGOS_RK4);
     static constexpr bool PERSISTENT = (MODE & MPGOS_MODE_PERSISTENT) != 0;
     static constexpr bool RECORD = (MODE & MODE_RECORD) != 0;
     using Inst = DfInstance<S>;
@@ -261,6 +298,7 @@ struct DfSolver {
         s.dense_next = s.t;
         const int ti = static_cast<int>(i), nti = static_cast<int>(nt);
         PerThread_Initialization(ti, nti, s.didx, s.t, s.dt, s.td, s.x, s.cp, g.sp, g.spi, s.acc, s.acci);
+        if constexpr (RK4) s.t64 = df_to_double(s.t, (s.t == s.td[0]) ? s.td64[0] : a.t[i]);
         if (NE > 0)
             PerThread_EventFunction(ti, nti, s.ga, s.t, s.dt, s.td, s.x, s.cp, g.sp, g.spi, s.acc, s.acci);
         if (o.ndo > 0)
@@ -268,7 +306,7 @@ struct DfSolver {
                                o.dense_min_dt, s.td[1]);
         if constexpr (RECORD) {
             // checkpoint 0: the state the first step starts from
-            a.tape.ckpt_t[i] = static_cast<double>(s.t);
+            a.tape.ckpt_t[i] = RK4 ? s.t64 : static_cast<double>(s.t);
 #pragma unroll
             for (int d = 0; d < SD; d++) a.tape.ckpt_x[d * nt + i] = static_cast<double>(s.x[d]);
         }
@@ -285,16 +323,35 @@ struct DfSolver {
         const int ti = static_cast<int>(s.i), nti = static_cast<int>(a.nt);
         int update = 1, finite = 1, end_reached = 0;
         dfloat xn[SD];
-        float err[SD];
-        s.dt = s.new_dt;
-        const dfloat rem = s.td[1] - s.t;
-        if (s.dt > rem) {
-            s.dt        = rem;
-            end_reached = 1;
+        double dt64 = 0.0;
+        if constexpr (RK4) {
+            // fixed step on the FP64 time grid of the reference (step counts and
+            // the clamped end step match it exactly); stages in double-float
+            dt64 = o.initial_dt64;
+            const double rem64 = s.td64[1] - s.t64;
+            if (dt64 > rem64) {
+                dt64        = rem64;
+                end_reached = 1;
+            }
+            s.dt = dfloat(dt64);
+            step_rk4_df<SD>(ti, nti, s.t, s.dt, s.x, xn, finite, s.cp, g.sp, g.spi, s.acc, s.acci);
+            if (finite == 0) {
+                s.terminate = 1;
+                s.status |= MPGOS_INSTANCE_NONFINITE;
+            }
+            s.new_dt = o.initial_dt;
+        } else {
+            float err[SD];
+            s.dt = s.new_dt;
+            const dfloat rem = s.td[1] - s.t;
+            if (s.dt > rem) {
+                s.dt        = rem;
+                end_reached = 1;
+            }
+            step_rkck45_df<SD>(ti, nti, s.t, s.dt, s.x, xn, err, finite, s.cp, g.sp, g.spi, s.acc, s.acci);
+            control_rkck45_df<SD>(o, s.dt, s.x, xn, err, g.rtol, g.atol, update, finite, s.terminate, s.new_dt,
+                                  s.status);
         }
-        step_rkck45_df<SD>(ti, nti, s.t, s.dt, s.x, xn, err, finite, s.cp, g.sp, g.spi, s.acc, s.acci);
-        control_rkck45_df<SD>(o, s.dt, s.x, xn, err, g.rtol, g.atol, update, finite, s.terminate, s.new_dt,
-                              s.status);
 
         dfloat gn[AtLeastOne<NE>::value];
         if (NE > 0) {
@@ -305,11 +362,19 @@ struct DfSolver {
 
         if (update == 1) {
             s.nacc++;
-            s.t = (end_reached == 1) ? s.td[1] : s.t + s.dt;
+            if constexpr (RK4) {
+                s.t64 += dt64;
+                s.t = dfloat(s.t64);
+            } else {
+                s.t = (end_reached == 1) ? s.td[1] : s.t + s.dt;
+            }
 #pragma unroll
             for (int k = 0; k < SD; k++) s.x[k] = xn[k];
             PerThread_ActionAfterSuccessfulTimeStep(ti, nti, s.udt, s.t, s.dt, s.td, s.x, s.cp, g.sp, g.spi,
                                                     s.acc, s.acci);
+            if constexpr (RK4) {
+                if (!(s.t == dfloat(s.t64))) s.t64 = static_cast<double>(s.t);  // a hook moved the time
+            }
             if (NE > 0) {
                 for (int e = 0; e < NE; e++) {
                     if (event_detected<dfloat>(s.ga[e], gn[e], g.etol[e], g.edir[e]))
@@ -330,10 +395,11 @@ struct DfSolver {
                 // frozen step size of accepted step nacc, checkpoint every seg steps
                 const int k = s.nacc - 1;
                 if (k < a.tape.max_steps) {
-                    a.tape.dt[static_cast<long long>(k) * a.nt + s.i] = static_cast<double>(s.dt);
+                    // RK4: the FP64 step and time themselves
+                    a.tape.dt[static_cast<long long>(k) * a.nt + s.i] = RK4 ? dt64 : static_cast<double>(s.dt);
                     if (s.nacc % a.tape.seg == 0) {
                         const long long c = s.nacc / a.tape.seg;
-                        a.tape.ckpt_t[c * a.nt + s.i] = static_cast<double>(s.t);
+                        a.tape.ckpt_t[c * a.nt + s.i] = RK4 ? s.t64 : static_cast<double>(s.t);
 #pragma unroll
                         for (int d = 0; d < SD; d++)
                             a.tape.ckpt_x[(c * SD + d) * a.nt + s.i] = static_cast<double>(s.x[d]);
@@ -364,7 +430,8 @@ struct DfSolver {
         for (int k = 0; k < NA; k++) a.acc[i + k * nt] = df_to_double(s.acc[k], a.acc[i + k * nt]);
 #pragma unroll
         for (int k = 0; k < NIA; k++) a.acci[i + k * nt] = s.acci[k];
-        a.t[i]    = df_to_double(s.t, s.td64[1]);  // ends exactly on the FP64 upper bound
+        if constexpr (RK4) a.t[i] = s.t64;  // the FP64 time grid
+        else a.t[i] = df_to_double(s.t, s.td64[1]);  // ends exactly on the FP64 upper bound
         a.didx[i] = s.didx;
         if (a.status) a.status[i] = s.status;
         if (a.n_acc) a.n_acc[i] = s.nacc;
@@ -373,11 +440,11 @@ struct DfSolver {
     }
 };
 
-// DF_STAGE kernel: same launch contract as perthread_kernel<S, RKCK45, double, *>.
-template <class S, int MODE>
+// DF_STAGE kernel: same launch contract as perthread_kernel<S, ALG, double, *>.
+template <class S, int MODE, int ALG = MPGOS_RKCK45>
 __global__ void __launch_bounds__(MPGOS_MAX_BLOCK) perthread_df_kernel(Args<double> a)
 {
-    using Sv = DfSolver<S, MODE>;
+    using Sv = DfSolver<S, MODE, ALG>;
     constexpr int SD = S::SD, NSP = S::NSP, NISP = S::NISP, NE = S::NE;
     extern __shared__ __align__(16) unsigned char mpgos_dyn_smem[];
     __shared__ dfloat s_rtol[SD];
@@ -410,6 +477,7 @@ __global__ void __launch_bounds__(MPGOS_MAX_BLOCK) perthread_df_kernel(Args<doub
 
     DfOptions o;
     o.initial_dt   = dfloat(a.o.initial_dt);
+    o.initial_dt64 = a.o.initial_dt;
     o.max_dt       = dfloat(a.o.max_dt);
     o.min_dt       = dfloat(a.o.min_dt);
     o.min_dt_guard = dfloat(a.o.min_dt_guard);

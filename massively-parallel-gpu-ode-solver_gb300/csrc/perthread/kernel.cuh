@@ -487,9 +487,10 @@ namespace pt {
 template <class S, int ALG, class P>
 struct KernelTable {
     static constexpr bool DOUBLE_ADAPTIVE = sizeof(P) == 8 && ALG == MPGOS_RKCK45;
-    static constexpr int MODES =
-        MPGOS_MODE_PERSISTENT |
-        (DOUBLE_ADAPTIVE ? (MPGOS_MODE_FAST_CONTROL | MPGOS_MODE_FP32_STAGE | MPGOS_MODE_DF_STAGE) : 0);
+    static constexpr bool DOUBLE = sizeof(P) == 8;  // DF_STAGE: both schemes
+    static constexpr int MODES = MPGOS_MODE_PERSISTENT |
+                                 (DOUBLE_ADAPTIVE ? (MPGOS_MODE_FAST_CONTROL | MPGOS_MODE_FP32_STAGE) : 0) |
+                                 (DOUBLE ? MPGOS_MODE_DF_STAGE : 0);
 
     // Modes a table can run; the runtime only asks for these. MODE_RECONVERGE
     // selects the twin of each kernel with the per-attempt warp ballot.
@@ -507,10 +508,16 @@ struct KernelTable {
                 case 3: return reinterpret_cast<void*>(&perthread_kernel<S, ALG, P, 3>);
                 case 5: return reinterpret_cast<void*>(&perthread_kernel<S, ALG, P, 5>);
                 case 7: return reinterpret_cast<void*>(&perthread_kernel<S, ALG, P, 7>);
-                case MPGOS_MODE_DF_STAGE: return reinterpret_cast<void*>(&perthread_df_kernel<S, MPGOS_MODE_DF_STAGE>);
+                default: break;
+            }
+        }
+        if constexpr (DOUBLE) {
+            switch (mode) {
+                case MPGOS_MODE_DF_STAGE:
+                    return reinterpret_cast<void*>(&perthread_df_kernel<S, MPGOS_MODE_DF_STAGE, ALG>);
                 case MPGOS_MODE_DF_STAGE | MPGOS_MODE_PERSISTENT:
                     return reinterpret_cast<void*>(
-                        &perthread_df_kernel<S, MPGOS_MODE_DF_STAGE | MPGOS_MODE_PERSISTENT>);
+                        &perthread_df_kernel<S, MPGOS_MODE_DF_STAGE | MPGOS_MODE_PERSISTENT, ALG>);
                 default: break;
             }
         }
@@ -531,11 +538,16 @@ struct KernelTable {
                 case 3: return reinterpret_cast<void*>(&perthread_kernel<S, ALG, P, R | 3>);
                 case 5: return reinterpret_cast<void*>(&perthread_kernel<S, ALG, P, R | 5>);
                 case 7: return reinterpret_cast<void*>(&perthread_kernel<S, ALG, P, R | 7>);
+                default: break;
+            }
+        }
+        if constexpr (DOUBLE) {
+            switch (mode) {
                 case MPGOS_MODE_DF_STAGE:
-                    return reinterpret_cast<void*>(&perthread_df_kernel<S, R | MPGOS_MODE_DF_STAGE>);
+                    return reinterpret_cast<void*>(&perthread_df_kernel<S, R | MPGOS_MODE_DF_STAGE, ALG>);
                 case MPGOS_MODE_DF_STAGE | MPGOS_MODE_PERSISTENT:
                     return reinterpret_cast<void*>(
-                        &perthread_df_kernel<S, R | MPGOS_MODE_DF_STAGE | MPGOS_MODE_PERSISTENT>);
+                        &perthread_df_kernel<S, R | MPGOS_MODE_DF_STAGE | MPGOS_MODE_PERSISTENT, ALG>);
                 default: break;
             }
         }

@@ -92,8 +92,9 @@ def _int_slack(mode):
 
 
 def _skip_unsupported(case, mode):
-    if MODES[mode] & capi.MODE_DF_STAGE and case.algorithm == 0:
-        pytest.skip("DF_STAGE is compiled for the adaptive RKCK45 scheme only")
+    """Every mode runs every scheme here (FAST_CONTROL and FP32_STAGE are
+    no-ops for the fixed-step RK4, DF_STAGE runs its stages in double-float on
+    the reference's FP64 time grid)."""
 
 
 @pytest.mark.parametrize("mode", list(MODES), ids=str)
@@ -400,3 +401,17 @@ def test_config1_duffing_rk4_full_size(native_libs):
         res = W.run_gpu(case, mode=mode, graph=True)
         assert_bitwise(res, ref, keys=["x", "t", "acc", "acci"])
     assert np.all(res["acci"][0] == 1024 * 401)
+
+
+def test_df_stage_rk4_keeps_the_reference_time_grid(native_libs):
+    """DF_STAGE with the fixed-step RK4: stages in double-float, time on the
+    FP64 grid of the reference, so the step counts (the 400 steps and the
+    clamped end step of every period) and the end times are those of the
+    reference kernel exactly and the states agree to ~1e-13."""
+    case = W.duffing_rk4_case(nt=1024, periods=8)
+    ref = W.run_gpu(case, mode=capi.MODE_PLAIN, graph=True)
+    res = W.run_gpu(case, mode=capi.MODE_DF_STAGE | capi.MODE_PERSISTENT, graph=True)
+    np.testing.assert_array_equal(res["acci"], ref["acci"])
+    np.testing.assert_array_equal(res["t"], ref["t"])
+    assert np.max(np.abs(res["x"] - ref["x"])) < 1e-11
+    assert np.max(np.abs(res["acc"] - ref["acc"])) < 1e-11
