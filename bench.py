@@ -78,6 +78,7 @@ def parse():
     ap.add_argument("--no-coupled", action="store_true", help="skip the coupled-configuration leg")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint-configuration leg")
     ap.add_argument("--no-uneven", action="store_true", help="skip the uneven (Keller-Miksis) leg")
+    ap.add_argument("--no-rk4", action="store_true", help="skip the fixed-step (Duffing RK4) leg")
     return ap.parse_args()
 
 
@@ -372,6 +373,62 @@ def adjoint_leg(local: int, flush) -> dict:
                 "gradient_max_rel_diff_df_vs_fp64_reverse_same_tape": rel(g64[DF], g64[FP64]),
                 # different (both 1e-9-controlled) step sequences
                 "gradient_max_rel_diff_df_stage_vs_fp64": rel(gdf[DF], g64[FP64])})
+    return out
+
+
+def rk4_leg(local: int, flush) -> dict:
+    """Fixed-step configuration: forced Duffing oscillator, 8192 instances,
+    RK4 with dt = 2 pi / 400 over 1024 forcing periods (1024 phases replayed
+    from one CUDA graph), running maximum of x as an accessory. Times PLAIN
+    (bit-identical to the reference kernel, checked), the double-float form
+    (same step counts on the same FP64 time grid) and the reference's kernel
+    launched once per period; one warm-up and two timed runs each."""
+    import torch
+    from mpgos_gb300 import capi, workloads as W
+    from oracle import ref_gpu as R
+    case = W.duffing_rk4_case(nt=8192, periods=1024)
+    out = {"workload": "duffing_rk4_8192_dt2pi/400_1024periods", "unit": "accepted instance-steps/s"}
+
+    def run(mode, reference=False, tune=False):
+        with W.load_solver(case, mode=mode, block=64, device=local) as s:
+            s.checkpoint_save()
+            kern = None
+            if reference:
+                kern = R.ReferenceKernel("duffing", 0, case.nt, 0)
+                kern.bind(s, case, block=32)
+            if tune:
+                s.autotune(arithmetic=mode & capi.MODE_DF_STAGE)
+            times = []
+            for i in range(3):
+                flush_l2(flush)
+                torch.cuda.synchronize()
+                s.checkpoint_restore()
+                s.timer_start()
+                if reference:
+                    for _ in range(case.phases):
+                        kern.launch()
+                else:
+                    s.SolvePhases(case.phases)
+                ms = s.timer_stop()
+                if i:
+                    times.append(ms)
+            res = W.read_results(s)
+            if kern is not None:
+                kern.close()
+        steps = float(res["acci"][0].sum())
+        return {"ms": statistics.median(times), "value": steps / (statistics.median(times) / 1e3)}, res
+
+    out["plain"], rp = run(capi.MODE_PLAIN)
+    out["df_stage_autotuned"], rd = run(capi.MODE_DF_STAGE, tune=True)
+    out["df_steps_equal_plain"] = bool(np.array_equal(rd["acci"], rp["acci"]))
+    out["df_max_abs_diff_vs_plain"] = float(np.max(np.abs(rd["x"] - rp["x"])))
+    if R.available("duffing", 0, case.nt, 0):
+        ref, rr = run(capi.MODE_PLAIN, reference=True)
+        out["reference_gpu"] = ref
+        out["speedup_df_vs_reference_gpu"] = out["df_stage_autotuned"]["value"] / ref["value"]
+        out["plain_bitwise_equal_to_reference_kernel"] = bool(all(
+            np.array_equal(np.asarray(rp[k]).view(np.uint8), np.asarray(rr[k]).view(np.uint8))
+            for k in ("x", "t", "acc", "acci")))
     return out
 
 
@@ -700,6 +757,7 @@ def main():
     coupled = None if args.no_coupled else coupled_leg(local, flush)
     adjoint = None if args.no_adjoint else adjoint_leg(local, flush)
     uneven = None if args.no_uneven else uneven_leg(local, flush)
+    rk4 = None if args.no_rk4 else rk4_leg(local, flush)
     plain = ref_gpu = p = None
     parity = {}
     if not args.no_plain:
@@ -762,6 +820,7 @@ def main():
         "coupled": coupled,
         "adjoint": adjoint,
         "uneven": uneven,
+        "rk4": rk4,
         "plain": plain,
         "reference_gpu": ref_gpu,
         "speedup_vs_reference_gpu": (value / ref_gpu["value"]) if ref_gpu else None,
