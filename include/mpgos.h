@@ -422,6 +422,9 @@ typedef struct mpgos_cb_launch {
     int32_t*       accepted_steps;              /* [NS]           */
     int32_t*       rejected_steps;              /* [NS]           */
     uint32_t*      work_counter;
+    /* DF_STAGE with the coupling matrices too large for shared memory: their
+     * double-float copy (pairs of floats, same layout), else NULL */
+    const void*    coupling_matrix_df;
 } mpgos_cb_launch;
 
 typedef struct mpgos_cb_kernels {

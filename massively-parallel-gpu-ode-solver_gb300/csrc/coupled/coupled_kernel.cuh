@@ -112,6 +112,7 @@ struct Args {
     unsigned int* work;
     int shared_global;
     int shared_coupling;
+    const void* cmat_df;  // DF_STAGE, matrices in global memory: their double-float copy
     Options<P> o;
     // adjoint tape of a recording launch (MODE_RECORD): dt [max_steps][NS],
     // ckpt_x [max_steps/seg + 1][UD][NS*UPS], ckpt_t [max_steps/seg + 1][NS],
@@ -783,10 +784,12 @@ __global__ void __launch_bounds__(MPGOS_CB_MAX_BLOCK) coupled_kernel(Args<typena
     __shared__ int s_cidx[AtLeastOne<NC>::value];
 
     // DF_STAGE converts every FP64 array it reads more than once into shared
-    // memory, so its layout always holds the global parameters and the
-    // coupling matrices (the runtime sizes the allocation accordingly)
+    // memory: its layout always holds the global parameters and, where they
+    // fit, the coupling matrices; otherwise the matrices are read from the
+    // double-float copy the runtime keeps in global memory (the runtime sizes
+    // the allocation and sets shared_coupling accordingly)
     constexpr bool CONVERT = IS_DF<P>;
-    const int sg = CONVERT ? 1 : a.shared_global, sc = CONVERT ? 1 : a.shared_coupling;
+    const int sg = CONVERT ? 1 : a.shared_global, sc = a.shared_coupling;
     P* dyn_gp = reinterpret_cast<P*>(mpgos_cb_smem);
     P* dyn_m = dyn_gp + (sg ? NGP : 0);
     int* dyn_igp = reinterpret_cast<int*>(dyn_m + (sc ? NC * S::MAT : 0));
@@ -818,7 +821,7 @@ __global__ void __launch_bounds__(MPGOS_CB_MAX_BLOCK) coupled_kernel(Args<typena
     if constexpr (CONVERT) {
         gp = dyn_gp;
         igp = dyn_igp;
-        M = dyn_m;
+        M = sc ? dyn_m : static_cast<const P*>(a.cmat_df);
     } else {
         gp = sg ? dyn_gp : reinterpret_cast<const P*>(a.gp);
         igp = sg ? dyn_igp : a.igp;
@@ -886,6 +889,7 @@ Args<P> make_args(const mpgos_cb_launch& L)
     a.work = L.work_counter;
     a.shared_global = L.shared_global;
     a.shared_coupling = L.shared_coupling;
+    a.cmat_df = L.coupling_matrix_df;
     a.o.initial_dt = static_cast<P>(L.initial_dt);
     a.o.max_dt = static_cast<P>(L.max_dt);
     a.o.min_dt = static_cast<P>(L.min_dt);

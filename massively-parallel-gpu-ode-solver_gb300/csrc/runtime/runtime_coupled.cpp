@@ -76,7 +76,23 @@ struct mpgos_cb_solver {
     int64_t max_attempts = 10000000;
     std::vector<void*> ckpt;
     mpgos_pt_tape tape{};  // discrete-adjoint tape (mpgos_cb_solve_record)
+    void* d_cmat_df = nullptr;  // DF_STAGE: double-float copy of matrices too large for shared memory
 };
+
+namespace {
+// FP64 coupling matrices to double-float pairs (hi = the nearest float, lo =
+// the nearest float to the remainder), converted on the solver's stream
+// before every DF_STAGE launch that reads them from global memory.
+__global__ void matrix_to_double_float(const double* in, float2* out, long long n)
+{
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const double d = in[i];
+        const float hi = static_cast<float>(d);
+        out[i] = make_float2(hi, static_cast<float>(d - static_cast<double>(hi)));
+    }
+}
+}  // namespace
 
 namespace {
 
@@ -141,7 +157,8 @@ MPGOS_EXPORT int mpgos_cb_destroy(mpgos_cb_solver* s)
         if (b.host) cudaFreeHost(b.host);
         if (b.device) cudaFree(b.device);
     }
-    for (void* p : {s->d_rtol, s->d_atol, s->d_etol, static_cast<void*>(s->d_edir), static_cast<void*>(s->d_work)})
+    for (void* p : {s->d_rtol, s->d_atol, s->d_etol, static_cast<void*>(s->d_edir), static_cast<void*>(s->d_work),
+                    s->d_cmat_df})
         if (p) cudaFree(p);
     for (void* p : s->ckpt)
         if (p) cudaFree(p);
@@ -381,13 +398,28 @@ int prepare_launch(mpgos_cb_solver* s, bool record, mpgos_cb_launch& L, int64_t&
     const bool df = (mode & MPGOS_MODE_DF_STAGE) != 0;
     int sg = df ? 1 : s->shared_global, sc = df ? 1 : s->shared_coupling;
     size_t smem = s->k->dynamic_smem(s->warps, sg, sc);
-    if (smem > 200 * 1024 && sc && !df) {  // coupling matrix too large for shared memory: read it from global
+    const void* cmat_df = nullptr;
+    if (smem > 200 * 1024 && sc) {  // coupling matrix too large for shared memory: read it from global
         sc = 0;
         smem = s->k->dynamic_smem(s->warps, sg, sc);
+        if (df) {
+            // the double-float kernels read a double-float copy, refreshed before every launch
+            const long long n = static_cast<long long>(s->sh.nc) * s->sh.matrix_entries;
+            if (s->d_cmat_df == nullptr && cudaMalloc(&s->d_cmat_df, static_cast<size_t>(n) * 8) != cudaSuccess) {
+                s->d_cmat_df = nullptr;
+                return fail(MPGOS_ERR_MEMORY, "double-float coupling matrix copy (%lld entries) allocation failed", n);
+            }
+            const int blocks = static_cast<int>(std::min<long long>((n + 255) / 256, 4096));
+            matrix_to_double_float<<<blocks, 256, 0, s->stream>>>(
+                static_cast<const double*>(s->var[MPGOS_CB_COUPLING_MATRIX].device), static_cast<float2*>(s->d_cmat_df),
+                n);
+            CB_CUDA(cudaGetLastError());
+            cmat_df = s->d_cmat_df;
+        }
     }
     if (smem > 227 * 1024)
-        return fail(MPGOS_ERR_ARGUMENT, "coupled launch needs %zu bytes of shared memory (DF_STAGE keeps the coupling "
-                    "matrices there); use fewer warps per block", smem);
+        return fail(MPGOS_ERR_ARGUMENT, "coupled launch needs %zu bytes of shared memory; use fewer warps per block",
+                    smem);
     int64_t grid = (s->n_active + s->warps - 1) / s->warps;
     if (mode & MPGOS_MODE_PERSISTENT) {
         int per_sm = 0;
@@ -428,6 +460,7 @@ int prepare_launch(mpgos_cb_solver* s, bool record, mpgos_cb_launch& L, int64_t&
     L.global_parameters = d(MPGOS_CB_GLOBAL_PARAMETERS);
     L.integer_global_parameters = static_cast<const int32_t*>(d(MPGOS_CB_INTEGER_GLOBAL_PARAMETERS));
     L.coupling_matrix = d(MPGOS_CB_COUPLING_MATRIX);
+    L.coupling_matrix_df = cmat_df;
     L.coupling_index = static_cast<const int32_t*>(d(MPGOS_CB_COUPLING_INDEX));
     L.relative_tolerance = s->d_rtol;
     L.absolute_tolerance = s->d_atol;

@@ -16,6 +16,7 @@ import pytest
 
 from tests.parity import assert_bitwise, scaled_close
 from mpgos_gb300 import capi, coupled_workloads as CW
+from mpgos_gb300.capi import CbVariable as V
 from oracle import oracle as O, ref_gpu as R
 
 pytestmark = pytest.mark.gpu
@@ -113,7 +114,7 @@ def test_coupled_matches_oracle(system, native_libs, oracle_libs):
     and a landing whose event value is a rounding error from the band edge
     takes one more refinement step under any change of rounding, which a
     finite set of perturbations samples but cannot exhaust."""
-    ns, periods = (128, 1) if system == "ring64" else (256, 2)
+    ns, periods = {"ring64": (128, 1), "ring256": (24, 1)}.get(system, (256, 2))
     case = CW.ring_case(system, ns=ns, periods=periods, seed=14)
     ora, spread, stable = _spread(case)
     assert stable.mean() > 0.5
@@ -130,14 +131,14 @@ def test_coupled_matches_oracle(system, native_libs, oracle_libs):
     np.testing.assert_array_equal(res["isacc"][0], res["nacc"])
 
 
-@pytest.mark.parametrize("system", ["ring16_full", "ring64"])
+@pytest.mark.parametrize("system", ["ring16_full", "ring64", "ring256"])
 def test_coupled_df_stage_matches_oracle(system, native_libs, oracle_libs):
     """DF_STAGE (double-float stages, coupling dot products and sin/cos on the
     FP32 pipe): end states within 1e-9 of the component scale or the oracle's
     own perturbation spread; integer outputs equal on the systems the
     perturbations leave unchanged, with the step-flip allowance."""
     from tests.parity import assert_ints_equal
-    ns, periods = (128, 1) if system == "ring64" else (256, 2)
+    ns, periods = {"ring64": (128, 1), "ring256": (24, 1)}.get(system, (256, 2))
     case = CW.ring_case(system, ns=ns, periods=periods, seed=14)
     ora, spread, stable = _spread(case)
     res = CW.run_coupled_gpu(case, mode=capi.MODE_DF_STAGE | capi.MODE_PERSISTENT, warps=4)
@@ -219,10 +220,28 @@ def test_large_systems_match_reference_kernels(tpb, native_libs):
         assert_bitwise(res, ref, keys=KEYS)
 
 
-def test_large_systems_double_float_needs_shared_matrices(native_libs):
-    """DF_STAGE keeps the coupling matrices in shared memory as double-floats;
-    a 256x256 matrix (512 KB) does not fit, and the launch is refused with an
-    error instead of running out of bounds."""
-    case = CW.ring_case("ring256", ns=8, periods=1, seed=14)
-    with pytest.raises(capi.MpgosError, match="shared memory"):
-        CW.run_coupled_gpu(case, mode=capi.MODE_DF_STAGE, warps=1)
+def test_large_systems_double_float_reads_global_matrices(native_libs):
+    """DF_STAGE with a 256x256 coupling matrix (512 KB as double-floats, more
+    than shared memory holds): the kernel reads the runtime's double-float copy
+    from global memory; the mapping changes nothing (bit-identical), and a
+    matrix changed on the host between solves is converted again."""
+    case = CW.ring_case("ring256", ns=24, periods=1, seed=14)
+    base = CW.run_coupled_gpu(case, mode=capi.MODE_DF_STAGE, warps=1)
+    assert np.all(base["status"] == 0)
+    assert_bitwise(base, CW.run_coupled_gpu(case, mode=capi.MODE_DF_STAGE | capi.MODE_PERSISTENT, warps=2))
+    other = case.copy()
+    other.arrays["cmat"] = other.arrays["cmat"] * 0.5
+    fresh = CW.run_coupled_gpu(other, mode=capi.MODE_DF_STAGE, warps=1)
+    with CW.load_coupled_solver(case, mode=capi.MODE_DF_STAGE, warps=1) as s:
+        s.Solve()
+        s.host(V.ActualTime)[:] = other.arrays["t"]
+        s.host(V.ActualState)[:] = other.arrays["x"]
+        s.host(V.IntegerUnitAccessories)[:] = other.arrays["iuacc"]
+        s.host(V.IntegerSystemAccessories)[:] = other.arrays["isacc"]
+        for i in range(s.NC):
+            s.SetCouplingMatrix(i, other.arrays["cmat"][i])
+        s.SynchroniseFromHostToDevice(V.All)
+        s.Solve()
+        again = CW.read_coupled_results(s)
+    assert not np.array_equal(fresh["x"], base["x"])
+    assert_bitwise(fresh, again)
