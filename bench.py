@@ -398,6 +398,10 @@ def rk4_leg(local: int, flush) -> dict:
                 kern.bind(s, case, block=32)
             if tune:
                 s.autotune(arithmetic=mode & capi.MODE_DF_STAGE)
+            cfg = {}
+            if not reference:
+                grid, blk, m = s.launch_config()
+                cfg = {"grid": grid, "block": blk, "mode": m}
             times = []
             for i in range(3):
                 flush_l2(flush)
@@ -416,7 +420,7 @@ def rk4_leg(local: int, flush) -> dict:
             if kern is not None:
                 kern.close()
         steps = float(res["acci"][0].sum())
-        return {"ms": statistics.median(times), "value": steps / (statistics.median(times) / 1e3)}, res
+        return {"ms": statistics.median(times), "value": steps / (statistics.median(times) / 1e3), **cfg}, res
 
     out["plain"], rp = run(capi.MODE_PLAIN)
     out["df_stage_autotuned"], rd = run(capi.MODE_DF_STAGE, tune=True)
