@@ -372,6 +372,12 @@ enum mpgos_cb_variable {
     MPGOS_CB_STATUS = 32, MPGOS_CB_ACCEPTED_STEPS = 33, MPGOS_CB_REJECTED_STEPS = 34
 };
 
+/* DF_STAGE keeps the coupling matrices in shared memory as double-floats when
+ * they take at most this many bytes (NC x matrix_entries x 8), else reads a
+ * double-float copy in global memory; fixed per system shape, so the kernel
+ * knows at compile time which memory it reads. */
+#define MPGOS_CB_DF_SHARED_MATRIX_BYTES (160 * 1024)
+
 /* ListOfSolverOptions of the coupled interface (CoupledSystems_PerBlock_Interface.cuh:53-66). */
 enum mpgos_cb_option {
     MPGOS_CB_INITIAL_TIME_STEP = 0, MPGOS_CB_ACTIVE_SYSTEMS = 1, MPGOS_CB_MAXIMUM_TIME_STEP = 2,

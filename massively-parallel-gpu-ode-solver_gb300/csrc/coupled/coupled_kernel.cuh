@@ -785,11 +785,16 @@ __global__ void __launch_bounds__(MPGOS_CB_MAX_BLOCK) coupled_kernel(Args<typena
 
     // DF_STAGE converts every FP64 array it reads more than once into shared
     // memory: its layout always holds the global parameters and, where they
-    // fit, the coupling matrices; otherwise the matrices are read from the
-    // double-float copy the runtime keeps in global memory (the runtime sizes
-    // the allocation and sets shared_coupling accordingly)
+    // fit MPGOS_CB_DF_SHARED_MATRIX_BYTES, the coupling matrices; larger
+    // matrices are read from the double-float copy the runtime keeps in global
+    // memory. Both are compile-time facts of the shape (the runtime applies
+    // the same rule), so the matrix loads are shared-memory loads whenever
+    // the matrices sit there.
     constexpr bool CONVERT = IS_DF<P>;
-    const int sg = CONVERT ? 1 : a.shared_global, sc = a.shared_coupling;
+    constexpr bool DF_SHARED_MATRIX =
+        static_cast<size_t>(NC) * S::MAT * sizeof(dfloat) <= static_cast<size_t>(MPGOS_CB_DF_SHARED_MATRIX_BYTES);
+    const int sg = CONVERT ? 1 : a.shared_global;
+    const int sc = CONVERT ? (DF_SHARED_MATRIX ? 1 : 0) : a.shared_coupling;
     P* dyn_gp = reinterpret_cast<P*>(mpgos_cb_smem);
     P* dyn_m = dyn_gp + (sg ? NGP : 0);
     int* dyn_igp = reinterpret_cast<int*>(dyn_m + (sc ? NC * S::MAT : 0));

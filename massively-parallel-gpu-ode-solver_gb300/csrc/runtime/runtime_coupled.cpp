@@ -396,26 +396,30 @@ int prepare_launch(mpgos_cb_solver* s, bool record, mpgos_cb_launch& L, int64_t&
     const int32_t mode = record ? (s->mode & (MPGOS_MODE_PERSISTENT | MPGOS_MODE_DF_STAGE)) : s->mode;
     const int block = 32 * s->warps;
     const bool df = (mode & MPGOS_MODE_DF_STAGE) != 0;
-    int sg = df ? 1 : s->shared_global, sc = df ? 1 : s->shared_coupling;
+    const long long n_matrix = static_cast<long long>(s->sh.nc) * s->sh.matrix_entries;
+    // DF_STAGE: matrices in shared memory exactly when the kernel's
+    // compile-time rule says so (MPGOS_CB_DF_SHARED_MATRIX_BYTES)
+    const int df_sc = n_matrix * 8 <= static_cast<long long>(MPGOS_CB_DF_SHARED_MATRIX_BYTES) ? 1 : 0;
+    int sg = df ? 1 : s->shared_global, sc = df ? df_sc : s->shared_coupling;
     size_t smem = s->k->dynamic_smem(s->warps, sg, sc);
     const void* cmat_df = nullptr;
-    if (smem > 200 * 1024 && sc) {  // coupling matrix too large for shared memory: read it from global
+    if (!df && smem > 200 * 1024 && sc) {  // coupling matrix too large for shared memory: read it from global
         sc = 0;
         smem = s->k->dynamic_smem(s->warps, sg, sc);
-        if (df) {
-            // the double-float kernels read a double-float copy, refreshed before every launch
-            const long long n = static_cast<long long>(s->sh.nc) * s->sh.matrix_entries;
-            if (s->d_cmat_df == nullptr && cudaMalloc(&s->d_cmat_df, static_cast<size_t>(n) * 8) != cudaSuccess) {
-                s->d_cmat_df = nullptr;
-                return fail(MPGOS_ERR_MEMORY, "double-float coupling matrix copy (%lld entries) allocation failed", n);
-            }
-            const int blocks = static_cast<int>(std::min<long long>((n + 255) / 256, 4096));
-            matrix_to_double_float<<<blocks, 256, 0, s->stream>>>(
-                static_cast<const double*>(s->var[MPGOS_CB_COUPLING_MATRIX].device), static_cast<float2*>(s->d_cmat_df),
-                n);
-            CB_CUDA(cudaGetLastError());
-            cmat_df = s->d_cmat_df;
+    }
+    if (df && !sc) {
+        // the double-float kernels read a double-float copy, refreshed before every launch
+        if (s->d_cmat_df == nullptr && cudaMalloc(&s->d_cmat_df, static_cast<size_t>(n_matrix) * 8) != cudaSuccess) {
+            s->d_cmat_df = nullptr;
+            return fail(MPGOS_ERR_MEMORY, "double-float coupling matrix copy (%lld entries) allocation failed",
+                        n_matrix);
         }
+        const int blocks = static_cast<int>(std::min<long long>((n_matrix + 255) / 256, 4096));
+        matrix_to_double_float<<<blocks, 256, 0, s->stream>>>(
+            static_cast<const double*>(s->var[MPGOS_CB_COUPLING_MATRIX].device), static_cast<float2*>(s->d_cmat_df),
+            n_matrix);
+        CB_CUDA(cudaGetLastError());
+        cmat_df = s->d_cmat_df;
     }
     if (smem > 227 * 1024)
         return fail(MPGOS_ERR_ARGUMENT, "coupled launch needs %zu bytes of shared memory; use fewer warps per block",
