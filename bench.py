@@ -514,6 +514,25 @@ def uneven_leg(local: int, flush) -> dict:
         out["plain_bitwise_equal_to_reference_kernel"] = bool(all(
             np.array_equal(np.asarray(rplain[k]).view(np.uint8), np.asarray(rref[k]).view(np.uint8))
             for k in ("x", "t", "acc", "acci")))
+        # double-float form against the reference kernel over the whole ensemble: end states
+        # and per-period maximum radii relative to each component's scale, integer outputs
+        # (event count, accepted steps) per instance
+        # (the FP64 FAST_CONTROL form beside it: what a different rounding of the step-size
+        # factor alone does on this ensemble)
+        def versus_reference(r):
+            rel = {}
+            for k in ("x", "acc"):
+                a, b = np.asarray(r[k], np.float64), np.asarray(rref[k], np.float64)
+                scale = np.max(np.abs(b), axis=1, keepdims=True)
+                rel[k] = (np.abs(a - b) / (np.abs(b) + 1e-3 * scale)).max(axis=0)
+            steps, ref_steps = float(r["acci"][1].sum()), float(rref["acci"][1].sum())
+            return {"instances_within_1e-9_end_state": float(np.mean(rel["x"] <= 1e-9)),
+                    "instances_within_1e-9_max_radius": float(np.mean(rel["acc"] <= 1e-9)),
+                    "event_count_equal_fraction": float(np.mean(r["acci"][0] == rref["acci"][0])),
+                    "accepted_steps_equal_fraction": float(np.mean(r["acci"][1] == rref["acci"][1])),
+                    "accepted_steps_total_rel_diff": abs(steps - ref_steps) / ref_steps}
+        out["df_vs_reference_gpu"] = versus_reference(results["df_static_b32"])
+        out["fp64_fast_vs_reference_gpu"] = versus_reference(results["fp64_static_b32"])
     return out
 
 

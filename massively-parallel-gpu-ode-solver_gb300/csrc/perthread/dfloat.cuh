@@ -21,9 +21,9 @@
 //                   floats, one float of tails), normalised once at the end
 //   div             two long-division correction steps on a float quotient
 //   sqrt            Karp & Markstein 1997 (Newton corrections from rsqrt)
-// sin, cos and sincospi run on the FP32 pipe too (Cody-Waite reduction and
-// Taylor series, below); exp, log and pow evaluate in FP64 through CUDA's
-// double functions and round back (one FP64 evaluation per call).
+// sin, cos, sincospi, exp, log and pow run on the FP32 pipe too (Cody-Waite
+// reductions, Taylor series, one Newton step for log; below); only arguments
+// outside their ranges fall back to CUDA's FP64 functions.
 //
 // Hook code templated on its precision (the reference's
 // `template <class Precision> __device__ void PerThread_OdeFunction(...)`)
@@ -103,7 +103,8 @@ struct dfloat {
     MPGOS_DF_HD constexpr dfloat(float h, float l) : hi(h), lo(l) {}
     MPGOS_DF_HD dfloat(double d) : hi(static_cast<float>(d)), lo(0.0f)
     {
-        lo = static_cast<float>(d - static_cast<double>(hi));
+        // beyond the float range hi is infinite and carries the value alone
+        if (!std::isinf(hi)) lo = static_cast<float>(d - static_cast<double>(hi));
     }
     MPGOS_DF_HD constexpr dfloat(float f) : hi(f), lo(0.0f) {}
     MPGOS_DF_HD constexpr dfloat(int i) : hi(static_cast<float>(i)), lo(0.0f) {}
@@ -144,6 +145,17 @@ MPGOS_DF_HD dfloat operator+(dfloat a, dfloat b)
 }
 
 MPGOS_DF_HD dfloat operator-(dfloat a) { return dfloat(-a.hi, -a.lo); }
+
+// a + b with the error bounded relative to the result rather than to the
+// operands (both parts summed by two_sum; 20 operations; the "IEEE" add of
+// the same source), for sums that cancel
+MPGOS_DF_HD dfloat add_accurate(dfloat a, dfloat b)
+{
+    dfloat s = two_sum(a.hi, b.hi);
+    const dfloat t = two_sum(a.lo, b.lo);
+    s = quick_two_sum(s.hi, f_add(s.lo, t.hi));
+    return quick_two_sum(s.hi, f_add(s.lo, t.lo));
+}
 
 MPGOS_DF_HD dfloat operator-(dfloat a, dfloat b) { return a + (-b); }
 
@@ -344,16 +356,182 @@ MPGOS_DF_HD dfloat cos(dfloat a)
         default: return detail::sin_kernel(r);
     }
 }
-MPGOS_DF_HD dfloat exp(dfloat a) { return dfloat(std::exp(static_cast<double>(a))); }
-MPGOS_DF_HD dfloat log(dfloat a) { return dfloat(std::log(static_cast<double>(a))); }
+// ---- exp, log and pow on the FP32 pipe ------------------------------------------
+// exp: Cody & Waite reduction x = k ln2 + r (k the nearest integer to x/ln2,
+// ln2 split into three floats so that every k * L_i is an exact double-float),
+// r scaled by 2^-2 (|r/4| <= ln2/8), expm1 of the scaled value by its Taylor
+// series (through r^5 in double-float by Horner's rule, the tail r^6..r^11
+// in float, below 6e-10 of the result), squared back twice through
+// (1 + e)^2 - 1 = e (e + 2), then 1 + e scaled by 2^k exactly.
+// log: a = 2^E m with m in [sqrt(1/2), sqrt(2)); log m = 2 atanh(s) with
+// s = (m - 1)/(m + 1), |s| <= 0.172, by its series s (2 + 2 z/3 + 2 z^2/5 ...)
+// in z = s^2 (through z^5 in double-float, z^6..z^10 in float), so log m
+// keeps double-float precision relative to itself; log a = E ln2 + log m.
+// pow(a, b) = exp(b log a) for a > 0, with the integer part of b E taken out
+// exactly: b log a = n ln2 + ((b E - n) ln2 + b log m), n the nearest integer
+// to b log2 a and b E - n formed from the exact products b.hi E and b.lo E,
+// so the reduced argument carries no rounding of the size of b E.
+// Arguments these do not cover (|x| > 80 for exp, a <= 0, non-finite or
+// subnormal a for log and pow) go through the FP64 functions.
+namespace detail {
+constexpr float LN2_1 = 0x1.62e430p-1f;
+constexpr float LN2_2 = -0x1.05c610p-29f;
+constexpr float LN2_3 = -0x1.950d88p-54f;
+constexpr float INV_LN2 = 0x1.715476p+0f;
+
+MPGOS_DF_HD float pow2i(int k)  // 2^k for -126 <= k <= 127
+{
+#if defined(__CUDA_ARCH__)
+    return __int_as_float((k + 127) << 23);
+#else
+    return std::ldexp(1.0f, k);
+#endif
+}
+
+// exp(x) - 1 for |x| <= ln2/8
+MPGOS_DF_HD dfloat expm1_kernel(dfloat x)
+{
+    const float xf = x.hi;
+    float tail = 1.0f / 39916800.0f;                    // 1/11!
+    tail = f_fma(xf, tail, 1.0f / 3628800.0f);          // 1/10!
+    tail = f_fma(xf, tail, 1.0f / 362880.0f);           // 1/9!
+    tail = f_fma(xf, tail, 1.0f / 40320.0f);            // 1/8!
+    tail = f_fma(xf, tail, 1.0f / 5040.0f);             // 1/7!
+    tail = f_fma(xf, tail, 1.0f / 720.0f);              // 1/6!
+    dfloat p = fma(x, dfloat(tail), dfloat(0x1.111112p-7f, -0x1.dddddep-32f));   // 1/5!
+    p = fma(x, p, dfloat(0x1.555556p-5f, -0x1.555556p-30f));                      // 1/4!
+    p = fma(x, p, dfloat(0x1.555556p-3f, -0x1.555556p-28f));                      // 1/3!
+    p = fma(x, p, dfloat(0.5f));
+    p = fma(x, p, dfloat(1.0f));
+    return x * p;
+}
+
+// exp(r) 2^k for |r| <= ln2/2 + a little and an integer k in [-126, 127]
+MPGOS_DF_HD dfloat exp_scaled(dfloat r, int k)
+{
+    dfloat e = expm1_kernel(dfloat(f_mul(r.hi, 0.25f), f_mul(r.lo, 0.25f)));
+#pragma unroll
+    for (int i = 0; i < 2; i++) {
+        const dfloat t = two_sum(e.hi, 2.0f);
+        e = e * quick_two_sum(t.hi, f_add(t.lo, e.lo));       // e (e + 2)
+    }
+    const dfloat s = quick_two_sum(1.0f, e.hi);                    // |e| < 1/2
+    const dfloat v = quick_two_sum(s.hi, f_add(s.lo, e.lo));
+    const float scale = pow2i(k);
+    return dfloat(f_mul(v.hi, scale), f_mul(v.lo, scale));
+}
+
+// x - k ln2 for an integer-valued float k (|k| < 2^8)
+MPGOS_DF_HD dfloat minus_k_ln2(dfloat x, float k)
+{
+    dfloat r = x - two_prod(k, LN2_1);
+    r = r - two_prod(k, LN2_2);
+    return r - two_prod(k, LN2_3);
+}
+
+// exp(x) for |x.hi| <= 80
+MPGOS_DF_HD dfloat exp_reduced(dfloat x)
+{
+    const float k = f_rint(f_mul(x.hi, INV_LN2));
+    return exp_scaled(minus_k_ln2(x, k), static_cast<int>(k));
+}
+
+// a = 2^E m, m in [sqrt(1/2), sqrt(2)), for a normal positive a.hi
+MPGOS_DF_HD dfloat split_exponent(dfloat a, int& E)
+{
+#if defined(__CUDA_ARCH__)
+    E = ((__float_as_int(a.hi) >> 23) & 0xff) - 127;
+#else
+    E = std::ilogb(a.hi);
+#endif
+    float f = pow2i(-E);
+    if (f_mul(a.hi, f) > 1.41421356f) {
+        E += 1;
+        f = f_mul(f, 0.5f);
+    }
+    return dfloat(f_mul(a.hi, f), f_mul(a.lo, f));   // exact
+}
+
+// a / b with three quotient digits (the "accurate" division of the same
+// source as the add; error ~2^-49 relative against ~2^-46 for operator/)
+MPGOS_DF_HD dfloat div_accurate(dfloat a, dfloat b)
+{
+    const float rb = f_rcp(b.hi);
+    const float q1 = f_mul(a.hi, rb);
+    dfloat r = a - mul_f(b, q1);
+    const float q2 = f_mul(r.hi, rb);
+    r = r - mul_f(b, q2);
+    const float q3 = f_mul(r.hi, rb);
+    const dfloat q = quick_two_sum(q1, q2);
+    return q + dfloat(q3);
+}
+
+// log m for m in [sqrt(1/2), sqrt(2)]
+MPGOS_DF_HD dfloat log_reduced(dfloat m)
+{
+    const dfloat num = two_sum(f_sub(m.hi, 1.0f), m.lo);   // m - 1 (m.hi - 1 exact)
+    const dfloat s = div_accurate(num, m + dfloat(1.0f));
+    const dfloat z = s * s;
+    const float zf = z.hi;
+    float tail = 1.0f / 21.0f;
+    tail = f_fma(zf, tail, 1.0f / 19.0f);
+    tail = f_fma(zf, tail, 1.0f / 17.0f);
+    tail = f_fma(zf, tail, 1.0f / 15.0f);
+    tail = f_fma(zf, tail, 1.0f / 13.0f);
+    dfloat p = fma(z, dfloat(tail), dfloat(0x1.745d18p-4f, -0x1.745d18p-29f));   // 1/11
+    p = fma(z, p, dfloat(0x1.c71c72p-4f, -0x1.c71c72p-31f));                      // 1/9
+    p = fma(z, p, dfloat(0x1.24924ap-3f, -0x1.b6db6ep-28f));                      // 1/7
+    p = fma(z, p, dfloat(0x1.99999ap-3f, -0x1.99999ap-29f));                      // 1/5
+    p = fma(z, p, dfloat(0x1.555556p-2f, -0x1.555556p-27f));                      // 1/3
+    p = fma(z, p, dfloat(1.0f));
+    const dfloat t = s * p;
+    return dfloat(f_mul(t.hi, 2.0f), f_mul(t.lo, 2.0f));
+}
+}  // namespace detail
+
+MPGOS_DF_HD dfloat exp(dfloat a)
+{
+    if (!(std::fabs(a.hi) <= 80.0f)) return dfloat(std::exp(static_cast<double>(a)));
+    return detail::exp_reduced(a);
+}
+
+MPGOS_DF_HD dfloat log(dfloat a)
+{
+    if (!(a.hi >= 0x1p-126f && a.hi <= 0x1.fffffep+127f)) return dfloat(std::log(static_cast<double>(a)));
+    int E;
+    const dfloat m = detail::split_exponent(a, E);
+    const dfloat l = detail::log_reduced(m);
+    return detail::minus_k_ln2(l, -static_cast<float>(E));
+}
+
 MPGOS_DF_HD dfloat pow(dfloat a, dfloat b)
 {
-    return dfloat(std::pow(static_cast<double>(a), static_cast<double>(b)));
+    if (!(a.hi >= 0x1p-126f && a.hi <= 0x1.fffffep+127f && std::fabs(b.hi) <= 0x1p+16f))
+        return dfloat(std::pow(static_cast<double>(a), static_cast<double>(b)));
+    int E;
+    const dfloat m = detail::split_exponent(a, E);
+    const dfloat bl = b * detail::log_reduced(m);          // b log m
+    const float ef = static_cast<float>(E);
+    const dfloat p = two_prod(b.hi, ef), q = two_prod(b.lo, ef);   // b E = p + q exactly
+    const float n = f_rint(f_add(p.hi, f_mul(bl.hi, detail::INV_LN2)));   // ~ b log2 a
+    if (!(std::fabs(n) <= 115.0f)) return dfloat(std::pow(static_cast<double>(a), static_cast<double>(b)));
+    const dfloat g = add_accurate(add_accurate(two_sum(p.hi, -n), dfloat(p.lo)), q);   // b E - n
+    const dfloat r = add_accurate(g * dfloat(detail::LN2_1, detail::LN2_2), bl);      // (b E - n) ln2 + b log m
+    return detail::exp_scaled(r, static_cast<int>(n));
 }
-MPGOS_DF_HD dfloat pow(dfloat a, double b) { return dfloat(std::pow(static_cast<double>(a), b)); }
+MPGOS_DF_HD dfloat pow(dfloat a, double b) { return pow(a, dfloat(b)); }
+// integer powers by repeated squaring (|n| <= 64), others as above
 MPGOS_DF_HD dfloat pow(dfloat a, int n)
 {
-    return dfloat(std::pow(static_cast<double>(a), static_cast<double>(n)));
+    if (n < -64 || n > 64) return pow(a, dfloat(static_cast<float>(n)));
+    unsigned m = static_cast<unsigned>(n < 0 ? -n : n);
+    dfloat r(1.0f), base = a;
+    while (m != 0) {
+        if (m & 1u) r = r * base;
+        m >>= 1;
+        if (m != 0) base = base * base;
+    }
+    return n < 0 ? dfloat(1.0f) / r : r;
 }
 // sin and cos of one argument with one reduction
 MPGOS_DF_HD void sincos(dfloat a, dfloat* s, dfloat* c)

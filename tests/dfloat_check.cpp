@@ -76,9 +76,46 @@ int main()
             m_trig_small = std::fmax(m_trig_small, (double)std::fmax(std::fabs(val(mpgos::df::sin(x)) - std::sin(X)),
                                                                      std::fabs(val(mpgos::df::cos(x)) - std::cos(X))));
     }
+    // exp, log, pow: exp relative to 2^-48 (|x| + 1) (the argument's own
+    // precision carried through; results above 2^-100, where the low float
+    // is still normal), log relative to 2^-48 (|log a| + 1), pow relative to
+    // 2^-48 (|b log a| + 1)
+    double m_exp = 0, m_log = 0, m_pow = 0, m_powi = 0, m_fallback = 0;
+    std::uniform_real_distribution<double> ex(-69.0, 80.0), small(-1.0, 1.0), lg(-30.0, 30.0), pb(-6.0, 6.0);
+    for (int n = 0; n < 200000; n++) {
+        const dfloat x = dfloat(n % 2 ? ex(rng) : small(rng));
+        const long double X = val(x);
+        const long double ulp48 = std::ldexp(1.0L, -48);
+        m_exp = std::fmax(m_exp, (double)(std::fabs(val(mpgos::df::exp(x)) - std::exp(X)) / std::exp(X) /
+                                          (ulp48 * (std::fabs(X) + 1.0L))));
+        const dfloat a = dfloat(std::exp((double)lg(rng)) * (n % 3 ? 1.0 : 1.0 + 1e-3 * small(rng)));
+        const long double A = val(a);
+        m_log = std::fmax(m_log, (double)(std::fabs(val(mpgos::df::log(a)) - std::log(A)) /
+                                          (ulp48 * (std::fabs(std::log(A)) + 1.0L))));
+        const dfloat b = dfloat(pb(rng));
+        const long double B = val(b);
+        if (std::fabs(B * std::log(A)) < 69.0L) {
+            const long double P = std::pow(A, B);
+            m_pow = std::fmax(m_pow, (double)(std::fabs(val(mpgos::df::pow(a, b)) - P) / P /
+                                              (ulp48 * (std::fabs(B * std::log(A)) + 1.0L))));
+        }
+        const int k = n % 13 - 6;
+        const dfloat c = dfloat(0.5 + small(rng));
+        const long double Pc = std::pow(val(c), (long double)k);
+        m_powi = std::fmax(m_powi, (double)(std::fabs(val(mpgos::df::pow(c, k)) - Pc) / std::fabs(Pc)));
+    }
+    // arguments outside the FP32-pipe ranges take the FP64 path
+    for (double v : {-100.0, 85.0, 100.0}) {
+        const double got = (double)mpgos::df::exp(dfloat(v)), want = (double)dfloat(std::exp(v));
+        if (!(got == want || (std::isinf(got) && std::isinf(want)))) m_fallback = 1;
+    }
+    if (!std::isnan((double)mpgos::df::log(dfloat(-1.0))) || !std::isinf((double)mpgos::df::log(dfloat(0.0))))
+        m_fallback = 1;
+    if ((double)mpgos::df::pow(dfloat(-2.0), dfloat(3.0)) != -8.0) m_fallback = 1;
     std::printf("add %.3e\nmul %.3e\ndiv %.3e\nsqrt %.3e\ncvt %.3e\ncmp %.0f\nnorm %.3f\ntrig %.3f\ntrig_small %.3e\n"
-                "fma %.3e\ndot2 %.3e\nprod_sum %.3e\nprod_sum_axpy %.3e\n",
+                "fma %.3e\ndot2 %.3e\nprod_sum %.3e\nprod_sum_axpy %.3e\nexp %.3f\nlog %.3f\npow %.3f\n"
+                "pow_int %.3e\nfallback %.0f\n",
                 m_add, m_mul, m_div, m_sqrt, m_cvt, m_cmp, m_norm, m_trig, m_trig_small, m_fma, m_dot, m_psum,
-                m_paxpy);
+                m_paxpy, m_exp, m_log, m_pow, m_powi, m_fallback);
     return 0;
 }

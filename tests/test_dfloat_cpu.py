@@ -36,6 +36,16 @@ def test_double_float_sine_cosine(errors):
     assert errors["trig_small"] < 2e-14, errors["trig_small"]
 
 
+def test_double_float_exp_log_pow(errors):
+    # FP32-pipe exp / log / pow: within a few units of 2^-48 (|x| + 1), the
+    # precision the argument carries (x = the exponent, log a, b log a)
+    assert errors["exp"] < 2.5, errors["exp"]
+    assert errors["log"] < 3.0, errors["log"]
+    assert errors["pow"] < 10.0, errors["pow"]
+    assert errors["pow_int"] < 1e-13, errors["pow_int"]    # repeated squaring, |n| <= 6
+    assert errors["fallback"] == 0                           # out-of-range arguments: the FP64 functions
+
+
 def test_double_float_invariants(errors):
     assert errors["cmp"] == 0             # comparisons order like the exact values
     assert errors["norm"] <= 0.5          # |lo| <= ulp(hi) / 2 after every operation
