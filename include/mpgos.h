@@ -346,6 +346,17 @@ int mpgos_pt_solve_record_static(mpgos_pt_solver* solver, int32_t max_steps, int
  * FP64-pipe-bound kernels. */
 int mpgos_probe_fma_peak(int device, int32_t precision_bytes, double* flops_per_second);
 
+/* Double-float math probe (extension, for tests): evaluates one DF_STAGE
+ * operation with the device build of the double-float arithmetic on n
+ * argument pairs (host arrays a, b, each converted to double-float), writing
+ * the result's two floats as doubles to out[2i] (hi) and out[2i + 1] (lo). */
+enum mpgos_df_op {
+    MPGOS_DF_EXP = 0, MPGOS_DF_LOG = 1, MPGOS_DF_POW = 2, MPGOS_DF_SIN = 3, MPGOS_DF_COS = 4,
+    MPGOS_DF_SQRT = 5, MPGOS_DF_DIV = 6, MPGOS_DF_MUL = 7, MPGOS_DF_ADD = 8,
+    MPGOS_DF_POW_INT = 9  /* pow(a, (int)b) */
+};
+int mpgos_probe_df_math(int device, int32_t op, int64_t n, const double* a, const double* b, double* out);
+
 /* Thread-local message of the last failing call ("" if none). */
 const char* mpgos_last_error(void);
 

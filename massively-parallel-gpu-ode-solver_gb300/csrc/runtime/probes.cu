@@ -1,6 +1,9 @@
 // FMA-throughput probe (mpgos_probe_fma_peak in mpgos.h): the measured FP64
-// and FP32 peaks the per-thread kernels are measured against.
+// and FP32 peaks the per-thread kernels are measured against; and the
+// double-float math probe (mpgos_probe_df_math): the device build of the
+// DF_STAGE arithmetic evaluated on given arguments.
 #include "mpgos.h"
+#include "dfloat.cuh"
 
 #include <cuda_runtime.h>
 
@@ -55,7 +58,57 @@ cudaError_t run(int sms, double* flops)
     return e;
 }
 
+// one double-float operation per element; out[2i], out[2i+1] = hi, lo
+__global__ void df_math(int32_t op, long long n, const double* a, const double* b, double* out)
+{
+    using mpgos::df::dfloat;
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const dfloat x(a[i]), y(b[i]);
+        dfloat r;
+        switch (op) {
+            case MPGOS_DF_EXP: r = mpgos::df::exp(x); break;
+            case MPGOS_DF_LOG: r = mpgos::df::log(x); break;
+            case MPGOS_DF_POW: r = mpgos::df::pow(x, y); break;
+            case MPGOS_DF_SIN: r = mpgos::df::sin(x); break;
+            case MPGOS_DF_COS: r = mpgos::df::cos(x); break;
+            case MPGOS_DF_SQRT: r = mpgos::df::sqrt(x); break;
+            case MPGOS_DF_DIV: r = x / y; break;
+            case MPGOS_DF_MUL: r = x * y; break;
+            case MPGOS_DF_ADD: r = x + y; break;
+            default: r = mpgos::df::pow(x, static_cast<int>(b[i])); break;
+        }
+        out[2 * i]     = static_cast<double>(r.hi);
+        out[2 * i + 1] = static_cast<double>(r.lo);
+    }
+}
+
 }  // namespace
+
+MPGOS_EXPORT int mpgos_probe_df_math(int device, int32_t op, int64_t n, const double* a, const double* b,
+                                     double* out)
+{
+    if (n < 0 || op < MPGOS_DF_EXP || op > MPGOS_DF_POW_INT || (n > 0 && (a == nullptr || b == nullptr || out == nullptr)))
+        return MPGOS_ERR_ARGUMENT;
+    if (n == 0) return MPGOS_OK;
+    if (cudaSetDevice(device) != cudaSuccess) return MPGOS_ERR_CUDA;
+    const size_t bytes = static_cast<size_t>(n) * sizeof(double);
+    double *da = nullptr, *db = nullptr, *dout = nullptr;
+    cudaError_t e = cudaMalloc(&da, bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&db, bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&dout, 2 * bytes);
+    if (e == cudaSuccess) e = cudaMemcpy(da, a, bytes, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(db, b, bytes, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        const int blocks = static_cast<int>(n / 256 + 1 < 4096 ? n / 256 + 1 : 4096);
+        df_math<<<blocks, 256>>>(op, n, da, db, dout);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(out, dout, 2 * bytes, cudaMemcpyDeviceToHost);
+    for (double* p : {da, db, dout})
+        if (p) cudaFree(p);
+    return e == cudaSuccess ? MPGOS_OK : MPGOS_ERR_CUDA;
+}
 
 MPGOS_EXPORT int mpgos_probe_fma_peak(int device, int32_t precision_bytes, double* flops_per_second)
 {

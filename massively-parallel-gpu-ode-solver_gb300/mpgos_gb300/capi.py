@@ -207,6 +207,7 @@ def _declare(lib):
         "mpgos_pt_checkpoint_save": (C.c_int, [P]),
         "mpgos_pt_checkpoint_restore": (C.c_int, [P]),
         "mpgos_probe_fma_peak": (C.c_int, [C.c_int, i32, C.POINTER(C.c_double)]),
+        "mpgos_probe_df_math": (C.c_int, [C.c_int, i32, i64, P, P, P]),
         "mpgos_pt_solve_record": (C.c_int, [P, i32, i32]),
         "mpgos_pt_adjoint": (C.c_int, [P, P, P, P]),
         "mpgos_pt_tape_info": (C.c_int, [P, C.POINTER(Tape)]),
@@ -246,7 +247,7 @@ RUNTIME_SYMBOLS = (
     "mpgos_pt_sync_h2d", "mpgos_pt_sync_d2h", "mpgos_pt_solve", "mpgos_pt_solve_phases",
     "mpgos_pt_insert_sync_point", "mpgos_pt_sync_solver", "mpgos_pt_sync_device", "mpgos_pt_stream",
     "mpgos_pt_launch_config", "mpgos_pt_timer_start", "mpgos_pt_timer_stop", "mpgos_pt_autotune",
-    "mpgos_pt_checkpoint_save", "mpgos_pt_checkpoint_restore", "mpgos_probe_fma_peak",
+    "mpgos_pt_checkpoint_save", "mpgos_pt_checkpoint_restore", "mpgos_probe_fma_peak", "mpgos_probe_df_math",
     "mpgos_pt_solve_record", "mpgos_pt_adjoint", "mpgos_pt_tape_info", "mpgos_pt_solve_record_static",
     "mpgos_pt_dense_interpolate",
     "mpgos_cb_create", "mpgos_cb_destroy", "mpgos_cb_get_shape", "mpgos_cb_set_option", "mpgos_cb_host_buffer",
@@ -333,6 +334,21 @@ def loaded_library_paths() -> list:
         out.append(str(_build.runtime_lib()))
     out.extend(str(_build.system_lib(n)) for n in _plugins)
     return out
+
+
+DF_OPS = {"exp": 0, "log": 1, "pow": 2, "sin": 3, "cos": 4, "sqrt": 5, "div": 6, "mul": 7, "add": 8, "pow_int": 9}
+
+
+def df_math(op: str, a, b=None, device: int = 0):
+    """Device double-float evaluation (mpgos_probe_df_math): (hi, lo) arrays of
+    op(a, b) with a, b converted to double-float."""
+    import numpy as np
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    b = np.ascontiguousarray(np.zeros_like(a) if b is None else b, dtype=np.float64)
+    out = np.empty(2 * a.size, dtype=np.float64)
+    check(runtime().mpgos_probe_df_math(int(device), DF_OPS[op], a.size, a.ctypes.data, b.ctypes.data,
+                                        out.ctypes.data))
+    return out[0::2].copy(), out[1::2].copy()
 
 
 def fma_peak(device: int = 0, precision_bytes: int = 8) -> float:

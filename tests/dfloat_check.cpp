@@ -6,7 +6,10 @@
 // the result and the operands' magnitude, the bound of a "sloppy" add).
 #include <cmath>
 #include <cstdio>
+#include <cstdint>
 #include <random>
+#include <string>
+#include <vector>
 
 #include "dfloat.cuh"
 
@@ -14,8 +17,44 @@ using mpgos::df::dfloat;
 
 static long double val(dfloat a) { return (long double)a.hi + (long double)a.lo; }
 
-int main()
+// "eval" mode: read int32 op, int64 n, double a[n], double b[n] from stdin and
+// write op(dfloat(a), dfloat(b)) as n pairs of doubles (hi, lo) to stdout; the
+// same operation codes as mpgos_probe_df_math (the device build), so a test can
+// compare the two builds bit for bit.
+static int eval_mode()
 {
+    int32_t op = 0;
+    int64_t n = 0;
+    if (std::fread(&op, sizeof(op), 1, stdin) != 1 || std::fread(&n, sizeof(n), 1, stdin) != 1 || n < 0) return 2;
+    std::vector<double> a(n), b(n), out(2 * n);
+    if (std::fread(a.data(), sizeof(double), n, stdin) != (size_t)n ||
+        std::fread(b.data(), sizeof(double), n, stdin) != (size_t)n)
+        return 2;
+    for (int64_t i = 0; i < n; i++) {
+        const dfloat x(a[i]), y(b[i]);
+        dfloat r;
+        switch (op) {
+            case 0: r = mpgos::df::exp(x); break;
+            case 1: r = mpgos::df::log(x); break;
+            case 2: r = mpgos::df::pow(x, y); break;
+            case 3: r = mpgos::df::sin(x); break;
+            case 4: r = mpgos::df::cos(x); break;
+            case 5: r = mpgos::df::sqrt(x); break;
+            case 6: r = x / y; break;
+            case 7: r = x * y; break;
+            case 8: r = x + y; break;
+            default: r = mpgos::df::pow(x, static_cast<int>(b[i])); break;
+        }
+        out[2 * i] = r.hi;
+        out[2 * i + 1] = r.lo;
+    }
+    std::fwrite(out.data(), sizeof(double), out.size(), stdout);
+    return 0;
+}
+
+int main(int argc, char** argv)
+{
+    if (argc > 1 && std::string(argv[1]) == "eval") return eval_mode();
     std::mt19937_64 rng(12345);
     std::uniform_real_distribution<double> u(-1.0, 1.0), e(-8.0, 8.0);
     auto draw = [&]() { return dfloat(u(rng) * std::pow(2.0, std::floor(e(rng)))); };
