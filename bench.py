@@ -401,7 +401,8 @@ def rk4_leg(local: int, flush) -> dict:
             cfg = {}
             if not reference:
                 grid, blk, m = s.launch_config()
-                cfg = {"grid": grid, "block": blk, "mode": m}
+                cfg = {"grid": grid, "block": blk, "mode": m,
+                       "outline_rhs": int(s.GetOption(capi.Option.OutlineRhs))}
             times = []
             for i in range(3):
                 flush_l2(flush)
@@ -467,6 +468,7 @@ def uneven_leg(local: int, flush) -> dict:
             if tune:
                 s.autotune(arithmetic=mode & (capi.MODE_FAST_CONTROL | capi.MODE_DF_STAGE))
             grid, blk, m = s.launch_config() if not reference else (kern.grid, kern.block, -1)
+            outline = int(s.GetOption(capi.Option.OutlineRhs)) if not reference else 0
             times = []
             for i in range(3):
                 flush_l2(flush)
@@ -487,7 +489,7 @@ def uneven_leg(local: int, flush) -> dict:
         # accepted steps of all phases, counted by the system's own hook (integer accessory 1)
         steps = float(res["acci"][1].sum())
         return {"ms": statistics.median(times), "value": steps / (statistics.median(times) / 1e3),
-                "grid": grid, "block": blk, "mode": m}, res
+                "grid": grid, "block": blk, "mode": m, "outline_rhs": outline}, res
 
     FAST, DF, P = capi.MODE_FAST_CONTROL, capi.MODE_DF_STAGE, capi.MODE_PERSISTENT
     # static mappings with the reference's one-warp blocks (the best static shape for uneven

@@ -88,10 +88,15 @@ enum mpgos_option {
     MPGOS_KERNEL_MODE                  = 32, /* MPGOS_MODE_* bit set             */
     MPGOS_MAXIMUM_ATTEMPTS             = 33, /* step attempts per instance and launch */
     MPGOS_INSTANCES_PER_THREAD         = 34, /* static mapping: instances each lane integrates in turn (grid stride) */
-    MPGOS_WARP_RECONVERGE              = 35  /* 1: the integrating lanes of a warp reconverge once per step attempt
+    MPGOS_WARP_RECONVERGE              = 35, /* 1: the integrating lanes of a warp reconverge once per step attempt
                                                 (a warp ballot; pays where lanes diverge: events, uneven
                                                 accept/reject); 0: leave it to the compiler. Default 1 for
                                                 systems with events, else 0; the autotuner tries both. */
+    MPGOS_OUTLINE_RHS                  = 36  /* DF_STAGE: 1 = the right-hand side as one out-of-line function
+                                                (its code once in the kernel instead of once per stage; pays
+                                                for large right-hand sides that overflow the instruction
+                                                cache), 0 = inlined (default); results are identical. The
+                                                autotuner tries both for double-float kernels. */
 };
 
 /* ---- kernel modes (extensions) -----------------------------------------
@@ -274,8 +279,9 @@ int mpgos_pt_timer_stop(mpgos_pt_solver* solver, float* milliseconds);
 /* Autotuner (extension): times one Solve() per candidate (block size x
  * mapping: static with 1, 2 or 4 instances per thread, or persistent x
  * placement of the shared parameters: shared memory or global loads, where the
- * system has any; then the warp reconvergence ballot on and off at the best
- * of those) on a scratch copy of the current device state,
+ * system has any x, for double-float kernels, the right-hand side inlined or
+ * out of line; then the warp reconvergence ballot on and off at the best of
+ * those) on a scratch copy of the current device state,
  * restores the state, keeps the fastest configuration and, if cache_path is
  * not NULL, records it in a JSON cache keyed by system, shape, NT and GPU.
  * `arithmetic` fixes the arithmetic the candidates share: 0 the reference's,

@@ -77,6 +77,27 @@ struct DfStaged {
 };
 
 // Controller of DF_STAGE (see the file comment).
+// The system's right-hand side in double-float: inlined, or (OUTLINE, the
+// MODE_OUTLINE_RHS kernels) one out-of-line function whose code is in the
+// kernel once instead of once per stage. Large right-hand sides (the
+// Keller-Miksis system's pow, sin, cos and divisions in double-float)
+// inlined six times per step overflow the instruction cache, and the warps
+// then wait on instruction fetch more than on anything else; a call costs a
+// few instructions and the arrays it passes by address.
+template <int SD, class P>
+__device__ __noinline__ void df_rhs_outlined(int tid, int nt, P* F, P* X, P T, P* cp, P* sp, int* spi, P* acc,
+                                             int* acci)
+{
+    PerThread_OdeFunction(tid, nt, F, X, T, cp, sp, spi, acc, acci);
+}
+
+template <int SD, bool OUTLINE, class P>
+__device__ __forceinline__ void df_rhs(int tid, int nt, P* F, P* X, P T, P* cp, P* sp, int* spi, P* acc, int* acci)
+{
+    if constexpr (OUTLINE) df_rhs_outlined<SD, P>(tid, nt, F, X, T, cp, sp, spi, acc, acci);
+    else PerThread_OdeFunction(tid, nt, F, X, T, cp, sp, spi, acc, acci);
+}
+
 // Cash-Karp 4(5) step in double-float: the scheme of step_rkck45
 // (SingleSystem_PerThread_ExplicitRungeKutta_Steppers.cuh:121-289, same
 // coefficients and stage order). Each stage sum sum_j a_j k_j is accumulated
@@ -86,7 +107,7 @@ struct DfStaged {
 // delivered in FP32: it cancels down to ~tol of terms of size |k| dt, so its
 // double-float rounding is already ~1e-6 of it at tol 1e-10 and the FP32
 // rounding of the result (6e-8) adds nothing the controller could see.
-template <int SD>
+template <int SD, bool OUTLINE>
 __device__ __forceinline__ void step_rkck45_df(int tid, int nt, dfloat t, dfloat dt, dfloat* x, dfloat* xn,
                                                float* err, int& finite, dfloat* cp, dfloat* sp, int* spi,
                                                dfloat* acc, int* acci)
@@ -99,11 +120,11 @@ __device__ __forceinline__ void step_rkck45_df(int tid, int nt, dfloat t, dfloat
     dfloat X[SD];
     dfloat k1[SD], k2[SD], k3[SD], k4[SD], k5[SD], k6[SD];
 
-    PerThread_OdeFunction(tid, nt, k1, x, t, cp, sp, spi, acc, acci);
+    df_rhs<SD, OUTLINE>(tid, nt, k1, x, t, cp, sp, spi, acc, acci);
 
 #pragma unroll
     for (int i = 0; i < SD; i++) X[i] = prod_sum_axpy(dt, prod_sum_start(dfloat(1.0 / 5.0), k1[i]), x[i]);
-    PerThread_OdeFunction(tid, nt, k2, X, fma(dt, dfloat(1.0 / 5.0), t), cp, sp, spi, acc, acci);
+    df_rhs<SD, OUTLINE>(tid, nt, k2, X, fma(dt, dfloat(1.0 / 5.0), t), cp, sp, spi, acc, acci);
 
 #pragma unroll
     for (int i = 0; i < SD; i++) {
@@ -111,7 +132,7 @@ __device__ __forceinline__ void step_rkck45_df(int tid, int nt, dfloat t, dfloat
         prod_sum_add(s, dfloat(9.0 / 40.0), k2[i]);
         X[i] = prod_sum_axpy(dt, s, x[i]);
     }
-    PerThread_OdeFunction(tid, nt, k3, X, fma(dt, dfloat(3.0 / 10.0), t), cp, sp, spi, acc, acci);
+    df_rhs<SD, OUTLINE>(tid, nt, k3, X, fma(dt, dfloat(3.0 / 10.0), t), cp, sp, spi, acc, acci);
 
 #pragma unroll
     for (int i = 0; i < SD; i++) {
@@ -120,7 +141,7 @@ __device__ __forceinline__ void step_rkck45_df(int tid, int nt, dfloat t, dfloat
         prod_sum_add(s, dfloat(6.0 / 5.0), k3[i]);
         X[i] = prod_sum_axpy(dt, s, x[i]);
     }
-    PerThread_OdeFunction(tid, nt, k4, X, fma(dt, dfloat(3.0 / 5.0), t), cp, sp, spi, acc, acci);
+    df_rhs<SD, OUTLINE>(tid, nt, k4, X, fma(dt, dfloat(3.0 / 5.0), t), cp, sp, spi, acc, acci);
 
 #pragma unroll
     for (int i = 0; i < SD; i++) {
@@ -130,7 +151,7 @@ __device__ __forceinline__ void step_rkck45_df(int tid, int nt, dfloat t, dfloat
         prod_sum_add(s, dfloat(35.0 / 27.0), k4[i]);
         X[i] = prod_sum_axpy(dt, s, x[i]);
     }
-    PerThread_OdeFunction(tid, nt, k5, X, t + dt, cp, sp, spi, acc, acci);
+    df_rhs<SD, OUTLINE>(tid, nt, k5, X, t + dt, cp, sp, spi, acc, acci);
 
 #pragma unroll
     for (int i = 0; i < SD; i++) {
@@ -141,7 +162,7 @@ __device__ __forceinline__ void step_rkck45_df(int tid, int nt, dfloat t, dfloat
         prod_sum_add(s, dfloat(253.0 / 4096.0), k5[i]);
         X[i] = prod_sum_axpy(dt, s, x[i]);
     }
-    PerThread_OdeFunction(tid, nt, k6, X, fma(dt, dfloat(7.0 / 8.0), t), cp, sp, spi, acc, acci);
+    df_rhs<SD, OUTLINE>(tid, nt, k6, X, fma(dt, dfloat(7.0 / 8.0), t), cp, sp, spi, acc, acci);
 
 #pragma unroll
     for (int i = 0; i < SD; i++) {
@@ -170,7 +191,7 @@ __device__ __forceinline__ void step_rkck45_df(int tid, int nt, dfloat t, dfloat
 // estimate's own), factor 0.9 (tol/err)^(1/5 or 1/4) through FP32 log2/exp2.
 // Classic RK4 step in double-float (SingleSystem_PerThread_ExplicitRungeKutta_Steppers.cuh:6-117:
 // x + dt (k1 + 2 k2 + 2 k3 + k4) / 6), stage sums as unnormalised product sums.
-template <int SD>
+template <int SD, bool OUTLINE>
 __device__ __forceinline__ void step_rk4_df(int tid, int nt, dfloat t, dfloat dt, dfloat* x, dfloat* xn, int& finite,
                                             dfloat* cp, dfloat* sp, int* spi, dfloat* acc, int* acci)
 {
@@ -181,16 +202,16 @@ __device__ __forceinline__ void step_rk4_df(int tid, int nt, dfloat t, dfloat dt
     dfloat X[SD], k1[SD], k2[SD], k3[SD], k4[SD];
     const dfloat half(0.5);
     const dfloat th = df::fma(dt, half, t);
-    PerThread_OdeFunction(tid, nt, k1, x, t, cp, sp, spi, acc, acci);
+    df_rhs<SD, OUTLINE>(tid, nt, k1, x, t, cp, sp, spi, acc, acci);
 #pragma unroll
     for (int i = 0; i < SD; i++) X[i] = prod_sum_axpy(dt, prod_sum_start(half, k1[i]), x[i]);
-    PerThread_OdeFunction(tid, nt, k2, X, th, cp, sp, spi, acc, acci);
+    df_rhs<SD, OUTLINE>(tid, nt, k2, X, th, cp, sp, spi, acc, acci);
 #pragma unroll
     for (int i = 0; i < SD; i++) X[i] = prod_sum_axpy(dt, prod_sum_start(half, k2[i]), x[i]);
-    PerThread_OdeFunction(tid, nt, k3, X, th, cp, sp, spi, acc, acci);
+    df_rhs<SD, OUTLINE>(tid, nt, k3, X, th, cp, sp, spi, acc, acci);
 #pragma unroll
     for (int i = 0; i < SD; i++) X[i] = prod_sum_axpy(dt, prod_sum{k3[i].hi, k3[i].lo}, x[i]);
-    PerThread_OdeFunction(tid, nt, k4, X, t + dt, cp, sp, spi, acc, acci);
+    df_rhs<SD, OUTLINE>(tid, nt, k4, X, t + dt, cp, sp, spi, acc, acci);
 #pragma unroll
     for (int i = 0; i < SD; i++) {
         prod_sum s = prod_sum_start(dfloat(1.0 / 6.0), k1[i]);
@@ -264,6 +285,7 @@ struct DfSolver {
     static constexpr bool RK4 = (ALG == MPGOS_RK4);
     static constexpr bool PERSISTENT = (MODE & MPGOS_MODE_PERSISTENT) != 0;
     static constexpr bool RECORD = (MODE & MODE_RECORD) != 0;
+    static constexpr bool OUTLINE = (MODE & MODE_OUTLINE_RHS) != 0;
     using Inst = DfInstance<S>;
 
     __device__ static void begin(Inst& s, long long i, const Args<double>& a, const DfStaged<S>& g,
@@ -334,7 +356,7 @@ struct DfSolver {
                 end_reached = 1;
             }
             s.dt = dfloat(dt64);
-            step_rk4_df<SD>(ti, nti, s.t, s.dt, s.x, xn, finite, s.cp, g.sp, g.spi, s.acc, s.acci);
+            step_rk4_df<SD, OUTLINE>(ti, nti, s.t, s.dt, s.x, xn, finite, s.cp, g.sp, g.spi, s.acc, s.acci);
             if (finite == 0) {
                 s.terminate = 1;
                 s.status |= MPGOS_INSTANCE_NONFINITE;
@@ -348,7 +370,7 @@ struct DfSolver {
                 s.dt        = rem;
                 end_reached = 1;
             }
-            step_rkck45_df<SD>(ti, nti, s.t, s.dt, s.x, xn, err, finite, s.cp, g.sp, g.spi, s.acc, s.acci);
+            step_rkck45_df<SD, OUTLINE>(ti, nti, s.t, s.dt, s.x, xn, err, finite, s.cp, g.sp, g.spi, s.acc, s.acci);
             control_rkck45_df<SD>(o, s.dt, s.x, xn, err, g.rtol, g.atol, update, finite, s.terminate, s.new_dt,
                                   s.status);
         }
@@ -490,7 +512,7 @@ __global__ void __launch_bounds__(MPGOS_MAX_BLOCK) perthread_df_kernel(Args<doub
 
     const long long total = static_cast<long long>(gridDim.x) * blockDim.x;
     long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
-    using Next = Solver<S, MPGOS_RKCK45, double, MODE & ~MODE_RECONVERGE>;
+    using Next = Solver<S, MPGOS_RKCK45, double, MODE & ~(MODE_RECONVERGE | MODE_OUTLINE_RHS)>;
     if constexpr ((MODE & MODE_RECONVERGE) != 0) {
         // one ballot over the integrating lanes per iteration reconverges the
         // warp once per step attempt (as in perthread_kernel)

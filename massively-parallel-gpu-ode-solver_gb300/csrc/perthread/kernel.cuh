@@ -493,9 +493,12 @@ struct KernelTable {
                                  (DOUBLE ? MPGOS_MODE_DF_STAGE : 0);
 
     // Modes a table can run; the runtime only asks for these. MODE_RECONVERGE
-    // selects the twin of each kernel with the per-attempt warp ballot.
+    // selects the twin of each kernel with the per-attempt warp ballot,
+    // MODE_OUTLINE_RHS (double-float kernels only) the twin with the
+    // right-hand side out of line.
     static void* kernel_for(int mode)
     {
+        if (mode & MODE_OUTLINE_RHS) return kernel_for_outline(mode & ~MODE_OUTLINE_RHS);
         if (mode & MODE_RECONVERGE) return kernel_for_rc(mode & ~MODE_RECONVERGE);
         switch (mode) {
             case 0: return reinterpret_cast<void*>(&perthread_kernel<S, ALG, P, 0>);
@@ -518,6 +521,22 @@ struct KernelTable {
                 case MPGOS_MODE_DF_STAGE | MPGOS_MODE_PERSISTENT:
                     return reinterpret_cast<void*>(
                         &perthread_df_kernel<S, MPGOS_MODE_DF_STAGE | MPGOS_MODE_PERSISTENT, ALG>);
+                default: break;
+            }
+        }
+        return nullptr;
+    }
+
+    static void* kernel_for_outline(int mode)
+    {
+        if constexpr (DOUBLE) {
+            constexpr int O = MODE_OUTLINE_RHS, R = MODE_RECONVERGE, DF = MPGOS_MODE_DF_STAGE,
+                          PS = MPGOS_MODE_PERSISTENT;
+            switch (mode) {
+                case DF: return reinterpret_cast<void*>(&perthread_df_kernel<S, O | DF, ALG>);
+                case DF | PS: return reinterpret_cast<void*>(&perthread_df_kernel<S, O | DF | PS, ALG>);
+                case R | DF: return reinterpret_cast<void*>(&perthread_df_kernel<S, O | R | DF, ALG>);
+                case R | DF | PS: return reinterpret_cast<void*>(&perthread_df_kernel<S, O | R | DF | PS, ALG>);
                 default: break;
             }
         }

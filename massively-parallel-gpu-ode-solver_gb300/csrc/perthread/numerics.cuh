@@ -38,6 +38,9 @@ constexpr int MODE_RECORD = 8;
 // Internal mode bit of the per-thread kernels (MPGOS_WARP_RECONVERGE): the
 // integrating lanes of a warp reconverge once per step attempt.
 constexpr int MODE_RECONVERGE = 32;
+// Internal mode bit of the double-float kernels (MPGOS_OUTLINE_RHS): the
+// right-hand side is one out-of-line function instead of inlined per stage.
+constexpr int MODE_OUTLINE_RHS = 64;
 
 // Solver options in the kernel's precision (Struct_SolverOptions of
 // SingleSystem_PerThread_Interface.cuh:105-115 plus the extensions).

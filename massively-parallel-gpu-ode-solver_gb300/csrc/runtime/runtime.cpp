@@ -114,6 +114,7 @@ struct mpgos_pt_solver {
     int32_t prefer_shared = 1;
     int32_t ipt = 1;  // instances per thread of the static mapping
     int32_t reconverge = -1;  // MPGOS_WARP_RECONVERGE; -1: by the system (events: 1)
+    int32_t outline = 0;      // MPGOS_OUTLINE_RHS (double-float kernels)
     int32_t mode = MPGOS_MODE_PLAIN;
     int64_t max_attempts = 10000000;
     uint64_t generation = 1;  // bumped by every change that alters a launch
@@ -217,14 +218,21 @@ size_t dynamic_smem(const mpgos_pt_solver* s)
 }
 
 // Bit 32 of a launch mode selects the kernels with the per-attempt warp
-// ballot (MPGOS_WARP_RECONVERGE; plugin side: MODE_RECONVERGE).
+// ballot (MPGOS_WARP_RECONVERGE; plugin side: MODE_RECONVERGE), bit 64 the
+// double-float kernels with the right-hand side out of line
+// (MPGOS_OUTLINE_RHS; plugin side: MODE_OUTLINE_RHS).
 constexpr int32_t kModeReconverge = 32;
+constexpr int32_t kModeOutlineRhs = 64;
 
 int32_t effective_mode(const mpgos_pt_solver* s, int32_t mode)
 {
     int32_t m = mode & (s->shape.modes | MPGOS_MODE_PERSISTENT);
-    if (m & MPGOS_MODE_DF_STAGE) m = MPGOS_MODE_DF_STAGE | (m & MPGOS_MODE_PERSISTENT);
-    else if (m & MPGOS_MODE_FP32_STAGE) m |= MPGOS_MODE_FAST_CONTROL;  // compiled together
+    if (m & MPGOS_MODE_DF_STAGE) {
+        m = MPGOS_MODE_DF_STAGE | (m & MPGOS_MODE_PERSISTENT);
+        if (s->outline) m |= kModeOutlineRhs;
+    } else if (m & MPGOS_MODE_FP32_STAGE) {
+        m |= MPGOS_MODE_FAST_CONTROL;  // compiled together
+    }
     const bool rc = s->reconverge >= 0 ? s->reconverge != 0 : s->shape.ne > 0;
     return rc ? (m | kModeReconverge) : m;
 }
@@ -530,6 +538,10 @@ MPGOS_EXPORT int mpgos_pt_set_option(mpgos_pt_solver* s, int32_t option, int32_t
             if (value != 0.0 && value != 1.0) return fail(MPGOS_ERR_ARGUMENT, "WarpReconverge %g must be 0 or 1", value);
             s->reconverge = static_cast<int32_t>(value);
             break;
+        case MPGOS_OUTLINE_RHS:
+            if (value != 0.0 && value != 1.0) return fail(MPGOS_ERR_ARGUMENT, "OutlineRhs %g must be 0 or 1", value);
+            s->outline = static_cast<int32_t>(value);
+            break;
         default:
             return fail(MPGOS_ERR_ARGUMENT, "unknown solver option %d", option);
     }
@@ -570,6 +582,7 @@ MPGOS_EXPORT int mpgos_pt_get_option(const mpgos_pt_solver* s, int32_t option, i
         case MPGOS_MAXIMUM_ATTEMPTS: *value = (double)s->max_attempts; break;
         case MPGOS_INSTANCES_PER_THREAD: *value = s->ipt; break;
         case MPGOS_WARP_RECONVERGE: *value = s->reconverge >= 0 ? s->reconverge : (s->shape.ne > 0 ? 1 : 0); break;
+        case MPGOS_OUTLINE_RHS: *value = s->outline; break;
         default: return fail(MPGOS_ERR_ARGUMENT, "unknown solver option %d", option);
     }
     return MPGOS_OK;
@@ -800,15 +813,17 @@ MPGOS_EXPORT int mpgos_pt_autotune(mpgos_pt_solver* s, int32_t arithmetic, const
             const std::string tag = "\"" + json_escape(k) + "\"";
             size_t pos = line.find(tag);
             if (pos == std::string::npos) continue;
-            int b = 0, m = 0, n = 1, ps = s->prefer_shared, rv = s->reconverge;
+            int b = 0, m = 0, n = 1, ps = s->prefer_shared, rv = s->reconverge, ol = 0;
             const char* bp = std::strstr(line.c_str() + pos, "\"block\":");
             const char* mp = std::strstr(line.c_str() + pos, "\"mode\":");
             const char* np = std::strstr(line.c_str() + pos, "\"instances_per_thread\":");
             const char* pp = std::strstr(line.c_str() + pos, "\"prefer_shared\":");
             const char* rp = std::strstr(line.c_str() + pos, "\"reconverge\":");
+            const char* op = std::strstr(line.c_str() + pos, "\"outline_rhs\":");
             if (np) sscanf(np, "\"instances_per_thread\": %d", &n);
             if (pp) sscanf(pp, "\"prefer_shared\": %d", &ps);
             if (rp) sscanf(rp, "\"reconverge\": %d", &rv);
+            if (op) sscanf(op, "\"outline_rhs\": %d", &ol);
             if (bp && mp && sscanf(bp, "\"block\": %d", &b) == 1 && sscanf(mp, "\"mode\": %d", &m) == 1 && b >= 1 &&
                 b <= 256 && n >= 1 && n <= 64) {
                 s->block = b;
@@ -816,6 +831,7 @@ MPGOS_EXPORT int mpgos_pt_autotune(mpgos_pt_solver* s, int32_t arithmetic, const
                 s->ipt = n;
                 s->prefer_shared = ps ? 1 : 0;
                 s->reconverge = (rv == 0 || rv == 1) ? rv : -1;
+                s->outline = ol ? 1 : 0;
                 s->generation++;
                 return MPGOS_OK;
             }
@@ -876,26 +892,36 @@ MPGOS_EXPORT int mpgos_pt_autotune(mpgos_pt_solver* s, int32_t arithmetic, const
     const int blocks[] = {32, 64, 96, 128, 192, 256};
     const int ipts[] = {1, 2, 4, 0};  // 0: persistent
     const bool has_shared = (s->shape.nsp + s->shape.nisp) > 0;
-    for (int ps = has_shared ? 0 : keep_ps; ps <= (has_shared ? 1 : keep_ps); ps++) {
-        for (int n : ipts) {
-            for (int b : blocks) {
-                const int32_t m = base | (n == 0 ? MPGOS_MODE_PERSISTENT : 0);
-                s->ipt = n == 0 ? 1 : n;
-                s->prefer_shared = ps;
-                float t = 0.f;
-                if ((rc = time_one(m, b, &t))) break;
-                if (t < best) {
-                    best = t;
-                    best_block = b;
-                    best_mode = m;
-                    best_ipt = s->ipt;
-                    best_ps = ps;
+    // double-float kernels: every candidate with the right-hand side inlined
+    // and out of line (the best mapping differs between the two)
+    const int keep_ol = s->outline;
+    int best_ol = keep_ol;
+    const bool df_base = (effective_mode(s, base) & MPGOS_MODE_DF_STAGE) != 0;
+    for (int ol = df_base ? 0 : keep_ol; ol <= (df_base ? 1 : keep_ol) && !rc; ol++) {
+        s->outline = ol;
+        for (int ps = has_shared ? 0 : keep_ps; ps <= (has_shared ? 1 : keep_ps); ps++) {
+            for (int n : ipts) {
+                for (int b : blocks) {
+                    const int32_t m = base | (n == 0 ? MPGOS_MODE_PERSISTENT : 0);
+                    s->ipt = n == 0 ? 1 : n;
+                    s->prefer_shared = ps;
+                    float t = 0.f;
+                    if ((rc = time_one(m, b, &t))) break;
+                    if (t < best) {
+                        best = t;
+                        best_block = b;
+                        best_mode = m;
+                        best_ipt = s->ipt;
+                        best_ps = ps;
+                        best_ol = ol;
+                    }
                 }
+                if (rc) break;
             }
             if (rc) break;
         }
-        if (rc) break;
     }
+    s->outline = best_ol;
     // the warp reconvergence ballot, on and off, at the best configuration
     const int keep_rv = s->reconverge;
     const int cur_rv = keep_rv >= 0 ? keep_rv : (s->shape.ne > 0 ? 1 : 0);
@@ -910,6 +936,7 @@ MPGOS_EXPORT int mpgos_pt_autotune(mpgos_pt_solver* s, int32_t arithmetic, const
             best_rv = 1 - cur_rv;
         }
     }
+    s->outline = keep_ol;
     s->reconverge = keep_rv;
     s->ipt = keep_ipt;
     s->prefer_shared = keep_ps;
@@ -928,13 +955,15 @@ MPGOS_EXPORT int mpgos_pt_autotune(mpgos_pt_solver* s, int32_t arithmetic, const
     s->ipt = best_ipt;
     s->prefer_shared = best_ps;
     s->reconverge = best_rv;
+    s->outline = best_ol;
     s->generation++;
 
     if (cache_path != nullptr) {
         std::ofstream outf(cache_path, std::ios::app);
         if (outf) outf << "{\"" << json_escape(k) << "\": {\"block\": " << best_block << ", \"mode\": " << best_mode
                        << ", \"instances_per_thread\": " << best_ipt << ", \"prefer_shared\": " << best_ps
-                       << ", \"reconverge\": " << best_rv << ", \"ms\": " << best << "}}\n";
+                       << ", \"reconverge\": " << best_rv << ", \"outline_rhs\": " << best_ol << ", \"ms\": " << best
+                       << "}}\n";
     }
     return MPGOS_OK;
 }

@@ -65,6 +65,7 @@ class Option(IntEnum):
     MaximumAttempts = 33
     InstancesPerThread = 34
     WarpReconverge = 35
+    OutlineRhs = 36
 
 
 MODE_PLAIN = 0

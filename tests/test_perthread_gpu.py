@@ -368,6 +368,29 @@ def test_autotuner_explores_mapping_and_placement(native_libs, tmp_path):
     assert_bitwise(res, tuned)
 
 
+def test_autotuner_double_float_tries_outlined_right_hand_side(native_libs, tmp_path):
+    """For double-float kernels the autotuner also times the out-of-line
+    right-hand side; its choice is cached and restored, and the tuned launch
+    integrates the ensemble exactly as the inlined default does."""
+    from mpgos_gb300.capi import Option
+    case = W.keller_miksis_case(n_amp=16, n_freq=16, periods=2)
+    cache = tmp_path / "tune_df.json"
+    with W.load_solver(case, mode=capi.MODE_DF_STAGE) as s:
+        s.autotune(arithmetic=capi.MODE_DF_STAGE, cache_path=str(cache))
+        ol = int(s.GetOption(Option.OutlineRhs))
+        assert ol in (0, 1)
+        _, _, m = s.launch_config()
+        assert m & capi.MODE_DF_STAGE and bool(m & 64) == bool(ol)
+    assert '"outline_rhs"' in cache.read_text()
+    with W.load_solver(case, mode=capi.MODE_DF_STAGE) as s:
+        s.autotune(arithmetic=capi.MODE_DF_STAGE, cache_path=str(cache))
+        assert int(s.GetOption(Option.OutlineRhs)) == ol
+        for _ in range(case.phases):
+            s.Solve()
+        tuned = W.read_results(s)
+    assert_bitwise(W.run_gpu(case, mode=capi.MODE_DF_STAGE), tuned)
+
+
 def test_warp_reconvergence_is_scheduling_only(native_libs):
     """The per-attempt warp ballot only changes how lanes are scheduled:
     results are bit-identical with it on and off (events make lanes diverge
@@ -384,6 +407,32 @@ def test_warp_reconvergence_is_scheduling_only(native_libs):
                     s.Solve()
                 out.append(W.read_results(s))
         assert_bitwise(out[0], out[1])
+
+
+@pytest.mark.parametrize("system", ["keller_miksis", "lorenz", "duffing_rk4"])
+def test_outlined_right_hand_side_is_code_layout_only(system, native_libs):
+    """OutlineRhs (double-float kernels: the right-hand side as one
+    out-of-line function) changes only where the code sits: results are
+    bit-identical to the inlined kernels, static and persistent, with and
+    without the warp reconvergence ballot, RKCK45 and RK4."""
+    from mpgos_gb300.capi import Option
+    case = {"keller_miksis": lambda: W.keller_miksis_case(n_amp=8, n_freq=16, periods=2),
+            "lorenz": lambda: W.lorenz_case(nt=512),
+            "duffing_rk4": lambda: W.duffing_rk4_case(nt=256, periods=4)}[system]()
+    for mode in (capi.MODE_DF_STAGE, capi.MODE_DF_STAGE | capi.MODE_PERSISTENT):
+        for rv in (0, 1):
+            out = []
+            for ol in (0, 1):
+                with W.load_solver(case, mode=mode, block=64) as s:
+                    s.SolverOption(Option.WarpReconverge, rv)
+                    s.SolverOption(Option.OutlineRhs, ol)
+                    assert int(s.GetOption(Option.OutlineRhs)) == ol
+                    _, _, m = s.launch_config()
+                    assert bool(m & 64) == bool(ol)
+                    for _ in range(case.phases):
+                        s.Solve()
+                    out.append(W.read_results(s))
+            assert_bitwise(out[0], out[1])
 
 
 def test_config1_duffing_rk4_full_size(native_libs):
