@@ -384,6 +384,8 @@ def _main(argv=None) -> int:
     ap.add_argument("--mode", type=int, default=0, help="MPGOS_MODE_* bits")
     ap.add_argument("--block", type=int, default=128)
     ap.add_argument("--launches", type=int, default=1)
+    ap.add_argument("--outline", action="store_true",
+                    help="double-float kernels: the right-hand side out of line (MPGOS_OUTLINE_RHS)")
     ap.add_argument("--periods", type=int, default=None, help="forcing periods (duffing_param, duffing_rk4)")
     ap.add_argument("--adjoint", type=int, default=0, metavar="SEG",
                     help="after the launches: one recording pass and one reverse pass with checkpoints every SEG steps")
@@ -399,6 +401,9 @@ def _main(argv=None) -> int:
         case = duffing_rk4_case(nt=a.nt, **({"periods": a.periods} if a.periods else {}))
     from .solver import Variable
     with load_solver(case, mode=a.mode, block=a.block) as s:
+        if a.outline:
+            from .capi import Option
+            s.SolverOption(Option.OutlineRhs, 1)
         s.checkpoint_save()
         times = []
         for _ in range(a.launches):
