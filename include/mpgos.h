@@ -359,7 +359,8 @@ int mpgos_probe_fma_peak(int device, int32_t precision_bytes, double* flops_per_
 enum mpgos_df_op {
     MPGOS_DF_EXP = 0, MPGOS_DF_LOG = 1, MPGOS_DF_POW = 2, MPGOS_DF_SIN = 3, MPGOS_DF_COS = 4,
     MPGOS_DF_SQRT = 5, MPGOS_DF_DIV = 6, MPGOS_DF_MUL = 7, MPGOS_DF_ADD = 8,
-    MPGOS_DF_POW_INT = 9  /* pow(a, (int)b) */
+    MPGOS_DF_POW_INT = 9, /* pow(a, (int)b) */
+    MPGOS_DF_SINPI = 10, MPGOS_DF_COSPI = 11  /* the two results of sincospi(a) */
 };
 int mpgos_probe_df_math(int device, int32_t op, int64_t n, const double* a, const double* b, double* out);
 

@@ -533,26 +533,40 @@ MPGOS_DF_HD dfloat pow(dfloat a, int n)
     }
     return n < 0 ? dfloat(1.0f) / r : r;
 }
+namespace detail {
+// sin(r + q pi/2) and cos(r + q pi/2) from both kernels of r, selected without
+// branches (lanes of a warp in different quadrants do not diverge)
+MPGOS_DF_HD void sincos_quadrant(dfloat r, int q, dfloat* s, dfloat* c)
+{
+    const dfloat sk = sin_kernel(r), ck = cos_kernel(r);
+    const bool odd = (q & 1) != 0;
+    const dfloat ss = odd ? ck : sk, cc = odd ? sk : ck;
+    *s = (q & 2) != 0 ? -ss : ss;
+    *c = ((q + 1) & 2) != 0 ? -cc : cc;
+}
+}  // namespace detail
+
 // sin and cos of one argument with one reduction
 MPGOS_DF_HD void sincos(dfloat a, dfloat* s, dfloat* c)
 {
     int q;
     const dfloat r = detail::reduce_pio2(a, q);
-    const dfloat sk = detail::sin_kernel(r), ck = detail::cos_kernel(r);
-    switch (q) {
-        case 0: *s = sk; *c = ck; break;
-        case 1: *s = ck; *c = -sk; break;
-        case 2: *s = -sk; *c = -ck; break;
-        default: *s = -ck; *c = sk; break;
-    }
+    detail::sincos_quadrant(r, q, s, c);
 }
 
-// sin(pi a) and cos(pi a) with pi a formed in double-float
+// sin(pi a) and cos(pi a): a = k/2 + f with k the nearest integer to 2a and
+// |f| <= 1/4, f exact (a.hi - k/2 is exact by Sterbenz's lemma, the low part
+// joins by two_sum), then both kernels of pi f; no rounding grows with |a|.
 MPGOS_DF_HD void sincospi(dfloat a, dfloat* s, dfloat* c)
 {
-    const dfloat x = a * dfloat(0x1.921fb6p+1f, -0x1.777a5cp-24f);   // pi
-    *s = sin(x);
-    *c = cos(x);
+    if (!(std::fabs(a.hi) < 0x1p+22f)) {   // beyond, a is an integer or half-integer multiple
+        sincos(a * dfloat(0x1.921fb6p+1f, -0x1.777a5cp-24f), s, c);
+        return;
+    }
+    const float k = f_rint(f_mul(a.hi, 2.0f));
+    const dfloat f = two_sum(f_sub(a.hi, f_mul(k, 0.5f)), a.lo);
+    const dfloat r = f * dfloat(0x1.921fb6p+1f, -0x1.777a5cp-24f);   // pi
+    detail::sincos_quadrant(r, static_cast<int>(k) & 3, s, c);
 }
 
 }  // namespace df

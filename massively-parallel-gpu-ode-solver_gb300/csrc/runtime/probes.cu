@@ -76,6 +76,8 @@ __global__ void df_math(int32_t op, long long n, const double* a, const double* 
             case MPGOS_DF_DIV: r = x / y; break;
             case MPGOS_DF_MUL: r = x * y; break;
             case MPGOS_DF_ADD: r = x + y; break;
+            case MPGOS_DF_SINPI: { dfloat c; mpgos::df::sincospi(x, &r, &c); break; }
+            case MPGOS_DF_COSPI: { dfloat s; mpgos::df::sincospi(x, &s, &r); break; }
             default: r = mpgos::df::pow(x, static_cast<int>(b[i])); break;
         }
         out[2 * i]     = static_cast<double>(r.hi);
@@ -88,7 +90,7 @@ __global__ void df_math(int32_t op, long long n, const double* a, const double* 
 MPGOS_EXPORT int mpgos_probe_df_math(int device, int32_t op, int64_t n, const double* a, const double* b,
                                      double* out)
 {
-    if (n < 0 || op < MPGOS_DF_EXP || op > MPGOS_DF_POW_INT || (n > 0 && (a == nullptr || b == nullptr || out == nullptr)))
+    if (n < 0 || op < MPGOS_DF_EXP || op > MPGOS_DF_COSPI || (n > 0 && (a == nullptr || b == nullptr || out == nullptr)))
         return MPGOS_ERR_ARGUMENT;
     if (n == 0) return MPGOS_OK;
     if (cudaSetDevice(device) != cudaSuccess) return MPGOS_ERR_CUDA;

@@ -337,7 +337,8 @@ def loaded_library_paths() -> list:
     return out
 
 
-DF_OPS = {"exp": 0, "log": 1, "pow": 2, "sin": 3, "cos": 4, "sqrt": 5, "div": 6, "mul": 7, "add": 8, "pow_int": 9}
+DF_OPS = {"exp": 0, "log": 1, "pow": 2, "sin": 3, "cos": 4, "sqrt": 5, "div": 6, "mul": 7, "add": 8, "pow_int": 9,
+          "sinpi": 10, "cospi": 11}
 
 
 def df_math(op: str, a, b=None, device: int = 0):

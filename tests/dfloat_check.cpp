@@ -43,6 +43,8 @@ static int eval_mode()
             case 6: r = x / y; break;
             case 7: r = x * y; break;
             case 8: r = x + y; break;
+            case 10: { dfloat c; mpgos::df::sincospi(x, &r, &c); break; }
+            case 11: { dfloat s; mpgos::df::sincospi(x, &s, &r); break; }
             default: r = mpgos::df::pow(x, static_cast<int>(b[i])); break;
         }
         out[2 * i] = r.hi;
@@ -115,6 +117,22 @@ int main(int argc, char** argv)
             m_trig_small = std::fmax(m_trig_small, (double)std::fmax(std::fabs(val(mpgos::df::sin(x)) - std::sin(X)),
                                                                      std::fabs(val(mpgos::df::cos(x)) - std::cos(X))));
     }
+    // sincospi: absolute error (the reduction by halves is exact, so it does not grow with |x|)
+    double m_trigpi = 0;
+    const long double PI = std::acos(-1.0L);
+    for (int n = 0; n < 200000; n++) {
+        const dfloat x = dfloat(n % 2 ? wide(rng) : narrow(rng));
+        const long double X = val(x);
+        dfloat s, c;
+        mpgos::df::sincospi(x, &s, &c);
+        // reduce X exactly by halves before the long double sin/cos
+        const long double k = std::nearbyint(2.0L * X), f = X - 0.5L * k;
+        const int q = (int)std::fmod(std::fmod(k, 4.0L) + 4.0L, 4.0L);
+        const long double sf = std::sin(PI * f), cf = std::cos(PI * f);
+        const long double S = q == 0 ? sf : q == 1 ? cf : q == 2 ? -sf : -cf;
+        const long double C = q == 0 ? cf : q == 1 ? -sf : q == 2 ? -cf : sf;
+        m_trigpi = std::fmax(m_trigpi, (double)std::fmax(std::fabs(val(s) - S), std::fabs(val(c) - C)));
+    }
     // exp, log, pow: exp relative to 2^-48 (|x| + 1) (the argument's own
     // precision carried through; results above 2^-100, where the low float
     // is still normal), log relative to 2^-48 (|log a| + 1), pow relative to
@@ -153,8 +171,8 @@ int main(int argc, char** argv)
     if ((double)mpgos::df::pow(dfloat(-2.0), dfloat(3.0)) != -8.0) m_fallback = 1;
     std::printf("add %.3e\nmul %.3e\ndiv %.3e\nsqrt %.3e\ncvt %.3e\ncmp %.0f\nnorm %.3f\ntrig %.3f\ntrig_small %.3e\n"
                 "fma %.3e\ndot2 %.3e\nprod_sum %.3e\nprod_sum_axpy %.3e\nexp %.3f\nlog %.3f\npow %.3f\n"
-                "pow_int %.3e\nfallback %.0f\n",
+                "pow_int %.3e\nfallback %.0f\ntrigpi %.3e\n",
                 m_add, m_mul, m_div, m_sqrt, m_cvt, m_cmp, m_norm, m_trig, m_trig_small, m_fma, m_dot, m_psum,
-                m_paxpy, m_exp, m_log, m_pow, m_powi, m_fallback);
+                m_paxpy, m_exp, m_log, m_pow, m_powi, m_fallback, m_trigpi);
     return 0;
 }

@@ -34,6 +34,8 @@ def test_double_float_sine_cosine(errors):
     # precision (|x| 2^-48 + 2^-50) up to |x| = 2000, ~1e-14 absolute for |x| < 1
     assert errors["trig"] < 4.0, errors["trig"]
     assert errors["trig_small"] < 2e-14, errors["trig_small"]
+    # sincospi reduces by halves exactly: absolute error of the kernels alone, any |x| <= 2000
+    assert errors["trigpi"] < 2e-14, errors["trigpi"]
 
 
 def test_double_float_exp_log_pow(errors):

@@ -47,7 +47,7 @@ def _inputs(op, rng, n=50000):
         return np.exp(u(-30.0, 30.0, n)), np.zeros(n)
     if op == "pow":
         return np.exp(u(-3.0, 3.0, n)), u(-6.0, 6.0, n)
-    if op in ("sin", "cos"):
+    if op in ("sin", "cos", "sinpi", "cospi"):
         return np.where(np.arange(n) % 2 == 0, u(-2000.0, 2000.0, n), u(-1.0, 1.0, n)), np.zeros(n)
     if op == "sqrt":
         return np.exp(u(-20.0, 20.0, n)), np.zeros(n)

@@ -117,7 +117,22 @@ def test_gpu_matches_oracle(name, case, mode, native_libs, oracle_libs):
     assert_cpu_parity(res, ref, case, key=name, rel=_perturbation(mode), tol_rel=_tol_perturbation(mode),
                       int_slack=_int_slack(mode))
     _, stable = perturbation_spread(case, _perturbation(mode), name, _tol_perturbation(mode))
-    assert_ints_equal(res, ref, ("nacc", "nrej", "status"), stable, _int_slack(mode))
+    assert_ints_equal(res, ref, ("nacc", "nrej", "status"), stable, _int_slack(mode),
+                      fraction=_rejection_fraction(case, mode))
+
+
+def _rejection_fraction(case, mode):
+    """With events, most rejected steps are the secant refinements that land
+    each event inside its tolerance band, and whether one landing takes an
+    iteration more or fewer turns on the last bits of the event function
+    there. Double-float stages round those values differently from FP64, so
+    (Keller-Miksis, ~20 landings and 30-80 rejections per instance and two
+    periods, accepted steps and event counts equal) a rejection count moves
+    by a few: 5 % of it per instance, accepted steps and status at the
+    default bar."""
+    if MODES[mode] & capi.MODE_DF_STAGE and W.SHAPES[case.system][4] > 0:
+        return {"nrej": 0.05}
+    return None
 
 
 @pytest.mark.parametrize("fast", [0, 1, 16])
