@@ -124,6 +124,15 @@ enum mpgos_option {
  * relative on non-chaotic instances. Exclusive with FP32_STAGE; FAST_CONTROL
  * is implied. */
 #define MPGOS_MODE_DF_STAGE     16
+/* SPLIT: the precision split of the FP32-stage mode with double-float stages:
+ * the right-hand side (the user's hook instantiated for double-float) and the
+ * stage sums in double-float on the FP32 pipe; the state update
+ * x + dt * sum b_i k_i, the time, the step size, the error estimate and norm,
+ * the accept test, the step-size factor (to FP64 accuracy), the event
+ * functions, the secant step toward events, dense output and every other hook
+ * in FP64. RKCK45 and RK4 (RK4 on the reference's FP64 time grid). Exclusive
+ * with FP32_STAGE and DF_STAGE; FAST_CONTROL is implied. */
+#define MPGOS_MODE_SPLIT        128
 #define MPGOS_MODE_CHOSEN       (MPGOS_MODE_FAST_CONTROL | MPGOS_MODE_PERSISTENT)
 
 /* ---- per-instance status flags (MPGOS_STATUS), extensions --------------
@@ -136,6 +145,10 @@ enum mpgos_option {
 #define MPGOS_INSTANCE_EVENT_OMITTED    4  /* warning: event step below minimum     */
 #define MPGOS_INSTANCE_ATTEMPT_LIMIT    8  /* stopped: MPGOS_MAXIMUM_ATTEMPTS hit   */
 #define MPGOS_INSTANCE_TAPE_OVERFLOW   16  /* adjoint: more accepted steps than the tape holds */
+#define MPGOS_INSTANCE_RANGE           32  /* warning (DF_STAGE, SPLIT): a value the double-float
+                                              arithmetic holds left float's exponent range
+                                              (|v| >= 2^128 or 0 < |v| < 2^-126); it loses
+                                              precision or overflows there */
 
 /* ---- kernel table handed from a system plugin to the runtime ----------- */
 
@@ -285,8 +298,9 @@ int mpgos_pt_timer_stop(mpgos_pt_solver* solver, float* milliseconds);
  * restores the state, keeps the fastest configuration and, if cache_path is
  * not NULL, records it in a JSON cache keyed by system, shape, NT and GPU.
  * `arithmetic` fixes the arithmetic the candidates share: 0 the reference's,
- * MPGOS_MODE_DF_STAGE double-float stages, any other non-zero value
- * FAST_CONTROL (each where compiled, else the reference's). */
+ * MPGOS_MODE_SPLIT the precision split, MPGOS_MODE_DF_STAGE double-float
+ * stages, any other non-zero value FAST_CONTROL (each where compiled, else
+ * the reference's). */
 int mpgos_pt_autotune(mpgos_pt_solver* solver, int32_t arithmetic, const char* cache_path);
 
 /* Device-side checkpoint of every array a launch writes (time domain, state,
@@ -305,7 +319,9 @@ int mpgos_pt_checkpoint_restore(mpgos_pt_solver* solver);
  * FP64: dL_dxT [SD][NT] in, dL_dx0 [SD][NT] and dL_dp [NCP][NT] out; the
  * gradient of the discrete map with the recorded step sequence frozen.
  * Under MPGOS_MODE_DF_STAGE both passes compute in double-float (the tape
- * stays FP64: a double-float value is a double exactly); otherwise in FP64.
+ * stays FP64: a double-float value is a double exactly); under
+ * MPGOS_MODE_SPLIT the recording runs the split kernel and the reverse pass
+ * computes in double-float; otherwise both in FP64.
  * The reverse arithmetic follows the mode set when mpgos_pt_adjoint is
  * called, so an FP64 tape can be reversed in double-float.
  * Instances whose step count exceeded the tape get MPGOS_INSTANCE_TAPE_OVERFLOW
@@ -338,10 +354,16 @@ int mpgos_pt_dense_interpolate(mpgos_pt_solver* solver, const double* times, int
  * mpgos_pt_adjoint and mpgos_pt_tape_info then read this tape until the next
  * mpgos_pt_solve_record. There is one such array per device and process:
  * overlapping calls (two solvers, or a second call before the first's reverse
- * pass has finished on the stream) race on it. The first call on a device
- * looks up the array's address (cudaGetSymbolAddress, which loads the
- * runtime's device module), so make that first call before any stream
- * capture begins. */
+ * pass has finished on the stream) race on it. The array is reserved when
+ * the runtime's device module loads: mpgos_pt_create looks up its address
+ * (cudaGetSymbolAddress) on every device it creates a solver on, so the
+ * 16 MiB are taken at start-up, before a serving process's memory pool
+ * reserves the free HBM. The recording and reverse kernels load lazily at
+ * their first launch (CUDA's module loading takes a little device memory
+ * then), so make one warm-up call at start-up, before any stream capture;
+ * later calls take no device memory. The cached address belongs to the
+ * device's primary context: after cudaDeviceReset this entry point must not
+ * be used. */
 #define MPGOS_STATIC_TAPE_BYTES (16u * 1024u * 1024u)
 int mpgos_pt_solve_record_static(mpgos_pt_solver* solver, int32_t max_steps, int32_t segment);
 
@@ -355,12 +377,17 @@ int mpgos_probe_fma_peak(int device, int32_t precision_bytes, double* flops_per_
 /* Double-float math probe (extension, for tests): evaluates one DF_STAGE
  * operation with the device build of the double-float arithmetic on n
  * argument pairs (host arrays a, b, each converted to double-float), writing
- * the result's two floats as doubles to out[2i] (hi) and out[2i + 1] (lo). */
+ * the result's two floats as doubles to out[2i] (hi) and out[2i + 1] (lo).
+ * The SPLIT-mode operations take a and b as doubles: MPGOS_DF_SPLIT converts a
+ * to double-float on the integer pipe (hi, lo out); MPGOS_DF_ROOT5 / ROOT4
+ * give the split controller's (a / b)^(1/5) / (a / b)^(1/4) (FP32 estimate,
+ * FP64 correction) in out[2i] and 0 in out[2i + 1]. */
 enum mpgos_df_op {
     MPGOS_DF_EXP = 0, MPGOS_DF_LOG = 1, MPGOS_DF_POW = 2, MPGOS_DF_SIN = 3, MPGOS_DF_COS = 4,
     MPGOS_DF_SQRT = 5, MPGOS_DF_DIV = 6, MPGOS_DF_MUL = 7, MPGOS_DF_ADD = 8,
     MPGOS_DF_POW_INT = 9, /* pow(a, (int)b) */
-    MPGOS_DF_SINPI = 10, MPGOS_DF_COSPI = 11  /* the two results of sincospi(a) */
+    MPGOS_DF_SINPI = 10, MPGOS_DF_COSPI = 11,  /* the two results of sincospi(a) */
+    MPGOS_DF_SPLIT = 12, MPGOS_DF_ROOT5 = 13, MPGOS_DF_ROOT4 = 14
 };
 int mpgos_probe_df_math(int device, int32_t op, int64_t n, const double* a, const double* b, double* out);
 

@@ -535,11 +535,9 @@ struct AdjointTable {
     {
         if (tape == nullptr || tape->segment < 1 || tape->segment > MAX_SEG) return static_cast<int>(cudaErrorInvalidValue);
         void* fn = nullptr;
-        if (L->mode & MPGOS_MODE_DF_STAGE) {
-            if (L->mode & MPGOS_MODE_PERSISTENT)
-                fn = reinterpret_cast<void*>(&perthread_df_kernel<S, MODE_RECORD | MPGOS_MODE_DF_STAGE | 2, ALG>);
-            else
-                fn = reinterpret_cast<void*>(&perthread_df_kernel<S, MODE_RECORD | MPGOS_MODE_DF_STAGE, ALG>);
+        const int arith = L->mode & (MPGOS_MODE_DF_STAGE | MPGOS_MODE_SPLIT);
+        if (arith == MPGOS_MODE_DF_STAGE || arith == MPGOS_MODE_SPLIT) {
+            fn = double_float_kernel<S, ALG>(arith, MODE_RECORD | (L->mode & MPGOS_MODE_PERSISTENT));
         } else {
             switch (L->mode & (MPGOS_MODE_FAST_CONTROL | MPGOS_MODE_PERSISTENT)) {
                 case 0: fn = reinterpret_cast<void*>(&perthread_kernel<S, ALG, double, MODE_RECORD>); break;
@@ -562,9 +560,11 @@ struct AdjointTable {
         Args<double> a = make_args<double>(*L);
         Tape t = tape_of(*tape);
         void* params[] = {&a, &t, &dLdxT, &dLdx0, &dLdp};
-        // a DF_STAGE solver differentiates in double-float as well
-        void* fn = (L->mode & MPGOS_MODE_DF_STAGE) ? reinterpret_cast<void*>(&adjoint_kernel<S, ALG, dfloat>)
-                                                  : reinterpret_cast<void*>(&adjoint_kernel<S, ALG, double>);
+        // DF_STAGE and SPLIT solvers (double-float stages) differentiate in
+        // double-float as well
+        void* fn = (L->mode & (MPGOS_MODE_DF_STAGE | MPGOS_MODE_SPLIT))
+                       ? reinterpret_cast<void*>(&adjoint_kernel<S, ALG, dfloat>)
+                       : reinterpret_cast<void*>(&adjoint_kernel<S, ALG, double>);
         return static_cast<int>(cudaLaunchKernel(fn, dim3(grid), dim3(block), params, smem,
                                                  static_cast<cudaStream_t>(stream)));
     }

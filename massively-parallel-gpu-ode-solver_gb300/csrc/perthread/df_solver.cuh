@@ -23,10 +23,11 @@
 // states of non-chaotic instances by ~1e-13 relative and the embedded error
 // estimate by ~1e-6 relative, both far inside the 1e-9 parity bar. The
 // exponent range is float's (|values| within ~1e-38..3e38); systems whose
-// states or parameters leave it must not use this mode.
+// states or parameters leave it must not use this mode; an instance that
+// starts from such a value gets MPGOS_INSTANCE_RANGE.
 #pragma once
 
-#include "dfloat.cuh"
+#include "df_convert.cuh"
 
 namespace mpgos {
 namespace pt {
@@ -288,6 +289,29 @@ struct DfSolver {
     static constexpr bool OUTLINE = (MODE & MODE_OUTLINE_RHS) != 0;
     using Inst = DfInstance<S>;
 
+    // MPGOS_INSTANCE_RANGE when a value the instance starts from (time domain,
+    // time, state, control parameters, accessories, tolerances, event
+    // tolerances) lies outside float's exponent range, which double-float
+    // arithmetic keeps: there it would overflow or lose its low part.
+    __device__ static int range_status(long long i, const Args<double>& a)
+    {
+        const long long nt = a.nt;
+        bool ok = df::in_float_range(a.t[i]);
+#pragma unroll
+        for (int k = 0; k < 2; k++) ok = ok && df::in_float_range(a.td[i + k * nt]);
+#pragma unroll
+        for (int k = 0; k < SD; k++)
+            ok = ok && df::in_float_range(a.x[i + k * nt]) && df::in_float_range(a.rtol[k]) &&
+                 df::in_float_range(a.atol[k]);
+#pragma unroll
+        for (int k = 0; k < NCP; k++) ok = ok && df::in_float_range(a.cp[i + k * nt]);
+#pragma unroll
+        for (int k = 0; k < NA; k++) ok = ok && df::in_float_range(a.acc[i + k * nt]);
+#pragma unroll
+        for (int k = 0; k < NE; k++) ok = ok && df::in_float_range(a.etol[k]);
+        return ok ? 0 : MPGOS_INSTANCE_RANGE;
+    }
+
     __device__ static void begin(Inst& s, long long i, const Args<double>& a, const DfStaged<S>& g,
                                  const DfOptions& o)
     {
@@ -313,7 +337,7 @@ struct DfSolver {
         s.skipped    = 0;
         s.terminate  = 0;
         s.udt        = 0;
-        s.status     = 0;
+        s.status     = range_status(i, a);
         s.nacc       = 0;
         s.nrej       = 0;
         s.attempts   = 0;

@@ -425,6 +425,7 @@ __global__ void __launch_bounds__(MPGOS_MAX_BLOCK) perthread_kernel(Args<P> a)
 }  // namespace mpgos
 
 #include "df_solver.cuh"
+#include "split_solver.cuh"
 
 namespace mpgos {
 namespace pt {
@@ -484,13 +485,66 @@ using AdjointFn = int (*)(const mpgos_pt_launch*, const mpgos_pt_tape*, const do
 namespace mpgos {
 namespace pt {
 
+// The double-float kernels of one scheme and arithmetic (ARITH: DF_STAGE or
+// SPLIT) with their twins: persistent mapping (MPGOS_MODE_PERSISTENT), warp
+// reconvergence (MODE_RECONVERGE), out-of-line right-hand side
+// (MODE_OUTLINE_RHS) and the adjoint's recording pass (MODE_RECORD, static or
+// persistent). get() takes the mode without the ARITH bit.
+template <class S, int ALG, int ARITH>
+struct DfKernelSet {
+    template <int M>
+    static void* k()
+    {
+        if constexpr (ARITH == MPGOS_MODE_DF_STAGE)
+            return reinterpret_cast<void*>(&perthread_df_kernel<S, M | MPGOS_MODE_DF_STAGE, ALG>);
+        else
+            return reinterpret_cast<void*>(&perthread_split_kernel<S, M | MPGOS_MODE_SPLIT, ALG>);
+    }
+
+    static void* get(int mode)
+    {
+        constexpr int PS = MPGOS_MODE_PERSISTENT, R = MODE_RECONVERGE, O = MODE_OUTLINE_RHS, REC = MODE_RECORD;
+        switch (mode) {
+            case 0: return k<0>();
+            case PS: return k<PS>();
+            case R: return k<R>();
+            case R | PS: return k<R | PS>();
+            case O: return k<O>();
+            case O | PS: return k<O | PS>();
+            case O | R: return k<O | R>();
+            case O | R | PS: return k<O | R | PS>();
+            case REC: return k<REC>();
+            case REC | PS: return k<REC | PS>();
+            default: return nullptr;
+        }
+    }
+};
+
+#ifdef MPGOS_PLUGIN_PARTS
+// A system plugin built from several translation units compiles each
+// double-float kernel set in a unit of its own, in parallel; this dispatcher
+// (defined by the plugin's main unit, plugin_export.cuh) returns them.
+void* plugin_part_kernel(int arith, int alg, int mode);
+#endif
+
+template <class S, int ALG>
+void* double_float_kernel(int arith, int mode)
+{
+#ifdef MPGOS_PLUGIN_PARTS
+    return plugin_part_kernel(arith, ALG, mode);
+#else
+    return arith == MPGOS_MODE_DF_STAGE ? DfKernelSet<S, ALG, MPGOS_MODE_DF_STAGE>::get(mode)
+                                        : DfKernelSet<S, ALG, MPGOS_MODE_SPLIT>::get(mode);
+#endif
+}
+
 template <class S, int ALG, class P>
 struct KernelTable {
     static constexpr bool DOUBLE_ADAPTIVE = sizeof(P) == 8 && ALG == MPGOS_RKCK45;
-    static constexpr bool DOUBLE = sizeof(P) == 8;  // DF_STAGE: both schemes
+    static constexpr bool DOUBLE = sizeof(P) == 8;  // DF_STAGE and SPLIT: both schemes
     static constexpr int MODES = MPGOS_MODE_PERSISTENT |
                                  (DOUBLE_ADAPTIVE ? (MPGOS_MODE_FAST_CONTROL | MPGOS_MODE_FP32_STAGE) : 0) |
-                                 (DOUBLE ? MPGOS_MODE_DF_STAGE : 0);
+                                 (DOUBLE ? (MPGOS_MODE_DF_STAGE | MPGOS_MODE_SPLIT) : 0);
 
     // Modes a table can run; the runtime only asks for these. MODE_RECONVERGE
     // selects the twin of each kernel with the per-attempt warp ballot,
@@ -498,79 +552,34 @@ struct KernelTable {
     // right-hand side out of line.
     static void* kernel_for(int mode)
     {
-        if (mode & MODE_OUTLINE_RHS) return kernel_for_outline(mode & ~MODE_OUTLINE_RHS);
-        if (mode & MODE_RECONVERGE) return kernel_for_rc(mode & ~MODE_RECONVERGE);
+        if constexpr (DOUBLE) {
+            for (int arith : {MPGOS_MODE_DF_STAGE, MPGOS_MODE_SPLIT})
+                if (mode & arith) return double_float_kernel<S, ALG>(arith, mode & ~arith);
+        }
+        if (mode & MODE_OUTLINE_RHS) return nullptr;
+        const int R = mode & MODE_RECONVERGE;
+        mode &= ~MODE_RECONVERGE;
         switch (mode) {
-            case 0: return reinterpret_cast<void*>(&perthread_kernel<S, ALG, P, 0>);
-            case 2: return reinterpret_cast<void*>(&perthread_kernel<S, ALG, P, 2>);
+            case 0: return R ? fp<MODE_RECONVERGE>() : fp<0>();
+            case 2: return R ? fp<MODE_RECONVERGE | 2>() : fp<2>();
             default: break;
         }
         if constexpr (DOUBLE_ADAPTIVE) {
             switch (mode) {
-                case 1: return reinterpret_cast<void*>(&perthread_kernel<S, ALG, P, 1>);
-                case 3: return reinterpret_cast<void*>(&perthread_kernel<S, ALG, P, 3>);
-                case 5: return reinterpret_cast<void*>(&perthread_kernel<S, ALG, P, 5>);
-                case 7: return reinterpret_cast<void*>(&perthread_kernel<S, ALG, P, 7>);
-                default: break;
-            }
-        }
-        if constexpr (DOUBLE) {
-            switch (mode) {
-                case MPGOS_MODE_DF_STAGE:
-                    return reinterpret_cast<void*>(&perthread_df_kernel<S, MPGOS_MODE_DF_STAGE, ALG>);
-                case MPGOS_MODE_DF_STAGE | MPGOS_MODE_PERSISTENT:
-                    return reinterpret_cast<void*>(
-                        &perthread_df_kernel<S, MPGOS_MODE_DF_STAGE | MPGOS_MODE_PERSISTENT, ALG>);
+                case 1: return R ? fp<MODE_RECONVERGE | 1>() : fp<1>();
+                case 3: return R ? fp<MODE_RECONVERGE | 3>() : fp<3>();
+                case 5: return R ? fp<MODE_RECONVERGE | 5>() : fp<5>();
+                case 7: return R ? fp<MODE_RECONVERGE | 7>() : fp<7>();
                 default: break;
             }
         }
         return nullptr;
     }
 
-    static void* kernel_for_outline(int mode)
+    template <int M>
+    static void* fp()
     {
-        if constexpr (DOUBLE) {
-            constexpr int O = MODE_OUTLINE_RHS, R = MODE_RECONVERGE, DF = MPGOS_MODE_DF_STAGE,
-                          PS = MPGOS_MODE_PERSISTENT;
-            switch (mode) {
-                case DF: return reinterpret_cast<void*>(&perthread_df_kernel<S, O | DF, ALG>);
-                case DF | PS: return reinterpret_cast<void*>(&perthread_df_kernel<S, O | DF | PS, ALG>);
-                case R | DF: return reinterpret_cast<void*>(&perthread_df_kernel<S, O | R | DF, ALG>);
-                case R | DF | PS: return reinterpret_cast<void*>(&perthread_df_kernel<S, O | R | DF | PS, ALG>);
-                default: break;
-            }
-        }
-        return nullptr;
-    }
-
-    static void* kernel_for_rc(int mode)
-    {
-        constexpr int R = MODE_RECONVERGE;
-        switch (mode) {
-            case 0: return reinterpret_cast<void*>(&perthread_kernel<S, ALG, P, R>);
-            case 2: return reinterpret_cast<void*>(&perthread_kernel<S, ALG, P, R | 2>);
-            default: break;
-        }
-        if constexpr (DOUBLE_ADAPTIVE) {
-            switch (mode) {
-                case 1: return reinterpret_cast<void*>(&perthread_kernel<S, ALG, P, R | 1>);
-                case 3: return reinterpret_cast<void*>(&perthread_kernel<S, ALG, P, R | 3>);
-                case 5: return reinterpret_cast<void*>(&perthread_kernel<S, ALG, P, R | 5>);
-                case 7: return reinterpret_cast<void*>(&perthread_kernel<S, ALG, P, R | 7>);
-                default: break;
-            }
-        }
-        if constexpr (DOUBLE) {
-            switch (mode) {
-                case MPGOS_MODE_DF_STAGE:
-                    return reinterpret_cast<void*>(&perthread_df_kernel<S, R | MPGOS_MODE_DF_STAGE, ALG>);
-                case MPGOS_MODE_DF_STAGE | MPGOS_MODE_PERSISTENT:
-                    return reinterpret_cast<void*>(
-                        &perthread_df_kernel<S, R | MPGOS_MODE_DF_STAGE | MPGOS_MODE_PERSISTENT, ALG>);
-                default: break;
-            }
-        }
-        return nullptr;
+        return reinterpret_cast<void*>(&perthread_kernel<S, ALG, P, M>);
     }
 
     static int launch(const mpgos_pt_launch* L, int grid, int block, size_t smem, void* stream)

@@ -3,7 +3,7 @@
 // double-float math probe (mpgos_probe_df_math): the device build of the
 // DF_STAGE arithmetic evaluated on given arguments.
 #include "mpgos.h"
-#include "dfloat.cuh"
+#include "df_convert.cuh"
 
 #include <cuda_runtime.h>
 
@@ -64,6 +64,20 @@ __global__ void df_math(int32_t op, long long n, const double* a, const double* 
     using mpgos::df::dfloat;
     for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
          i += static_cast<long long>(gridDim.x) * blockDim.x) {
+        if (op >= MPGOS_DF_SPLIT) {
+            // SPLIT-mode operations on the doubles themselves
+            if (op == MPGOS_DF_SPLIT) {
+                const dfloat r = mpgos::df::split(a[i]);
+                out[2 * i]     = static_cast<double>(r.hi);
+                out[2 * i + 1] = static_cast<double>(r.lo);
+            } else {
+                const bool fifth = op == MPGOS_DF_ROOT5;
+                const float l    = mpgos::df::log2_estimate(a[i]) - mpgos::df::log2_estimate(b[i]);
+                out[2 * i]       = mpgos::df::root_refine(mpgos::df::root_estimate(l, fifth), a[i], b[i], fifth);
+                out[2 * i + 1]   = 0.0;
+            }
+            continue;
+        }
         const dfloat x(a[i]), y(b[i]);
         dfloat r;
         switch (op) {
@@ -90,7 +104,7 @@ __global__ void df_math(int32_t op, long long n, const double* a, const double* 
 MPGOS_EXPORT int mpgos_probe_df_math(int device, int32_t op, int64_t n, const double* a, const double* b,
                                      double* out)
 {
-    if (n < 0 || op < MPGOS_DF_EXP || op > MPGOS_DF_COSPI || (n > 0 && (a == nullptr || b == nullptr || out == nullptr)))
+    if (n < 0 || op < MPGOS_DF_EXP || op > MPGOS_DF_ROOT4 || (n > 0 && (a == nullptr || b == nullptr || out == nullptr)))
         return MPGOS_ERR_ARGUMENT;
     if (n == 0) return MPGOS_OK;
     if (cudaSetDevice(device) != cudaSuccess) return MPGOS_ERR_CUDA;

@@ -52,6 +52,10 @@ int fail(int code, const char* fmt, ...)
 
 constexpr int kVarCount = 64;
 
+// Device address of the static tape array on `device` (defined with the
+// array, near mpgos_pt_solve_record_static).
+int static_tape_base(int device, unsigned char** base);
+
 // Host and device copy of one SoA array.
 struct Buffer {
     void* host   = nullptr;
@@ -227,7 +231,10 @@ constexpr int32_t kModeOutlineRhs = 64;
 int32_t effective_mode(const mpgos_pt_solver* s, int32_t mode)
 {
     int32_t m = mode & (s->shape.modes | MPGOS_MODE_PERSISTENT);
-    if (m & MPGOS_MODE_DF_STAGE) {
+    if (m & MPGOS_MODE_SPLIT) {
+        m = MPGOS_MODE_SPLIT | (m & MPGOS_MODE_PERSISTENT);
+        if (s->outline) m |= kModeOutlineRhs;
+    } else if (m & MPGOS_MODE_DF_STAGE) {
         m = MPGOS_MODE_DF_STAGE | (m & MPGOS_MODE_PERSISTENT);
         if (s->outline) m |= kModeOutlineRhs;
     } else if (m & MPGOS_MODE_FP32_STAGE) {
@@ -334,6 +341,14 @@ MPGOS_EXPORT int mpgos_pt_create(const mpgos_pt_kernels* kernels, int64_t nt, in
     s->sm_count = prop.multiProcessorCount;
     s->gpu_name = prop.name;
     s->block = prop.warpSize;  // reference default: one warp (:343)
+    {
+        // the static tape of mpgos_pt_solve_record_static: its device module
+        // is loaded (and its array reserved) here, at solver creation, not at
+        // the first recording call
+        unsigned char* base = nullptr;
+        int rc0 = static_tape_base(device, &base);
+        if (rc0 != MPGOS_OK) return cleanup(rc0);
+    }
     if ((e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking)) != cudaSuccess ||
         (e = cudaEventCreateWithFlags(&s->sync_event, cudaEventDisableTiming)) != cudaSuccess ||
         (e = cudaEventCreate(&s->timer_begin)) != cudaSuccess || (e = cudaEventCreate(&s->timer_end)) != cudaSuccess)
@@ -507,7 +522,8 @@ MPGOS_EXPORT int mpgos_pt_set_option(mpgos_pt_solver* s, int32_t option, int32_t
             break;
         case MPGOS_KERNEL_MODE: {
             const int32_t m = static_cast<int32_t>(value);
-            if (m < 0 || m > 23 || (m & 8) || m != value)
+            if (m < 0 || (m & ~(MPGOS_MODE_FAST_CONTROL | MPGOS_MODE_PERSISTENT | MPGOS_MODE_FP32_STAGE |
+                                 MPGOS_MODE_DF_STAGE | MPGOS_MODE_SPLIT)) || m != value)
                 return fail(MPGOS_ERR_ARGUMENT, "kernel mode %g is not a set of MPGOS_MODE_* bits", value);
             // FAST_CONTROL only changes the adaptive FP64 controller and is a
             // no-op elsewhere; FP32_STAGE and DF_STAGE change the arithmetic
@@ -518,6 +534,10 @@ MPGOS_EXPORT int mpgos_pt_set_option(mpgos_pt_solver* s, int32_t option, int32_t
                 return fail(MPGOS_ERR_UNSUPPORTED, "DF_STAGE mode not compiled for this table (modes 0x%x)", s->shape.modes);
             if ((m & MPGOS_MODE_DF_STAGE) && (m & MPGOS_MODE_FP32_STAGE))
                 return fail(MPGOS_ERR_ARGUMENT, "DF_STAGE and FP32_STAGE are exclusive");
+            if ((m & MPGOS_MODE_SPLIT) && !(s->shape.modes & MPGOS_MODE_SPLIT))
+                return fail(MPGOS_ERR_UNSUPPORTED, "SPLIT mode not compiled for this table (modes 0x%x)", s->shape.modes);
+            if ((m & MPGOS_MODE_SPLIT) && (m & (MPGOS_MODE_DF_STAGE | MPGOS_MODE_FP32_STAGE)))
+                return fail(MPGOS_ERR_ARGUMENT, "SPLIT is exclusive with DF_STAGE and FP32_STAGE");
             s->mode = m;
             break;
         }
@@ -795,7 +815,9 @@ MPGOS_EXPORT int mpgos_pt_autotune(mpgos_pt_solver* s, int32_t arithmetic, const
     if (s->n_active <= 0) return MPGOS_OK;
     MPGOS_CUDA(cudaSetDevice(s->device));
     int32_t base = 0;
-    if ((arithmetic & MPGOS_MODE_DF_STAGE) && (s->shape.modes & MPGOS_MODE_DF_STAGE))
+    if ((arithmetic & MPGOS_MODE_SPLIT) && (s->shape.modes & MPGOS_MODE_SPLIT))
+        base = MPGOS_MODE_SPLIT;
+    else if ((arithmetic & MPGOS_MODE_DF_STAGE) && (s->shape.modes & MPGOS_MODE_DF_STAGE))
         base = MPGOS_MODE_DF_STAGE;
     else if (arithmetic && (s->shape.modes & MPGOS_MODE_FAST_CONTROL))
         base = MPGOS_MODE_FAST_CONTROL;
@@ -896,7 +918,7 @@ MPGOS_EXPORT int mpgos_pt_autotune(mpgos_pt_solver* s, int32_t arithmetic, const
     // and out of line (the best mapping differs between the two)
     const int keep_ol = s->outline;
     int best_ol = keep_ol;
-    const bool df_base = (effective_mode(s, base) & MPGOS_MODE_DF_STAGE) != 0;
+    const bool df_base = (effective_mode(s, base) & (MPGOS_MODE_DF_STAGE | MPGOS_MODE_SPLIT)) != 0;
     for (int ol = df_base ? 0 : keep_ol; ol <= (df_base ? 1 : keep_ol) && !rc; ol++) {
         s->outline = ol;
         for (int ps = has_shared ? 0 : keep_ps; ps <= (has_shared ? 1 : keep_ps); ps++) {
@@ -1019,6 +1041,9 @@ MPGOS_EXPORT int mpgos_pt_solve_record(mpgos_pt_solver* s, int32_t max_steps, in
         return fail(MPGOS_ERR_UNSUPPORTED, "system %s has no adjoint kernels compiled (FP64 only)", s->k->name);
     if (max_steps < 1 || segment < 1 || segment > 64)
         return fail(MPGOS_ERR_ARGUMENT, "tape: max_steps %d must be >= 1 and segment %d within 1..64", max_steps, segment);
+    // from here on the reverse pass reads this call's tape (or, if this call
+    // fails, none that a later static recording did not write)
+    s->use_static_tape = false;
     MPGOS_CUDA(cudaSetDevice(s->device));
     const size_t nt = static_cast<size_t>(s->nt), sd = static_cast<size_t>(s->shape.sd);
     const size_t nck = static_cast<size_t>(max_steps / segment + 1);
@@ -1041,7 +1066,8 @@ MPGOS_EXPORT int mpgos_pt_solve_record(mpgos_pt_solver* s, int32_t max_steps, in
         s->tape_bytes = b_dt + b_cx + b_ct + nt * 4;
     }
     if (s->n_active <= 0) return MPGOS_OK;
-    const int32_t m = effective_mode(s, s->mode) & (MPGOS_MODE_FAST_CONTROL | MPGOS_MODE_PERSISTENT | MPGOS_MODE_DF_STAGE);
+    const int32_t m = effective_mode(s, s->mode) & (MPGOS_MODE_FAST_CONTROL | MPGOS_MODE_PERSISTENT | MPGOS_MODE_DF_STAGE |
+                                                   MPGOS_MODE_SPLIT);
     int grid = 0;
     if ((rc = grid_for(s, m, s->block, &grid))) return rc;
     if (m & MPGOS_MODE_PERSISTENT) MPGOS_CUDA(cudaMemsetAsync(s->d_work, 0, sizeof(uint32_t), s->stream));
@@ -1049,7 +1075,6 @@ MPGOS_EXPORT int mpgos_pt_solve_record(mpgos_pt_solver* s, int32_t max_steps, in
     fill_launch(s, L, m);
     rc = s->k->launch_record(&L, &s->tape, grid, s->block, dynamic_smem(s), s->stream);
     if (rc != 0) return fail(MPGOS_ERR_CUDA, "recording launch failed: %s", cudaGetErrorString((cudaError_t)rc));
-    s->use_static_tape = false;
     return MPGOS_OK;
 }
 
@@ -1068,7 +1093,7 @@ MPGOS_EXPORT int mpgos_pt_adjoint(mpgos_pt_solver* s, const double* dLdxT, doubl
     const int64_t grid = (s->n_active + block - 1) / block;
     mpgos_pt_launch L;
     // the reverse pass computes in double-float when the solver does
-    fill_launch(s, L, effective_mode(s, s->mode) & MPGOS_MODE_DF_STAGE);
+    fill_launch(s, L, effective_mode(s, s->mode) & (MPGOS_MODE_DF_STAGE | MPGOS_MODE_SPLIT));
     rc = s->k->launch_adjoint(&L, &tape, dLdxT, dLdx0, dLdp, static_cast<int>(grid), block, dynamic_smem(s), s->stream);
     if (rc != 0) return fail(MPGOS_ERR_CUDA, "adjoint launch failed: %s", cudaGetErrorString((cudaError_t)rc));
     return MPGOS_OK;
@@ -1117,8 +1142,11 @@ void* g_static_tape_addr[kMaxDevices] = {};
 
 size_t align256(size_t b) { return (b + 255) / 256 * 256; }
 
-// Device address of g_static_tape on the current device (looked up once per
-// device; the lookup loads this library's device module on first use).
+// Device address of g_static_tape on the current device, looked up once per
+// device ordinal at the first solver creation on it (the lookup loads this
+// library's device module, which reserves the array). The cached address
+// belongs to the device's primary context: it is stale after
+// cudaDeviceReset, which the static entry point therefore does not support.
 int static_tape_base(int device, unsigned char** base)
 {
     if (device < 0 || device >= kMaxDevices) return fail(MPGOS_ERR_ARGUMENT, "device ordinal %d out of range", device);
@@ -1169,7 +1197,8 @@ MPGOS_EXPORT int mpgos_pt_solve_record_static(mpgos_pt_solver* s, int32_t max_st
     // step counts of instances this launch does not integrate read as zero
     MPGOS_CUDA(cudaMemsetAsync(t.n_steps, 0, nt * 4, s->stream));
     if (s->n_active <= 0) return MPGOS_OK;
-    const int32_t m = effective_mode(s, s->mode) & (MPGOS_MODE_FAST_CONTROL | MPGOS_MODE_PERSISTENT | MPGOS_MODE_DF_STAGE);
+    const int32_t m = effective_mode(s, s->mode) & (MPGOS_MODE_FAST_CONTROL | MPGOS_MODE_PERSISTENT | MPGOS_MODE_DF_STAGE |
+                                                   MPGOS_MODE_SPLIT);
     int grid = 0;
     if ((rc = grid_for(s, m, s->block, &grid))) return rc;
     if (m & MPGOS_MODE_PERSISTENT) MPGOS_CUDA(cudaMemsetAsync(s->d_work, 0, sizeof(uint32_t), s->stream));

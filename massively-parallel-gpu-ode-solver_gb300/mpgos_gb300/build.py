@@ -96,6 +96,15 @@ def build_runtime(force: bool = False) -> Path:
     return out
 
 
+# Per-thread system plugins are compiled as several translation units in
+# parallel (plugin_export.cuh, MPGOS_PLUGIN_PARTS): the main unit (tables, FP64
+# and float kernels, adjoint) and one unit per double-float kernel set,
+# (arithmetic, scheme) = DF_STAGE or SPLIT x RK4 or RKCK45, then linked.
+PART_SETS = [(16, 0), (16, 1), (128, 0), (128, 1)]
+
+_COMPILE_POOL = cf.ThreadPoolExecutor(max_workers=max(2, os.cpu_count() or 4))
+
+
 def build_system(name: str, force: bool = False, extra: list | None = None) -> Path:
     out = system_lib(name)
     src = SYSTEMS_DIR / f"{name}.cu"
@@ -103,8 +112,26 @@ def build_system(name: str, force: bool = False, extra: list | None = None) -> P
             *SYSTEMS_DIR.glob("*.cuh")]
     if not force and _newer(out, deps):
         return out
-    cmd = [nvcc_path(), *ARCH, *_common_flags(), *(extra or []), str(src), "-o", str(out)]
-    _run(cmd, f"libmpgos_{name}.so")
+    if "coupled_plugin_export.cuh" in src.read_text():
+        cmd = [nvcc_path(), *ARCH, *_common_flags(), *(extra or []), str(src), "-o", str(out)]
+        _run(cmd, f"libmpgos_{name}.so")
+        return out
+    objdir = BUILD_DIR / "obj"
+    objdir.mkdir(parents=True, exist_ok=True)
+    flags = [f for f in _common_flags() if f != "-shared"]
+    units = [("main", ["-DMPGOS_PLUGIN_PARTS"])] + [
+        (f"part{a}_{g}", ["-DMPGOS_PLUGIN_PARTS", f"-DMPGOS_PART_ARITH={a}", f"-DMPGOS_PART_ALG={g}"])
+        for a, g in PART_SETS]
+    futs, objs = [], []
+    for tag, defs in units:
+        obj = objdir / f"{name}.{tag}.o"
+        objs.append(obj)
+        cmd = [nvcc_path(), *ARCH, *flags, *defs, *(extra or []), "-c", str(src), "-o", str(obj)]
+        futs.append(_COMPILE_POOL.submit(_run, cmd, f"libmpgos_{name}.so ({tag})"))
+    for f in futs:
+        f.result()
+    cmd = [nvcc_path(), *ARCH, *_common_flags(), *(extra or []), *map(str, objs), "-o", str(out)]
+    _run(cmd, f"libmpgos_{name}.so (link)")
     return out
 
 

@@ -73,6 +73,7 @@ MODE_FAST_CONTROL = 1
 MODE_PERSISTENT = 2
 MODE_FP32_STAGE = 4
 MODE_DF_STAGE = 16
+MODE_SPLIT = 128
 MODE_CHOSEN = MODE_FAST_CONTROL | MODE_PERSISTENT
 
 INSTANCE_OK = 0
@@ -81,6 +82,7 @@ INSTANCE_MINIMUM_STEP = 2
 INSTANCE_EVENT_OMITTED = 4
 INSTANCE_ATTEMPT_LIMIT = 8
 INSTANCE_TAPE_OVERFLOW = 16
+INSTANCE_RANGE = 32
 
 ABI_VERSION = 1
 STATIC_TAPE_BYTES = 16 * 1024 * 1024  # MPGOS_STATIC_TAPE_BYTES of mpgos.h
@@ -338,7 +340,7 @@ def loaded_library_paths() -> list:
 
 
 DF_OPS = {"exp": 0, "log": 1, "pow": 2, "sin": 3, "cos": 4, "sqrt": 5, "div": 6, "mul": 7, "add": 8, "pow_int": 9,
-          "sinpi": 10, "cospi": 11}
+          "sinpi": 10, "cospi": 11, "split": 12, "root5": 13, "root4": 14}
 
 
 def df_math(op: str, a, b=None, device: int = 0):

@@ -245,7 +245,8 @@ class ProblemSolver:
 
     def autotune(self, fast_control: bool = True, cache_path: str | None = None, arithmetic: int | None = None):
         """Pick block size and mapping by timing; ``arithmetic`` (a MPGOS_MODE_*
-        value: 0, MODE_FAST_CONTROL or MODE_DF_STAGE) overrides ``fast_control``."""
+        value: 0, MODE_FAST_CONTROL, MODE_DF_STAGE or MODE_SPLIT) overrides
+        ``fast_control``."""
         arith = int(bool(fast_control)) if arithmetic is None else int(arithmetic)
         capi.check(self._lib.mpgos_pt_autotune(self._h, arith, cache_path.encode() if cache_path else None))
         return self.launch_config()

@@ -11,7 +11,7 @@
 #include <string>
 #include <vector>
 
-#include "dfloat.cuh"
+#include "df_convert.cuh"
 
 using mpgos::df::dfloat;
 
@@ -31,6 +31,12 @@ static int eval_mode()
         std::fread(b.data(), sizeof(double), n, stdin) != (size_t)n)
         return 2;
     for (int64_t i = 0; i < n; i++) {
+        if (op == 12) {   // the SPLIT mode's integer-pipe conversion of the double itself
+            const dfloat r = mpgos::df::split(a[i]);
+            out[2 * i] = r.hi;
+            out[2 * i + 1] = r.lo;
+            continue;
+        }
         const dfloat x(a[i]), y(b[i]);
         dfloat r;
         switch (op) {

@@ -51,3 +51,31 @@ def test_double_float_exp_log_pow(errors):
 def test_double_float_invariants(errors):
     assert errors["cmp"] == 0             # comparisons order like the exact values
     assert errors["norm"] <= 0.5          # |lo| <= ulp(hi) / 2 after every operation
+
+
+@pytest.fixture(scope="module")
+def conversions(tmp_path_factory):
+    exe = tmp_path_factory.mktemp("df_convert") / "df_convert_check"
+    subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", f"-I{HEADER_DIR}",
+                    str(REPO / "tests" / "df_convert_check.cpp"), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout
+    return {k: float(v) for k, v in (line.split() for line in out.strip().splitlines())}
+
+
+def test_integer_pipe_conversions(conversions):
+    """FP64 <-> double-float conversions of the precision split
+    (df_convert.cuh): widen is the exact float->double conversion, to_double
+    the nearest double to hi + lo, split keeps 47+ bits and normalises."""
+    assert conversions["widen_mismatches"] == 0
+    assert conversions["to_double_mismatches"] == 0
+    assert conversions["split_bound_violations"] == 0
+    assert conversions["split_max_rel_err"] <= 2.0 ** -47
+    assert conversions["split_unnormalised"] == 0
+    assert conversions["range_mismatches"] == 0
+
+
+def test_split_step_factor_is_fp64_accurate(conversions):
+    """0.9 R^(1/5) / R^(1/4) of the split controller: the FP32 estimate
+    corrected in FP64 lands within a few ulp of the exact root (CUDA's FP64
+    pow is specified to 2 ulp)."""
+    assert conversions["root_max_ulp"] <= 4.0, conversions["root_max_ulp"]

@@ -53,11 +53,15 @@ def _inputs(op, rng, n=50000):
         return np.exp(u(-20.0, 20.0, n)), np.zeros(n)
     if op == "pow_int":
         return u(0.5, 1.5, n), rng.integers(-6, 7, n).astype(np.float64)
+    if op == "split":   # doubles across float's range, both signs, plus the fallback's ranges
+        v = rng.choice([-1.0, 1.0], n) * (1.0 + u(0.0, 1.0, n)) * 2.0 ** rng.integers(-140, 140, n)
+        v[:8] = [0.0, -0.0, 1.0, 10.0, 1e-30, 3e38, 1e300, 1e-300]
+        return v, np.zeros(n)
     signs = rng.choice([-1.0, 1.0], (2, n))
     return signs[0] * u(0.5, 1.0, n) * 2.0 ** rng.integers(-8, 8, n), signs[1] * u(0.5, 1.0, n) * 2.0 ** rng.integers(-8, 8, n)
 
 
-@pytest.mark.parametrize("op", sorted(capi.DF_OPS))
+@pytest.mark.parametrize("op", sorted(k for k in capi.DF_OPS if not k.startswith("root")))
 def test_device_build_equals_host_build(op, host_eval, native_libs):
     a, b = _inputs(op, np.random.default_rng(7))
     dh, dl = capi.df_math(op, a, b)
@@ -92,3 +96,19 @@ def test_device_exp_log_pow_sin_cos_accuracy(native_libs):
     bound = np.abs(X) * ulp48 + np.longdouble(2.0) ** -50
     for op, f in (("sin", np.sin), ("cos", np.cos)):
         assert np.max(np.abs(value(op, x) - f(X)) / bound) < 4.0, op
+
+
+def test_device_split_step_factor_is_fp64_accurate(native_libs):
+    """The split controller's R^(1/5) and R^(1/4) on the device (FP32 log2 /
+    exp2 estimate on the MUFU unit, FP64 correction): within 4 ulp of the
+    exact root for ratios over twelve decades and errors over 60 binades."""
+    rng = np.random.default_rng(13)
+    n = 50000
+    err = (1.0 + rng.uniform(0.0, 1.0, n)) * 2.0 ** -rng.integers(0, 60, n)
+    tol = err * 10.0 ** rng.uniform(-6.0, 6.0, n)
+    for op, p in (("root5", 5), ("root4", 4)):
+        y, lo = capi.df_math(op, tol, err)
+        exact = (tol.astype(np.longdouble) / err.astype(np.longdouble)) ** (np.longdouble(1) / p)
+        ulp = np.spacing(exact.astype(np.float64)).astype(np.longdouble)
+        assert np.all(lo == 0.0)
+        assert float(np.max(np.abs(y.astype(np.longdouble) - exact) / ulp)) <= 4.0, op

@@ -24,7 +24,11 @@ from oracle import oracle as O, ref_gpu as R
 
 pytestmark = pytest.mark.gpu
 
-MODES = {"plain": 0, "fast": 1, "persistent": 2, "chosen": 3, "df": 16, "df_persistent": 18}
+MODES = {"plain": 0, "fast": 1, "persistent": 2, "chosen": 3, "df": 16, "df_persistent": 18, "split": 128,
+         "split_persistent": 130}
+# modes whose stage arithmetic is double-float (DF_STAGE, and SPLIT: double-float
+# right-hand side and stage sums, FP64 state, error norm and control)
+DF_STAGES = capi.MODE_DF_STAGE | capi.MODE_SPLIT
 
 
 def _ref_available(case):
@@ -69,15 +73,17 @@ def _perturbation(mode):
     legitimate GPU/CPU difference: one ulp of the initial state for the
     reference arithmetic, 1e-9 relative for FAST_CONTROL and DF_STAGE (whose
     step sizes differ by ~1e-7 relative, i.e. ~1e-11 of the local error, and
-    whose double-float stages round at ~4e-15)."""
-    return 1e-9 if MODES[mode] & (capi.MODE_FAST_CONTROL | capi.MODE_DF_STAGE) else 0.0
+    whose double-float stages round at ~4e-15; SPLIT's as well)."""
+    return 1e-9 if MODES[mode] & (capi.MODE_FAST_CONTROL | DF_STAGES) else 0.0
 
 
 def _tol_perturbation(mode):
     """FAST_CONTROL and DF_STAGE round the step-size factor in FP32 (~1e-7
     relative): the same step-grid shift as moving the tolerances by ~1e-6
-    relative."""
-    return 1e-6 if MODES[mode] & (capi.MODE_FAST_CONTROL | capi.MODE_DF_STAGE) else 0.0
+    relative. SPLIT forms the factor to FP64 accuracy, but its error estimate
+    carries the stages' double-float rounding, ~1e-6 of it at tol 1e-10: the
+    same shift."""
+    return 1e-6 if MODES[mode] & (capi.MODE_FAST_CONTROL | DF_STAGES) else 0.0
 
 
 def _int_slack(mode):
@@ -87,8 +93,9 @@ def _int_slack(mode):
     estimate at tol 1e-10 (FP64: ~5e-8). Accept/reject decisions within that
     band of the threshold flip; over thousands of steps per instance a step
     count may differ by one on a few percent of the instances (see
-    parity.assert_ints_equal), never by more."""
-    return 0.02 if MODES[mode] & capi.MODE_DF_STAGE else 0.0
+    parity.assert_ints_equal), never by more. SPLIT's estimate carries the
+    same rounding."""
+    return 0.02 if MODES[mode] & DF_STAGES else 0.0
 
 
 def _skip_unsupported(case, mode):
@@ -108,7 +115,7 @@ def test_gpu_matches_reference_golden(name, case, ref, mode, native_libs, oracle
 
 
 # ---- parity with the oracle ----------------------------------------------
-@pytest.mark.parametrize("mode", ["plain", "chosen", "df_persistent"], ids=str)
+@pytest.mark.parametrize("mode", ["plain", "chosen", "df_persistent", "split_persistent"], ids=str)
 @pytest.mark.parametrize("name,case", RANDOM, ids=lambda v: v if isinstance(v, str) else "")
 def test_gpu_matches_oracle(name, case, mode, native_libs, oracle_libs):
     _skip_unsupported(case, mode)
@@ -130,12 +137,12 @@ def _rejection_fraction(case, mode):
     periods, accepted steps and event counts equal) a rejection count moves
     by a few: 5 % of it per instance, accepted steps and status at the
     default bar."""
-    if MODES[mode] & capi.MODE_DF_STAGE and W.SHAPES[case.system][4] > 0:
+    if MODES[mode] & DF_STAGES and W.SHAPES[case.system][4] > 0:
         return {"nrej": 0.05}
     return None
 
 
-@pytest.mark.parametrize("fast", [0, 1, 16])
+@pytest.mark.parametrize("fast", [0, 1, 16, 128])
 def test_mapping_and_block_size_do_not_change_results(fast, native_libs):
     case = W.keller_miksis_case(n_amp=8, n_freq=32, periods=2)
     base = W.run_gpu(case, mode=fast, block=32)
@@ -144,7 +151,7 @@ def test_mapping_and_block_size_do_not_change_results(fast, native_libs):
     assert_bitwise(base, W.run_gpu(case, mode=fast | capi.MODE_PERSISTENT, block=128))
 
 
-@pytest.mark.parametrize("mode", [0, 3])
+@pytest.mark.parametrize("mode", [0, 3, capi.MODE_SPLIT])
 def test_graph_phases_equal_individual_solves(mode, native_libs):
     case = W.duffing_rk4_case(nt=1024, periods=16)
     a = W.run_gpu(case, mode=mode, graph=False)
@@ -221,6 +228,71 @@ def test_lorenz_full_size_df_stage(native_libs, oracle_libs):
     assert_ints_equal(got, ref, ("nacc", "acci"), calm, _int_slack("df"))
 
 
+def test_lorenz_full_size_split(native_libs, oracle_libs):
+    """2^20-instance Lorenz at 1e-10 in SPLIT (double-float right-hand side and
+    stage sums; FP64 state update, time, error norm, step-size control): the
+    headline form. 512 instances replayed through the FP64 oracle: every
+    instance whose end state the oracle itself keeps within 1e-10 under a
+    1e-13 relative perturbation of the initial state is within 1e-9 of it,
+    step counts equal up to the bounded accept/reject flips of the stages'
+    double-float rounding (_int_slack)."""
+    case = W.lorenz_case(nt=1 << 20)
+    sp = W.run_gpu(case, mode=capi.MODE_SPLIT | capi.MODE_PERSISTENT, block=128)
+    assert np.all(sp["t"] == 10.0) and np.all(sp["status"] == 0)
+    assert sp["acci"][0].sum() == sp["nacc"].sum()
+    idx = np.unique(np.concatenate([np.linspace(0, case.nt - 1, 448).astype(np.int64),
+                                    np.random.default_rng(1).integers(0, case.nt, 64)]))
+    sub = case.subset(idx)
+    ref = O.run_oracle(sub)
+    pert = sub.copy()
+    pert.arrays["x"] = pert.arrays["x"] * (1.0 + 1e-13)
+    moved = O.run_oracle(pert)
+    calm = scaled_close(moved["x"], ref["x"], 1e-10).all(axis=0)
+    assert calm.mean() > 0.95, calm.mean()
+    got = {k: v[..., idx] for k, v in sp.items() if np.ndim(v) and np.shape(v)[-1] == case.nt}
+    assert_close(got, ref, mask=calm, keys=("x", "t"), ints=False)
+    assert_ints_equal(got, ref, ("nacc", "acci"), calm, _int_slack("split"))
+
+
+@pytest.mark.parametrize("mode", [capi.MODE_DF_STAGE, capi.MODE_SPLIT])
+def test_double_float_modes_flag_values_outside_float_range(mode, native_libs):
+    """DF_STAGE and SPLIT compute with float's exponent range: an instance
+    that starts from a value outside it (a parameter of 1e40, a state
+    component of 1e-40) gets MPGOS_INSTANCE_RANGE, the others do not; the FP64
+    modes never set it."""
+    case = W.lorenz_case(nt=64, rho=(0.0, 13.9))
+    case.arrays["cp"][0, 3] = 1e40
+    case.arrays["x"][1, 7] = 1e-40
+    res = W.run_gpu(case, mode=mode)
+    flagged = (res["status"] & capi.INSTANCE_RANGE) != 0
+    assert flagged[3] and flagged[7]
+    assert not flagged[np.setdiff1d(np.arange(64), [3, 7])].any()
+    plain = W.run_gpu(case, mode=capi.MODE_PLAIN)
+    assert not np.any(plain["status"] & capi.INSTANCE_RANGE)
+
+
+@pytest.mark.parametrize("mode", [capi.MODE_DF_STAGE, capi.MODE_SPLIT])
+def test_double_float_static_and_persistent_agree(mode, native_libs):
+    case = W.keller_miksis_case(n_amp=8, n_freq=16, periods=2)
+    a = W.run_gpu(case, mode=mode, block=64)
+    b = W.run_gpu(case, mode=mode | capi.MODE_PERSISTENT, block=128)
+    assert_bitwise(a, b)
+
+
+def test_split_rk4_keeps_the_reference_time_grid(native_libs):
+    """SPLIT with the fixed-step RK4: stages in double-float, the state update
+    x + (dt/6)(k1 + 2 k2 + 2 k3 + k4) and the time in FP64 on the reference's
+    grid: step counts and end times are the reference kernel's exactly (PLAIN
+    is bit-identical to it), the states agree to ~1e-13."""
+    case = W.duffing_rk4_case(nt=1024, periods=8)
+    ref = W.run_gpu(case, mode=capi.MODE_PLAIN, graph=True)
+    res = W.run_gpu(case, mode=capi.MODE_SPLIT | capi.MODE_PERSISTENT, graph=True)
+    np.testing.assert_array_equal(res["acci"], ref["acci"])
+    np.testing.assert_array_equal(res["t"], ref["t"])
+    assert np.max(np.abs(res["x"] - ref["x"])) < 1e-11
+    assert np.max(np.abs(res["acc"] - ref["acc"])) < 1e-11
+
+
 def test_df_stage_static_and_persistent_agree(native_libs):
     case = W.keller_miksis_case(n_amp=8, n_freq=16, periods=2)
     a = W.run_gpu(case, mode=capi.MODE_DF_STAGE, block=64)
@@ -252,7 +324,7 @@ def scaled_rel(a, b):
     return np.max(np.abs(a - b) / (np.abs(b) + 1e-3 * scale), axis=0)
 
 
-@pytest.mark.parametrize("mode", [0, 3])
+@pytest.mark.parametrize("mode", [0, 3, capi.MODE_SPLIT])
 def test_status_flags_and_attempt_limit(mode, native_libs, oracle_libs):
     case = W.lorenz_case(nt=64)
     case.arrays["x"][0, 5] = np.nan
@@ -344,7 +416,7 @@ def test_instances_per_thread_is_a_mapping_only(ipt, native_libs):
     instance per lane, for the reference arithmetic and for DF_STAGE."""
     from mpgos_gb300.capi import Option
     case = W.keller_miksis_case(n_amp=8, n_freq=16, periods=2)
-    for mode in (capi.MODE_PLAIN, capi.MODE_DF_STAGE):
+    for mode in (capi.MODE_PLAIN, capi.MODE_DF_STAGE, capi.MODE_SPLIT):
         a = W.run_gpu(case, mode=mode, block=32)
         with W.load_solver(case, mode=mode, block=32) as s:
             s.SolverOption(Option.InstancesPerThread, ipt)
@@ -412,7 +484,8 @@ def test_warp_reconvergence_is_scheduling_only(native_libs):
     on this system, so both code paths run divergent warps)."""
     from mpgos_gb300.capi import Option
     case = W.keller_miksis_case(n_amp=8, n_freq=16, periods=2)
-    for mode in (capi.MODE_PLAIN, capi.MODE_CHOSEN, capi.MODE_DF_STAGE | capi.MODE_PERSISTENT):
+    for mode in (capi.MODE_PLAIN, capi.MODE_CHOSEN, capi.MODE_DF_STAGE | capi.MODE_PERSISTENT,
+                 capi.MODE_SPLIT | capi.MODE_PERSISTENT):
         out = []
         for rv in (0, 1):
             with W.load_solver(case, mode=mode, block=64) as s:
@@ -434,7 +507,8 @@ def test_outlined_right_hand_side_is_code_layout_only(system, native_libs):
     case = {"keller_miksis": lambda: W.keller_miksis_case(n_amp=8, n_freq=16, periods=2),
             "lorenz": lambda: W.lorenz_case(nt=512),
             "duffing_rk4": lambda: W.duffing_rk4_case(nt=256, periods=4)}[system]()
-    for mode in (capi.MODE_DF_STAGE, capi.MODE_DF_STAGE | capi.MODE_PERSISTENT):
+    for mode in (capi.MODE_DF_STAGE, capi.MODE_DF_STAGE | capi.MODE_PERSISTENT, capi.MODE_SPLIT,
+                 capi.MODE_SPLIT | capi.MODE_PERSISTENT):
         for rv in (0, 1):
             out = []
             for ol in (0, 1):

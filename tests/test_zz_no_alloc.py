@@ -5,8 +5,10 @@ cudaMalloc'd buffers.
 Collected last (file name) so that it runs both alone and after every other
 GPU test in one process. Two recordings in a row through each entry point,
 each followed by the reverse pass: tapes, end states and gradients must be
-bit-identical between the static-scratch and the allocating entry point, and
-an oversized tape must be refused with a clear error.
+bit-identical between the static-scratch and the allocating entry point, the
+second static recording and its reverse pass (after the first call has
+loaded the kernels) must leave the device's free memory unchanged, and an
+oversized tape must be refused with a clear error.
 """
 import numpy as np
 import pytest
@@ -23,6 +25,7 @@ MAX_STEPS, SEGMENT = 4096, 32
 def _two_calls(case, target, static: bool):
     import torch
     out = []
+    free = []   # device free bytes before and after each recording + reverse pass
     with W.load_solver(case, mode=0) as s:
         a = case.arrays
         g = torch.empty((s.SD, s.NT), dtype=torch.float64, device="cuda")
@@ -34,6 +37,8 @@ def _two_calls(case, target, static: bool):
             s.host(Variable.TimeDomain)[:] = a["td"]
             s.host(Variable.IntegerAccessories)[:] = a["acci"]
             s.SynchroniseFromHostToDevice(Variable.All)
+            s.SynchroniseDevice()
+            before = torch.cuda.mem_get_info()[0]
             (s.SolveRecordStatic if static else s.SolveRecord)(MAX_STEPS, SEGMENT)
             s.SynchroniseFromDeviceToHost(Variable.ActualState)
             s.SynchroniseDevice()
@@ -42,11 +47,12 @@ def _two_calls(case, target, static: bool):
             torch.cuda.synchronize()
             s.Adjoint(g.data_ptr(), gx0.data_ptr(), gcp.data_ptr())
             s.SynchroniseDevice()
+            free.append((before, torch.cuda.mem_get_info()[0]))
             t = s.tape_info()
             n = R.device_to_host(t.n_steps, (case.nt,), np.int32)
             dt = R.device_to_host(t.dt, (t.max_steps, case.nt), np.float64)
             out.append(dict(xT=xT, gx0=gx0.cpu().numpy(), gcp=gcp.cpu().numpy(), n=n, dt=dt,
-                            status=s.host(Variable.Status).copy()))
+                            status=s.host(Variable.Status).copy(), free=free[-1]))
     return out
 
 
@@ -64,6 +70,9 @@ def test_static_scratch_recording_matches_allocating_entry_point(native_libs):
     # the second call repeats the first
     for k in ("xT", "gx0", "gcp", "n"):
         assert np.array_equal(stat[0][k], stat[1][k]), k
+    # the second static recording and reverse pass took no device memory
+    before, after = stat[1]["free"]
+    assert before == after, f"free device memory changed by {before - after} bytes"
 
 
 def test_static_scratch_rejects_an_oversized_tape(native_libs):
