@@ -22,10 +22,16 @@ TEST INFRASTRUCTURE ONLY.
   - the reference's own coupled kernels (all four variants, picked from
   SPB, UPS and TPB as its Solve() does) built for sm_103a
   (ref_gpu_coupled_entry.cu).
+* ``oracle/_ref/ref_print_check`` - the reference's own Print /
+  WriteToFileGeneral (SingleSystem_PerThread_Interface.cuh:1083-1276) built
+  for the host (ref_print_entry.cpp), for the byte comparison of the text
+  files (tests/test_textout_cpu.py).
 * ``oracle/_ref/libref_cpu_<system>.so`` - the reference's own
   SourceCodes/SingleSystem_PerThread_Solver.cuh compiled for the CPU through
   ref_cpu_entry.cpp, straight from the reference checkout (MPGOS_REFERENCE_ROOT,
-  default /root/reference). Built only where that checkout exists; used to
+  else a checkout named ``reference`` beside this repository; elsewhere the
+  staged copy of its per-thread headers in the git-ignored baseline/_ref),
+  with OpenMP. Built only where those sources exist; used to
   pin the oracle and to generate tests/golden fixtures.
 
 Both use ``-ffp-contract=off`` so that no multiply-add is fused: built with the
@@ -43,7 +49,46 @@ REPO_ROOT = ORACLE_DIR.parent
 SYSTEMS_DIR = REPO_ROOT / "massively-parallel-gpu-ode-solver_gb300" / "systems"
 BUILD_DIR = ORACLE_DIR / "_build"
 REF_DIR = ORACLE_DIR / "_ref"
-REFERENCE_ROOT = Path(os.environ.get("MPGOS_REFERENCE_ROOT", "/root/reference"))
+# The reference's per-thread solver headers, staged by stage_reference_sources()
+# from a checkout into this git-ignored directory, which travels with the
+# working tree to machines without the checkout (the GPU host), so the
+# reference's CPU build can be made there for the CPU baseline.
+STAGED_ROOT = REPO_ROOT / "baseline" / "_ref"
+STAGED_HEADERS = ["MPGOS_Overloaded_MathFunction.cuh", "SingleSystem_PerThread_Solver.cuh",
+                  "SingleSystem_PerThread_DenseOutput.cuh", "SingleSystem_PerThread_ExplicitRungeKutta_Steppers.cuh",
+                  "SingleSystem_PerThread_ExplicitRungeKutta_ErrorControllers.cuh",
+                  "SingleSystem_PerThread_EventHandling.cuh", "SingleSystem_PerThread_Interface.cuh"]
+CHECKOUT_ROOT = Path(os.environ.get("MPGOS_REFERENCE_ROOT", str(REPO_ROOT.parent / "reference")))
+
+
+def _solver_header(root: Path) -> Path:
+    return root / "SourceCodes" / "SingleSystem_PerThread_Solver.cuh"
+
+
+# the checkout where it exists, else the staged headers (CPU builds only)
+REFERENCE_ROOT = CHECKOUT_ROOT if _solver_header(CHECKOUT_ROOT).exists() else STAGED_ROOT
+
+
+def full_checkout() -> bool:
+    """The reference checkout itself (not the staged copy) is present: the
+    GPU cubins and the coupled builds need it."""
+    return _solver_header(CHECKOUT_ROOT).exists()
+
+
+def stage_reference_sources() -> Path | None:
+    """Copy the reference's per-thread solver headers from the checkout into
+    baseline/_ref/SourceCodes (git-ignored), where they differ."""
+    if not full_checkout():
+        return None
+    import shutil
+    dst = STAGED_ROOT / "SourceCodes"
+    dst.mkdir(parents=True, exist_ok=True)
+    for name in STAGED_HEADERS:
+        src = CHECKOUT_ROOT / "SourceCodes" / name
+        out = dst / name
+        if not out.exists() or out.read_bytes() != src.read_bytes():
+            shutil.copyfile(src, out)
+    return dst
 
 SYSTEMS = ["lorenz", "duffing", "duffing_param", "duffing_param_sens", "duffing_events", "bouncing_ball",
            "keller_miksis"]
@@ -112,7 +157,7 @@ def ref_cb_cubin(system: str, algorithm: int, ns: int, tpb: int, spb: int, ndo: 
 
 def build_ref_gpu_coupled(system: str, algorithm: int, ns: int, tpb: int, spb: int, ndo: int,
                           force: bool = False) -> Path | None:
-    if not (REFERENCE_ROOT / "SourceCodes" / "CoupledSystmes_PerBlock_Solver.cuh").exists():
+    if not full_checkout():
         return None
     out = ref_cb_cubin(system, algorithm, ns, tpb, spb, ndo)
     src = ORACLE_DIR / "ref_gpu_coupled_entry.cu"
@@ -146,7 +191,7 @@ def ref_lib(system: str) -> Path:
 
 
 def reference_available() -> bool:
-    return (REFERENCE_ROOT / "SourceCodes" / "SingleSystem_PerThread_Solver.cuh").exists()
+    return _solver_header(REFERENCE_ROOT).exists()
 
 
 def _newer(out: Path, deps) -> bool:
@@ -182,10 +227,20 @@ def build_ref(system: str, force: bool = False) -> Path | None:
     hdr = SYSTEMS_DIR / f"{system}.cuh"
     if not force and _newer(out, [src, hdr, ORACLE_DIR / "host_shim.hpp", Path(__file__)]):
         return out
-    cmd = ["g++", *FLAGS, "-w", f"-I{ORACLE_DIR}", f"-I{SYSTEMS_DIR}", f"-I{REFERENCE_ROOT / 'SourceCodes'}",
-           f'-DMPGOS_SYSTEM_HEADER="{system}.cuh"', str(src), "-o", str(out)]
+    # -fno-extern-tls-init: the kernel's `extern __shared__` (thread_local here)
+    # array is statically initialised; no TLS init wrapper is needed or emitted
+    cmd = ["g++", *FLAGS, "-fopenmp", "-fno-extern-tls-init", "-w", f"-I{ORACLE_DIR}", f"-I{SYSTEMS_DIR}",
+           f"-I{REFERENCE_ROOT / 'SourceCodes'}", f'-DMPGOS_SYSTEM_HEADER="{system}.cuh"',
+           *([f"-DMPGOS_REF_NT_EXTRA={REF_CPU_NT_EXTRA[system]}"] if system in REF_CPU_NT_EXTRA else []),
+           str(src), "-o", str(out)]
     _run(cmd, out.name)
     return out
+
+
+# Extra ensemble sizes of the reference CPU build (RKCK45, no dense output):
+# the CPU-baseline samples of the 2^20 Lorenz ensemble (every 16th and every
+# 8th instance).
+REF_CPU_NT_EXTRA = {"lorenz": "X(65536) X(131072)"}
 
 
 # Reference GPU kernels built as cubins: (system, algorithm, NT, NDO). The
@@ -200,6 +255,7 @@ def build_ref(system: str, force: bool = False) -> Path | None:
 REF_GPU_EVENT_FIX = {"keller_miksis"}
 REF_GPU_KERNELS = [
     ("keller_miksis", 1, 64, 0), ("keller_miksis", 1, 256, 0), ("keller_miksis", 1, 65536, 0),
+    ("keller_miksis", 1, 1 << 18, 0),
     ("lorenz", 1, 256, 0), ("lorenz", 1, 1000, 0), ("lorenz", 0, 64, 0), ("lorenz", 1, 1 << 20, 0),
     ("duffing", 0, 64, 0), ("duffing", 0, 8192, 0),
     ("duffing_param", 1, 256, 0), ("duffing_param", 1, 1000, 0),
@@ -208,25 +264,37 @@ REF_GPU_KERNELS = [
 ]
 # Register caps of the reference's own makefiles (T2_Lorenz/makefile: 64).
 REF_GPU_RREG = {"lorenz": 64}
+# Launch-shape sweep of the reference kernel (the timing baselines): the
+# reference stages its tolerances and event options into shared memory with
+# no barrier before other warps read them (SingleSystem_PerThread_Solver.cuh:
+# 37-88), which is harmless only with one warp per block, its default. These
+# cubins are built from a temporary copy of the reference sources with one
+# __syncthreads() added after that staging (nothing else changed), so that
+# blocks of 64..256 threads read defined tolerances; (system, algorithm, NT,
+# NDO, register cap or None).
+REF_GPU_SYNC_KERNELS = [
+    ("lorenz", 1, 1 << 20, 0, None), ("lorenz", 1, 1 << 20, 0, 64),
+    ("keller_miksis", 1, 1 << 18, 0, None), ("duffing", 0, 8192, 0, None),
+]
 
 
-def ref_cubin(system: str, algorithm: int, nt: int, ndo: int, rreg: int | None = None) -> Path:
-    tag = f"_rr{rreg}" if rreg else ""
+def ref_cubin(system: str, algorithm: int, nt: int, ndo: int, rreg: int | None = None, sync: bool = False) -> Path:
+    tag = (f"_rr{rreg}" if rreg else "") + ("_sync" if sync else "")
     return REF_DIR / f"ref_gpu_{system}_{'rkck45' if algorithm else 'rk4'}_nt{nt}_ndo{ndo}{tag}.cubin"
 
 
 def build_ref_gpu(system: str, algorithm: int, nt: int, ndo: int, rreg: int | None = None,
-                  force: bool = False) -> Path | None:
-    if not reference_available():
+                  force: bool = False, sync: bool = False) -> Path | None:
+    if not full_checkout():
         return None
-    out = ref_cubin(system, algorithm, nt, ndo, rreg)
+    out = ref_cubin(system, algorithm, nt, ndo, rreg, sync)
     src = ORACLE_DIR / "ref_gpu_entry.cu"
     hdr = SYSTEMS_DIR / f"{system}.cuh"
     if not force and _newer(out, [src, hdr, ORACLE_DIR / "ref_types.hpp", Path(__file__)]):
         return out
     src_dir, tmp = REFERENCE_ROOT / "SourceCodes", None
-    if system in REF_GPU_EVENT_FIX:
-        tmp, src_dir = _event_fixed_sources()
+    if system in REF_GPU_EVENT_FIX or sync:
+        tmp, src_dir = _patched_sources(event_fix=system in REF_GPU_EVENT_FIX, barrier=sync)
         if src_dir is None:
             return None
     cmd = ["nvcc", "-cubin", "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17", "-lineinfo", "-w",
@@ -245,31 +313,76 @@ def build_ref_gpu(system: str, algorithm: int, nt: int, ndo: int, rreg: int | No
     return out
 
 
-def _event_fixed_sources():
-    """Copy the reference's SourceCodes to a temporary directory and change the
-    event-option staging condition of SingleSystem_PerThread_Solver.cuh from
-    `ltid < SD` to `ltid < NE` (the only change). Returns (temporary
-    directory, patched SourceCodes path), or (None, None) if the line is not
-    found as expected."""
+def _patched_sources(event_fix: bool, barrier: bool):
+    """Copy the reference's SourceCodes to a temporary directory and patch
+    SingleSystem_PerThread_Solver.cuh there: with ``event_fix`` the
+    event-option staging condition reads `ltid < NE` instead of `ltid < SD`;
+    with ``barrier`` one `__syncthreads();` goes in front of the per-instance
+    part of the kernel (`if (tid < ThreadConfiguration.NumberOfActiveThreads)`),
+    after the shared-memory staging, which every thread of a block reaches.
+    Nothing else changes. Returns (temporary directory, patched SourceCodes
+    path), or (None, None) if a line is not found exactly once."""
     import shutil
     import tempfile
-    tmp = Path(tempfile.mkdtemp(prefix="mpgos_ref_evfix_"))
+    tmp = Path(tempfile.mkdtemp(prefix="mpgos_ref_patch_"))
     dst = tmp / "SourceCodes"
     shutil.copytree(REFERENCE_ROOT / "SourceCodes", dst)
     f = dst / "SingleSystem_PerThread_Solver.cuh"
     lines = f.read_text().split("\n")
-    hits = [i for i, l in enumerate(lines) if l.strip() == "if ( ltid < SD)" and "EventTolerance" in "".join(lines[i:i + 4])]
-    if len(hits) != 1:
-        shutil.rmtree(tmp, ignore_errors=True)
-        return None, None
-    lines[hits[0]] = lines[hits[0]].replace("ltid < SD", "ltid < NE")
+    if event_fix:
+        hits = [i for i, l in enumerate(lines)
+                if l.strip() == "if ( ltid < SD)" and "EventTolerance" in "".join(lines[i:i + 4])]
+        if len(hits) != 1:
+            shutil.rmtree(tmp, ignore_errors=True)
+            return None, None
+        lines[hits[0]] = lines[hits[0]].replace("ltid < SD", "ltid < NE")
+    if barrier:
+        hits = [i for i, l in enumerate(lines) if l.strip() == "if (tid < ThreadConfiguration.NumberOfActiveThreads)"]
+        if len(hits) != 1:
+            shutil.rmtree(tmp, ignore_errors=True)
+            return None, None
+        lines.insert(hits[0], "\t__syncthreads();")
     f.write_text("\n".join(lines))
     return tmp, dst
+
+
+def ref_print_exe() -> Path:
+    return REF_DIR / "ref_print_check"
+
+
+def build_ref_print(force: bool = False) -> Path | None:
+    """The reference's WriteToFileGeneral and Print member definitions
+    (SingleSystem_PerThread_Interface.cuh:1083-1276), copied unchanged from
+    its header into oracle/_ref/ref_print_members.inc, compiled on the host
+    with ref_print_entry.cpp (which declares the class they belong to)."""
+    hdr = REFERENCE_ROOT / "SourceCodes" / "SingleSystem_PerThread_Interface.cuh"
+    if not hdr.exists():
+        return None
+    out = ref_print_exe()
+    src = ORACLE_DIR / "ref_print_entry.cpp"
+    if not force and _newer(out, [src, hdr, Path(__file__)]):
+        return out
+    lines = hdr.read_text().split("\n")
+    start = [i for i, l in enumerate(lines) if "::WriteToFileGeneral(std::string FileName" in l]
+    if len(start) != 1:
+        return None
+    first = start[0] - 2   # the two template lines of the definition
+    end = [i for i in range(first, len(lines)) if lines[i].strip().startswith("// SOLVE")]
+    if not end or not lines[first].startswith("template <int NT"):
+        return None
+    frag = "\n".join(lines[first:end[0]])
+    if "::Print(ListOfVariables Variable, int ThreadID)" not in frag:
+        return None
+    REF_DIR.mkdir(exist_ok=True)
+    (REF_DIR / "ref_print_members.inc").write_text(frag + "\n")
+    _run(["g++", "-O1", "-std=c++17", "-w", f"-I{REF_DIR}", str(src), "-o", str(out)], out.name)
+    return out
 
 
 def build_all(force: bool = False) -> dict:
     BUILD_DIR.mkdir(exist_ok=True)
     REF_DIR.mkdir(exist_ok=True)
+    stage_reference_sources()
     res = {}
     with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 4)) as ex:
         futs = {}
@@ -282,6 +395,9 @@ def build_all(force: bool = False) -> dict:
             futs[ex.submit(build_oracle_coupled, s, force, True)] = ("oracle_cb_fma", s)
         for k in REF_GPU_CB_KERNELS:
             futs[ex.submit(build_ref_gpu_coupled, *k, force)] = ("ref_gpu_cb", *k)
+        futs[ex.submit(build_ref_print, force)] = ("ref_print",)
+        for (s, alg, nt, ndo, rr) in REF_GPU_SYNC_KERNELS:
+            futs[ex.submit(build_ref_gpu, s, alg, nt, ndo, rr, force, True)] = ("ref_gpu_sync", s, alg, nt, ndo, rr)
         for (s, alg, nt, ndo) in REF_GPU_KERNELS:
             futs[ex.submit(build_ref_gpu, s, alg, nt, ndo, None, force)] = ("ref_gpu", s, alg, nt, ndo)
             if s in REF_GPU_RREG:

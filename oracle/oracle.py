@@ -49,6 +49,8 @@ def _ref(system: str):
         lib.ref_cpu_solve.argtypes = [
             C.c_int, C.c_longlong, C.c_longlong, C.c_int,
             _D, _D, _D, _D, _D, _I, _D, _I, _D, _D, _D, _I, _I, _D, _D, _D, C.c_int]
+        lib.ref_cpu_set_threads.restype = C.c_int
+        lib.ref_cpu_set_threads.argtypes = [C.c_int]
         _ref_libs[system] = lib
     return _ref_libs[system]
 
@@ -162,10 +164,17 @@ def time_oracle(case, threads: int = 0) -> float:
     return time.perf_counter() - t0
 
 
-def run_ref_cpu(case) -> dict:
+def ref_cpu_available(system: str) -> bool:
+    """The reference's CPU build can be made (checkout or staged headers)."""
+    return _b.reference_available()
+
+
+def run_ref_cpu(case, threads: int = 1) -> dict:
     """Integrate ``case`` with the reference's own kernel compiled for the CPU
-    (nt in {64, 256, 1024}, ndo in {0, 16})."""
+    (nt in {64, 256, 1024}, ndo in {0, 16}; Lorenz RKCK45 also 65536 and
+    131072), instances spread over ``threads`` host threads (0: all)."""
     lib = _ref(case.system)
+    lib.ref_cpu_set_threads(int(threads))
     a, tol, opt6 = _prepare(case)
     nt = case.nt
     n_active = case.n_active if case.n_active is not None else nt

@@ -20,7 +20,9 @@ size, SingleSystem_PerThread_Interface.cuh:343): the reference kernel stages
 tolerances and event options into shared memory from threads 0..SD-1 and
 reads them from every thread without a barrier
 (SingleSystem_PerThread_Solver.cuh:37-65), so with several warps per block the
-later warps can read the shared arrays before they are written.
+later warps can read the shared arrays before they are written. Larger blocks
+are launched only with the ``sync`` cubins, built with one barrier added
+after that staging (build_oracle.REF_GPU_SYNC_KERNELS).
 """
 from __future__ import annotations
 
@@ -89,15 +91,17 @@ def _ck(rc, what):
         raise RuntimeError(f"{what}: CUDA driver error {rc} ({s.value.decode() if s.value else '?'})")
 
 
-def available(system: str, algorithm: int, nt: int, ndo: int, rreg: int | None = None) -> bool:
-    return _b.ref_cubin(system, algorithm, nt, ndo, rreg).exists()
+def available(system: str, algorithm: int, nt: int, ndo: int, rreg: int | None = None, sync: bool = False) -> bool:
+    return _b.ref_cubin(system, algorithm, nt, ndo, rreg, sync).exists()
 
 
 class ReferenceKernel:
     """One loaded reference kernel (system, algorithm, NT, NDO)."""
 
-    def __init__(self, system: str, algorithm: int, nt: int, ndo: int = 0, rreg: int | None = None):
-        path = _b.ref_cubin(system, algorithm, nt, ndo, rreg)
+    def __init__(self, system: str, algorithm: int, nt: int, ndo: int = 0, rreg: int | None = None,
+                 sync: bool = False):
+        path = _b.ref_cubin(system, algorithm, nt, ndo, rreg, sync)
+        self.sync = sync
         if not path.exists():
             raise FileNotFoundError(f"{path} not built (needs the reference checkout at build time)")
         cu = _driver()
@@ -147,6 +151,8 @@ class ReferenceKernel:
         from mpgos_gb300.solver import Variable as V
         if solver.NT != self.nt or solver.NDO != self.ndo:
             raise ValueError("solver size does not match the compiled reference kernel")
+        if block > 32 and not self.sync:
+            raise ValueError("blocks of more than one warp need the cubin with the staging barrier (sync=True)")
         sd, ne = solver.SD, solver.NE
         pad = max(sd, ne, 1)
         tol = lambda v, dt: np.concatenate([np.asarray(v, dt), np.zeros(pad, dt)])[:pad]

@@ -1,8 +1,11 @@
 """The Print text formats: the C++ writers of the drop-in headers
 (include/mpgos/dropin_print.h, compiled here with g++) and the Python ones
-(mpgos_gb300.textout) produce byte-identical files for the same arrays, and
-spot checks of the reference's layout (width 18, precision 10, scientific;
-trailing commas in the coupled files; PADDING rows of a padded launch)."""
+(mpgos_gb300.textout) produce byte-identical files for the same arrays; the
+per-thread files are byte-identical to the ones the reference's own Print
+writes (its member functions compiled for the host from its header,
+oracle/ref_print_entry.cpp); and spot checks of the reference's layout
+(width 18, precision 10, scientific; trailing commas in the coupled files;
+PADDING rows of a padded launch)."""
 import shutil
 import subprocess
 from pathlib import Path
@@ -84,3 +87,21 @@ def test_reference_layout_spot_checks(cpp_files):
     assert dense[0] == "UnitParameters:" and "Time series:" in dense
     t = dense.index("Time series:")
     assert len(dense) - t - 2 == 4      # header line + 4 stored points of system 1
+
+
+def test_per_thread_files_match_the_reference_print(cpp_files, tmp_path):
+    """SingleSystem_PerThread_Interface.cuh:1083-1276 (the reference's
+    WriteToFileGeneral and Print, built for the host) against the drop-in
+    writers on the same arrays: the general layout for a double and an int
+    variable, and the dense-output file of one thread, byte for byte."""
+    import sys
+    sys.path.insert(0, str(REPO))
+    from oracle import build_oracle
+    exe = build_oracle.build_ref_print()
+    if exe is None:
+        pytest.skip("the reference's SingleSystem_PerThread_Interface.cuh is not available here")
+    subprocess.run([str(exe), str(tmp_path)], check=True)
+    pairs = {"ActualStateInSolverObject.txt": "general_double.txt",
+             "IntegerAccessoriesInSolverObject.txt": "general_int.txt", "DenseOutput_2.txt": "pt_dense.txt"}
+    for ref_name, ours in pairs.items():
+        assert (tmp_path / ref_name).read_bytes() == (cpp_files / ours).read_bytes(), ref_name
