@@ -2,28 +2,34 @@
 
 Workload (headline): Lorenz ensemble, 2^20 instances, rho = linspace(0, 21),
 initial state (10, 10, 10), adaptive Cash-Karp 4(5) at rtol = atol = 1e-10
-over t in [0, 10], FP64. One step = one integration of the whole ensemble
-from the initial state (one Solve() launch, after a device-side restore of
-the initial state). Metric: accepted instance-steps per second.
+over t in [0, 10]. One step = one integration of the whole ensemble from the
+initial state (one Solve() launch, after a device-side restore of the initial
+state). Metric: accepted instance-steps per second.
 
 Arms:
-  default           the GB300 kernels through the C-ABI, chosen form:
-                    DF_STAGE (double-float stage arithmetic on the FP32 pipe,
-                    log-domain step control) on the persistent work queue,
-                    launch shape autotuned. Measured in the same run and
-                    reported beside it: the FP64 FAST_CONTROL form ("fast_fp64"),
-                    the PLAIN form (reference arithmetic, static mapping,
-                    "plain") and the reference's own kernel built for sm_103a
-                    ("reference_gpu"); and the coupled configuration (rings of
-                    64 Duffing units) in DF_STAGE and FP64 beside the
-                    reference's coupled kernel ("coupled"), and the
-                    adjoint configuration's adjoint/forward time ratio
-                    ("adjoint").
-  --impl reference  the reference's CPU implementation of the path: the
-                    reference solver compiled for this host where its build
-                    exists (oracle/_ref), else the oracle port
-                    (oracle/oracle_perthread.cpp), OpenMP on all host cores,
-                    each step a bounded sample of the workload.
+  default           the GB300 kernels through the C-ABI, headline form SPLIT
+                    (the precision split: the right-hand side and the stage
+                    sums in double-float on the FP32 pipe; the state update,
+                    time, step size, error estimate and norm, accept test,
+                    step-size factor and events in FP64) on the persistent
+                    work queue, launch shape autotuned. Measured in the same
+                    run and reported beside it: the all-double-float form
+                    ("df_stage"), the FP64 FAST_CONTROL form ("fast_fp64"),
+                    the FP32-stage form, the PLAIN form (reference
+                    arithmetic, bit-identical to the reference kernel) and the
+                    reference's own kernel built for sm_103a at block sizes
+                    32..256 ("reference_gpu", the best shape divides); the
+                    parity of every form against the reference kernel on the
+                    perturbation-stable instances; and the other
+                    configurations: fixed-step Duffing RK4 ("rk4"), the
+                    Keller-Miksis grid ("uneven"), the coupled rings
+                    ("coupled") and the discrete adjoint ("adjoint").
+  --impl reference  the reference's CPU implementation of the path: its own
+                    solver kernel compiled for this host with OpenMP over all
+                    host cores where its sources are present (checkout or the
+                    staged copy in baseline/_ref), else the oracle port
+                    (oracle/oracle_perthread.cpp), each step a bounded sample
+                    of the workload.
 
 Timing: W untimed warm-up steps, then exactly K steps, each timed with CUDA
 events on the solver's stream; L2 (129 MB) is flushed before every step by
@@ -52,10 +58,13 @@ for p in (str(REPO), str(PKG)):
         sys.path.insert(0, p)
 
 WORKLOAD = "lorenz_rkck45_tol1e-10_t0-10_2^20"
-CHOSEN_MODE = 16 | 2   # MPGOS_MODE_DF_STAGE | MPGOS_MODE_PERSISTENT (the autotuner may drop persistence)
+SPLIT, DF, FAST, PERS = 128, 16, 1, 2          # MPGOS_MODE_SPLIT / DF_STAGE / FAST_CONTROL / PERSISTENT
+CHOSEN_MODE = SPLIT | PERS                     # the autotuner may drop persistence
 METRIC = "accepted instance-steps/s (Lorenz RKCK45, rtol=atol=1e-10, 2^20 instances)"
 UNIT = "instance-steps/s"
 NT = 1 << 20
+DTYPE = ("f64 state update, time, step size, error estimate/norm, accept test, step factor, events; "
+         "df64 (float pairs, ~48-bit) right-hand side and stage sums")
 
 # Algorithmic FP64 FLOP per RKCK45 step attempt of the Lorenz system
 # (1 add/sub/mul/div = 1 FLOP, an FMA = 2): six right-hand sides of 9 FLOP,
@@ -65,6 +74,14 @@ NT = 1 << 20
 # special-function evaluation, not as FLOP.
 FLOP_PER_ATTEMPT = 6 * 9 + 3 * 55 + 3 * 2
 
+# Perturbations that define the stable instances (the reference arithmetic's
+# own sensitivity, measured with the PLAIN kernel, bit-identical to the
+# reference kernel): initial state moved by 1e-13 relative (end states), and
+# that plus tolerances moved by +-1e-6 relative (integer outputs: the
+# double-float stage rounding moves each error estimate by ~1e-6 of itself at
+# tol 1e-10, the same step-grid shift).
+X_REL, TOL_REL = 1e-13, 1e-6
+
 
 def parse():
     ap = argparse.ArgumentParser()
@@ -73,12 +90,14 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--nt", type=int, default=NT, help="instances per GPU (default 2^20)")
-    ap.add_argument("--no-plain", action="store_true", help="skip the PLAIN-form measurement")
+    ap.add_argument("--no-plain", action="store_true", help="skip the PLAIN / reference-kernel / parity legs")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--no-coupled", action="store_true", help="skip the coupled-configuration leg")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint-configuration leg")
     ap.add_argument("--no-uneven", action="store_true", help="skip the uneven (Keller-Miksis) leg")
     ap.add_argument("--no-rk4", action="store_true", help="skip the fixed-step (Duffing RK4) leg")
+    ap.add_argument("--uneven-periods", type=int, default=16, help="Keller-Miksis acoustic periods (config: 1024)")
+    ap.add_argument("--coupled-periods", type=int, default=16, help="coupled forcing periods (config: 256)")
     return ap.parse_args()
 
 
@@ -184,55 +203,61 @@ def load_peaks() -> dict:
 
 
 def load_traffic() -> dict:
-    """Per-launch DRAM bytes of the dominant kernel from the committed ncu summary."""
+    """Per-attempt instruction counts and per-launch DRAM bytes of the
+    dominant kernels from the committed ncu summaries."""
     p = REPO / "profiles" / "roofline_traffic.json"
     return json.loads(p.read_text()) if p.exists() else {}
 
 
+def flush_l2(buf):
+    buf.fill_(1)
+
+
+# ---- the CPU baseline ----------------------------------------------------------
 def cpu_sample_case(nt: int, stride: int):
     from mpgos_gb300 import workloads as W
     full = W.lorenz_case(nt=nt)
     return full.subset(np.arange(0, nt, stride))
 
 
-def cpu_baseline(nt: int, stride: int = 8):
-    """Oracle port (OpenMP, all host cores) on every stride-th instance; the
-    baseline line, the oracle's results and the sampled case."""
+def cpu_runner(kind_wanted: str = "reference"):
+    """(kind, run(case, threads), threads): the reference's own solver built
+    for the host with OpenMP where its sources exist, else the oracle port."""
     from oracle import oracle as O
+    threads = os.cpu_count() or 1
+    if kind_wanted == "reference" and O.ref_cpu_available("lorenz"):
+        try:
+            O.run_ref_cpu(cpu_sample_case(1 << 20, 1 << 14), threads=1)   # build / load
+            return "reference", (lambda c, th: O.run_ref_cpu(c, threads=th)), threads
+        except (FileNotFoundError, RuntimeError, OSError):
+            pass
+    return "port", (lambda c, th: O.run_oracle(c, threads=th)), O.max_threads("lorenz")
+
+
+def cpu_baseline(nt: int, stride: int = 8):
+    """The CPU implementations on every stride-th instance (all host cores):
+    the reference's own solver built for the host (kind "reference") where it
+    can be built, and the oracle port beside it. Returns the baseline line,
+    the results (bit-identical between the two) and the sampled case."""
     case = cpu_sample_case(nt, stride)
-    threads = O.max_threads("lorenz")
-    O.run_oracle(cpu_sample_case(nt, nt // 64))  # load + warm
+    kind, run, threads = cpu_runner("reference")
     t0 = time.perf_counter()
-    res = O.run_oracle(case, threads=threads)
+    res = run(case, threads)
     dt = time.perf_counter() - t0
-    steps = float(res["nacc"].sum())
-    return {"value": steps / dt, "unit": UNIT, "cores": threads, "kind": "port",
+    steps = float(res["acci"][0].sum())
+    line = {"value": steps / dt, "unit": UNIT, "cores": threads, "kind": kind,
             "sample": f"{case.nt} of {nt} instances (every {stride}th, same rho distribution), "
-                      f"{int(steps)} accepted steps in {dt:.2f} s"}, res, case
-
-
-def end_state_errors(results: dict, oracle_res: dict, sample: "W.Case", stride: int) -> dict:
-    """End-state error of each GPU mode against the FP64 oracle (the CPU
-    restatement of the reference solver) on the oracle's sample instances:
-    per instance the largest component error scaled by |oracle| + 1e-3 x the
-    component's ensemble scale; quantiles over all sampled instances and over
-    the non-chaotic ones (rho < 13.9: the Lorenz system from (10, 10, 10) shows
-    transient chaos above, where rounding differences are amplified)."""
-    ref = oracle_res["x"]
-    scale = np.max(np.abs(ref), axis=1, keepdims=True)
-    calm = sample.arrays["cp"][0] < 13.9
-    out = {"sample": f"every {stride}th instance ({ref.shape[1]}), oracle rtol = atol = 1e-10",
-           "non_chaotic_instances": int(calm.sum())}
-    for name, res in results.items():
-        if res is None:
-            continue
-        x = res["x"][:, ::stride]
-        per = np.max(np.abs(x - ref) / (np.abs(ref) + 1e-3 * scale), axis=0)
-        out[name] = {"median": float(np.median(per)), "q99_non_chaotic": float(np.quantile(per[calm], 0.99)),
-                     "max_non_chaotic": float(per[calm].max()), "max_all": float(per.max()),
-                     "within_1e-9_non_chaotic": float(np.mean(per[calm] <= 1e-9)),
-                     "accepted_steps_vs_oracle": float(res["nacc"][::stride].sum() / oracle_res["nacc"].sum())}
-    return out
+                      f"{int(steps)} accepted steps in {dt:.2f} s"}
+    if kind == "reference":
+        _, prun, pthreads = cpu_runner("port")
+        t0 = time.perf_counter()
+        pres = prun(case, pthreads)
+        pdt = time.perf_counter() - t0
+        line["port"] = {"value": float(pres["acci"][0].sum()) / pdt, "cores": pthreads,
+                        "bitwise_equal_to_reference_build": bool(
+                            np.array_equal(pres["x"].view(np.uint8), res["x"].view(np.uint8)) and
+                            np.array_equal(pres["acci"], res["acci"]))}
+    return line, res, case
 
 
 def run_reference(args):
@@ -240,75 +265,178 @@ def run_reference(args):
     world, rank, local = dist_setup()
     if rank != 0:
         return
-    from oracle import oracle as O
     stride = 16
     case = cpu_sample_case(args.nt, stride)
-    # The oracle port (OpenMP over instances): the CPU restatement of the
-    # reference's per-thread solver, pinned bit for bit to the reference's own
-    # kernel compiled for the CPU (tests/test_oracle.py). That reference build
-    # runs one instance at a time through static thread indices, so it cannot
-    # use more than one core, and it only exists where the reference checkout
-    # was present at build time; the port is what runs here.
-    kind = "port"
-    runner = lambda c: O.run_oracle(c, threads=0)
-    threads = O.max_threads("lorenz")
+    kind, run, threads = cpu_runner("reference")
     for _ in range(args.warmup):
-        runner(cpu_sample_case(args.nt, args.nt // 256))
+        run(cpu_sample_case(args.nt, args.nt // 256), threads)
     times, steps = [], 0.0
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        res = runner(case)
+        res = run(case, threads)
         times.append(time.perf_counter() - t0)
-        steps += float(res["nacc"].sum())
+        steps += float(res["acci"][0].sum())
     total = sum(times)
     value = steps / total
+    desc = ("the reference's SingleSystem_PerThread solver kernel compiled for this host (g++ -O3 -fopenmp, "
+            "one instance per loop iteration)" if kind == "reference" else
+            "the oracle port of the reference solver (OpenMP)")
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "impl": "reference",
             "config": {"workload": WORKLOAD, "instances": args.nt, "sample_stride": stride},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind,
-                             "sample": f"{case.nt} of {args.nt} instances (every {stride}th) per step"},
+                             "sample": f"{case.nt} of {args.nt} instances (every {stride}th) per step; {desc}"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
 
-def flush_l2(buf):
-    buf.fill_(1)
+# ---- shared helpers ----------------------------------------------------------------
+def reference_shapes(system: str, algorithm: int, nt: int, ndo: int = 0, rregs=(None,)):
+    """Launch shapes of the reference kernel that can be run: one warp per
+    block with the unmodified cubin, and 64..256-thread blocks with the cubin
+    that has a barrier after the reference's shared-memory staging."""
+    from oracle import ref_gpu as R
+    out = []
+    for rr in rregs:
+        if R.available(system, algorithm, nt, ndo, rr):
+            out.append((32, rr, False))
+        for b in (64, 128, 256):
+            if R.available(system, algorithm, nt, ndo, rr, sync=True):
+                out.append((b, rr, True))
+    return out
 
 
+def time_reference(solver, case, shape, phases: int, flush, reps: int) -> tuple:
+    """Median ms of `reps` runs (after one warm-up) of the reference kernel in
+    `shape` = (block, register cap, sync) over `phases` launches on the
+    solver's buffers, state restored before each; the last run's results."""
+    import torch
+    from mpgos_gb300 import workloads as W
+    from oracle import ref_gpu as R
+    block, rr, sync = shape
+    kern = R.ReferenceKernel(case.system, case.algorithm, case.nt, case.ndo, rr, sync=sync)
+    try:
+        kern.bind(solver, case, block=block)
+        times = []
+        for i in range(reps + 1):
+            flush_l2(flush)
+            torch.cuda.synchronize()
+            solver.checkpoint_restore()
+            solver.timer_start()
+            for _ in range(phases):
+                kern.launch()
+            ms = solver.timer_stop()
+            if i:
+                times.append(ms)
+        res = W.read_results(solver)
+    finally:
+        kern.close()
+    return statistics.median(times), res
+
+
+def shape_name(shape) -> str:
+    block, rr, sync = shape
+    return f"block{block}" + (f"_rreg{rr}" if rr else "") + ("_barrier" if sync else "")
+
+
+def scaled_rel(a, b):
+    """Per instance: the largest component difference scaled by |b| + 1e-3 x
+    the component's largest |b| over the ensemble."""
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    scale = np.max(np.abs(b), axis=1, keepdims=True)
+    return (np.abs(a - b) / (np.abs(b) + 1e-3 * scale)).max(axis=0)
+
+
+def stable_sets(case, local, base, keys=("acci",), tol_perturb: bool = True):
+    """The reference arithmetic's own sensitivity, measured with the PLAIN
+    kernel (bit-identical to the reference kernel) on the GPU: instances
+    whose end state moves by at most 1e-10 (scaled) when the initial state is
+    moved by 1e-13 relative (``end``), and, of those, the ones whose integer
+    outputs no perturbation changes (initial state; tolerances moved by
+    +-1e-6 relative when ``tol_perturb``) (``ints``)."""
+    from mpgos_gb300 import capi, workloads as W
+    runs = []
+    c = case.copy()
+    c.arrays["x"] = c.arrays["x"] * (1.0 + X_REL) + (c.arrays["x"] == 0) * X_REL
+    moved = W.run_gpu(c, mode=capi.MODE_PLAIN, device=local, graph=case.phases > 1)
+    runs.append(moved)
+    end = scaled_rel(moved["x"], base["x"]) <= 1e-10
+    if tol_perturb:
+        for sgn in (1.0, -1.0):
+            c = case.copy()
+            c.rtol = c.rtol * (1.0 + sgn * TOL_REL)
+            c.atol = c.atol * (1.0 + sgn * TOL_REL)
+            runs.append(W.run_gpu(c, mode=capi.MODE_PLAIN, device=local, graph=case.phases > 1))
+    ints = end.copy()
+    for r in runs:
+        for k in keys:
+            ints &= np.all(np.asarray(r[k]) == np.asarray(base[k]), axis=0)
+    return end, ints
+
+
+def versus(res, ref, end, ints, int_key=("acci", 0)) -> dict:
+    """A form's results against the reference kernel's: end states within
+    1e-9 (scaled) and step counts equal, on the stable instances and on all."""
+    rel = scaled_rel(res["x"], ref["x"])
+    k, row = int_key
+    eq = np.asarray(res[k])[row] == np.asarray(ref[k])[row]
+    return {"within_1e-9_stable": float(np.mean(rel[end] <= 1e-9)) if end.any() else None,
+            "max_scaled_rel_stable": float(rel[end].max()) if end.any() else None,
+            "within_1e-9_all": float(np.mean(rel <= 1e-9)),
+            "step_count_equal_stable": float(np.mean(eq[ints])) if ints.any() else None,
+            "step_count_equal_all": float(np.mean(eq)),
+            "accepted_steps_total_rel_diff": float(abs(np.asarray(res[k])[row].sum() - np.asarray(ref[k])[row].sum())
+                                                   / max(1.0, float(np.asarray(ref[k])[row].sum())))}
+
+
+# ---- configuration legs ----------------------------------------------------------------
 def adjoint_leg(local: int, flush) -> dict:
     """Adjoint configuration: forced Duffing ensemble of 2^18 instances with
     per-instance (k, B), RKCK45 1e-9 over 64 forcing periods, loss = squared
     distance of the terminal state to per-instance targets; gradients with
     respect to (x0, v0, k, B) by the discrete adjoint with a checkpoint every
-    32 accepted steps. On the same inputs, persistent mapping, three forms:
+    32 accepted steps. On the same inputs, persistent mapping:
       fp64                 FP64 (FAST_CONTROL) forward, recording and reverse;
       fp64_fwd_df_reverse  the same FP64 forward and recording, reverse pass
                            in double-float (KERNEL_MODE switched to DF_STAGE
                            between SolveRecord and Adjoint);
+      split                SPLIT forward and recording, reverse in double-float;
       df_stage             double-float forward, recording and reverse.
     Each times the forward pass alone, the recording forward pass and the
     reverse pass; adjoint/forward = (recording + reverse) / forward of the
-    same forward arithmetic. The headline is the FP64-forward form with the
-    double-float reverse pass (the configuration integrates in FP64)."""
+    same forward arithmetic. Gradient check: a seeded block of 256
+    consecutive instances (random parameters and initial states) of the
+    full run, every gradient component against FP64 central differences of
+    the recorded discrete map (the oracle replays the frozen steps)."""
     import torch
     from mpgos_gb300 import capi, workloads as W
     from mpgos_gb300.solver import Variable
+    from oracle import oracle as O
     nt, seg = 1 << 18, 32
     case = W.duffing_param_case(nt=nt, periods=64, tol=1e-9)
-    target = torch.tensor(W.duffing_param_targets(nt), device=f"cuda:{local}")
+    target_np = W.duffing_param_targets(nt)
+    target = torch.tensor(target_np, device=f"cuda:{local}")
     out = {"workload": "duffing_param_2^18_rkck45_tol1e-9_64periods_seg32", "unit": "ms",
            "gradients_per_instance": 4}
-    FP64 = capi.MODE_FAST_CONTROL | capi.MODE_PERSISTENT
-    DF = capi.MODE_DF_STAGE | capi.MODE_PERSISTENT
+    FP64M = capi.MODE_FAST_CONTROL | capi.MODE_PERSISTENT
+    DFM = capi.MODE_DF_STAGE | capi.MODE_PERSISTENT
+    SPM = capi.MODE_SPLIT | capi.MODE_PERSISTENT
+    i0 = int(np.random.default_rng(20261204).integers(0, nt - 256))
+    fd_block = slice(i0, i0 + 256)
 
-    def run(mode, reverse_modes):
+    class _Cuda:
+        """A device array of the tape, for torch to view without copying."""
+        def __init__(self, ptr, shape, typestr):
+            self.__cuda_array_interface__ = {"shape": shape, "typestr": typestr, "data": (int(ptr), False),
+                                             "version": 3, "strides": None}
+
+    def run(mode, reverse_modes, fd=False):
         """Forward and recording in `mode`; one reverse pass per entry of
         `reverse_modes` on the same tape."""
         with W.load_solver(case, mode=mode, block=128, device=local) as s:
             s.checkpoint_save()
-            # tape capacity: the largest accepted-step count of a plain forward pass
             s.Solve()
             s.SynchroniseFromDeviceToHost(Variable.AcceptedSteps)
             s.SynchroniseDevice()
@@ -318,6 +446,7 @@ def adjoint_leg(local: int, flush) -> dict:
             x_dev = torch.empty_like(g)
             fwd, rec, rev = [], [], {m: [] for m in reverse_modes}
             grads = {}
+            tape_block = None
             for i in range(3):
                 s.set_mode(mode)
                 flush_l2(flush)
@@ -348,6 +477,11 @@ def adjoint_leg(local: int, flush) -> dict:
                 if i:
                     fwd.append(t_f)
                     rec.append(t_r)
+            if fd:
+                t = s.tape_info()
+                dt = torch.as_tensor(_Cuda(t.dt, (t.max_steps, nt), "<f8"), device=f"cuda:{local}")
+                ns = torch.as_tensor(_Cuda(t.n_steps, (nt,), "<i4"), device=f"cuda:{local}")
+                tape_block = (dt[:, fd_block].cpu().numpy().copy(), ns[fd_block].cpu().numpy().copy())
             s.SynchroniseFromDeviceToHost(Variable.Status)
             s.SynchroniseDevice()
             overflow = int(np.count_nonzero(s.host(Variable.Status) & capi.INSTANCE_TAPE_OVERFLOW))
@@ -358,21 +492,45 @@ def adjoint_leg(local: int, flush) -> dict:
             res[m] = {"forward_ms": f, "recording_forward_ms": r, "reverse_ms": b,
                       "adjoint_over_forward": (r + b) / f, "tape_overflow_instances": overflow,
                       "tape_steps": max_steps}
-        return res, grads
+        return res, grads, tape_block
 
     def rel(a, b):
         return float(np.max(np.abs(a - b) / np.maximum(np.max(np.abs(b), axis=1, keepdims=True), 1e-300)))
 
-    r64, g64 = run(FP64, (FP64, DF))
-    rdf, gdf = run(DF, (DF,))
-    head = r64[DF]
-    out.update({"fp64": r64[FP64], "fp64_fwd_df_reverse": head, "df_stage": rdf[DF],
+    r64, g64, tape = run(FP64M, (FP64M, DFM), fd=True)
+    rsp, gsp, _ = run(SPM, (SPM,))
+    rdf, gdf, _ = run(DFM, (DFM,))
+    head = r64[DFM]
+    out.update({"fp64": r64[FP64M], "fp64_fwd_df_reverse": head, "split": rsp[SPM], "df_stage": rdf[DFM],
                 "adjoint_over_forward": head["adjoint_over_forward"],
                 "headline_form": "FP64 forward + recording, double-float reverse",
-                # one FP64 tape reversed in FP64 and in double-float: the reverse arithmetic's own error
-                "gradient_max_rel_diff_df_vs_fp64_reverse_same_tape": rel(g64[DF], g64[FP64]),
-                # different (both 1e-9-controlled) step sequences
-                "gradient_max_rel_diff_df_stage_vs_fp64": rel(gdf[DF], g64[FP64])})
+                "gradient_max_rel_diff_df_vs_fp64_reverse_same_tape": rel(g64[DFM], g64[FP64M]),
+                "gradient_max_rel_diff_df_stage_vs_fp64": rel(gdf[DFM], g64[FP64M]),
+                "gradient_max_rel_diff_split_vs_fp64": rel(gsp[SPM], g64[FP64M])})
+    # central differences of the recorded map on the 256-instance block
+    dt_tape, n_steps = tape
+    sub = case.subset(np.arange(i0, i0 + 256))
+    tgt = target_np[:, fd_block]
+    grad = g64[DFM][:, fd_block]          # rows: dL/dx0, dL/dv0, dL/dk, dL/dB
+    fdv = np.zeros_like(grad)
+    for row in range(4):
+        base_x, base_cp = sub.arrays["x"].copy(), sub.arrays["cp"].copy()
+        arr, j = (base_x, row) if row < 2 else (base_cp, row - 2)
+        h = 1e-6 * np.maximum(np.abs(arr[j]), 1.0)
+        loss = []
+        for sgn in (1.0, -1.0):
+            x0, cp = base_x.copy(), base_cp.copy()
+            (x0 if row < 2 else cp)[j] += sgn * h
+            xt = O.replay(sub, dt_tape, n_steps, x0=x0, cp=cp)
+            loss.append(np.sum((xt - tgt) ** 2, axis=0))
+        fdv[row] = (loss[0] - loss[1]) / (2.0 * h)
+    err = np.abs(grad - fdv) / np.maximum(np.abs(fdv), 1e-8)
+    out["gradient_check_vs_central_differences"] = {
+        "sample": f"instances {i0}..{i0 + 255} of the full run (seeded offset), FP64 forward tape, double-float "
+                  "reverse; central differences (h = 1e-6 max(|p|, 1)) of the same recorded step sequence replayed "
+                  "in FP64 by the oracle",
+        "max_rel_error": float(err.max()), "median_rel_error": float(np.median(err)),
+        "per_parameter_max": {n: float(err[i].max()) for i, n in enumerate(("x0", "v0", "k", "B"))}}
     return out
 
 
@@ -380,176 +538,180 @@ def rk4_leg(local: int, flush) -> dict:
     """Fixed-step configuration: forced Duffing oscillator, 8192 instances,
     RK4 with dt = 2 pi / 400 over 1024 forcing periods (1024 phases replayed
     from one CUDA graph), running maximum of x as an accessory. Times PLAIN
-    (bit-identical to the reference kernel, checked), the double-float form
-    (same step counts on the same FP64 time grid) and the reference's kernel
-    launched once per period; one warm-up and two timed runs each."""
+    (bit-identical to the reference kernel, checked), SPLIT and the
+    double-float form (same step counts on the same FP64 time grid) and the
+    reference's kernel launched once per period at each block size it can
+    run (the best divides); one warm-up and two timed runs each."""
     import torch
     from mpgos_gb300 import capi, workloads as W
-    from oracle import ref_gpu as R
     case = W.duffing_rk4_case(nt=8192, periods=1024)
     out = {"workload": "duffing_rk4_8192_dt2pi/400_1024periods", "unit": "accepted instance-steps/s"}
 
-    def run(mode, reference=False, tune=False):
+    def run(mode, tune=False):
         with W.load_solver(case, mode=mode, block=64, device=local) as s:
             s.checkpoint_save()
-            kern = None
-            if reference:
-                kern = R.ReferenceKernel("duffing", 0, case.nt, 0)
-                kern.bind(s, case, block=32)
             if tune:
-                s.autotune(arithmetic=mode & capi.MODE_DF_STAGE)
-            cfg = {}
-            if not reference:
-                grid, blk, m = s.launch_config()
-                cfg = {"grid": grid, "block": blk, "mode": m,
-                       "outline_rhs": int(s.GetOption(capi.Option.OutlineRhs))}
+                s.autotune(arithmetic=mode & (capi.MODE_DF_STAGE | capi.MODE_SPLIT))
+            grid, blk, m = s.launch_config()
+            cfg = {"grid": grid, "block": blk, "mode": m, "outline_rhs": int(s.GetOption(capi.Option.OutlineRhs))}
             times = []
             for i in range(3):
                 flush_l2(flush)
                 torch.cuda.synchronize()
                 s.checkpoint_restore()
                 s.timer_start()
-                if reference:
-                    for _ in range(case.phases):
-                        kern.launch()
-                else:
-                    s.SolvePhases(case.phases)
+                s.SolvePhases(case.phases)
                 ms = s.timer_stop()
                 if i:
                     times.append(ms)
             res = W.read_results(s)
-            if kern is not None:
-                kern.close()
         steps = float(res["acci"][0].sum())
         return {"ms": statistics.median(times), "value": steps / (statistics.median(times) / 1e3), **cfg}, res
 
     out["plain"], rp = run(capi.MODE_PLAIN)
+    out["split_autotuned"], rs = run(capi.MODE_SPLIT, tune=True)
     out["df_stage_autotuned"], rd = run(capi.MODE_DF_STAGE, tune=True)
+    out["split_steps_equal_plain"] = bool(np.array_equal(rs["acci"], rp["acci"]))
+    out["split_max_abs_diff_vs_plain"] = float(np.max(np.abs(rs["x"] - rp["x"])))
     out["df_steps_equal_plain"] = bool(np.array_equal(rd["acci"], rp["acci"]))
     out["df_max_abs_diff_vs_plain"] = float(np.max(np.abs(rd["x"] - rp["x"])))
-    if R.available("duffing", 0, case.nt, 0):
-        ref, rr = run(capi.MODE_PLAIN, reference=True)
-        out["reference_gpu"] = ref
-        out["speedup_df_vs_reference_gpu"] = out["df_stage_autotuned"]["value"] / ref["value"]
-        out["plain_bitwise_equal_to_reference_kernel"] = bool(all(
-            np.array_equal(np.asarray(rp[k]).view(np.uint8), np.asarray(rr[k]).view(np.uint8))
-            for k in ("x", "t", "acc", "acci")))
+    shapes = reference_shapes("duffing", 0, case.nt)
+    if shapes:
+        ref = {}
+        with W.load_solver(case, mode=0, device=local) as s:
+            s.checkpoint_save()
+            for shape in shapes:
+                ms, rr = time_reference(s, case, shape, case.phases, flush, reps=2)
+                steps = float(rr["acci"][0].sum())
+                ref[shape_name(shape)] = {"ms": ms, "value": steps / (ms / 1e3)}
+                if shape == (32, None, False):
+                    out["plain_bitwise_equal_to_reference_kernel"] = bool(all(
+                        np.array_equal(np.asarray(rp[k]).view(np.uint8), np.asarray(rr[k]).view(np.uint8))
+                        for k in ("x", "t", "acc", "acci")))
+        best = max(ref, key=lambda k: ref[k]["value"])
+        out["reference_gpu"] = {"shapes": ref, "best_shape": best, **ref[best]}
+        out["speedup_split_vs_reference_gpu"] = out["split_autotuned"]["value"] / ref[best]["value"]
+        out["speedup_df_vs_reference_gpu"] = out["df_stage_autotuned"]["value"] / ref[best]["value"]
     return out
 
 
-def uneven_leg(local: int, flush) -> dict:
-    """Uneven configuration at reduced size: Keller-Miksis bubbles on a
-    256 x 256 grid of driving amplitude x frequency (2^16 instances; the
-    configuration's 512 x 512 grid and 1024 periods scaled down to keep the
-    bench short), RKCK45 1e-10, 4 acoustic periods as 4 phases captured in
-    one CUDA graph, the per-period maximum radius streamed out after every
-    phase. Step counts per instance differ by two orders of magnitude. Times
-    the static and persistent mappings of the FP64 (FAST_CONTROL) and
-    double-float forms and the reference's kernel (sm_103a cubin, event
-    options fixed, one launch per period) on the same inputs; checks PLAIN
-    against the reference kernel bit for bit."""
+def uneven_leg(local: int, flush, periods: int) -> dict:
+    """Uneven configuration at the stated grid: Keller-Miksis bubbles on the
+    512 x 512 grid of driving amplitude x frequency (2^18 instances),
+    RKCK45 1e-10, `periods` acoustic periods (the configuration's 1024 scaled
+    down to keep the bench within minutes; the count is in the workload name)
+    as phases captured in one CUDA graph, the per-period maximum radius
+    streamed out after every phase. Step counts per instance differ by two
+    orders of magnitude. Times SPLIT, the double-float form and the FP64
+    FAST_CONTROL form (static one-warp blocks, persistent queue, autotuned)
+    and the reference's kernel (sm_103a cubin, event options fixed; its
+    launch shape swept over one period, the best shape timed over all);
+    parity of every form against the reference kernel over the whole grid,
+    on the perturbation-stable instances and on all."""
     import torch
     from mpgos_gb300 import capi, workloads as W
-    from mpgos_gb300.solver import Variable
-    from oracle import ref_gpu as R
-    case = W.keller_miksis_case(n_amp=256, n_freq=256, periods=4)
-    nt, phases = case.nt, case.phases
-    out = {"workload": "keller_miksis_256x256_rkck45_tol1e-10_4periods", "unit": "accepted instance-steps/s",
-           "phases": phases}
-    per_phase = torch.empty((phases, nt), dtype=torch.float64, device=f"cuda:{local}")
+    case = W.keller_miksis_case(n_amp=512, n_freq=512, periods=periods)
+    nt = case.nt
+    out = {"workload": f"keller_miksis_512x512_rkck45_tol1e-10_{periods}periods", "unit": "accepted instance-steps/s",
+           "phases": periods}
+    per_phase = torch.empty((periods, nt), dtype=torch.float64, device=f"cuda:{local}")
 
-    def run(mode, block=128, reference=False, tune=False):
+    def run(mode, block=128, tune=False, reps=2):
         with W.load_solver(case, mode=mode, block=block, device=local) as s:
             s.checkpoint_save()
-            kern = None
-            if reference:
-                kern = R.ReferenceKernel("keller_miksis", 1, nt, 0)
-                kern.bind(s, case, block=32)
-            if tune:
-                s.autotune(arithmetic=mode & (capi.MODE_FAST_CONTROL | capi.MODE_DF_STAGE))
-            grid, blk, m = s.launch_config() if not reference else (kern.grid, kern.block, -1)
-            outline = int(s.GetOption(capi.Option.OutlineRhs)) if not reference else 0
+            if tune:   # one Solve() (one period) per candidate
+                s.autotune(arithmetic=mode & (capi.MODE_FAST_CONTROL | capi.MODE_DF_STAGE | capi.MODE_SPLIT))
+            grid, blk, m = s.launch_config()
+            outline = int(s.GetOption(capi.Option.OutlineRhs))
             times = []
-            for i in range(3):
+            for i in range(reps + 1):
                 flush_l2(flush)
                 torch.cuda.synchronize()
                 s.checkpoint_restore()
                 s.timer_start()
-                if reference:
-                    for _ in range(phases):
-                        kern.launch()
-                else:
-                    s.SolvePhases(phases, 0, per_phase.data_ptr())
+                s.SolvePhases(periods, 0, per_phase.data_ptr())
                 ms = s.timer_stop()
                 if i:
                     times.append(ms)
             res = W.read_results(s)
-            if kern is not None:
-                kern.close()
-        # accepted steps of all phases, counted by the system's own hook (integer accessory 1)
-        steps = float(res["acci"][1].sum())
+        steps = float(res["acci"][1].sum())   # accepted steps of all periods, counted by the system's hook
         return {"ms": statistics.median(times), "value": steps / (statistics.median(times) / 1e3),
                 "grid": grid, "block": blk, "mode": m, "outline_rhs": outline}, res
 
-    FAST, DF, P = capi.MODE_FAST_CONTROL, capi.MODE_DF_STAGE, capi.MODE_PERSISTENT
-    # static mappings with the reference's one-warp blocks (the best static shape for uneven
-    # work: a finished warp frees its block), persistent with 128-thread blocks, and the
-    # autotuned double-float choice
-    forms = {"fp64_static_b32": (FAST, 32), "fp64_persistent": (FAST | P, 128), "df_static_b32": (DF, 32),
-             "df_persistent": (DF | P, 128)}
+    P = capi.MODE_PERSISTENT
+    forms = {"split_static_b32": (SPLIT, 32, False), "split_persistent": (SPLIT | P, 128, False),
+             "split_autotuned": (SPLIT, 128, True), "df_static_b32": (DF, 32, False),
+             "df_persistent": (DF | P, 128, False), "df_autotuned": (DF, 128, True),
+             "fp64_persistent": (capi.MODE_FAST_CONTROL | P, 128, False)}
     results = {}
-    for name, (mode, block) in forms.items():
-        out[name], results[name] = run(mode, block)
-    out["df_autotuned"], _ = run(DF, tune=True)
-    plain, rplain = run(capi.MODE_PLAIN, 32)
-    out["plain_static_b32"] = plain
-    n = results["fp64_static_b32"]["acci"][1]
+    for name, (mode, block, tune) in forms.items():
+        out[name], results[name] = run(mode, block, tune, reps=1 if name.startswith("fp64") else 2)
+    n = results["split_autotuned"]["acci"][1]
     out["steps_per_instance_min_max"] = [int(n.min()), int(n.max())]
-    out["persistent_over_static_fp64"] = out["fp64_static_b32"]["ms"] / out["fp64_persistent"]["ms"]
+    out["persistent_over_static_split"] = out["split_static_b32"]["ms"] / out["split_persistent"]["ms"]
     out["persistent_over_static_df"] = out["df_static_b32"]["ms"] / out["df_persistent"]["ms"]
-    if R.available("keller_miksis", 1, nt, 0):
-        ref, rref = run(capi.MODE_PLAIN, reference=True)
-        out["reference_gpu"] = ref
-        best = max(out[k]["value"] for k in ("df_persistent", "df_autotuned", "df_static_b32"))
-        out["speedup_best_df_vs_reference_gpu"] = best / ref["value"]
-        out["speedup_fp64_persistent_vs_reference_gpu"] = out["fp64_persistent"]["value"] / ref["value"]
-        out["plain_bitwise_equal_to_reference_kernel"] = bool(all(
-            np.array_equal(np.asarray(rplain[k]).view(np.uint8), np.asarray(rref[k]).view(np.uint8))
-            for k in ("x", "t", "acc", "acci")))
-        # double-float form against the reference kernel over the whole ensemble: end states
-        # and per-period maximum radii relative to each component's scale, integer outputs
-        # (event count, accepted steps) per instance
-        # (the FP64 FAST_CONTROL form beside it: what a different rounding of the step-size
-        # factor alone does on this ensemble)
-        def versus_reference(r):
-            rel = {}
-            for k in ("x", "acc"):
-                a, b = np.asarray(r[k], np.float64), np.asarray(rref[k], np.float64)
-                scale = np.max(np.abs(b), axis=1, keepdims=True)
-                rel[k] = (np.abs(a - b) / (np.abs(b) + 1e-3 * scale)).max(axis=0)
-            steps, ref_steps = float(r["acci"][1].sum()), float(rref["acci"][1].sum())
-            return {"instances_within_1e-9_end_state": float(np.mean(rel["x"] <= 1e-9)),
-                    "instances_within_1e-9_max_radius": float(np.mean(rel["acc"] <= 1e-9)),
-                    "event_count_equal_fraction": float(np.mean(r["acci"][0] == rref["acci"][0])),
-                    "accepted_steps_equal_fraction": float(np.mean(r["acci"][1] == rref["acci"][1])),
-                    "accepted_steps_total_rel_diff": abs(steps - ref_steps) / ref_steps}
-        out["df_vs_reference_gpu"] = versus_reference(results["df_static_b32"])
-        out["fp64_fast_vs_reference_gpu"] = versus_reference(results["fp64_static_b32"])
+    shapes = reference_shapes("keller_miksis", 1, nt)
+    if not shapes:
+        return out
+    # the reference kernel's launch shape: swept over one period, the best timed over all
+    one = case.copy()
+    one.phases = 1
+    sweep = {}
+    with W.load_solver(one, mode=0, device=local) as s:
+        s.checkpoint_save()
+        for shape in shapes:
+            ms, _ = time_reference(s, one, shape, 1, flush, reps=1)
+            sweep[shape_name(shape)] = ms
+    best = min(sweep, key=sweep.get)
+    best_shape = next(sh for sh in shapes if shape_name(sh) == best)
+    with W.load_solver(case, mode=0, device=local) as s:
+        s.checkpoint_save()
+        ms, rref = time_reference(s, case, best_shape, periods, flush, reps=1)
+    steps = float(rref["acci"][1].sum())
+    out["reference_gpu"] = {"ms": ms, "value": steps / (ms / 1e3), "best_shape": best,
+                            "one_period_ms_by_shape": sweep}
+    for k in ("split_autotuned", "df_autotuned", "fp64_persistent"):
+        out[f"speedup_{k}_vs_reference_gpu"] = out[k]["value"] / out["reference_gpu"]["value"]
+    # PLAIN against the reference kernel bit for bit (two periods; one-warp blocks)
+    two = case.copy()
+    two.phases = 2
+    with W.load_solver(two, mode=0, device=local) as s:
+        s.checkpoint_save()
+        _, r2 = time_reference(s, two, (32, None, False), 2, flush, reps=1)
+    p2 = W.run_gpu(two, mode=capi.MODE_PLAIN, block=32, device=local, graph=True)
+    out["plain_bitwise_equal_to_reference_kernel_2periods"] = bool(all(
+        np.array_equal(np.asarray(p2[k]).view(np.uint8), np.asarray(r2[k]).view(np.uint8))
+        for k in ("x", "t", "acc", "acci")))
+    # stable instances: PLAIN (= the reference kernel) with the initial state moved by 1e-13
+    end, ints = stable_sets(case, local, rref, keys=("acci",), tol_perturb=False)
+    out["stable"] = {"criterion": "PLAIN end state within 1e-10 (scaled) and event / step counts unchanged when "
+                                  "the initial state moves by 1e-13 relative",
+                     "end_state_instances": int(end.sum()), "integer_instances": int(ints.sum()), "of": nt}
+    for k in ("split_autotuned", "df_static_b32", "fp64_persistent"):
+        r = results[k]
+        v = versus(r, rref, end, ints, ("acci", 1))
+        ev = np.asarray(r["acci"][0]) == np.asarray(rref["acci"][0])
+        v["event_count_equal_stable"] = float(np.mean(ev[ints])) if ints.any() else None
+        v["event_count_equal_all"] = float(np.mean(ev))
+        v["event_count_differs_at"] = np.flatnonzero(~ev)[:8].tolist()
+        v["max_radius_within_1e-9_all"] = float(np.mean(scaled_rel(r["acc"], rref["acc"]) <= 1e-9))
+        out[f"{k}_vs_reference_gpu"] = v
     return out
 
 
-def coupled_leg(local: int, flush) -> dict:
-    """Coupled configuration beside the headline: 16384 rings of 64 Duffing
-    units (dense coupling, RKCK45 1e-9, crossing events), two forcing periods
-    per launch. Times the DF_STAGE and FP64 warp-per-system kernels and the
-    reference's own coupled kernel (sm_103a cubin, TPB 256 / SPB 4) on the same
-    inputs; one warm-up and two timed launches each, L2 flushed before each."""
+def coupled_leg(local: int, flush, periods: int) -> dict:
+    """Coupled configuration: 16384 rings of 64 Duffing units (dense
+    coupling, RKCK45 1e-9, crossing events), `periods` forcing periods per
+    launch. Times the DF_STAGE and FP64 warp-per-system kernels and the
+    reference's own coupled kernel (sm_103a cubin, TPB 256 / SPB 4) on the
+    same inputs, L2 flushed before each; crossing counts and end states
+    against the reference kernel. The discrete adjoint of the summed terminal
+    energy with respect to B is timed on two periods."""
     import torch
     from mpgos_gb300 import capi, coupled_workloads as CW
     from mpgos_gb300.capi import CbVariable as V
-    case = CW.ring_case("ring64", ns=16384, periods=2, seed=5)
 
-    def run(mode=None, warps=4, ref=None):
+    def run(case, mode=None, warps=4, ref=None, reps=1):
         with CW.load_coupled_solver(case, mode=mode or 0, warps=warps, device=local) as s:
             s.checkpoint_save()
             kern = None
@@ -559,7 +721,7 @@ def coupled_leg(local: int, flush) -> dict:
                 kern.bind(s, case, shared_global=1, shared_coupling=0)
             launch = kern.launch if kern is not None else s.Solve
             times = []
-            for i in range(3):
+            for i in range(reps + 1):
                 flush_l2(flush)
                 torch.cuda.synchronize()
                 s.checkpoint_restore()
@@ -574,7 +736,7 @@ def coupled_leg(local: int, flush) -> dict:
         steps = float(res["isacc"][0].sum())  # accepted steps, counted by the systems' own hook
         return {"ms": statistics.median(times), "value": steps / (statistics.median(times) / 1e3)}, res
 
-    def adjoint(mode, reverse_modes, warps, seg=32):
+    def adjoint(case, mode, reverse_modes, warps, seg=32):
         """Recording forward pass in `mode` and one reverse pass per entry of
         `reverse_modes` on that tape, for the gradient of the summed terminal
         energy E = sum_i (v_i^2/2 + x_i^2/2 + x_i^4/4) with respect to B (and
@@ -620,27 +782,17 @@ def coupled_leg(local: int, flush) -> dict:
                     "tape_steps": max_steps, "segment": seg, "tape_overflow_systems": overflow}
                 for m in reverse_modes}
 
-    out = {"workload": "ring64_16384x64_dense_rkck45_tol1e-9_2periods", "unit": "accepted system-steps/s"}
-    df, rdf = run(capi.MODE_DF_STAGE | capi.MODE_PERSISTENT, warps=2)
-    fp, rfp = run(capi.MODE_PERSISTENT, warps=4)
+    case = CW.ring_case("ring64", ns=16384, periods=periods, seed=5)
+    out = {"workload": f"ring64_16384x64_dense_rkck45_tol1e-9_{periods}periods", "unit": "accepted system-steps/s"}
+    df, rdf = run(case, capi.MODE_DF_STAGE | capi.MODE_PERSISTENT, warps=2, reps=2)
+    fp, rfp = run(case, capi.MODE_PERSISTENT, warps=4, reps=1)
     out["df_stage"], out["fp64"] = df, fp
-    FP, DFM = capi.MODE_PERSISTENT, capi.MODE_DF_STAGE | capi.MODE_PERSISTENT
-    a64 = adjoint(FP, (FP, DFM), warps=4)
-    adf = adjoint(DFM, (DFM,), warps=2)
-    forms = {"fp64": (a64[FP], fp), "fp64_fwd_df_reverse": (a64[DFM], fp), "df_stage": (adf[DFM], df)}
-    adj = {}
-    for name, (r, f) in forms.items():
-        r["forward_ms"] = f["ms"]
-        r["adjoint_over_forward"] = (r["recording_forward_ms"] + r["reverse_ms"]) / f["ms"]
-        adj[name] = r
-    adj["adjoint_over_forward"] = adj["fp64_fwd_df_reverse"]["adjoint_over_forward"]
-    adj["headline_form"] = "FP64 forward + recording, double-float reverse"
-    out["adjoint_wrt_B"] = adj
     from oracle import ref_gpu as R
     if R.coupled_available("ring64", 1, case.ns, 256, 4, 0):
-        ref, rref = run(ref=(256, 4))
+        ref, rref = run(case, ref=(256, 4), reps=1)
         out["reference_gpu"] = ref
         out["speedup_df_vs_reference_gpu"] = df["value"] / ref["value"]
+        out["speedup_fp64_vs_reference_gpu"] = fp["value"] / ref["value"]
         out["fp64_bitwise_equal_to_reference_kernel"] = bool(
             all(np.array_equal(rfp[k], rref[k]) for k in ("x", "iuacc", "isacc")))
         mag = np.max(np.abs(rref["x"]), axis=1, keepdims=True)
@@ -648,9 +800,26 @@ def coupled_leg(local: int, flush) -> dict:
         out["df_systems_within_1e-9_of_reference"] = float(np.mean(err <= 1e-9))
         out["df_crossing_counts_equal_fraction"] = float(np.mean(np.all(
             rdf["iuacc"].reshape(case.ns, -1) == rref["iuacc"].reshape(case.ns, -1), axis=1)))
+    # adjoint on two periods
+    small = CW.ring_case("ring64", ns=16384, periods=2, seed=5)
+    fp2, _r = run(small, capi.MODE_PERSISTENT, warps=4, reps=1)
+    df2, _r = run(small, capi.MODE_DF_STAGE | capi.MODE_PERSISTENT, warps=2, reps=1)
+    FP, DFM = capi.MODE_PERSISTENT, capi.MODE_DF_STAGE | capi.MODE_PERSISTENT
+    a64 = adjoint(small, FP, (FP, DFM), warps=4)
+    adf = adjoint(small, DFM, (DFM,), warps=2)
+    forms = {"fp64": (a64[FP], fp2), "fp64_fwd_df_reverse": (a64[DFM], fp2), "df_stage": (adf[DFM], df2)}
+    adj = {"workload": "ring64_16384x64_dense_rkck45_tol1e-9_2periods"}
+    for name, (r, f) in forms.items():
+        r["forward_ms"] = f["ms"]
+        r["adjoint_over_forward"] = (r["recording_forward_ms"] + r["reverse_ms"]) / f["ms"]
+        adj[name] = r
+    adj["adjoint_over_forward"] = adj["fp64_fwd_df_reverse"]["adjoint_over_forward"]
+    adj["headline_form"] = "FP64 forward + recording, double-float reverse"
+    out["adjoint_wrt_B"] = adj
     return out
 
 
+# ---- the headline -----------------------------------------------------------------
 def main():
     args = parse()
     if args.impl == "reference":
@@ -666,27 +835,18 @@ def main():
     case = W.lorenz_case(nt=args.nt)
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=f"cuda:{local}")
 
-    def measure(mode, steps, warmup, clocks=None, tune=False, reference=False):
-        """Time ``steps`` integrations of the whole ensemble: our kernels in
-        ``mode`` (autotuned launch shape if ``tune``) or, with ``reference``,
-        the reference's own kernel (sm_103a cubin) on the same buffers."""
+    def measure(mode, steps, warmup, clocks=None, tune=False):
+        """Time ``steps`` integrations of the whole ensemble in ``mode``
+        (autotuned launch shape if ``tune``)."""
         s = W.load_solver(case, mode=mode, block=128, device=local)
         s.checkpoint_save()
-        kern = None
-        if reference:
-            from oracle import ref_gpu
-            kern = ref_gpu.ReferenceKernel("lorenz", 1, args.nt, 0)
-            kern.bind(s, case, block=32)   # reference default: one warp per block
-            launch = kern.launch
-        else:
-            if tune:
-                s.autotune(arithmetic=mode & (capi.MODE_FAST_CONTROL | capi.MODE_DF_STAGE))
-            launch = s.Solve
+        if tune:
+            s.autotune(arithmetic=mode & (capi.MODE_FAST_CONTROL | capi.MODE_DF_STAGE | capi.MODE_SPLIT))
         for _ in range(warmup):
             s.checkpoint_restore()
-            launch()
+            s.Solve()
         s.SynchroniseDevice()
-        grid, block, m = s.launch_config() if not reference else (kern.grid, kern.block, -1)
+        grid, block, m = s.launch_config()
         kernel_ms, step_ms = [], []
         dist_barrier(world)
         torch.cuda.synchronize()
@@ -698,21 +858,15 @@ def main():
                 torch.cuda.synchronize()
                 s.timer_start()
                 s.checkpoint_restore()
-                launch()
+                s.Solve()
                 step_ms.append(s.timer_stop())
-                if reference:
-                    s.SynchroniseFromDeviceToHost(Variable.IntegerAccessories)
-                    s.InsertSynchronisationPoint()
-                    s.SynchroniseSolver()
-                    accepted += float(s.host(Variable.IntegerAccessories)[0].sum())
-                else:
-                    for v in (Variable.AcceptedSteps, Variable.RejectedSteps):
-                        s.SynchroniseFromDeviceToHost(v)
-                    s.InsertSynchronisationPoint()
-                    s.SynchroniseSolver()
-                    na = float(s.host(Variable.AcceptedSteps).sum())
-                    accepted += na
-                    attempts += na + float(s.host(Variable.RejectedSteps).sum())
+                for v in (Variable.AcceptedSteps, Variable.RejectedSteps):
+                    s.SynchroniseFromDeviceToHost(v)
+                s.InsertSynchronisationPoint()
+                s.SynchroniseSolver()
+                na = float(s.host(Variable.AcceptedSteps).sum())
+                accepted += na
+                attempts += na + float(s.host(Variable.RejectedSteps).sum())
             torch.cuda.synchronize()
         # kernel-only time of the dominant kernel (events on its stream around the launch)
         for _ in range(min(steps, 3)):
@@ -720,12 +874,10 @@ def main():
             torch.cuda.synchronize()
             s.checkpoint_restore()
             s.timer_start()
-            launch()
+            s.Solve()
             kernel_ms.append(s.timer_stop())
         dist_barrier(world)
         res = W.read_results(s)
-        if kern is not None:
-            kern.close()
         s.close()
         return dict(step_ms=step_ms, kernel_ms=kernel_ms, accepted=accepted, attempts=attempts, grid=grid,
                     block=block, mode=m, res=res)
@@ -737,14 +889,14 @@ def main():
     value = acc_all / t_step
     ms_per_step = 1e3 * t_step / args.steps
 
-    # e2e through the public API with host buffers: H2D of the step's inputs,
-    # Solve, D2H of the end states and step counters, every step.
+    # e2e through the public API with host buffers: H2D of every per-instance
+    # input of the step (time domain, state, time, rho, step counter), Solve,
+    # D2H of the end states and step counters, every step.
     with W.load_solver(case, mode=chosen["mode"], block=chosen["block"], device=local) as s:
-        host_x0 = s.host(Variable.ActualState).copy()
-        host_t0 = s.host(Variable.ActualTime).copy()
-        host_c0 = s.host(Variable.IntegerAccessories).copy()
-        h2d = [Variable.ActualState, Variable.ActualTime, Variable.IntegerAccessories]
+        h2d = [Variable.TimeDomain, Variable.ActualState, Variable.ActualTime, Variable.ControlParameters,
+               Variable.IntegerAccessories]
         d2h = [Variable.ActualState, Variable.IntegerAccessories]
+        host0 = {v: s.host(v).copy() for v in h2d}
         s.Solve()
         s.SynchroniseDevice()
         e2e_steps = max(1, min(args.steps, 3))
@@ -752,10 +904,8 @@ def main():
         acc = 0.0
         t0 = time.perf_counter()
         for _ in range(e2e_steps):
-            s.host(Variable.ActualState)[:] = host_x0
-            s.host(Variable.ActualTime)[:] = host_t0
-            s.host(Variable.IntegerAccessories)[:] = host_c0
             for v in h2d:
+                s.host(v)[:] = host0[v]
                 s.SynchroniseFromHostToDevice(v)
             s.Solve()
             for v in d2h:
@@ -766,7 +916,9 @@ def main():
         dt = dist_max(world, time.perf_counter() - t0)
         e2e = {"value": dist_sum(world, acc) / dt, "unit": UNIT,
                "h2d_bytes_per_step": int(sum(s.host(v).nbytes for v in h2d)),
-               "d2h_bytes_per_step": int(sum(s.host(v).nbytes for v in d2h)), "steps": e2e_steps}
+               "d2h_bytes_per_step": int(sum(s.host(v).nbytes for v in d2h)), "steps": e2e_steps,
+               "path": "ProblemSolver.SynchroniseFromHostToDevice / Solve / SynchroniseFromDeviceToHost (C-ABI, "
+                       "pinned host buffers)"}
 
     def summarize(r):
         tp = dist_max(world, sum(r["step_ms"]) / 1e3)
@@ -774,50 +926,72 @@ def main():
                 "kernel_ms": statistics.median(r["kernel_ms"]), "grid": r["grid"], "block": r["block"],
                 "mode": r["mode"]}
 
-    fast_r = measure(capi.MODE_CHOSEN, max(1, min(args.steps, 3)), 1, tune=True)
-    fast = summarize(fast_r)
-    # the FP32-stage form on the same inputs (end-state error reported below)
+    few = max(1, min(args.steps, 3))
+    df_r = measure(capi.MODE_DF_STAGE | capi.MODE_PERSISTENT, few, 1, tune=True)
+    fast_r = measure(capi.MODE_CHOSEN, few, 1, tune=True)
     f32_r = measure(capi.MODE_FP32_STAGE | capi.MODE_CHOSEN, 1, 1)
-    fp32_stage = summarize(f32_r)
-    coupled = None if args.no_coupled else coupled_leg(local, flush)
-    adjoint = None if args.no_adjoint else adjoint_leg(local, flush)
-    uneven = None if args.no_uneven else uneven_leg(local, flush)
-    rk4 = None if args.no_rk4 else rk4_leg(local, flush)
+    df_stage, fast, fp32_stage = summarize(df_r), summarize(fast_r), summarize(f32_r)
+
     plain = ref_gpu = p = None
-    parity = {}
+    parity, stable = {}, None
     if not args.no_plain:
-        p = measure(capi.MODE_PLAIN, max(1, min(args.steps, 3)), 1)
+        p = measure(capi.MODE_PLAIN, few, 1)
         plain = summarize(p)
-        from oracle import ref_gpu as R
-        if R.available("lorenz", 1, args.nt, 0):
-            r = measure(capi.MODE_PLAIN, max(1, min(args.steps, 3)), 1, reference=True)
-            ref_gpu = summarize(r)
-            ref_gpu["kernel"] = "reference SingleSystem_PerThread built for sm_103a (oracle/_ref cubin), block 32"
-            same = all(np.array_equal(np.asarray(p["res"][k]).view(np.uint8), np.asarray(r["res"][k]).view(np.uint8))
-                       for k in ("x", "t", "acci"))
-            parity["plain_bitwise_equal_to_reference_kernel"] = bool(same)
-            ref_res = r["res"]
-        else:
-            ref_res = p["res"]
-        a, b = chosen["res"]["x"], ref_res["x"]
-        scale = np.max(np.abs(b), axis=1, keepdims=True)
-        rel = np.abs(a - b) / (np.abs(b) + 1e-3 * scale)
-        per_inst = rel.max(axis=0)
-        parity.update({"chosen_vs_reference_max_scaled_rel": float(per_inst.max()),
-                       "chosen_instances_within_1e-9": float(np.mean(per_inst <= 1e-9)),
-                       "chosen_step_count_equal_fraction": float(np.mean(chosen["res"]["acci"][0] == ref_res["acci"][0]))})
+        shapes = reference_shapes("lorenz", 1, args.nt, rregs=(None, 64))
+        ref_res = p["res"]
+        if shapes:
+            sweep = {}
+            with W.load_solver(case, mode=0, block=32, device=local) as s:
+                s.checkpoint_save()
+                for shape in shapes:
+                    ms, rr = time_reference(s, case, shape, 1, flush, reps=2)
+                    sweep[shape_name(shape)] = {"ms": ms, "value": float(rr["acci"][0].sum()) / (ms / 1e3)}
+                    if shape == (32, None, False):
+                        ref_res = rr
+            best = max(sweep, key=lambda k: sweep[k]["value"])
+            ref_gpu = {"kernel": "reference SingleSystem_PerThread built for sm_103a (oracle/_ref cubins); block 32 "
+                                 "unmodified, blocks 64..256 with a barrier after its shared-memory staging; "
+                                 "rreg64 = the register cap of the reference's own Lorenz makefile",
+                       "shapes": sweep, "best_shape": best, **sweep[best]}
+            parity["plain_bitwise_equal_to_reference_kernel"] = bool(all(
+                np.array_equal(np.asarray(p["res"][k]).view(np.uint8), np.asarray(ref_res[k]).view(np.uint8))
+                for k in ("x", "t", "acci")))
+        end, ints = stable_sets(case, local, ref_res, keys=("acci",))
+        stable = (end, ints)
+        parity.update({
+            "against": "the reference kernel's results (block 32) on the same inputs",
+            "stable_criterion": "end states: the reference arithmetic's end state (PLAIN, bit-identical to the "
+                                "reference kernel) moves by <= 1e-10 (scaled) when the initial state moves by "
+                                "1e-13 relative; step counts: additionally unchanged under that move and under "
+                                "tolerances moved by +-1e-6 relative",
+            "stable_end_state_instances": int(end.sum()), "stable_step_count_instances": int(ints.sum()),
+            "instances": args.nt,
+            "split": versus(chosen["res"], ref_res, end, ints), "df_stage": versus(df_r["res"], ref_res, end, ints),
+            "fast_fp64": versus(fast_r["res"], ref_res, end, ints),
+            "step_count_cause": "the right-hand side and stage sums round at ~4e-15 (double-float) instead of "
+                                "1.1e-16, which moves each embedded error estimate (which cancels to ~tol from "
+                                "terms of size |k| dt) by ~1e-6 of itself at tol 1e-10; an accept/reject decision "
+                                "whose ratio lies within that of 1 flips and the step sequence after it shifts. "
+                                "FAST_CONTROL's FP32 step factor (~1e-7) does the same through the step size"})
+
+    coupled = None if args.no_coupled else coupled_leg(local, flush, args.coupled_periods)
+    adjoint = None if args.no_adjoint else adjoint_leg(local, flush)
+    uneven = None if args.no_uneven else uneven_leg(local, flush, args.uneven_periods)
+    rk4 = None if args.no_rk4 else rk4_leg(local, flush)
 
     if rank != 0:
         return
 
-    peak_fp64 = capi.fma_peak(local, 8)
-    peak_fp32_ops = capi.fma_peak(local, 4) / 2.0   # FP32 FMA instructions per second
+    peak_fp64 = capi.fma_peak(local, 8) / 2.0   # FP64 FMA instructions per second (one thread-operation each)
+    peak_fp32 = capi.fma_peak(local, 4) / 2.0   # FP32 FMA instructions per second (the issue ceiling)
     kernel_s = statistics.median(chosen["kernel_ms"]) / 1e3
     attempts_per_launch = chosen["attempts"] / args.steps
     prof = load_traffic()
-    instr = prof.get("lorenz_df_thread_instr_per_attempt")
-    traffic = prof.get("lorenz_df_dram_bytes_per_launch")
-    achieved = (instr * attempts_per_launch / kernel_s) if instr else None
+    fp64_instr = prof.get("lorenz_split_fp64_thread_instr_per_attempt")
+    all_instr = prof.get("lorenz_split_thread_instr_per_attempt")
+    traffic = prof.get("lorenz_split_dram_bytes_per_launch")
+    achieved = fp64_instr * attempts_per_launch / kernel_s if fp64_instr else None
+    issue = all_instr * attempts_per_launch / kernel_s if all_instr else None
     peaks = load_peaks()
     # per instance: x (3), t, td (2), rho read and x, t written in FP64; the
     # step-counter accessory read and written, status and the two step
@@ -827,41 +1001,59 @@ def main():
     if not args.no_cpu:
         stride = 8
         cpu, oracle_res, sample = cpu_baseline(args.nt, stride)
-        errors = end_state_errors({"plain": p["res"] if p else None, "fast_fp64": fast_r["res"],
-                                   "df_stage": chosen["res"], "fp32_stage": f32_r["res"]}, oracle_res, sample, stride)
+        mask = stable[0][::stride] if stable is not None else np.ones(sample.nt, bool)
+        errors = {"sample": f"every {stride}th instance ({sample.nt}), FP64 reference CPU build at rtol = atol = "
+                            f"1e-10; stable = the end-state stable set above", "stable_instances": int(mask.sum())}
+        for name, r in (("split", chosen["res"]), ("df_stage", df_r["res"]), ("fast_fp64", fast_r["res"]),
+                        ("fp32_stage", f32_r["res"]), ("plain", p["res"] if p is not None else None)):
+            if r is None:
+                continue
+            per = scaled_rel(r["x"][:, ::stride], oracle_res["x"])
+            errors[name] = {"median": float(np.median(per)), "max_stable": float(per[mask].max()),
+                            "q99_stable": float(np.quantile(per[mask], 0.99)), "max_all": float(per.max()),
+                            "within_1e-9_stable": float(np.mean(per[mask] <= 1e-9)),
+                            "within_1e-9_all": float(np.mean(per <= 1e-9)),
+                            "accepted_steps_vs_oracle": float(r["nacc"][::stride].sum() / oracle_res["acci"][0].sum())}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "df64 (float pairs, ~48-bit) stages; f64 state in HBM", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "instances": args.nt, "form": "chosen: DF_STAGE + persistent",
+        "vs_baseline": None, "dtype": DTYPE, "data": "synthetic",
+        "config": {"workload": WORKLOAD, "instances": args.nt, "form": "SPLIT (precision split) + persistent queue",
                    "mode": chosen["mode"], "grid": chosen["grid"], "block": chosen["block"],
                    "l2": "flushed before every step (512 MB write), outside the timed events",
                    "accepted_steps_per_launch": chosen["accepted"] / args.steps,
                    "attempts_per_launch": attempts_per_launch},
         "e2e": e2e,
+        "df_stage": df_stage,
         "fast_fp64": fast,
         "fp32_stage": fp32_stage,
+        "plain": plain,
+        "reference_gpu": ref_gpu,
+        "speedup_vs_reference_gpu": (value / ref_gpu["value"]) if ref_gpu else None,
+        "speedup_df_stage_vs_reference_gpu": (df_stage["value"] / ref_gpu["value"]) if ref_gpu else None,
+        "speedup_fast_fp64_vs_reference_gpu": (fast["value"] / ref_gpu["value"]) if ref_gpu else None,
+        "parity": parity,
         "end_state_error_vs_fp64_oracle": errors,
         "coupled": coupled,
         "adjoint": adjoint,
         "uneven": uneven,
         "rk4": rk4,
-        "plain": plain,
-        "reference_gpu": ref_gpu,
-        "speedup_vs_reference_gpu": (value / ref_gpu["value"]) if ref_gpu else None,
-        "parity": parity,
-        "roofline": {"bound": "instruction issue (FP32 pipe)",
+        "roofline": {"bound": "fp64 pipe (instruction throughput)",
                      "achieved": achieved / 1e12 if achieved else None,
-                     "peak": peak_fp32_ops / 1e12, "unit": "T thread-instructions/s",
-                     "frac": achieved / peak_fp32_ops if achieved else None, "traffic": traffic,
-                     "thread_instructions_per_attempt": instr,
-                     "instructions_source": "smsp__inst_executed x thread/inst per step attempt, ncu capture "
-                                            "of the same kernel on 2^18 instances (profiles/roofline_traffic.json)",
+                     "peak": peak_fp64 / 1e12, "unit": "T FP64 thread-instructions/s",
+                     "frac": achieved / peak_fp64 if achieved else None, "traffic": traffic,
+                     "fp64_thread_instructions_per_attempt": fp64_instr,
+                     "instructions_source": "ncu capture of the same kernel on 2^18 instances "
+                                            "(profiles/roofline_traffic.json, profiles/perthread_split_kernel_lorenz_2e18.md)",
                      "kernel_ms": kernel_s * 1e3,
-                     "peak_source": "measured FFMA instruction rate (mpgos_probe_fma_peak, precision 4), same GPU, "
-                                    "same run: the issue ceiling every instruction shares",
+                     "peak_source": "measured FP64 FMA instruction rate (mpgos_probe_fma_peak, precision 8), same GPU, "
+                                    "same run; an FP64 add, multiply or float<->double conversion occupies the pipe "
+                                    "as long",
+                     "issue": {"thread_instructions_per_attempt": all_instr,
+                               "achieved": issue / 1e12 if issue else None, "peak": peak_fp32 / 1e12,
+                               "unit": "T thread-instructions/s", "frac": issue / peak_fp32 if issue else None,
+                               "peak_source": "measured FFMA instruction rate (precision 4)"},
                      "algorithmic_fp64_equivalent_tflops": FLOP_PER_ATTEMPT * attempts_per_launch / kernel_s / 1e12,
-                     "fp64_fma_peak_tflops": peak_fp64 / 1e12,
                      "hbm_peak_gbs_measured": peaks.get("hbm_gbs"),
                      # the HBM side of the same launch: algorithmic bytes (state, time, time
                      # domain and rho read; state, time, step counter and status words written)
