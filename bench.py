@@ -76,10 +76,10 @@ FLOP_PER_ATTEMPT = 6 * 9 + 3 * 55 + 3 * 2
 
 # Perturbations that define the stable instances (the reference arithmetic's
 # own sensitivity, measured with the PLAIN kernel, bit-identical to the
-# reference kernel): initial state moved by 1e-13 relative (end states), and
-# that plus tolerances moved by +-1e-6 relative (integer outputs: the
-# double-float stage rounding moves each error estimate by ~1e-6 of itself at
-# tol 1e-10, the same step-grid shift).
+# reference kernel): the initial state moved by 1e-13 relative (the
+# double-float rounding of the stage inputs) and the tolerances moved by
+# +-1e-6 relative (the double-float stage rounding moves each error estimate
+# by ~1e-6 of itself at tol 1e-10, the same step-grid shift).
 X_REL, TOL_REL = 1e-13, 1e-6
 
 
@@ -349,26 +349,26 @@ def scaled_rel(a, b):
     return (np.abs(a - b) / (np.abs(b) + 1e-3 * scale)).max(axis=0)
 
 
-def stable_sets(case, local, base, keys=("acci",), tol_perturb: bool = True):
+def stable_sets(case, local, base, keys=("acci",)):
     """The reference arithmetic's own sensitivity, measured with the PLAIN
-    kernel (bit-identical to the reference kernel) on the GPU: instances
-    whose end state moves by at most 1e-10 (scaled) when the initial state is
-    moved by 1e-13 relative (``end``), and, of those, the ones whose integer
-    outputs no perturbation changes (initial state; tolerances moved by
-    +-1e-6 relative when ``tol_perturb``) (``ints``)."""
+    kernel (bit-identical to the reference kernel) on the GPU, under three
+    perturbations: the initial state moved by 1e-13 relative and the
+    tolerances moved by +1e-6 and -1e-6 relative. ``end``: instances whose end
+    state moves by at most 1e-10 (scaled) under each; ``ints``: of those, the
+    ones whose integer outputs (``keys``) none of them changes."""
     from mpgos_gb300 import capi, workloads as W
     runs = []
     c = case.copy()
     c.arrays["x"] = c.arrays["x"] * (1.0 + X_REL) + (c.arrays["x"] == 0) * X_REL
-    moved = W.run_gpu(c, mode=capi.MODE_PLAIN, device=local, graph=case.phases > 1)
-    runs.append(moved)
-    end = scaled_rel(moved["x"], base["x"]) <= 1e-10
-    if tol_perturb:
-        for sgn in (1.0, -1.0):
-            c = case.copy()
-            c.rtol = c.rtol * (1.0 + sgn * TOL_REL)
-            c.atol = c.atol * (1.0 + sgn * TOL_REL)
-            runs.append(W.run_gpu(c, mode=capi.MODE_PLAIN, device=local, graph=case.phases > 1))
+    runs.append(W.run_gpu(c, mode=capi.MODE_PLAIN, device=local, graph=case.phases > 1))
+    for sgn in (1.0, -1.0):
+        c = case.copy()
+        c.rtol = c.rtol * (1.0 + sgn * TOL_REL)
+        c.atol = c.atol * (1.0 + sgn * TOL_REL)
+        runs.append(W.run_gpu(c, mode=capi.MODE_PLAIN, device=local, graph=case.phases > 1))
+    end = np.ones(case.nt, bool)
+    for r in runs:
+        end &= scaled_rel(r["x"], base["x"]) <= 1e-10
     ints = end.copy()
     for r in runs:
         for k in keys:
@@ -512,25 +512,42 @@ def adjoint_leg(local: int, flush) -> dict:
     sub = case.subset(np.arange(i0, i0 + 256))
     tgt = target_np[:, fd_block]
     grad = g64[DFM][:, fd_block]          # rows: dL/dx0, dL/dv0, dL/dk, dL/dB
-    fdv = np.zeros_like(grad)
+    # central differences at h = 10^-k max(|p|, 1), k = 4..10: over 64 forcing
+    # periods the map is strongly nonlinear for some instances (derivatives
+    # up to ~1e5), so no single h is accurate for all; per element the
+    # difference quotient of the pair of consecutive h that agree best (the
+    # converged plateau between truncation and rounding error) is the
+    # reference, and its disagreement with the next h is its own uncertainty
+    hs = [10.0 ** -k for k in range(4, 11)]
+    fd_all = np.zeros((len(hs),) + grad.shape)
     for row in range(4):
         base_x, base_cp = sub.arrays["x"].copy(), sub.arrays["cp"].copy()
         arr, j = (base_x, row) if row < 2 else (base_cp, row - 2)
-        h = 1e-6 * np.maximum(np.abs(arr[j]), 1.0)
-        loss = []
-        for sgn in (1.0, -1.0):
-            x0, cp = base_x.copy(), base_cp.copy()
-            (x0 if row < 2 else cp)[j] += sgn * h
-            xt = O.replay(sub, dt_tape, n_steps, x0=x0, cp=cp)
-            loss.append(np.sum((xt - tgt) ** 2, axis=0))
-        fdv[row] = (loss[0] - loss[1]) / (2.0 * h)
+        for ih, hrel in enumerate(hs):
+            h = hrel * np.maximum(np.abs(arr[j]), 1.0)
+            loss = []
+            for sgn in (1.0, -1.0):
+                x0, cp = base_x.copy(), base_cp.copy()
+                (x0 if row < 2 else cp)[j] += sgn * h
+                xt = O.replay(sub, dt_tape, n_steps, x0=x0, cp=cp)
+                loss.append(np.sum((xt - tgt) ** 2, axis=0))
+            fd_all[ih, row] = (loss[0] - loss[1]) / (2.0 * h)
+    scale = np.maximum(np.abs(fd_all), 1e-8)
+    spread = np.abs(np.diff(fd_all, axis=0)) / scale[1:]          # pair (h_k, h_k+1)
+    pick = np.argmin(spread, axis=0)                              # per element
+    fdv = np.take_along_axis(fd_all[1:], pick[None], 0)[0]
+    unc = np.take_along_axis(spread, pick[None], 0)[0]
     err = np.abs(grad - fdv) / np.maximum(np.abs(fdv), 1e-8)
     out["gradient_check_vs_central_differences"] = {
         "sample": f"instances {i0}..{i0 + 255} of the full run (seeded offset), FP64 forward tape, double-float "
-                  "reverse; central differences (h = 1e-6 max(|p|, 1)) of the same recorded step sequence replayed "
-                  "in FP64 by the oracle",
+                  "reverse; central differences of the same recorded step sequence replayed in FP64 by the oracle, "
+                  "h = 10^-k max(|p|, 1) for k = 4..10, per element the best-converged h",
         "max_rel_error": float(err.max()), "median_rel_error": float(np.median(err)),
-        "per_parameter_max": {n: float(err[i].max()) for i, n in enumerate(("x0", "v0", "k", "B"))}}
+        "per_parameter_max": {n: float(err[i].max()) for i, n in enumerate(("x0", "v0", "k", "B"))},
+        "within_1e-6_fraction": float(np.mean(err <= 1e-6)),
+        "max_rel_error_where_differences_converged_to_1e-7": float(err[unc <= 1e-7].max()) if (unc <= 1e-7).any()
+        else None,
+        "elements_converged_to_1e-7": float(np.mean(unc <= 1e-7))}
     return out
 
 
@@ -670,8 +687,11 @@ def uneven_leg(local: int, flush, periods: int) -> dict:
     steps = float(rref["acci"][1].sum())
     out["reference_gpu"] = {"ms": ms, "value": steps / (ms / 1e3), "best_shape": best,
                             "one_period_ms_by_shape": sweep}
-    for k in ("split_autotuned", "df_autotuned", "fp64_persistent"):
+    for k in forms:
         out[f"speedup_{k}_vs_reference_gpu"] = out[k]["value"] / out["reference_gpu"]["value"]
+    for arith in ("split", "df"):
+        best_form = max((k for k in forms if k.startswith(arith)), key=lambda k: out[k]["value"])
+        out[f"best_{arith}_form"] = best_form
     # PLAIN against the reference kernel bit for bit (two periods; one-warp blocks)
     two = case.copy()
     two.phases = 2
@@ -683,11 +703,12 @@ def uneven_leg(local: int, flush, periods: int) -> dict:
         np.array_equal(np.asarray(p2[k]).view(np.uint8), np.asarray(r2[k]).view(np.uint8))
         for k in ("x", "t", "acc", "acci")))
     # stable instances: PLAIN (= the reference kernel) with the initial state moved by 1e-13
-    end, ints = stable_sets(case, local, rref, keys=("acci",), tol_perturb=False)
+    end, ints = stable_sets(case, local, rref, keys=("acci",))
     out["stable"] = {"criterion": "PLAIN end state within 1e-10 (scaled) and event / step counts unchanged when "
-                                  "the initial state moves by 1e-13 relative",
+                                  "the initial state moves by 1e-13 relative and when the tolerances move by "
+                                  "+-1e-6 relative",
                      "end_state_instances": int(end.sum()), "integer_instances": int(ints.sum()), "of": nt}
-    for k in ("split_autotuned", "df_static_b32", "fp64_persistent"):
+    for k in (out["best_split_form"], out["best_df_form"], "fp64_persistent"):
         r = results[k]
         v = versus(r, rref, end, ints, ("acci", 1))
         ev = np.asarray(r["acci"][0]) == np.asarray(rref["acci"][0])
@@ -962,8 +983,8 @@ def main():
             "against": "the reference kernel's results (block 32) on the same inputs",
             "stable_criterion": "end states: the reference arithmetic's end state (PLAIN, bit-identical to the "
                                 "reference kernel) moves by <= 1e-10 (scaled) when the initial state moves by "
-                                "1e-13 relative; step counts: additionally unchanged under that move and under "
-                                "tolerances moved by +-1e-6 relative",
+                                "1e-13 relative and when the tolerances move by +-1e-6 relative; step counts: "
+                                "additionally unchanged under those moves",
             "stable_end_state_instances": int(end.sum()), "stable_step_count_instances": int(ints.sum()),
             "instances": args.nt,
             "split": versus(chosen["res"], ref_res, end, ints), "df_stage": versus(df_r["res"], ref_res, end, ints),

@@ -486,9 +486,15 @@ struct DfSolver {
     }
 };
 
+// Minimum resident blocks of MPGOS_MAX_BLOCK threads the DF_STAGE kernels are
+// compiled for (a register cap: 65536 / (256 x this)); a plugin may raise it.
+#ifndef MPGOS_DF_MIN_BLOCKS
+#define MPGOS_DF_MIN_BLOCKS 1
+#endif
+
 // DF_STAGE kernel: same launch contract as perthread_kernel<S, ALG, double, *>.
 template <class S, int MODE, int ALG = MPGOS_RKCK45>
-__global__ void __launch_bounds__(MPGOS_MAX_BLOCK) perthread_df_kernel(Args<double> a)
+__global__ void __launch_bounds__(MPGOS_MAX_BLOCK, MPGOS_DF_MIN_BLOCKS) perthread_df_kernel(Args<double> a)
 {
     using Sv = DfSolver<S, MODE, ALG>;
     constexpr int SD = S::SD, NSP = S::NSP, NISP = S::NISP, NE = S::NE;

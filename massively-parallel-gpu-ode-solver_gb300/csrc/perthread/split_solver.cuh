@@ -523,9 +523,15 @@ struct SplitSolver {
     }
 };
 
+// Minimum resident blocks of MPGOS_MAX_BLOCK threads the SPLIT kernels are
+// compiled for (a register cap: 65536 / (256 x this)); a plugin may raise it.
+#ifndef MPGOS_SPLIT_MIN_BLOCKS
+#define MPGOS_SPLIT_MIN_BLOCKS 1
+#endif
+
 // SPLIT kernel: same launch contract as perthread_kernel<S, ALG, double, *>.
 template <class S, int MODE, int ALG = MPGOS_RKCK45>
-__global__ void __launch_bounds__(MPGOS_MAX_BLOCK) perthread_split_kernel(Args<double> a)
+__global__ void __launch_bounds__(MPGOS_MAX_BLOCK, MPGOS_SPLIT_MIN_BLOCKS) perthread_split_kernel(Args<double> a)
 {
     using Sv = SplitSolver<S, MODE, ALG>;
     constexpr int SD = S::SD, NSP = S::NSP, NISP = S::NISP, NE = S::NE;

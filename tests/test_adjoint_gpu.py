@@ -147,6 +147,26 @@ def test_adjoint_matches_forward_sensitivities(duffing_case, native_libs, oracle
     assert np.max(rel) < 1e-4, np.max(rel)
 
 
+def test_adjoint_converges_to_forward_sensitivities(duffing_case, native_libs, oracle_libs):
+    """The comparison above with the recorded forward pass at rtol = atol =
+    1e-12 instead of 1e-9: the discrete gradient of the finer discretisation
+    and the sensitivities of the exact flow then differ by the integration
+    errors of both, and every gradient component of every instance is within
+    1e-6 relative of the forward sensitivities (the bar of the adjoint
+    against finite differences)."""
+    case, target = duffing_case
+    fine = case.copy()
+    fine.rtol = np.full_like(case.rtol, 1e-12)
+    fine.atol = np.full_like(case.atol, 1e-12)
+    xT, gx0, gcp, _ = forward_adjoint(fine, target)
+    sens = O.run_oracle(W.duffing_param_sens_case(fine, tol=1e-12))
+    S = sens["x"][2:].reshape(4, 2, case.nt)
+    lam = 2.0 * (xT - target)
+    grad_sens = np.einsum("jri,ri->ji", S, lam)
+    rel = rel_err(np.concatenate([gx0, gcp], axis=0), grad_sens)
+    assert np.max(rel) < 1e-6, np.max(rel)
+
+
 def test_adjoint_mapping_and_segments_agree(duffing_case, native_libs):
     case, target = duffing_case
     _, a0, c0, _ = forward_adjoint(case, target, mode=0, segment=32)
