@@ -633,9 +633,10 @@ def uneven_leg(local: int, flush, periods: int) -> dict:
            "phases": periods}
     per_phase = torch.empty((periods, nt), dtype=torch.float64, device=f"cuda:{local}")
 
-    def run(mode, block=128, tune=False, reps=2):
+    def run(mode, block=128, tune=False, outline=0, reps=2):
         with W.load_solver(case, mode=mode, block=block, device=local) as s:
             s.checkpoint_save()
+            s.SolverOption(capi.Option.OutlineRhs, outline)
             if tune:   # one Solve() (one period) per candidate
                 s.autotune(arithmetic=mode & (capi.MODE_FAST_CONTROL | capi.MODE_DF_STAGE | capi.MODE_SPLIT))
             grid, blk, m = s.launch_config()
@@ -656,17 +657,22 @@ def uneven_leg(local: int, flush, periods: int) -> dict:
                 "grid": grid, "block": blk, "mode": m, "outline_rhs": outline}, res
 
     P = capi.MODE_PERSISTENT
-    forms = {"split_static_b32": (SPLIT, 32, False), "split_persistent": (SPLIT | P, 128, False),
-             "split_autotuned": (SPLIT, 128, True), "df_static_b32": (DF, 32, False),
-             "df_persistent": (DF | P, 128, False), "df_autotuned": (DF, 128, True),
-             "fp64_persistent": (capi.MODE_FAST_CONTROL | P, 128, False)}
+    # (mode, block, autotuned, right-hand side out of line)
+    forms = {"split_static_b32": (SPLIT, 32, False, 0), "split_persistent": (SPLIT | P, 128, False, 0),
+             "split_static_b32_outlined": (SPLIT, 32, False, 1), "split_persistent_outlined": (SPLIT | P, 128, False, 1),
+             "split_autotuned": (SPLIT, 128, True, 0), "df_static_b32": (DF, 32, False, 0),
+             "df_persistent": (DF | P, 128, False, 0), "df_static_b32_outlined": (DF, 32, False, 1),
+             "df_persistent_outlined": (DF | P, 128, False, 1), "df_autotuned": (DF, 128, True, 0),
+             "fp64_persistent": (capi.MODE_FAST_CONTROL | P, 128, False, 0)}
     results = {}
-    for name, (mode, block, tune) in forms.items():
-        out[name], results[name] = run(mode, block, tune, reps=1 if name.startswith("fp64") else 2)
+    for name, (mode, block, tune, outline) in forms.items():
+        out[name], results[name] = run(mode, block, tune, outline, reps=1 if name.startswith("fp64") else 2)
     n = results["split_autotuned"]["acci"][1]
     out["steps_per_instance_min_max"] = [int(n.min()), int(n.max())]
-    out["persistent_over_static_split"] = out["split_static_b32"]["ms"] / out["split_persistent"]["ms"]
-    out["persistent_over_static_df"] = out["df_static_b32"]["ms"] / out["df_persistent"]["ms"]
+    for arith in ("split", "df"):
+        for tag in ("", "_outlined"):
+            out[f"persistent_over_static_{arith}{tag}"] = (out[f"{arith}_static_b32{tag}"]["ms"] /
+                                                          out[f"{arith}_persistent{tag}"]["ms"])
     shapes = reference_shapes("keller_miksis", 1, nt)
     if not shapes:
         return out
@@ -805,30 +811,74 @@ def coupled_leg(local: int, flush, periods: int) -> dict:
 
     case = CW.ring_case("ring64", ns=16384, periods=periods, seed=5)
     out = {"workload": f"ring64_16384x64_dense_rkck45_tol1e-9_{periods}periods", "unit": "accepted system-steps/s"}
-    df, rdf = run(case, capi.MODE_DF_STAGE | capi.MODE_PERSISTENT, warps=2, reps=2)
-    fp, rfp = run(case, capi.MODE_PERSISTENT, warps=4, reps=1)
-    out["df_stage"], out["fp64"] = df, fp
+    PM = capi.MODE_PERSISTENT
+    SPM, DFM = capi.MODE_SPLIT | PM, capi.MODE_DF_STAGE | PM
+    splits = {w: run(case, SPM, warps=w, reps=2) for w in (2, 4)}
+    sw = min(splits, key=lambda w: splits[w][0]["ms"])
+    sp, rsp = splits[sw]
+    sp["warps_per_block"] = sw
+    sp["by_warps_per_block_ms"] = {str(w): splits[w][0]["ms"] for w in splits}
+    df, rdf = run(case, DFM, warps=2, reps=2)
+    fp, rfp = run(case, PM, warps=4, reps=1)
+    out["split"], out["df_stage"], out["fp64"] = sp, df, fp
     from oracle import ref_gpu as R
     if R.coupled_available("ring64", 1, case.ns, 256, 4, 0):
         ref, rref = run(case, ref=(256, 4), reps=1)
         out["reference_gpu"] = ref
-        out["speedup_df_vs_reference_gpu"] = df["value"] / ref["value"]
-        out["speedup_fp64_vs_reference_gpu"] = fp["value"] / ref["value"]
+        for name, r in (("split", sp), ("df", df), ("fp64", fp)):
+            out[f"speedup_{name}_vs_reference_gpu"] = r["value"] / ref["value"]
         out["fp64_bitwise_equal_to_reference_kernel"] = bool(
             all(np.array_equal(rfp[k], rref[k]) for k in ("x", "iuacc", "isacc")))
+        # stable systems: the reference arithmetic (the FP64 kernel,
+        # bit-identical to the reference kernel) under the initial state
+        # moved by 1e-13 relative and the tolerances by +-1e-6 relative
+        moved = []
+        c = case.copy()
+        c.arrays["x"] = c.arrays["x"] * (1.0 + X_REL) + (c.arrays["x"] == 0) * X_REL
+        moved.append(CW.run_coupled_gpu(c, mode=PM, warps=4, device=local))
+        for sgn in (1.0, -1.0):
+            c = case.copy()
+            c.rtol = c.rtol * (1.0 + sgn * TOL_REL)
+            c.atol = c.atol * (1.0 + sgn * TOL_REL)
+            moved.append(CW.run_coupled_gpu(c, mode=PM, warps=4, device=local))
         mag = np.max(np.abs(rref["x"]), axis=1, keepdims=True)
-        err = (np.abs(rdf["x"] - rref["x"]) / mag).max(axis=0).reshape(case.ns, -1).max(axis=1)
-        out["df_systems_within_1e-9_of_reference"] = float(np.mean(err <= 1e-9))
-        out["df_crossing_counts_equal_fraction"] = float(np.mean(np.all(
-            rdf["iuacc"].reshape(case.ns, -1) == rref["iuacc"].reshape(case.ns, -1), axis=1)))
+
+        def sys_err(r):
+            return (np.abs(r["x"] - rref["x"]) / mag).max(axis=0).reshape(case.ns, -1).max(axis=1)
+
+        def sys_ints(r):
+            return np.all(r["iuacc"].reshape(case.ns, -1) == rref["iuacc"].reshape(case.ns, -1), axis=1) & \
+                np.all(r["isacc"].reshape(-1, case.ns) == rref["isacc"].reshape(-1, case.ns), axis=0)
+
+        end = np.ones(case.ns, bool)
+        ints = np.ones(case.ns, bool)
+        for m in moved:
+            end &= sys_err(m) <= 1e-10
+            ints &= sys_ints(m)
+        ints &= end
+        out["stable"] = {"criterion": "FP64 kernel (bit-identical to the reference kernel) end state within 1e-10 "
+                                      "and crossing / step counts unchanged when the initial state moves by 1e-13 "
+                                      "relative and when the tolerances move by +-1e-6 relative",
+                         "end_state_systems": int(end.sum()), "integer_systems": int(ints.sum()), "of": case.ns}
+        for name, r in (("split", rsp), ("df", rdf)):
+            e, same = sys_err(r), sys_ints(r)
+            out[f"{name}_vs_reference_gpu"] = {
+                "systems_within_1e-9_all": float(np.mean(e <= 1e-9)),
+                "systems_within_1e-9_stable": float(np.mean(e[end] <= 1e-9)) if end.any() else None,
+                "max_scaled_rel_stable": float(e[end].max()) if end.any() else None,
+                "crossing_and_step_counts_equal_all": float(np.mean(same)),
+                "crossing_and_step_counts_equal_stable": float(np.mean(same[ints])) if ints.any() else None}
     # adjoint on two periods
     small = CW.ring_case("ring64", ns=16384, periods=2, seed=5)
-    fp2, _r = run(small, capi.MODE_PERSISTENT, warps=4, reps=1)
-    df2, _r = run(small, capi.MODE_DF_STAGE | capi.MODE_PERSISTENT, warps=2, reps=1)
-    FP, DFM = capi.MODE_PERSISTENT, capi.MODE_DF_STAGE | capi.MODE_PERSISTENT
+    fp2, _r = run(small, PM, warps=4, reps=1)
+    df2, _r = run(small, DFM, warps=2, reps=1)
+    sp2, _r = run(small, SPM, warps=sw, reps=1)
+    FP = PM
     a64 = adjoint(small, FP, (FP, DFM), warps=4)
     adf = adjoint(small, DFM, (DFM,), warps=2)
-    forms = {"fp64": (a64[FP], fp2), "fp64_fwd_df_reverse": (a64[DFM], fp2), "df_stage": (adf[DFM], df2)}
+    asp = adjoint(small, SPM, (SPM,), warps=sw)
+    forms = {"fp64": (a64[FP], fp2), "fp64_fwd_df_reverse": (a64[DFM], fp2), "df_stage": (adf[DFM], df2),
+             "split": (asp[SPM], sp2)}
     adj = {"workload": "ring64_16384x64_dense_rkck45_tol1e-9_2periods"}
     for name, (r, f) in forms.items():
         r["forward_ms"] = f["ms"]

@@ -131,7 +131,10 @@ enum mpgos_option {
  * the accept test, the step-size factor (to FP64 accuracy), the event
  * functions, the secant step toward events, dense output and every other hook
  * in FP64. RKCK45 and RK4 (RK4 on the reference's FP64 time grid). Exclusive
- * with FP32_STAGE and DF_STAGE; FAST_CONTROL is implied. */
+ * with FP32_STAGE and DF_STAGE; FAST_CONTROL is implied. The coupled solver
+ * has it too: the unit right-hand sides, the coupling values and terms and
+ * the stage sums in double-float; the warp's accept test, minimum ratio and
+ * step factor (safety factor 0.8) in FP64. */
 #define MPGOS_MODE_SPLIT        128
 #define MPGOS_MODE_CHOSEN       (MPGOS_MODE_FAST_CONTROL | MPGOS_MODE_PERSISTENT)
 
@@ -432,7 +435,7 @@ enum mpgos_cb_option {
     MPGOS_CB_DENSE_OUTPUT_MINIMUM_TIME_STEP = 11, MPGOS_CB_SHARED_GLOBAL_VARIABLES = 12,
     MPGOS_CB_SHARED_COUPLING_MATRICES = 13,
     /* extensions */
-    MPGOS_CB_KERNEL_MODE = 32,          /* PERSISTENT and/or DF_STAGE bits  */
+    MPGOS_CB_KERNEL_MODE = 32,          /* PERSISTENT, and DF_STAGE or SPLIT */
     MPGOS_CB_MAXIMUM_ATTEMPTS = 33,     /* step attempts per system         */
     MPGOS_CB_WARPS_PER_BLOCK = 34       /* systems per CTA (one per warp)   */
 };

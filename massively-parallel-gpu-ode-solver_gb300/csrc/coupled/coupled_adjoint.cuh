@@ -462,6 +462,10 @@ struct CoupledAdjointTable {
         if (L->mode & MPGOS_MODE_DF_STAGE)
             fn = pers ? reinterpret_cast<void*>(&coupled_kernel<S, ALG, dfloat, MODE_RECORD | MPGOS_MODE_PERSISTENT>)
                       : reinterpret_cast<void*>(&coupled_kernel<S, ALG, dfloat, MODE_RECORD>);
+        else if (L->mode & MPGOS_MODE_SPLIT)
+            fn = pers ? reinterpret_cast<void*>(
+                            &coupled_kernel<S, ALG, double, MODE_RECORD | MPGOS_MODE_SPLIT | MPGOS_MODE_PERSISTENT>)
+                      : reinterpret_cast<void*>(&coupled_kernel<S, ALG, double, MODE_RECORD | MPGOS_MODE_SPLIT>);
         else
             fn = pers ? reinterpret_cast<void*>(&coupled_kernel<S, ALG, double, MODE_RECORD | MPGOS_MODE_PERSISTENT>)
                       : reinterpret_cast<void*>(&coupled_kernel<S, ALG, double, MODE_RECORD>);
@@ -481,7 +485,7 @@ struct CoupledAdjointTable {
     {
         if (tape == nullptr || tape->segment < 1 || tape->segment > pt::MAX_SEG)
             return static_cast<int>(cudaErrorInvalidValue);
-        // a DF_STAGE solver differentiates in double-float
+        // a DF_STAGE or SPLIT solver differentiates in double-float
         void* fn = adjoint_fn(L->mode);
         if (smem > 48 * 1024) {
             cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
@@ -496,8 +500,9 @@ struct CoupledAdjointTable {
 
     static void* adjoint_fn(int32_t mode)
     {
-        return (mode & MPGOS_MODE_DF_STAGE) ? reinterpret_cast<void*>(&coupled_adjoint_kernel<S, ALG, dfloat>)
-                                            : reinterpret_cast<void*>(&coupled_adjoint_kernel<S, ALG, double>);
+        return (mode & (MPGOS_MODE_DF_STAGE | MPGOS_MODE_SPLIT))
+                   ? reinterpret_cast<void*>(&coupled_adjoint_kernel<S, ALG, dfloat>)
+                   : reinterpret_cast<void*>(&coupled_adjoint_kernel<S, ALG, double>);
     }
 
     static int occupancy(int32_t mode, int block, size_t smem, int* blocks)
@@ -512,7 +517,8 @@ struct CoupledAdjointTable {
 
     static size_t smem(int warps, int32_t mode)
     {
-        return (mode & MPGOS_MODE_DF_STAGE) ? adjoint_smem_bytes<S, dfloat>(warps) : adjoint_smem_bytes<S, double>(warps);
+        return (mode & (MPGOS_MODE_DF_STAGE | MPGOS_MODE_SPLIT)) ? adjoint_smem_bytes<S, dfloat>(warps)
+                                                                 : adjoint_smem_bytes<S, double>(warps);
     }
 };
 

@@ -40,6 +40,7 @@
 
 #include "../perthread/numerics.cuh"
 #include "../perthread/dfloat.cuh"
+#include "../perthread/df_convert.cuh"
 
 #ifndef MPGOS_CB_MAX_BLOCK
 #define MPGOS_CB_MAX_BLOCK 256
@@ -137,6 +138,22 @@ struct WarpSlot {
     int didx, udt, skipped, update;
 };
 
+// SPLIT: the slot of the FP64 solver with the coupling strengths and the
+// coupling terms, which only the right-hand side reads, held as double-float
+// in the same bytes (the size and the offsets of WarpSlot<S, double>).
+template <class S>
+struct WarpSlotSplit {
+    double td[2];
+    double td_in[2];
+    double t, dt, newdt, dense_next, evdt, ratio;
+    double sp[AtLeastOne<S::NSP>::value];
+    double sacc[AtLeastOne<S::NSA>::value];
+    dfloat cstr[AtLeastOne<S::NC>::value];
+    dfloat cpt[S::UPS][AtLeastOne<S::NC>::value];
+    int isacc[AtLeastOne<S::NISA>::value];
+    int didx, udt, skipped, update;
+};
+
 template <class S, class P>
 __host__ __device__ constexpr size_t block_smem_bytes()
 {
@@ -156,8 +173,8 @@ __device__ __forceinline__ void df_dot_acc(float& sh, float& sl, dfloat m, dfloa
     sl = df::f_add(sl, df::f_add(t.lo, df::f_fma(m.hi, c.lo, df::f_fma(m.lo, c.hi, p.lo))));
 }
 
-template <class S, class P>
-__device__ __forceinline__ P coupling_value(const P* M, const WarpSlot<S, P>& w, int unit, int i)
+template <class S, class P, class W>
+__device__ __forceinline__ P coupling_value(const P* M, const W& w, int unit, int i)
 {
     constexpr int UPS = S::UPS, CBW = S::CBW, CCI = S::CCI;
     if constexpr (IS_DF<P> && CCI == 0 && CBW == 0) {
@@ -223,6 +240,46 @@ __device__ __forceinline__ float warp_minf(float v)
     return v;
 }
 
+// ---- SPLIT helpers -----------------------------------------------------------------
+// Width (log2 units) of the band around a decision inside which the FP32
+// log2 estimates (good to ~4e-6) do not decide and the exact FP64 comparison
+// runs instead; log2(1e30), the cap of the minimum ratio
+// (CoupledSystems_PerBlock_ExplicitRungeKutta_ErrorControllers.cuh starts it
+// at 1e30).
+constexpr float SPLIT_BAND = 1e-4f;
+constexpr float SPLIT_LOG2_RATIO_CAP = 99.65784f;
+
+__device__ __forceinline__ long long bits_of(double x) { return __double_as_longlong(x); }
+__device__ __forceinline__ double from_bits(long long b) { return __longlong_as_double(b); }
+__device__ __forceinline__ long long abs_bits(double x) { return bits_of(x) & 0x7FFFFFFFFFFFFFFFLL; }
+__device__ __forceinline__ long long max_bits(long long a, long long b) { return a > b ? a : b; }
+__device__ __forceinline__ long long min_bits(long long a, long long b) { return a < b ? a : b; }
+__device__ __forceinline__ bool finite_bits(double x) { return abs_bits(x) < 0x7FF0000000000000LL; }
+
+// double-float copy of an FP64 value the right-hand side reads; `range` set
+// when the value leaves float's exponent range
+__device__ __forceinline__ dfloat split_checked(double v, int& range)
+{
+    if (!df::in_float_range(v)) range = 1;
+    return df::split(v);
+}
+
+// The exact FP64 forms behind the estimates, out of line: they run only
+// inside the band.
+static __device__ __noinline__ double split_tolerance(double rtol, double atol, long long mag_bits)
+{
+    return from_bits(max_bits(bits_of(rtol * from_bits(mag_bits)), bits_of(atol)));
+}
+static __device__ __noinline__ int split_accepts(double rtol, double atol, long long mag_bits, double err)
+{
+    return bits_of(err) < bits_of(split_tolerance(rtol, atol, mag_bits));
+}
+// tol_a / err_a < tol_b / err_b for positive values, by cross multiplication
+static __device__ __noinline__ bool split_ratio_less(double tol_a, double err_a, double tol_b, double err_b)
+{
+    return tol_a * err_b < tol_b * err_a;
+}
+
 template <class S, int ALG, class P, int MODE>
 struct Solver {
     static constexpr int UPS = S::UPS, UD = S::UD, NC = S::NC, NUP = S::NUP, NUA = S::NUA, NIUA = S::NIUA;
@@ -230,7 +287,12 @@ struct Solver {
     static constexpr bool PERSISTENT = (MODE & MPGOS_MODE_PERSISTENT) != 0;
     // the tape is FP64 for both arithmetics (a double-float value is a double exactly)
     static constexpr bool RECORD = (MODE & MODE_RECORD) != 0;
-    using Slot = WarpSlot<S, P>;
+    // SPLIT: the right-hand side, the coupling and the stage sums in
+    // double-float; state, time, step, error estimate and norm, control,
+    // events and every other hook in FP64 (P = double)
+    static constexpr bool SPLIT = (MODE & MPGOS_MODE_SPLIT) != 0;
+    static_assert(!SPLIT || std::is_same<P, double>::value, "the split integrates an FP64 state");
+    using Slot = typename std::conditional<SPLIT, WarpSlotSplit<S>, WarpSlot<S, P>>::type;
     using SP   = typename StorageOf<P>::type;  // precision of the arrays in HBM
 
     // Registers of the lane's units.
@@ -241,6 +303,17 @@ struct Solver {
         int iuacc[UPL][AtLeastOne<NIUA>::value];
         P ga[UPL][AtLeastOne<NE>::value];
         P cpf[UPL][AtLeastOne<NC>::value];
+        // SPLIT: double-float copies of what the right-hand side reads (the
+        // lane's units and, per lane, the system's parameters and
+        // accessories), the coupling factors it writes, and whether a copied
+        // value left float's exponent range
+        dfloat xd[UPL][UD];
+        dfloat upd[UPL][AtLeastOne<NUP>::value];
+        dfloat uaccd[UPL][AtLeastOne<NUA>::value];
+        dfloat cpfd[UPL][AtLeastOne<NC>::value];
+        dfloat spd[AtLeastOne<NSP>::value];
+        dfloat saccd[AtLeastOne<NSA>::value];
+        int range;
     };
 
     __device__ static bool has(int lane, int j) { return lane + 32 * j < UPS; }
@@ -377,12 +450,319 @@ struct Solver {
             }
     }
 
+    // ---- SPLIT ---------------------------------------------------------------------
+    // double-float copies of the lane's unit states
+    __device__ static void split_refresh_state(int lane, Units& u)
+    {
+#pragma unroll
+        for (int j = 0; j < UPL; j++)
+            if (has(lane, j))
+#pragma unroll
+                for (int d = 0; d < UD; d++) u.xd[j][d] = split_checked(u.x[j][d], u.range);
+    }
+
+    // double-float copies of the parameters and accessories (after the hooks
+    // that may change them)
+    __device__ static void split_refresh_params(int lane, const Slot& w, Units& u)
+    {
+#pragma unroll
+        for (int k = 0; k < NSP; k++) u.spd[k] = split_checked(w.sp[k], u.range);
+#pragma unroll
+        for (int k = 0; k < NSA; k++) u.saccd[k] = split_checked(w.sacc[k], u.range);
+#pragma unroll
+        for (int j = 0; j < UPL; j++) {
+            if (!has(lane, j)) continue;
+#pragma unroll
+            for (int k = 0; k < NUP; k++) u.upd[j][k] = split_checked(u.up[j][k], u.range);
+#pragma unroll
+            for (int k = 0; k < NUA; k++) u.uaccd[j][k] = split_checked(u.uacc[j][k], u.range);
+        }
+    }
+
+    // stage_rhs of the split: the hook instantiated for dfloat on the
+    // double-float copies, the coupling value and term in double-float
+    __device__ static void stage_rhs_split(long long s, int lane, Slot& w, Units& u, const dfloat* gpd,
+                                           const int* igp, const dfloat* Md, const int* cidx, dfloat T,
+                                           dfloat (&X)[UPL][UD], dfloat (&F)[UPL][UD])
+    {
+        const int sid = static_cast<int>(s);
+#pragma unroll
+        for (int j = 0; j < UPL; j++) {
+            if (has(lane, j)) {
+                const int uid = unit_of(lane, j);
+                CoupledSystems_PerBlock_OdeFunction<dfloat>(sid, uid, F[j], X[j], T, u.upd[j], u.spd,
+                                                            const_cast<dfloat*>(gpd), const_cast<int*>(igp),
+                                                            u.uaccd[j], u.iuacc[j], u.saccd, w.isacc, w.cpt[uid],
+                                                            u.cpfd[j]);
+            }
+        }
+        __syncwarp();
+#pragma unroll
+        for (int j = 0; j < UPL; j++) {
+            if (has(lane, j)) {
+                const int uid = unit_of(lane, j);
+                for (int i = 0; i < NC; i++) {
+                    const dfloat value = coupling_value<S, dfloat>(Md, w, uid, i);
+                    const int c = cidx[i];
+                    if (c >= 0 && c < UD) F[j][c] += w.cstr[i] * u.cpfd[j][i] * value;
+                }
+            }
+        }
+        __syncwarp();
+    }
+
+    // RK4 step of the split: stages in double-float, then
+    // x + dt (k1 + 2 k2 + 2 k3 + k4) / 6 in FP64 from the stage sum rounded
+    // to FP64 (the reference's grouping, Steppers.cuh:1483-1692)
+    __device__ static void step_rk4_split(long long s, int lane, Slot& w, Units& u, const dfloat* gpd, const int* igp,
+                                          const dfloat* Md, const int* cidx, double t, double dt,
+                                          double (&xn)[UPL][UD], int& finite)
+    {
+        using df::prod_sum;
+        using df::prod_sum_add;
+        using df::prod_sum_axpy;
+        using df::prod_sum_start;
+        const dfloat td = df::split(t), dtd = df::split(dt), half(0.5f);
+        const dfloat th = df::fma(dtd, half, td);
+        dfloat X[UPL][UD], k1[UPL][UD], k2[UPL][UD], k3[UPL][UD], k4[UPL][UD];
+        stage_rhs_split(s, lane, w, u, gpd, igp, Md, cidx, td, u.xd, k1);
+#pragma unroll
+        for (int j = 0; j < UPL; j++)
+#pragma unroll
+            for (int d = 0; d < UD; d++) X[j][d] = prod_sum_axpy(dtd, prod_sum_start(half, k1[j][d]), u.xd[j][d]);
+        stage_rhs_split(s, lane, w, u, gpd, igp, Md, cidx, th, X, k2);
+#pragma unroll
+        for (int j = 0; j < UPL; j++)
+#pragma unroll
+            for (int d = 0; d < UD; d++) X[j][d] = prod_sum_axpy(dtd, prod_sum_start(half, k2[j][d]), u.xd[j][d]);
+        stage_rhs_split(s, lane, w, u, gpd, igp, Md, cidx, th, X, k3);
+#pragma unroll
+        for (int j = 0; j < UPL; j++)
+#pragma unroll
+            for (int d = 0; d < UD; d++) X[j][d] = prod_sum_axpy(dtd, prod_sum{k3[j][d].hi, k3[j][d].lo}, u.xd[j][d]);
+        stage_rhs_split(s, lane, w, u, gpd, igp, Md, cidx, td + dtd, X, k4);
+        const double sixth = dt * static_cast<double>(1.0 / 6.0);
+#pragma unroll
+        for (int j = 0; j < UPL; j++)
+#pragma unroll
+            for (int d = 0; d < UD; d++) {
+                prod_sum sm = prod_sum_start(dfloat(1.0f), k1[j][d]);
+                prod_sum_add(sm, dfloat(2.0f), k2[j][d]);
+                prod_sum_add(sm, dfloat(2.0f), k3[j][d]);
+                prod_sum_add(sm, dfloat(1.0f), k4[j][d]);
+                xn[j][d] = __fma_rn(sixth, df::widen(sm.h) + df::widen(sm.l), u.x[j][d]);
+                if (has(lane, j) && !finite_bits(xn[j][d])) finite = 0;
+            }
+    }
+
+    // Cash-Karp 4(5) step of the split: stages and stage sums in
+    // double-float (the per-thread split's sums and order), the update
+    // x + dt sum b k and the error estimate dt |sum e k| + 1e-18 in FP64
+    __device__ static void step_rkck45_split(long long s, int lane, Slot& w, Units& u, const dfloat* gpd,
+                                             const int* igp, const dfloat* Md, const int* cidx, double t, double dt,
+                                             double (&xn)[UPL][UD], double (&err)[UPL][UD], int& finite)
+    {
+        using df::fma;
+        using df::prod_sum;
+        using df::prod_sum_add;
+        using df::prod_sum_axpy;
+        using df::prod_sum_start;
+        const dfloat td = df::split(t), dtd = df::split(dt);
+        dfloat X[UPL][UD];
+        dfloat k1[UPL][UD], k2[UPL][UD], k3[UPL][UD], k4[UPL][UD], k5[UPL][UD], k6[UPL][UD];
+        stage_rhs_split(s, lane, w, u, gpd, igp, Md, cidx, td, u.xd, k1);
+#pragma unroll
+        for (int j = 0; j < UPL; j++)
+#pragma unroll
+            for (int d = 0; d < UD; d++)
+                X[j][d] = prod_sum_axpy(dtd, prod_sum_start(dfloat(1.0 / 5.0), k1[j][d]), u.xd[j][d]);
+        stage_rhs_split(s, lane, w, u, gpd, igp, Md, cidx, fma(dtd, dfloat(1.0 / 5.0), td), X, k2);
+#pragma unroll
+        for (int j = 0; j < UPL; j++)
+#pragma unroll
+            for (int d = 0; d < UD; d++) {
+                prod_sum sm = prod_sum_start(dfloat(3.0 / 40.0), k1[j][d]);
+                prod_sum_add(sm, dfloat(9.0 / 40.0), k2[j][d]);
+                X[j][d] = prod_sum_axpy(dtd, sm, u.xd[j][d]);
+            }
+        stage_rhs_split(s, lane, w, u, gpd, igp, Md, cidx, fma(dtd, dfloat(3.0 / 10.0), td), X, k3);
+#pragma unroll
+        for (int j = 0; j < UPL; j++)
+#pragma unroll
+            for (int d = 0; d < UD; d++) {
+                prod_sum sm = prod_sum_start(dfloat(3.0 / 10.0), k1[j][d]);
+                prod_sum_add(sm, dfloat(-9.0 / 10.0), k2[j][d]);
+                prod_sum_add(sm, dfloat(6.0 / 5.0), k3[j][d]);
+                X[j][d] = prod_sum_axpy(dtd, sm, u.xd[j][d]);
+            }
+        stage_rhs_split(s, lane, w, u, gpd, igp, Md, cidx, fma(dtd, dfloat(3.0 / 5.0), td), X, k4);
+#pragma unroll
+        for (int j = 0; j < UPL; j++)
+#pragma unroll
+            for (int d = 0; d < UD; d++) {
+                prod_sum sm = prod_sum_start(dfloat(-11.0 / 54.0), k1[j][d]);
+                prod_sum_add(sm, dfloat(5.0 / 2.0), k2[j][d]);
+                prod_sum_add(sm, dfloat(-70.0 / 27.0), k3[j][d]);
+                prod_sum_add(sm, dfloat(35.0 / 27.0), k4[j][d]);
+                X[j][d] = prod_sum_axpy(dtd, sm, u.xd[j][d]);
+            }
+        stage_rhs_split(s, lane, w, u, gpd, igp, Md, cidx, td + dtd, X, k5);
+#pragma unroll
+        for (int j = 0; j < UPL; j++)
+#pragma unroll
+            for (int d = 0; d < UD; d++) {
+                prod_sum sm = prod_sum_start(dfloat(1631.0 / 55296.0), k1[j][d]);
+                prod_sum_add(sm, dfloat(175.0 / 512.0), k2[j][d]);
+                prod_sum_add(sm, dfloat(575.0 / 13824.0), k3[j][d]);
+                prod_sum_add(sm, dfloat(44275.0 / 110592.0), k4[j][d]);
+                prod_sum_add(sm, dfloat(253.0 / 4096.0), k5[j][d]);
+                X[j][d] = prod_sum_axpy(dtd, sm, u.xd[j][d]);
+            }
+        stage_rhs_split(s, lane, w, u, gpd, igp, Md, cidx, fma(dtd, dfloat(7.0 / 8.0), td), X, k6);
+#pragma unroll
+        for (int j = 0; j < UPL; j++)
+#pragma unroll
+            for (int d = 0; d < UD; d++) {
+                prod_sum sb = prod_sum_start(dfloat(37.0 / 378.0), k1[j][d]);
+                prod_sum_add(sb, dfloat(250.0 / 621.0), k3[j][d]);
+                prod_sum_add(sb, dfloat(125.0 / 594.0), k4[j][d]);
+                prod_sum_add(sb, dfloat(512.0 / 1771.0), k6[j][d]);
+                prod_sum se = prod_sum_start(dfloat(37.0 / 378.0 - 2825.0 / 27648.0), k1[j][d]);
+                prod_sum_add(se, dfloat(250.0 / 621.0 - 18575.0 / 48384.0), k3[j][d]);
+                prod_sum_add(se, dfloat(125.0 / 594.0 - 13525.0 / 55296.0), k4[j][d]);
+                prod_sum_add(se, dfloat(0.0 - 277.0 / 14336.0), k5[j][d]);
+                prod_sum_add(se, dfloat(512.0 / 1771.0 - 1.0 / 4.0), k6[j][d]);
+                const double b = df::widen(sb.h) + df::widen(sb.l);
+                const double e = df::widen(se.h) + df::widen(se.l);
+                xn[j][d]  = __fma_rn(dt, b, u.x[j][d]);
+                err[j][d] = __fma_rn(dt, fabs(e), 1e-18);
+                if (has(lane, j) && (!finite_bits(xn[j][d]) || !finite_bits(err[j][d]))) finite = 0;
+            }
+    }
+
+    // Step-size control of the split over the warp (the reference's coupled
+    // controller, ErrorControllers.cuh:320-423, safety factor 0.8) on FP64
+    // values with exact decisions and an FP64-accurate factor: every lane
+    // scans its components with FP32 log2 estimates of
+    // d = log2 tol - log2 err, deciding the accept test and its smallest ratio
+    // exactly in FP64 inside a 1e-4 band; the warp takes the smallest
+    // estimate and, where lanes tie within the band, the exact minimum of
+    // their ratios by cross-multiplied FP64 products; then
+    // q = 0.8 R^(1/5) (1/4 after a rejection) to FP64 accuracy where the
+    // clamp to [shrink, grow] does not decide it alone.
+    __device__ static void control_split(int lane, const Options<double>& o, float shrink_f, float grow_f, double dt,
+                                         const Units& u, const double (&xn)[UPL][UD], const double (&err)[UPL][UD],
+                                         const double* rtol, const double* atol, const float* lrtol,
+                                         const float* latol, int& update, int& finite, int& terminate,
+                                         double& new_dt, int& status)
+    {
+        float dmin = INFINITY;
+        long long mag_m = 0;
+        double err_m = 1.0, rtol_m = 0.0, atol_m = 0.0, tol_m = 0.0;
+        bool tol_known = false, any = false;
+        int lane_update = 1;
+#pragma unroll
+        for (int j = 0; j < UPL; j++) {
+            if (!has(lane, j)) continue;
+#pragma unroll
+            for (int d = 0; d < UD; d++) {
+                const long long mag = max_bits(abs_bits(xn[j][d]), abs_bits(u.x[j][d]));
+                const float lt = fmaxf(lrtol[d] + df::log2_estimate(from_bits(mag)), latol[d]);
+                const float di = lt - df::log2_estimate(err[j][d]);
+                int accept_i;
+                if (di > SPLIT_BAND) accept_i = 1;
+                else if (di < -SPLIT_BAND) accept_i = 0;
+                else accept_i = split_accepts(rtol[d], atol[d], mag, err[j][d]);
+                lane_update = lane_update & accept_i;
+                bool take, settled = false;
+                if (!any || di < dmin - SPLIT_BAND) {
+                    take = true;
+                } else if (di > dmin + SPLIT_BAND) {
+                    take = false;
+                } else {
+                    const double tol_i = split_tolerance(rtol[d], atol[d], mag);
+                    if (!tol_known) tol_m = split_tolerance(rtol_m, atol_m, mag_m);
+                    take    = split_ratio_less(tol_i, err[j][d], tol_m, err_m);
+                    settled = true;
+                    if (take) tol_m = tol_i;
+                }
+                tol_known = settled || (!take && tol_known);
+                if (take) {
+                    dmin   = di;
+                    mag_m  = mag;
+                    err_m  = err[j][d];
+                    rtol_m = rtol[d];
+                    atol_m = atol[d];
+                }
+                any = true;
+            }
+        }
+        update = warp_all(lane_update != 0) ? 1 : 0;
+        // the warp's smallest ratio: the lanes within the band of the
+        // smallest estimate, their ratios compared exactly where several are
+        const float wmin = warp_minf(dmin);
+        const bool cand = any && !(dmin > wmin + SPLIT_BAND);
+        const unsigned cmask = __ballot_sync(0xffffffffu, cand);
+        if (cand && !tol_known) tol_m = from_bits(max_bits(bits_of(rtol_m * from_bits(mag_m)), bits_of(atol_m)));
+        int src = __ffs(cmask) - 1;
+        double tol_w = __shfl_sync(0xffffffffu, tol_m, src);
+        double err_w = __shfl_sync(0xffffffffu, err_m, src);
+        float d_w = __shfl_sync(0xffffffffu, dmin, src);
+        for (unsigned rest = cmask & (cmask - 1); rest != 0; rest &= rest - 1) {
+            src = __ffs(rest) - 1;
+            const double tol_o = __shfl_sync(0xffffffffu, tol_m, src);
+            const double err_o = __shfl_sync(0xffffffffu, err_m, src);
+            const float d_o = __shfl_sync(0xffffffffu, dmin, src);
+            if (split_ratio_less(tol_o, err_o, tol_w, err_w)) {
+                tol_w = tol_o;
+                err_w = err_o;
+                d_w = d_o;
+            }
+        }
+        // the reference's initial ratio 1e30 caps R
+        if (d_w > SPLIT_LOG2_RATIO_CAP + SPLIT_BAND ||
+            (!(d_w < SPLIT_LOG2_RATIO_CAP - SPLIT_BAND) && !split_ratio_less(tol_w, err_w, 1e30, 1.0))) {
+            d_w   = SPLIT_LOG2_RATIO_CAP;
+            tol_w = 1e30;
+            err_w = 1.0;
+        }
+        const bool fifth = (update == 1);
+        const float y0 = df::root_estimate(d_w, fifth);
+        const float qf = 0.8f * y0;
+        double q;
+        if (qf > shrink_f * (1.0f - 1e-5f) && qf < grow_f * (1.0f + 1e-5f))
+            q = 0.8 * df::root_refine(y0, tol_w, err_w, fifth);
+        else
+            q = df::widen(qf);   // outside the limits by more than the estimate's error: the clamp decides
+        if (!finite_bits(q)) finite = 0;
+        const long long dtb = bits_of(dt), guardb = bits_of(o.min_dt_guard);
+        if (finite == 0) {
+            q      = o.shrink;
+            update = 0;
+            if (dtb < guardb) {
+                terminate = 1;
+                status |= MPGOS_INSTANCE_NONFINITE;
+            }
+        } else if (dtb < guardb) {
+            update = 1;
+            status |= MPGOS_INSTANCE_MINIMUM_STEP;
+        }
+        long long qb = min_bits(bits_of(q), bits_of(o.grow));
+        qb = max_bits(qb, bits_of(o.shrink));
+        const double nd = dt * from_bits(qb);
+        new_dt = from_bits(max_bits(min_bits(bits_of(nd), bits_of(o.max_dt)), bits_of(o.min_dt)));
+    }
+
     // Integrate system s with the calling warp: the body of the reference's
     // MultipleSystems_SingleBlockLaunch kernel for one system
     // (CoupledSystmes_PerBlock_Solver.cuh:1575-2211).
+    // SPLIT: gpd / Md the double-float global parameters and matrices the
+    // right-hand side reads, lrtol / latol the log2 of the tolerances.
     __device__ static void system(long long s, int lane, Slot& w, const Args<SP>& a, const Options<P>& o,
                                   const P* gp, const int* igp, const P* M, const int* cidx, const P* rtol,
-                                  const P* atol, const P* etol, const int* edir)
+                                  const P* atol, const P* etol, const int* edir, const dfloat* gpd = nullptr,
+                                  const dfloat* Md = nullptr, const float* lrtol = nullptr,
+                                  const float* latol = nullptr)
     {
         const long long ns = a.ns, nu = a.ns * UPS;
         const int sid = static_cast<int>(s);
@@ -440,6 +820,14 @@ struct Solver {
         }
         if (o.ndo > 0) dense_store(s, lane, w, u, a, o, 1, 1);
         if constexpr (RECORD) record_checkpoint(s, lane, w, u, a, 0);
+        float shrink_f = 0.0f, grow_f = 0.0f;
+        if constexpr (SPLIT) {
+            u.range = 0;
+            split_refresh_state(lane, u);
+            split_refresh_params(lane, w, u);
+            shrink_f = static_cast<float>(o.shrink);
+            grow_f = static_cast<float>(o.grow);
+        }
 
         int status = 0, nacc = 0, nrej = 0, terminate = 0;
         long long attempts = 0;
@@ -463,7 +851,10 @@ struct Solver {
 
             // ---- stepper
             P xn[UPL][UD], err[UPL][UD];
-            if (ALG == MPGOS_RK4) {
+            if constexpr (SPLIT) {
+                if (ALG == MPGOS_RK4) step_rk4_split(s, lane, w, u, gpd, igp, Md, cidx, t, dt, xn, finite);
+                else step_rkck45_split(s, lane, w, u, gpd, igp, Md, cidx, t, dt, xn, err, finite);
+            } else if (ALG == MPGOS_RK4) {
                 step_rk4(s, lane, w, u, gp, igp, M, cidx, t, dt, xn, finite);
             } else {
                 step_rkck45(s, lane, w, u, gp, igp, M, cidx, t, dt, xn, err, finite);
@@ -481,6 +872,9 @@ struct Solver {
                     status |= MPGOS_INSTANCE_NONFINITE;
                 }
                 newdt = o.initial_dt;
+            } else if constexpr (SPLIT) {
+                control_split(lane, o, shrink_f, grow_f, dt, u, xn, err, rtol, atol, lrtol, latol, update, finite,
+                              terminate, newdt, status);
             } else if constexpr (IS_DF<P>) {
                 // DF_STAGE: exact double-float accept test, step factor
                 // 0.8 * (min tol/err)^(1/5 or 1/4) from FP32 logarithms of the
@@ -632,6 +1026,11 @@ struct Solver {
 #pragma unroll
                         for (int e = 0; e < NE; e++) u.ga[j][e] = gn[j][e];
                 }
+                if constexpr (SPLIT) {
+                    // the accepted state and whatever the hooks changed
+                    split_refresh_state(lane, u);
+                    split_refresh_params(lane, w, u);
+                }
                 if constexpr (RECORD) {
                     // frozen step size of accepted step nacc, checkpoint every seg steps
                     const int k = nacc - 1;
@@ -659,6 +1058,9 @@ struct Solver {
                                                         u.up[j], w.sp, gpm, igpm, u.uacc[j], u.iuacc[j], w.sacc,
                                                         w.isacc);
         __syncwarp();
+        if constexpr (SPLIT) {
+            if (warp_any(u.range != 0)) status |= MPGOS_INSTANCE_RANGE;
+        }
 #pragma unroll
         for (int j = 0; j < UPL; j++) {
             if (!has(lane, j)) continue;
@@ -776,9 +1178,15 @@ __global__ void __launch_bounds__(MPGOS_CB_MAX_BLOCK) coupled_kernel(Args<typena
     using Sv = Solver<S, ALG, P, MODE>;
     constexpr int UD = S::UD, NE = S::NE, NC = S::NC, NGP = S::NGP, NIGP = S::NIGP;
     constexpr bool ADAPTIVE = (ALG == MPGOS_RKCK45);
+    constexpr bool SPLIT = Sv::SPLIT;
+    // precision of the staged global parameters and matrices (those the
+    // right-hand side reads)
+    using RP = typename std::conditional<SPLIT, dfloat, P>::type;
     extern __shared__ __align__(16) unsigned char mpgos_cb_smem[];
     __shared__ P s_rtol[ADAPTIVE ? UD : 1];
     __shared__ P s_atol[ADAPTIVE ? UD : 1];
+    __shared__ float s_lrtol[(ADAPTIVE && SPLIT) ? UD : 1];
+    __shared__ float s_latol[(ADAPTIVE && SPLIT) ? UD : 1];
     __shared__ P s_etol[AtLeastOne<NE>::value];
     __shared__ int s_edir[AtLeastOne<NE>::value];
     __shared__ int s_cidx[AtLeastOne<NC>::value];
@@ -789,22 +1197,29 @@ __global__ void __launch_bounds__(MPGOS_CB_MAX_BLOCK) coupled_kernel(Args<typena
     // matrices are read from the double-float copy the runtime keeps in global
     // memory. Both are compile-time facts of the shape (the runtime applies
     // the same rule), so the matrix loads are shared-memory loads whenever
-    // the matrices sit there.
-    constexpr bool CONVERT = IS_DF<P>;
+    // the matrices sit there. SPLIT stages the same double-float copies for
+    // its right-hand side; its FP64 hooks read the global parameters in HBM.
+    constexpr bool CONVERT = IS_DF<P> || SPLIT;
     constexpr bool DF_SHARED_MATRIX =
         static_cast<size_t>(NC) * S::MAT * sizeof(dfloat) <= static_cast<size_t>(MPGOS_CB_DF_SHARED_MATRIX_BYTES);
     const int sg = CONVERT ? 1 : a.shared_global;
     const int sc = CONVERT ? (DF_SHARED_MATRIX ? 1 : 0) : a.shared_coupling;
-    P* dyn_gp = reinterpret_cast<P*>(mpgos_cb_smem);
-    P* dyn_m = dyn_gp + (sg ? NGP : 0);
+    static_assert(sizeof(RP) == sizeof(P), "the staged layout is sized by the FP64 element");
+    RP* dyn_gp = reinterpret_cast<RP*>(mpgos_cb_smem);
+    RP* dyn_m = dyn_gp + (sg ? NGP : 0);
     int* dyn_igp = reinterpret_cast<int*>(dyn_m + (sc ? NC * S::MAT : 0));
-    using Slot = WarpSlot<S, P>;
+    using Slot = typename Sv::Slot;
+    static_assert(sizeof(Slot) == sizeof(WarpSlot<S, P>), "one slot size for every arithmetic");
     Slot* slots = reinterpret_cast<Slot*>(mpgos_cb_smem + block_part_bytes<S, P>(sg, sc));
 
     for (int k = threadIdx.x; k < UD; k += blockDim.x) {
         if (ADAPTIVE) {
             s_rtol[k] = P(a.rtol[k]);
             s_atol[k] = P(a.atol[k]);
+            if constexpr (SPLIT) {
+                s_lrtol[k] = df::log2_estimate(a.rtol[k]);
+                s_latol[k] = df::log2_estimate(a.atol[k]);
+            }
         }
     }
     for (int k = threadIdx.x; k < NE; k += blockDim.x) {
@@ -813,17 +1228,25 @@ __global__ void __launch_bounds__(MPGOS_CB_MAX_BLOCK) coupled_kernel(Args<typena
     }
     for (int k = threadIdx.x; k < NC; k += blockDim.x) s_cidx[k] = a.cidx[k];
     if (sg) {
-        for (int k = threadIdx.x; k < NGP; k += blockDim.x) dyn_gp[k] = P(a.gp[k]);
+        for (int k = threadIdx.x; k < NGP; k += blockDim.x) dyn_gp[k] = RP(a.gp[k]);
         for (int k = threadIdx.x; k < NIGP; k += blockDim.x) dyn_igp[k] = a.igp[k];
     }
     if (sc)
-        for (int k = threadIdx.x; k < NC * S::MAT; k += blockDim.x) dyn_m[k] = P(a.cmat[k]);
+        for (int k = threadIdx.x; k < NC * S::MAT; k += blockDim.x) dyn_m[k] = RP(a.cmat[k]);
     __syncthreads();
 
     const P* gp;
     const int* igp;
     const P* M;
-    if constexpr (CONVERT) {
+    const dfloat* gpd = nullptr;
+    const dfloat* Md = nullptr;
+    if constexpr (SPLIT) {
+        gp = reinterpret_cast<const P*>(a.gp);
+        igp = dyn_igp;
+        M = reinterpret_cast<const P*>(a.cmat);
+        gpd = dyn_gp;
+        Md = sc ? dyn_m : static_cast<const dfloat*>(a.cmat_df);
+    } else if constexpr (CONVERT) {
         gp = dyn_gp;
         igp = dyn_igp;
         M = sc ? dyn_m : static_cast<const P*>(a.cmat_df);
@@ -851,7 +1274,7 @@ __global__ void __launch_bounds__(MPGOS_CB_MAX_BLOCK) coupled_kernel(Args<typena
     long long s = static_cast<long long>(blockIdx.x) * warps + warp;
     const long long total = static_cast<long long>(gridDim.x) * warps;
     while (s < a.n_active) {
-        Sv::system(s, lane, w, a, o, gp, igp, M, s_cidx, s_rtol, s_atol, s_etol, s_edir);
+        Sv::system(s, lane, w, a, o, gp, igp, M, s_cidx, s_rtol, s_atol, s_etol, s_edir, gpd, Md, s_lrtol, s_latol);
         if (!Sv::PERSISTENT) break;
         unsigned next = 0;
         if (lane == 0) next = atomicAdd(a.work, 1u);
@@ -919,6 +1342,11 @@ struct KernelTable {
                 return (mode & MPGOS_MODE_PERSISTENT)
                            ? reinterpret_cast<void*>(&coupled_kernel<S, ALG, dfloat, MPGOS_MODE_PERSISTENT>)
                            : reinterpret_cast<void*>(&coupled_kernel<S, ALG, dfloat, 0>);
+            if (mode & MPGOS_MODE_SPLIT)
+                return (mode & MPGOS_MODE_PERSISTENT)
+                           ? reinterpret_cast<void*>(
+                                 &coupled_kernel<S, ALG, double, MPGOS_MODE_SPLIT | MPGOS_MODE_PERSISTENT>)
+                           : reinterpret_cast<void*>(&coupled_kernel<S, ALG, double, MPGOS_MODE_SPLIT>);
         }
         return (mode & MPGOS_MODE_PERSISTENT) ? reinterpret_cast<void*>(&coupled_kernel<S, ALG, P, MPGOS_MODE_PERSISTENT>)
                                               : reinterpret_cast<void*>(&coupled_kernel<S, ALG, P, 0>);

@@ -22,8 +22,9 @@
 //   div             two long-division correction steps on a float quotient
 //   sqrt            Karp & Markstein 1997 (Newton corrections from rsqrt)
 // sin, cos, sincospi, exp, log and pow run on the FP32 pipe too (Cody-Waite
-// reductions, Taylor series, one Newton step for log; below); only arguments
-// outside their ranges fall back to CUDA's FP64 functions.
+// reductions, a table of sin / cos at multiples of pi/128 (Tang 1991), Taylor
+// series, one Newton step for log; below); only arguments outside their
+// ranges fall back to CUDA's FP64 functions.
 //
 // Hook code templated on its precision (the reference's
 // `template <class Precision> __device__ void PerThread_OdeFunction(...)`)
@@ -33,6 +34,8 @@
 #pragma once
 
 #include <cmath>
+
+#include "dfloat_trig_table.h"
 
 #if defined(__CUDACC__)
 #include <cuda_runtime.h>
@@ -333,8 +336,108 @@ MPGOS_DF_HD dfloat cos_kernel(dfloat r)
 }
 }  // namespace detail
 
+// ---- table-driven sine and cosine (Tang 1991) ------------------------------------
+// x = k pi/128 + r: k the nearest integer to x 128/pi, r by Cody & Waite with
+// pi/128 in three floats (the pi/2 split above scaled by 2^-6, each product
+// k P_i exact by two_prod; |r| <= 0.58 pi/128 for |x| < 2^14). With k = 64 q + j
+// the table gives sin and cos of the angle a = q pi/2 + j pi/128 (entries of
+// three floats, rotated by the quadrant q); with z = r^2
+//   h = 1 - cos r = z/2 - z^2/24 + z^3/720,   s = sin r = r - r z (1/6 - z/120)
+// (the next terms are below 1e-19 at |r| <= 0.58 pi/128), and
+//   cos x = C - (C h + S s),   sin x = S - (S h - C s)
+// so that the table value enters exactly and only the small correction
+// (|.| < 0.015) carries the rounding of the polynomials and products.
+// About 100 FP32 operations for either function against ~150 for the series
+// on |r| <= pi/4, and half the dependent chain.
+namespace detail {
+constexpr float INV_PIO128 = 0x1.45f306p+5f;   // 128/pi
+constexpr float PIO128_1 = PIO2_1 * 0x1p-6f;   // pi/128 = (PIO2_1 + PIO2_2 + PIO2_3) 2^-6
+constexpr float PIO128_2 = PIO2_2 * 0x1p-6f;
+constexpr float PIO128_3 = PIO2_3 * 0x1p-6f;
+constexpr float SIXTH_HI = 0x1.555556p-3f;     // 1/6 = SIXTH_HI + SIXTH_LO
+constexpr float SIXTH_LO = -0x1.555556p-28f;
+constexpr float TRIG_TABLE_LIMIT = 0x1p+14f;   // |x| below: the table path
+
+#if defined(__CUDACC__)
+static __device__ const float4 TRIG_MAIN_DEV[64] = {MPGOS_DF_TRIG_TABLE_MAIN};
+static __device__ const float2 TRIG_TAIL_DEV[64] = {MPGOS_DF_TRIG_TABLE_TAIL};
+#endif
+static const float TRIG_MAIN_HOST[64][4] = {MPGOS_DF_TRIG_TABLE_MAIN};
+static const float TRIG_TAIL_HOST[64][2] = {MPGOS_DF_TRIG_TABLE_TAIL};
+
+// x - k pi/128 for |x| < 2^14, k the nearest integer to x 128/pi
+MPGOS_DF_HD dfloat reduce_pio128(dfloat x, int& k)
+{
+    const float kf = f_rint(f_mul(x.hi, INV_PIO128));
+    const dfloat p1 = two_prod(kf, PIO128_1);
+    const dfloat p2 = two_prod(kf, PIO128_2);
+    const dfloat a = two_sum(x.hi, -p1.hi);                       // exact (Sterbenz)
+    const dfloat u = two_sum(a.hi, f_add(f_sub(x.lo, p1.lo), a.lo));   // the only rounding at ~2^-24 |x|
+    const dfloat b = two_sum(u.hi, -p2.hi);
+    float e = f_sub(u.lo, p2.lo);                                  // the rest at ~2^-24 |r|
+    e = f_fma(-kf, PIO128_3, e);
+    e = f_add(e, b.lo);
+    k = static_cast<int>(kf);
+    return two_sum(b.hi, e);
+}
+
+// A + A2 - w for a table value A + A2 (A2 the third float) and a small w:
+// the accurate add (both parts by two_sum), A2 joining the last tail, so the
+// result carries one rounding of its own low float
+MPGOS_DF_HD dfloat table_minus(dfloat A, float A2, dfloat w)
+{
+    const dfloat t = two_sum(A.hi, -w.hi);
+    const dfloat u = two_sum(A.lo, -w.lo);
+    const dfloat v = quick_two_sum(t.hi, f_add(t.lo, u.hi));
+    return quick_two_sum(v.hi, f_add(v.lo, f_add(u.lo, A2)));
+}
+
+// sin and cos of k pi/128 + r, |r| <= 0.6 pi/128
+MPGOS_DF_HD void sincos_table(dfloat r, int k, dfloat* s_out, dfloat* c_out)
+{
+    const int j = k & 63, q = (k >> 6) & 3;
+#if defined(__CUDA_ARCH__)
+    const float4 m = __ldg(&TRIG_MAIN_DEV[j]);
+    const float2 t = __ldg(&TRIG_TAIL_DEV[j]);
+    const dfloat S(m.x, m.y), C(m.z, m.w);
+    const float S2 = t.x, C2 = t.y;
+#else
+    const dfloat S(TRIG_MAIN_HOST[j][0], TRIG_MAIN_HOST[j][1]), C(TRIG_MAIN_HOST[j][2], TRIG_MAIN_HOST[j][3]);
+    const float S2 = TRIG_TAIL_HOST[j][0], C2 = TRIG_TAIL_HOST[j][1];
+#endif
+    // rotate by the quadrant without branches: (sin a, cos a) of a = q pi/2 + j pi/128
+    const bool odd = (q & 1) != 0, sneg = (q & 2) != 0, cneg = ((q + 1) & 2) != 0;
+    dfloat Sa = odd ? C : S, Ca = odd ? S : C;
+    float Sa2 = odd ? C2 : S2, Ca2 = odd ? S2 : C2;
+    Sa = sneg ? -Sa : Sa;
+    Sa2 = sneg ? -Sa2 : Sa2;
+    Ca = cneg ? -Ca : Ca;
+    Ca2 = cneg ? -Ca2 : Ca2;
+    // z = r^2 (unnormalised pair), h = 1 - cos r, s = sin r
+    const dfloat zz = two_prod(r.hi, r.hi);
+    const float zh = zz.hi, zl = f_fma(f_add(r.hi, r.hi), r.lo, zz.lo);
+    const float g = f_mul(f_mul(zh, zh), f_fma(zh, -1.0f / 720.0f, 1.0f / 24.0f));
+    const dfloat h(f_mul(0.5f, zh), f_fma(0.5f, zl, -g));
+    const dfloat rz = two_prod(r.hi, zh);                                  // r z
+    const float rzl = f_fma(r.hi, zl, f_fma(r.lo, zh, rz.lo));
+    const dfloat m6 = two_prod(rz.hi, SIXTH_HI);                           // r z (1/6 - z/120)
+    const float m6l = f_fma(rz.hi, f_fma(zh, -1.0f / 120.0f, SIXTH_LO), f_fma(rzl, SIXTH_HI, m6.lo));
+    const dfloat s0 = quick_two_sum(r.hi, -m6.hi);
+    const dfloat s(s0.hi, f_add(s0.lo, f_sub(r.lo, m6l)));
+    *c_out = table_minus(Ca, Ca2, dot2(Ca, h, Sa, s));
+    *s_out = table_minus(Sa, Sa2, dot2(Sa, h, -Ca, s));
+}
+}  // namespace detail
+
 MPGOS_DF_HD dfloat sin(dfloat a)
 {
+    if (std::fabs(a.hi) < detail::TRIG_TABLE_LIMIT) {
+        int k;
+        const dfloat r = detail::reduce_pio128(a, k);
+        dfloat s, c;
+        detail::sincos_table(r, k, &s, &c);
+        return s;
+    }
     int q;
     const dfloat r = detail::reduce_pio2(a, q);
     switch (q) {
@@ -347,6 +450,13 @@ MPGOS_DF_HD dfloat sin(dfloat a)
 
 MPGOS_DF_HD dfloat cos(dfloat a)
 {
+    if (std::fabs(a.hi) < detail::TRIG_TABLE_LIMIT) {
+        int k;
+        const dfloat r = detail::reduce_pio128(a, k);
+        dfloat s, c;
+        detail::sincos_table(r, k, &s, &c);
+        return c;
+    }
     int q;
     const dfloat r = detail::reduce_pio2(a, q);
     switch (q) {
@@ -549,16 +659,30 @@ MPGOS_DF_HD void sincos_quadrant(dfloat r, int q, dfloat* s, dfloat* c)
 // sin and cos of one argument with one reduction
 MPGOS_DF_HD void sincos(dfloat a, dfloat* s, dfloat* c)
 {
+    if (std::fabs(a.hi) < detail::TRIG_TABLE_LIMIT) {
+        int k;
+        const dfloat r = detail::reduce_pio128(a, k);
+        detail::sincos_table(r, k, s, c);
+        return;
+    }
     int q;
     const dfloat r = detail::reduce_pio2(a, q);
     detail::sincos_quadrant(r, q, s, c);
 }
 
-// sin(pi a) and cos(pi a): a = k/2 + f with k the nearest integer to 2a and
-// |f| <= 1/4, f exact (a.hi - k/2 is exact by Sterbenz's lemma, the low part
-// joins by two_sum), then both kernels of pi f; no rounding grows with |a|.
+// sin(pi a) and cos(pi a): a = k/128 + f with k the nearest integer to 128 a
+// and |f| <= 1/256, f exact (a.hi - k/128 is exact by Sterbenz's lemma, the
+// low part joins by two_sum), then the table path on pi f (|a| < 2^16; up to
+// 2^22 the same with k/2 and both series kernels); no rounding grows with |a|.
 MPGOS_DF_HD void sincospi(dfloat a, dfloat* s, dfloat* c)
 {
+    if (std::fabs(a.hi) < 0x1p+16f) {
+        const float k = f_rint(f_mul(a.hi, 128.0f));
+        const dfloat f = two_sum(f_sub(a.hi, f_mul(k, 0x1p-7f)), a.lo);
+        const dfloat r = f * dfloat(0x1.921fb6p+1f, -0x1.777a5cp-24f);   // pi
+        detail::sincos_table(r, static_cast<int>(k), s, c);
+        return;
+    }
     if (!(std::fabs(a.hi) < 0x1p+22f)) {   // beyond, a is an integer or half-integer multiple
         sincos(a * dfloat(0x1.921fb6p+1f, -0x1.777a5cp-24f), s, c);
         return;

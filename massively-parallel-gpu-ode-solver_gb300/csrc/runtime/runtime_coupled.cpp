@@ -303,11 +303,15 @@ MPGOS_EXPORT int mpgos_cb_set_option(mpgos_cb_solver* s, int32_t option, int32_t
             return push_options(s);
         case MPGOS_CB_KERNEL_MODE:
             if (value < 0 || value != static_cast<int>(value) ||
-                (static_cast<int32_t>(value) & ~(MPGOS_MODE_PERSISTENT | MPGOS_MODE_DF_STAGE | MPGOS_MODE_FAST_CONTROL)))
-                return fail(MPGOS_ERR_ARGUMENT, "coupled kernel mode %g: only PERSISTENT and DF_STAGE apply", value);
-            if ((static_cast<int32_t>(value) & MPGOS_MODE_DF_STAGE) && s->sh.precision_bytes != 8)
-                return fail(MPGOS_ERR_UNSUPPORTED, "DF_STAGE needs a double-precision coupled table");
-            s->mode = static_cast<int32_t>(value) & (MPGOS_MODE_PERSISTENT | MPGOS_MODE_DF_STAGE);
+                (static_cast<int32_t>(value) &
+                 ~(MPGOS_MODE_PERSISTENT | MPGOS_MODE_DF_STAGE | MPGOS_MODE_SPLIT | MPGOS_MODE_FAST_CONTROL)))
+                return fail(MPGOS_ERR_ARGUMENT, "coupled kernel mode %g: only PERSISTENT, DF_STAGE and SPLIT apply",
+                            value);
+            if ((static_cast<int32_t>(value) & MPGOS_MODE_DF_STAGE) && (static_cast<int32_t>(value) & MPGOS_MODE_SPLIT))
+                return fail(MPGOS_ERR_ARGUMENT, "coupled kernel mode %g: DF_STAGE and SPLIT exclude each other", value);
+            if ((static_cast<int32_t>(value) & (MPGOS_MODE_DF_STAGE | MPGOS_MODE_SPLIT)) && s->sh.precision_bytes != 8)
+                return fail(MPGOS_ERR_UNSUPPORTED, "DF_STAGE and SPLIT need a double-precision coupled table");
+            s->mode = static_cast<int32_t>(value) & (MPGOS_MODE_PERSISTENT | MPGOS_MODE_DF_STAGE | MPGOS_MODE_SPLIT);
             break;
         case MPGOS_CB_MAXIMUM_ATTEMPTS:
             if (value < 1) return fail(MPGOS_ERR_ARGUMENT, "MaximumAttempts must be >= 1");
@@ -393,9 +397,12 @@ namespace {
 int prepare_launch(mpgos_cb_solver* s, bool record, mpgos_cb_launch& L, int64_t& grid_out, int& block_out,
                    size_t& smem_out)
 {
-    const int32_t mode = record ? (s->mode & (MPGOS_MODE_PERSISTENT | MPGOS_MODE_DF_STAGE)) : s->mode;
+    const int32_t mode =
+        record ? (s->mode & (MPGOS_MODE_PERSISTENT | MPGOS_MODE_DF_STAGE | MPGOS_MODE_SPLIT)) : s->mode;
     const int block = 32 * s->warps;
-    const bool df = (mode & MPGOS_MODE_DF_STAGE) != 0;
+    // the double-float kernels (DF_STAGE, and SPLIT for its right-hand side)
+    // stage double-float copies of the global parameters and matrices
+    const bool df = (mode & (MPGOS_MODE_DF_STAGE | MPGOS_MODE_SPLIT)) != 0;
     const long long n_matrix = static_cast<long long>(s->sh.nc) * s->sh.matrix_entries;
     // DF_STAGE: matrices in shared memory exactly when the kernel's
     // compile-time rule says so (MPGOS_CB_DF_SHARED_MATRIX_BYTES)
@@ -534,8 +541,8 @@ MPGOS_EXPORT int mpgos_cb_adjoint(mpgos_cb_solver* s, const double* dLdxT, doubl
         return fail(MPGOS_ERR_ARGUMENT, "null gradient buffer");
     if (s->n_active <= 0) return MPGOS_OK;
     CB_CUDA(cudaSetDevice(s->device));
-    // the reverse pass computes in double-float when the solver does
-    const int32_t amode = s->mode & MPGOS_MODE_DF_STAGE;
+    // the reverse pass computes in double-float when the solver's stages do
+    const int32_t amode = (s->mode & (MPGOS_MODE_DF_STAGE | MPGOS_MODE_SPLIT)) ? MPGOS_MODE_DF_STAGE : 0;
     // warps (systems) per block: the most resident warps per SM, the smaller
     // block on ties (shared memory holds the coupling matrices once per block)
     int warps = 0, best = -1;

@@ -218,7 +218,7 @@ def _main(argv=None) -> int:
     ap.add_argument("--system", default="ring64", choices=sorted(CB_SHAPES))
     ap.add_argument("--ns", type=int, default=2048)
     ap.add_argument("--periods", type=float, default=2)
-    ap.add_argument("--mode", type=int, default=0, help="MPGOS_MODE_* bits (PERSISTENT 2, DF_STAGE 16)")
+    ap.add_argument("--mode", type=int, default=0, help="MPGOS_MODE_* bits (PERSISTENT 2, DF_STAGE 16, SPLIT 128)")
     ap.add_argument("--warps", type=int, default=4)
     ap.add_argument("--launches", type=int, default=1)
     ap.add_argument("--adjoint", type=int, default=0, metavar="SEG",

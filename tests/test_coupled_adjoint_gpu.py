@@ -93,14 +93,15 @@ def test_coupled_adjoint_matches_central_differences(system, native_libs, oracle
 DF_PERSISTENT = capi.MODE_DF_STAGE | capi.MODE_PERSISTENT
 
 
+@pytest.mark.parametrize("arith", [capi.MODE_DF_STAGE, capi.MODE_SPLIT], ids=["df_stage", "split"])
 @pytest.mark.parametrize("system", ["ring16_full", "ring16_band", "ring64"])
-def test_coupled_df_adjoint_matches_central_differences(system, native_libs, oracle_libs):
-    """DF_STAGE records its double-float step sequence and reverses in
+def test_coupled_df_adjoint_matches_central_differences(system, arith, native_libs, oracle_libs):
+    """DF_STAGE and SPLIT record their step sequences and reverse in
     double-float; same 1e-6 bar against FP64 central differences of the
     replayed map."""
     ns = 32 if system == "ring64" else 64
     case = CW.ring_case(system, ns=ns, periods=1, seed=44)
-    xT, status, dt, n, gx0, gsp = forward_adjoint(case, mode=DF_PERSISTENT)
+    xT, status, dt, n, gx0, gsp = forward_adjoint(case, mode=arith | capi.MODE_PERSISTENT)
     assert np.all(status & capi.INSTANCE_TAPE_OVERFLOW == 0)
     base = O.replay_coupled(case, dt, n)
     assert np.max(np.abs(base - xT)) < 1e-9

@@ -131,17 +131,23 @@ def test_coupled_matches_oracle(system, native_libs, oracle_libs):
     np.testing.assert_array_equal(res["isacc"][0], res["nacc"])
 
 
+DF_MODES = [capi.MODE_DF_STAGE, capi.MODE_SPLIT]
+DF_IDS = ["df_stage", "split"]
+
+
+@pytest.mark.parametrize("arith", DF_MODES, ids=DF_IDS)
 @pytest.mark.parametrize("system", ["ring16_full", "ring64", "ring256"])
-def test_coupled_df_stage_matches_oracle(system, native_libs, oracle_libs):
+def test_coupled_double_float_modes_match_oracle(system, arith, native_libs, oracle_libs):
     """DF_STAGE (double-float stages, coupling dot products and sin/cos on the
-    FP32 pipe): end states within 1e-9 of the component scale or the oracle's
-    own perturbation spread; integer outputs equal on the systems the
-    perturbations leave unchanged, with the step-flip allowance."""
-    from tests.parity import assert_ints_equal
+    FP32 pipe) and SPLIT (the same right-hand side, coupling and stage sums;
+    FP64 update, error norm, control and events): end states within 1e-9 of
+    the component scale or the oracle's own perturbation spread; integer
+    outputs equal on the systems the perturbations leave unchanged, with the
+    step-flip allowance."""
     ns, periods = {"ring64": (128, 1), "ring256": (24, 1)}.get(system, (256, 2))
     case = CW.ring_case(system, ns=ns, periods=periods, seed=14)
     ora, spread, stable = _spread(case)
-    res = CW.run_coupled_gpu(case, mode=capi.MODE_DF_STAGE | capi.MODE_PERSISTENT, warps=4)
+    res = CW.run_coupled_gpu(case, mode=arith | capi.MODE_PERSISTENT, warps=4)
     assert np.all(res["status"] == 0) and np.all(res["t"] == case.arrays["td"][1])
     mag = np.max(np.abs(case.arrays["x"]), axis=-1)
     ok = scaled_close(res["x"], ora["x"], 1e-9, mag, floor=1.0) | (np.abs(res["x"] - ora["x"]) <= 1e3 * spread)
@@ -162,11 +168,38 @@ def test_coupled_df_stage_matches_oracle(system, native_libs, oracle_libs):
     np.testing.assert_array_equal(res["isacc"][0], res["nacc"])
 
 
-def test_coupled_df_stage_mapping_is_invariant(native_libs):
+@pytest.mark.parametrize("arith", DF_MODES, ids=DF_IDS)
+def test_coupled_double_float_mapping_is_invariant(arith, native_libs):
     case = CW.ring_case("ring64", ns=96, periods=1, seed=12)
-    base = CW.run_coupled_gpu(case, mode=capi.MODE_DF_STAGE, warps=1)
+    base = CW.run_coupled_gpu(case, mode=arith, warps=1)
     for warps in (2, 4, 8):
-        assert_bitwise(base, CW.run_coupled_gpu(case, mode=capi.MODE_DF_STAGE | capi.MODE_PERSISTENT, warps=warps))
+        assert_bitwise(base, CW.run_coupled_gpu(case, mode=arith | capi.MODE_PERSISTENT, warps=warps))
+
+
+def test_coupled_split_rk4_keeps_the_reference_time_grid(native_libs, oracle_libs):
+    """SPLIT RK4: the FP64 time grid of the reference (t += dt in FP64), so
+    every system takes exactly the oracle's steps; end states within 1e-11
+    of the component scale (double-float stages, FP64 update)."""
+    case = CW.ring_case("ring16_full", ns=128, periods=2, seed=16, algorithm=0)
+    ora = O.run_oracle_coupled(case)
+    res = CW.run_coupled_gpu(case, mode=capi.MODE_SPLIT | capi.MODE_PERSISTENT, warps=4)
+    assert np.all(res["status"] == 0)
+    np.testing.assert_array_equal(res["t"], ora["t"])
+    np.testing.assert_array_equal(res["nacc"], ora["nacc"])
+    mag = np.max(np.abs(case.arrays["x"]), axis=-1)
+    assert scaled_close(res["x"], ora["x"], 1e-11, mag, floor=1.0).all()
+
+
+def test_coupled_split_flags_values_outside_float_range(native_libs):
+    """A system parameter below float's normal range (1e-40) cannot be held
+    by a double-float: SPLIT flags the system MPGOS_INSTANCE_RANGE and keeps
+    integrating; the other systems are unflagged."""
+    case = CW.ring_case("ring16_full", ns=64, periods=1, seed=17)
+    case.arrays["sp"][0, 5] = 1e-40
+    res = CW.run_coupled_gpu(case, mode=capi.MODE_SPLIT, warps=4)
+    flagged = (res["status"] & capi.INSTANCE_RANGE) != 0
+    assert flagged[5] and flagged.sum() == 1
+    assert np.all(res["t"] == case.arrays["td"][1])
 
 
 @pytest.mark.parametrize("tpb,spb,alg", [(64, 1, 1), (32, 1, 1), (64, 2, 1), (32, 1, 0)],
@@ -220,19 +253,21 @@ def test_large_systems_match_reference_kernels(tpb, native_libs):
         assert_bitwise(res, ref, keys=KEYS)
 
 
-def test_large_systems_double_float_reads_global_matrices(native_libs):
-    """DF_STAGE with a 256x256 coupling matrix (512 KB as double-floats, more
-    than shared memory holds): the kernel reads the runtime's double-float copy
-    from global memory; the mapping changes nothing (bit-identical), and a
-    matrix changed on the host between solves is converted again."""
+@pytest.mark.parametrize("arith", DF_MODES, ids=DF_IDS)
+def test_large_systems_double_float_reads_global_matrices(arith, native_libs):
+    """DF_STAGE and SPLIT with a 256x256 coupling matrix (512 KB as
+    double-floats, more than shared memory holds): the kernel reads the
+    runtime's double-float copy from global memory; the mapping changes
+    nothing (bit-identical), and a matrix changed on the host between solves
+    is converted again."""
     case = CW.ring_case("ring256", ns=24, periods=1, seed=14)
-    base = CW.run_coupled_gpu(case, mode=capi.MODE_DF_STAGE, warps=1)
+    base = CW.run_coupled_gpu(case, mode=arith, warps=1)
     assert np.all(base["status"] == 0)
-    assert_bitwise(base, CW.run_coupled_gpu(case, mode=capi.MODE_DF_STAGE | capi.MODE_PERSISTENT, warps=2))
+    assert_bitwise(base, CW.run_coupled_gpu(case, mode=arith | capi.MODE_PERSISTENT, warps=2))
     other = case.copy()
     other.arrays["cmat"] = other.arrays["cmat"] * 0.5
-    fresh = CW.run_coupled_gpu(other, mode=capi.MODE_DF_STAGE, warps=1)
-    with CW.load_coupled_solver(case, mode=capi.MODE_DF_STAGE, warps=1) as s:
+    fresh = CW.run_coupled_gpu(other, mode=arith, warps=1)
+    with CW.load_coupled_solver(case, mode=arith, warps=1) as s:
         s.Solve()
         s.host(V.ActualTime)[:] = other.arrays["t"]
         s.host(V.ActualState)[:] = other.arrays["x"]
