@@ -846,28 +846,40 @@ def coupled_leg(local: int, flush, periods: int) -> dict:
         def sys_err(r):
             return (np.abs(r["x"] - rref["x"]) / mag).max(axis=0).reshape(case.ns, -1).max(axis=1)
 
-        def sys_ints(r):
-            return np.all(r["iuacc"].reshape(case.ns, -1) == rref["iuacc"].reshape(case.ns, -1), axis=1) & \
-                np.all(r["isacc"].reshape(-1, case.ns) == rref["isacc"].reshape(-1, case.ns), axis=0)
+        def crossings(r):   # every unit's zero-crossing count (the unit event, an integer accessory)
+            return np.all(r["iuacc"].reshape(case.ns, -1) == rref["iuacc"].reshape(case.ns, -1), axis=1)
+
+        def steps(r):       # accepted steps (the system accessory counted by unit 0's hook)
+            return np.all(r["isacc"].reshape(-1, case.ns) == rref["isacc"].reshape(-1, case.ns), axis=0)
 
         end = np.ones(case.ns, bool)
-        ints = np.ones(case.ns, bool)
+        cross_ok = np.ones(case.ns, bool)
+        steps_ok = np.ones(case.ns, bool)
         for m in moved:
             end &= sys_err(m) <= 1e-10
-            ints &= sys_ints(m)
-        ints &= end
-        out["stable"] = {"criterion": "FP64 kernel (bit-identical to the reference kernel) end state within 1e-10 "
-                                      "and crossing / step counts unchanged when the initial state moves by 1e-13 "
-                                      "relative and when the tolerances move by +-1e-6 relative",
-                         "end_state_systems": int(end.sum()), "integer_systems": int(ints.sum()), "of": case.ns}
+            cross_ok &= crossings(m)
+            steps_ok &= steps(m)
+        cross_ok &= end
+        steps_ok &= end
+        out["stable"] = {"criterion": "FP64 kernel (bit-identical to the reference kernel) end state within 1e-10, "
+                                      "and crossing (resp. step) counts unchanged, when the initial state moves by "
+                                      "1e-13 relative and when the tolerances move by +-1e-6 relative",
+                         "end_state_systems": int(end.sum()), "crossing_count_systems": int(cross_ok.sum()),
+                         "step_count_systems": int(steps_ok.sum()), "of": case.ns,
+                         "step_count_cause": "each system lands ~4 zero crossings per unit and period on the "
+                                             "+-1e-6 event band (hundreds per system); a landing whose event value is "
+                                             "a rounding error from the band edge takes one more secant step under "
+                                             "any change of rounding, so the step counts of most systems move"}
         for name, r in (("split", rsp), ("df", rdf)):
-            e, same = sys_err(r), sys_ints(r)
+            e, cr, st = sys_err(r), crossings(r), steps(r)
             out[f"{name}_vs_reference_gpu"] = {
                 "systems_within_1e-9_all": float(np.mean(e <= 1e-9)),
                 "systems_within_1e-9_stable": float(np.mean(e[end] <= 1e-9)) if end.any() else None,
                 "max_scaled_rel_stable": float(e[end].max()) if end.any() else None,
-                "crossing_and_step_counts_equal_all": float(np.mean(same)),
-                "crossing_and_step_counts_equal_stable": float(np.mean(same[ints])) if ints.any() else None}
+                "crossing_counts_equal_all": float(np.mean(cr)),
+                "crossing_counts_equal_stable": float(np.mean(cr[cross_ok])) if cross_ok.any() else None,
+                "step_counts_equal_all": float(np.mean(st)),
+                "step_counts_equal_stable": float(np.mean(st[steps_ok])) if steps_ok.any() else None}
     # adjoint on two periods
     small = CW.ring_case("ring64", ns=16384, periods=2, seed=5)
     fp2, _r = run(small, PM, warps=4, reps=1)

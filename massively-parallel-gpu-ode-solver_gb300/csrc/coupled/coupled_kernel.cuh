@@ -340,10 +340,16 @@ struct Solver {
         for (int j = 0; j < UPL; j++) {
             if (has(lane, j)) {
                 const int uid = unit_of(lane, j);
+#pragma unroll
                 for (int i = 0; i < NC; i++) {
                     const P value = coupling_value<S, P>(M, w, uid, i);
-                    const int c = cidx[i];  // validated on the host; guarded against a stale device copy
-                    if (c >= 0 && c < UD) F[j][c] += w.cstr[i] * u.cpf[j][i] * value;
+                    // the component by a compile-time loop: a run-time index
+                    // would put the stage array in local memory
+                    const int c = cidx[i];  // validated on the host; out of range adds nothing
+                    const P term = w.cstr[i] * u.cpf[j][i] * value;
+#pragma unroll
+                    for (int d = 0; d < UD; d++)
+                        if (d == c) F[j][d] += term;
                 }
             }
         }
@@ -501,10 +507,14 @@ struct Solver {
         for (int j = 0; j < UPL; j++) {
             if (has(lane, j)) {
                 const int uid = unit_of(lane, j);
+#pragma unroll
                 for (int i = 0; i < NC; i++) {
                     const dfloat value = coupling_value<S, dfloat>(Md, w, uid, i);
                     const int c = cidx[i];
-                    if (c >= 0 && c < UD) F[j][c] += w.cstr[i] * u.cpfd[j][i] * value;
+                    const dfloat term = w.cstr[i] * u.cpfd[j][i] * value;
+#pragma unroll
+                    for (int d = 0; d < UD; d++)
+                        if (d == c) F[j][d] += term;
                 }
             }
         }

@@ -293,7 +293,7 @@ struct DfSolver {
     // time, state, control parameters, accessories, tolerances, event
     // tolerances) lies outside float's exponent range, which double-float
     // arithmetic keeps: there it would overflow or lose its low part.
-    __device__ static int range_status(long long i, const Args<double>& a)
+    __device__ __forceinline__ static int range_status(long long i, const Args<double>& a)
     {
         const long long nt = a.nt;
         bool ok = df::in_float_range(a.t[i]);
@@ -312,7 +312,7 @@ struct DfSolver {
         return ok ? 0 : MPGOS_INSTANCE_RANGE;
     }
 
-    __device__ static void begin(Inst& s, long long i, const Args<double>& a, const DfStaged<S>& g,
+    __device__ __forceinline__ static void begin(Inst& s, long long i, const Args<double>& a, const DfStaged<S>& g,
                                  const DfOptions& o)
     {
         const long long nt = a.nt;
@@ -358,7 +358,7 @@ struct DfSolver {
         }
     }
 
-    __device__ static void attempt(Inst& s, const Args<double>& a, const DfStaged<S>& g, const DfOptions& o)
+    __device__ __forceinline__ static void attempt(Inst& s, const Args<double>& a, const DfStaged<S>& g, const DfOptions& o)
     {
         if (s.attempts >= o.max_attempts) {
             s.status |= MPGOS_INSTANCE_ATTEMPT_LIMIT;
@@ -460,7 +460,7 @@ struct DfSolver {
         }
     }
 
-    __device__ static void end(Inst& s, const Args<double>& a, const DfStaged<S>& g)
+    __device__ __forceinline__ static void end(Inst& s, const Args<double>& a, const DfStaged<S>& g)
     {
         const long long i = s.i, nt = a.nt;
         const int ti = static_cast<int>(i), nti = static_cast<int>(nt);
@@ -486,15 +486,18 @@ struct DfSolver {
     }
 };
 
-// Minimum resident blocks of MPGOS_MAX_BLOCK threads the DF_STAGE kernels are
-// compiled for (a register cap: 65536 / (256 x this)); a plugin may raise it.
-#ifndef MPGOS_DF_MIN_BLOCKS
-#define MPGOS_DF_MIN_BLOCKS 1
+// A plugin may define MPGOS_DF_MIN_BLOCKS, the minimum resident blocks of
+// MPGOS_MAX_BLOCK threads the DF_STAGE kernels are compiled for (a register
+// cap: 65536 / (MPGOS_MAX_BLOCK x this)); left undefined, ptxas chooses.
+#ifdef MPGOS_DF_MIN_BLOCKS
+#define MPGOS_DF_BOUNDS __launch_bounds__(MPGOS_MAX_BLOCK, MPGOS_DF_MIN_BLOCKS)
+#else
+#define MPGOS_DF_BOUNDS __launch_bounds__(MPGOS_MAX_BLOCK)
 #endif
 
 // DF_STAGE kernel: same launch contract as perthread_kernel<S, ALG, double, *>.
 template <class S, int MODE, int ALG = MPGOS_RKCK45>
-__global__ void __launch_bounds__(MPGOS_MAX_BLOCK, MPGOS_DF_MIN_BLOCKS) perthread_df_kernel(Args<double> a)
+__global__ void MPGOS_DF_BOUNDS perthread_df_kernel(Args<double> a)
 {
     using Sv = DfSolver<S, MODE, ALG>;
     constexpr int SD = S::SD, NSP = S::NSP, NISP = S::NISP, NE = S::NE;
@@ -548,13 +551,18 @@ __global__ void __launch_bounds__(MPGOS_MAX_BLOCK, MPGOS_DF_MIN_BLOCKS) perthrea
         // warp once per step attempt (as in perthread_kernel)
         unsigned live = __ballot_sync(__activemask(), i < a.n_active);
         if (i >= a.n_active) return;
+        // one call site each of begin, attempt and end (all inlined: an
+        // out-of-line call would put the instance in local memory)
         typename Sv::Inst s;
-        Sv::begin(s, i, a, g, o);
+        bool loaded = false;
         while (true) {
             bool stop = false;
-            if (s.terminate) {
-                Sv::end(s, a, g);
-                i = Next::next_index(a, total, i);
+            if (!loaded || s.terminate) {
+                if (loaded) {
+                    Sv::end(s, a, g);
+                    i = Next::next_index(a, total, i);
+                }
+                loaded = true;
                 if (i >= a.n_active) stop = true;
                 else Sv::begin(s, i, a, g, o);
             }
@@ -565,12 +573,15 @@ __global__ void __launch_bounds__(MPGOS_MAX_BLOCK, MPGOS_DF_MIN_BLOCKS) perthrea
     } else {
         if (i >= a.n_active) return;
         typename Sv::Inst s;
-        Sv::begin(s, i, a, g, o);
+        bool loaded = false;
         while (true) {
-            if (s.terminate) {
-                Sv::end(s, a, g);
-                i = Next::next_index(a, total, i);
-                if (i >= a.n_active) break;
+            if (!loaded || s.terminate) {
+                if (loaded) {
+                    Sv::end(s, a, g);
+                    i = Next::next_index(a, total, i);
+                    if (i >= a.n_active) break;
+                }
+                loaded = true;
                 Sv::begin(s, i, a, g, o);
             }
             Sv::attempt(s, a, g, o);

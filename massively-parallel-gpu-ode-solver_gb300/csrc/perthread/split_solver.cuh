@@ -336,7 +336,7 @@ struct SplitSolver {
 
     // double-float copies the right-hand side reads: all of them when an
     // instance is loaded
-    __device__ static void refresh(Inst& s)
+    __device__ __forceinline__ static void refresh(Inst& s)
     {
 #pragma unroll
         for (int k = 0; k < SD; k++) s.xd[k] = split_guarded(s.x[k], s.status);
@@ -351,7 +351,7 @@ struct SplitSolver {
     // after an attempt: the parameters and accessories the FP64 hooks
     // changed (compared with their values when the attempt began; where the
     // hooks never write them the compiler removes the test)
-    __device__ static void refresh_changed(Inst& s, const double* cp0, const double* acc0)
+    __device__ __forceinline__ static void refresh_changed(Inst& s, const double* cp0, const double* acc0)
     {
 #pragma unroll
         for (int k = 0; k < NCP; k++)
@@ -361,7 +361,7 @@ struct SplitSolver {
             if (bits_of(s.acc[k]) != bits_of(acc0[k])) s.accd[k] = split_guarded(s.acc[k], s.status);
     }
 
-    __device__ static void begin(Inst& s, long long i, const Args<double>& a, const SplitStaged<S>& g)
+    __device__ __forceinline__ static void begin(Inst& s, long long i, const Args<double>& a, const SplitStaged<S>& g)
     {
         const long long nt = a.nt;
         s.i = i;
@@ -406,7 +406,7 @@ struct SplitSolver {
         }
     }
 
-    __device__ static void attempt(Inst& s, const Args<double>& a, const SplitStaged<S>& g)
+    __device__ __forceinline__ static void attempt(Inst& s, const Args<double>& a, const SplitStaged<S>& g)
     {
         const Options<double>& o = a.o;
         if (s.attempts >= o.max_attempts) {
@@ -499,7 +499,7 @@ struct SplitSolver {
         refresh_changed(s, cp0, acc0);
     }
 
-    __device__ static void end(Inst& s, const Args<double>& a, const SplitStaged<S>& g)
+    __device__ __forceinline__ static void end(Inst& s, const Args<double>& a, const SplitStaged<S>& g)
     {
         const long long i = s.i, nt = a.nt;
         const int ti = static_cast<int>(i), nti = static_cast<int>(nt);
@@ -523,15 +523,20 @@ struct SplitSolver {
     }
 };
 
-// Minimum resident blocks of MPGOS_MAX_BLOCK threads the SPLIT kernels are
-// compiled for (a register cap: 65536 / (256 x this)); a plugin may raise it.
-#ifndef MPGOS_SPLIT_MIN_BLOCKS
-#define MPGOS_SPLIT_MIN_BLOCKS 1
+// A plugin may define MPGOS_SPLIT_MIN_BLOCKS, the minimum resident blocks of
+// MPGOS_MAX_BLOCK threads the SPLIT kernels are compiled for (a register cap:
+// 65536 / (MPGOS_MAX_BLOCK x this)). Left undefined, ptxas chooses: stating 1
+// explicitly lets it use more registers (119 instead of 94 on Lorenz, two
+// fewer resident blocks of 64, 5 % slower).
+#ifdef MPGOS_SPLIT_MIN_BLOCKS
+#define MPGOS_SPLIT_BOUNDS __launch_bounds__(MPGOS_MAX_BLOCK, MPGOS_SPLIT_MIN_BLOCKS)
+#else
+#define MPGOS_SPLIT_BOUNDS __launch_bounds__(MPGOS_MAX_BLOCK)
 #endif
 
 // SPLIT kernel: same launch contract as perthread_kernel<S, ALG, double, *>.
 template <class S, int MODE, int ALG = MPGOS_RKCK45>
-__global__ void __launch_bounds__(MPGOS_MAX_BLOCK, MPGOS_SPLIT_MIN_BLOCKS) perthread_split_kernel(Args<double> a)
+__global__ void MPGOS_SPLIT_BOUNDS perthread_split_kernel(Args<double> a)
 {
     using Sv = SplitSolver<S, MODE, ALG>;
     constexpr int SD = S::SD, NSP = S::NSP, NISP = S::NISP, NE = S::NE;
@@ -582,13 +587,18 @@ __global__ void __launch_bounds__(MPGOS_MAX_BLOCK, MPGOS_SPLIT_MIN_BLOCKS) perth
     if constexpr ((MODE & MODE_RECONVERGE) != 0) {
         unsigned live = __ballot_sync(__activemask(), i < a.n_active);
         if (i >= a.n_active) return;
+        // one call site each of begin, attempt and end (all inlined: an
+        // out-of-line call would put the instance in local memory)
         typename Sv::Inst s;
-        Sv::begin(s, i, a, g);
+        bool loaded = false;
         while (true) {
             bool stop = false;
-            if (s.terminate) {
-                Sv::end(s, a, g);
-                i = Next::next_index(a, total, i);
+            if (!loaded || s.terminate) {
+                if (loaded) {
+                    Sv::end(s, a, g);
+                    i = Next::next_index(a, total, i);
+                }
+                loaded = true;
                 if (i >= a.n_active) stop = true;
                 else Sv::begin(s, i, a, g);
             }
@@ -599,12 +609,15 @@ __global__ void __launch_bounds__(MPGOS_MAX_BLOCK, MPGOS_SPLIT_MIN_BLOCKS) perth
     } else {
         if (i >= a.n_active) return;
         typename Sv::Inst s;
-        Sv::begin(s, i, a, g);
+        bool loaded = false;
         while (true) {
-            if (s.terminate) {
-                Sv::end(s, a, g);
-                i = Next::next_index(a, total, i);
-                if (i >= a.n_active) break;
+            if (!loaded || s.terminate) {
+                if (loaded) {
+                    Sv::end(s, a, g);
+                    i = Next::next_index(a, total, i);
+                    if (i >= a.n_active) break;
+                }
+                loaded = true;
                 Sv::begin(s, i, a, g);
             }
             Sv::attempt(s, a, g);
