@@ -46,6 +46,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 from pathlib import Path
 
@@ -917,6 +918,12 @@ def main():
     build.build_all()
     case = W.lorenz_case(nt=args.nt)
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+    # this run's autotuner choices: a solver made later for the same ensemble
+    # and arithmetic (the e2e leg) reads the same launch configuration back
+    tune_cache = os.path.join(tempfile.mkdtemp(prefix="mpgos_bench_"), "autotune.json")
+
+    def arith_of(mode):
+        return mode & (capi.MODE_FAST_CONTROL | capi.MODE_DF_STAGE | capi.MODE_SPLIT)
 
     def measure(mode, steps, warmup, clocks=None, tune=False):
         """Time ``steps`` integrations of the whole ensemble in ``mode``
@@ -924,7 +931,7 @@ def main():
         s = W.load_solver(case, mode=mode, block=128, device=local)
         s.checkpoint_save()
         if tune:
-            s.autotune(arithmetic=mode & (capi.MODE_FAST_CONTROL | capi.MODE_DF_STAGE | capi.MODE_SPLIT))
+            s.autotune(arithmetic=arith_of(mode), cache_path=tune_cache)
         for _ in range(warmup):
             s.checkpoint_restore()
             s.Solve()
@@ -975,7 +982,9 @@ def main():
     # e2e through the public API with host buffers: H2D of every per-instance
     # input of the step (time domain, state, time, rho, step counter), Solve,
     # D2H of the end states and step counters, every step.
-    with W.load_solver(case, mode=chosen["mode"], block=chosen["block"], device=local) as s:
+    with W.load_solver(case, mode=CHOSEN_MODE, block=128, device=local) as s:
+        s.autotune(arithmetic=arith_of(CHOSEN_MODE), cache_path=tune_cache)   # the timed form's configuration
+        e2e_same_config = s.launch_config() == (chosen["grid"], chosen["block"], chosen["mode"])
         h2d = [Variable.TimeDomain, Variable.ActualState, Variable.ActualTime, Variable.ControlParameters,
                Variable.IntegerAccessories]
         d2h = [Variable.ActualState, Variable.IntegerAccessories]
@@ -1001,7 +1010,9 @@ def main():
                "h2d_bytes_per_step": int(sum(s.host(v).nbytes for v in h2d)),
                "d2h_bytes_per_step": int(sum(s.host(v).nbytes for v in d2h)), "steps": e2e_steps,
                "path": "ProblemSolver.SynchroniseFromHostToDevice / Solve / SynchroniseFromDeviceToHost (C-ABI, "
-                       "pinned host buffers)"}
+                       "pinned host buffers)",
+               "launch_configuration": "the timed form's, read back from this run's autotuner cache"
+               if e2e_same_config else "re-tuned (differs from the timed form's)"}
 
     def summarize(r):
         tp = dist_max(world, sum(r["step_ms"]) / 1e3)

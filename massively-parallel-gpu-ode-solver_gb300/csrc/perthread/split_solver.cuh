@@ -13,7 +13,9 @@
 //     the minimum ratio R = min(1e30, min_i tol_i/err_i) are FP64 quantities;
 //     comparisons of these non-negative doubles run exactly on their bit
 //     patterns or, outside a narrow band where FP32 log2 estimates decide
-//     them, as FP64 products (control_rkck45_split);
+//     them, as FP64 products (control_rkck45_split); the FP64 values are
+//     formed only where a decision or the factor needs them (the estimate of
+//     log2 err comes from the double-float error sum directly);
 //   * the step factor 0.9 R^(1/5) (0.9 R^(1/4) after a rejection,
 //     ErrorControllers.cuh:44-53) is evaluated to FP64 accuracy (a few ulp):
 //     an FP32 estimate corrected in FP64 by a second-order binomial series
@@ -81,6 +83,8 @@ struct SplitStaged {
 };
 
 // double -> double-float with the range guard
+__device__ __forceinline__ bool finite_float(float f) { return (__float_as_uint(f) & 0x7f800000u) != 0x7f800000u; }
+
 __device__ __forceinline__ dfloat split_guarded(double v, int& status)
 {
     if (!df::in_float_range(v)) status |= MPGOS_INSTANCE_RANGE;
@@ -92,8 +96,8 @@ __device__ __forceinline__ dfloat split_guarded(double v, int& status)
 // update and error estimate from the two sums rounded to FP64.
 template <int SD, bool OUTLINE>
 __device__ __forceinline__ void step_rkck45_split(int tid, int nt, dfloat t, double dt, dfloat dtd, const double* x,
-                                                  dfloat* xd, double* xn, double* err, int& finite, dfloat* cp,
-                                                  dfloat* sp, int* spi, dfloat* acc, int* acci)
+                                                  dfloat* xd, double* xn, df::prod_sum* esum, int& finite,
+                                                  dfloat* cp, dfloat* sp, int* spi, dfloat* acc, int* acci)
 {
     using df::fma;
     using df::prod_sum;
@@ -158,12 +162,13 @@ __device__ __forceinline__ void step_rkck45_split(int tid, int nt, dfloat t, dou
         prod_sum_add(e, dfloat(125.0 / 594.0 - 13525.0 / 55296.0), k4[i]);
         prod_sum_add(e, dfloat(0.0 - 277.0 / 14336.0), k5[i]);
         prod_sum_add(e, dfloat(512.0 / 1771.0 - 1.0 / 4.0), k6[i]);
-        // the unnormalised sums h + l rounded once to FP64
+        // the unnormalised sum h + l rounded once to FP64; the error sum is
+        // kept as its pair (its FP64 estimate dt |h + l| + 1e-18 is formed
+        // by the controller where a decision needs it)
         const double sb = df::widen(s.h) + df::widen(s.l);
-        const double se = df::widen(e.h) + df::widen(e.l);
-        xn[i]  = __fma_rn(dt, sb, x[i]);
-        err[i] = __fma_rn(dt, fabs(se), 1e-18);
-        if (!finite_bits(xn[i]) || !finite_bits(err[i])) finite = 0;
+        xn[i]   = __fma_rn(dt, sb, x[i]);
+        esum[i] = e;
+        if (!finite_bits(xn[i]) || !finite_float(e.h) || !finite_float(e.l)) finite = 0;
     }
 }
 
@@ -209,6 +214,21 @@ __device__ __forceinline__ void step_rk4_split(int tid, int nt, dfloat t, double
 // runs instead.
 constexpr float SPLIT_BAND = 1e-4f;
 
+// The FP64 error estimate dt |sum_j e_j k_j| + 1e-18 of Steppers.cuh:280-285
+// from the double-float error sum h + l (rounded once to FP64).
+__device__ __forceinline__ double split_error(double dt, float h, float l)
+{
+    return __fma_rn(dt, fabs(df::widen(h) + df::widen(l)), 1e-18);
+}
+
+// FP32 estimate of log2 of that error from the float sum of the pair
+// (correctly rounded) and the leading float of dt (within 2^-23 of it):
+// relative error below 2^-21, far inside the 1e-4 decision band
+__device__ __forceinline__ float split_log2_error(float dt_hi, float h, float l)
+{
+    return __log2f(fmaf(dt_hi, fabsf(h + l), 1e-18f));
+}
+
 // The exact FP64 forms behind the estimates, out of line: they run only
 // inside the band (a rare branch, not predicated into every attempt).
 static __device__ __noinline__ double split_tolerance(double rtol, double atol, long long mag_bits)
@@ -216,9 +236,10 @@ static __device__ __noinline__ double split_tolerance(double rtol, double atol, 
     return from_bits(max_bits(bits_of(rtol * from_bits(mag_bits)), bits_of(atol)));
 }
 
-static __device__ __noinline__ int split_accepts(double rtol, double atol, long long mag_bits, double err)
+static __device__ __noinline__ int split_accepts(double rtol, double atol, long long mag_bits, double dt, float h,
+                                                 float l)
 {
-    return bits_of(err) < bits_of(split_tolerance(rtol, atol, mag_bits));
+    return bits_of(split_error(dt, h, l)) < bits_of(split_tolerance(rtol, atol, mag_bits));
 }
 
 // tol_a / err_a < tol_b / err_b for positive values, by cross multiplication
@@ -234,37 +255,41 @@ constexpr float SPLIT_LOG2_RATIO_CAP = 99.65784f;
 // Step-size control of the split (ErrorControllers.cuh:23-85) on FP64 values
 // with exact decisions and an FP64-accurate factor:
 //   accept iff err_i < tol_i = max(rtol_i max(|xn_i|, |x_i|), atol_i) for
-//   every i: decided by d_i = log2 tol_i - log2 err_i (FP32 estimates, with
-//   log2 tol_i = max(log2 rtol_i + log2 m_i, log2 atol_i)) outside a 1e-4
-//   band, by the FP64 comparison inside it;
+//   every i, err_i = dt |h_i + l_i| + 1e-18 the FP64 error estimate of the
+//   double-float error sum: decided by d_i = log2 tol_i - log2 err_i (FP32
+//   estimates, with log2 tol_i = max(log2 rtol_i + log2 m_i, log2 atol_i) and
+//   log2 err_i from the float sum of the pair) outside a 1e-4 band, by the
+//   FP64 comparison inside it;
 //   R = min(1e30, min_i tol_i / err_i): the component of the smallest d_i,
-//   ties inside the band settled by cross-multiplied FP64 products; tol of
-//   that component formed in FP64;
+//   ties inside the band settled by cross-multiplied FP64 products; tol and
+//   err formed in FP64 for that component only;
 //   q = 0.9 R^(1/5) (1/4 after a rejection) to FP64 accuracy
 //   (df::root_refine), where the clamp to [shrink, grow] does not decide it
 //   from the estimate alone; new step dt q clamped to [min_dt, max_dt].
 // lrtol / latol: log2 of the tolerances (per block, FP32); shrink_f /
-// grow_f: the limits as floats.
+// grow_f: the limits as floats; dt_hi: the leading float of dt.
 template <int SD>
 __device__ __forceinline__ void control_rkck45_split(const Options<double>& o, float shrink_f, float grow_f,
-                                                     double dt, const double* x, const double* xn, const double* err,
-                                                     const double* rtol, const double* atol, const float* lrtol,
-                                                     const float* latol, int& update, int& finite, int& terminate,
-                                                     double& new_dt, int& status)
+                                                     double dt, float dt_hi, const double* x, const double* xn,
+                                                     const df::prod_sum* esum, const double* rtol,
+                                                     const double* atol, const float* lrtol, const float* latol,
+                                                     int& update, int& finite, int& terminate, double& new_dt,
+                                                     int& status)
 {
     float dmin = INFINITY;
     long long mag_m = 0;
+    float eh_m = 0.0f, el_m = 0.0f;
     double err_m = 1.0, rtol_m = 0.0, atol_m = 0.0, tol_m = 0.0;
-    bool tol_known = false;   // tol_m already formed (a tie was settled)
+    bool exact_known = false;   // tol_m and err_m already formed (a tie was settled)
 #pragma unroll
     for (int i = 0; i < SD; i++) {
         const long long mag = max_bits(abs_bits(xn[i]), abs_bits(x[i]));
         const float lt = fmaxf(lrtol[i] + df::log2_estimate(from_bits(mag)), latol[i]);
-        const float d  = lt - df::log2_estimate(err[i]);
+        const float d  = lt - split_log2_error(dt_hi, esum[i].h, esum[i].l);
         int accept_i;
         if (d > SPLIT_BAND) accept_i = 1;
         else if (d < -SPLIT_BAND) accept_i = 0;
-        else accept_i = split_accepts(rtol[i], atol[i], mag, err[i]);
+        else accept_i = split_accepts(rtol[i], atol[i], mag, dt, esum[i].h, esum[i].l);
         update = update && accept_i;
         bool take, settled = false;
         if (i == 0 || d < dmin - SPLIT_BAND) {
@@ -273,23 +298,34 @@ __device__ __forceinline__ void control_rkck45_split(const Options<double>& o, f
             take = false;
         } else {
             // a tie within the estimates' error: compare the ratios exactly;
-            // tol_m is then the exact tolerance of whichever component wins
+            // tol_m and err_m are then those of whichever component wins
             const double tol_i = split_tolerance(rtol[i], atol[i], mag);
-            if (!tol_known) tol_m = split_tolerance(rtol_m, atol_m, mag_m);
-            take    = split_ratio_less(tol_i, err[i], tol_m, err_m);
+            const double err_i = split_error(dt, esum[i].h, esum[i].l);
+            if (!exact_known) {
+                tol_m = split_tolerance(rtol_m, atol_m, mag_m);
+                err_m = split_error(dt, eh_m, el_m);
+            }
+            take    = split_ratio_less(tol_i, err_i, tol_m, err_m);
             settled = true;
-            if (take) tol_m = tol_i;
+            if (take) {
+                tol_m = tol_i;
+                err_m = err_i;
+            }
         }
-        tol_known = settled || (!take && tol_known);
+        exact_known = settled || (!take && exact_known);
         if (take) {
             dmin   = d;
             mag_m  = mag;
-            err_m  = err[i];
+            eh_m   = esum[i].h;
+            el_m   = esum[i].l;
             rtol_m = rtol[i];
             atol_m = atol[i];
         }
     }
-    if (!tol_known) tol_m = from_bits(max_bits(bits_of(rtol_m * from_bits(mag_m)), bits_of(atol_m)));
+    if (!exact_known) {
+        tol_m = from_bits(max_bits(bits_of(rtol_m * from_bits(mag_m)), bits_of(atol_m)));
+        err_m = split_error(dt, eh_m, el_m);
+    }
     // the reference's initial ratio 1e30 caps R
     if (dmin > SPLIT_LOG2_RATIO_CAP + SPLIT_BAND ||
         (!(dmin < SPLIT_LOG2_RATIO_CAP - SPLIT_BAND) && !split_ratio_less(tol_m, err_m, 1e30, 1.0))) {
@@ -436,11 +472,11 @@ struct SplitSolver {
                                         s.accd, s.acci);
             control_rk4<double>(o, finite, s.terminate, s.new_dt, s.status);
         } else {
-            double err[SD];
-            step_rkck45_split<SD, OUTLINE>(ti, nti, s.tdf, s.dt, dtd, s.x, s.xd, xn, err, finite, s.cpd, g.spd,
+            df::prod_sum esum[SD];
+            step_rkck45_split<SD, OUTLINE>(ti, nti, s.tdf, s.dt, dtd, s.x, s.xd, xn, esum, finite, s.cpd, g.spd,
                                            g.spi, s.accd, s.acci);
-            control_rkck45_split<SD>(o, g.shrink_f, g.grow_f, s.dt, s.x, xn, err, g.rtol, g.atol, g.lrtol, g.latol,
-                                     update, finite, s.terminate, s.new_dt, s.status);
+            control_rkck45_split<SD>(o, g.shrink_f, g.grow_f, s.dt, dtd.hi, s.x, xn, esum, g.rtol, g.atol, g.lrtol,
+                                     g.latol, update, finite, s.terminate, s.new_dt, s.status);
         }
 
         double gn[AtLeastOne<NE>::value];
