@@ -29,6 +29,23 @@
 
 #include "df_convert.cuh"
 
+// The solver steps (begin, attempt, end) take the instance by reference from
+// one call site each. Left out of line, the whole instance lives in local
+// memory: the compiler does that for the Keller-Miksis kernels with the
+// right-hand side inlined six times (448-592 bytes of stack per thread), not
+// for the out-of-line twins that the autotuner picks for that system, nor for
+// small systems. Forcing the steps inline removes it but multiplies the
+// optimiser's time (a Keller-Miksis kernel set 57 s -> 356 s, the drop-in
+// tutorial's translation unit 95 s -> over 20 min), so it is opt-in: define
+// MPGOS_FORCE_INLINE_STEPS.
+#ifndef MPGOS_STEP_INLINE
+#if defined(MPGOS_FORCE_INLINE_STEPS)
+#define MPGOS_STEP_INLINE __forceinline__
+#else
+#define MPGOS_STEP_INLINE
+#endif
+#endif
+
 namespace mpgos {
 namespace pt {
 
@@ -293,7 +310,7 @@ struct DfSolver {
     // time, state, control parameters, accessories, tolerances, event
     // tolerances) lies outside float's exponent range, which double-float
     // arithmetic keeps: there it would overflow or lose its low part.
-    __device__ __forceinline__ static int range_status(long long i, const Args<double>& a)
+    __device__ MPGOS_STEP_INLINE static int range_status(long long i, const Args<double>& a)
     {
         const long long nt = a.nt;
         bool ok = df::in_float_range(a.t[i]);
@@ -312,7 +329,7 @@ struct DfSolver {
         return ok ? 0 : MPGOS_INSTANCE_RANGE;
     }
 
-    __device__ __forceinline__ static void begin(Inst& s, long long i, const Args<double>& a, const DfStaged<S>& g,
+    __device__ MPGOS_STEP_INLINE static void begin(Inst& s, long long i, const Args<double>& a, const DfStaged<S>& g,
                                  const DfOptions& o)
     {
         const long long nt = a.nt;
@@ -358,7 +375,7 @@ struct DfSolver {
         }
     }
 
-    __device__ __forceinline__ static void attempt(Inst& s, const Args<double>& a, const DfStaged<S>& g, const DfOptions& o)
+    __device__ MPGOS_STEP_INLINE static void attempt(Inst& s, const Args<double>& a, const DfStaged<S>& g, const DfOptions& o)
     {
         if (s.attempts >= o.max_attempts) {
             s.status |= MPGOS_INSTANCE_ATTEMPT_LIMIT;
@@ -460,7 +477,7 @@ struct DfSolver {
         }
     }
 
-    __device__ __forceinline__ static void end(Inst& s, const Args<double>& a, const DfStaged<S>& g)
+    __device__ MPGOS_STEP_INLINE static void end(Inst& s, const Args<double>& a, const DfStaged<S>& g)
     {
         const long long i = s.i, nt = a.nt;
         const int ti = static_cast<int>(i), nti = static_cast<int>(nt);

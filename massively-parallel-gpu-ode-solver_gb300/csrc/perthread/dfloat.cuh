@@ -356,7 +356,15 @@ constexpr float PIO128_2 = PIO2_2 * 0x1p-6f;
 constexpr float PIO128_3 = PIO2_3 * 0x1p-6f;
 constexpr float SIXTH_HI = 0x1.555556p-3f;     // 1/6 = SIXTH_HI + SIXTH_LO
 constexpr float SIXTH_LO = -0x1.555556p-28f;
-constexpr float TRIG_TABLE_LIMIT = 0x1p+14f;   // |x| below: the table path
+// |x| below: the table path (a plugin may define MPGOS_DF_TRIG_SERIES to take
+// the series path for every argument)
+#ifdef MPGOS_DF_TRIG_SERIES
+constexpr float TRIG_TABLE_LIMIT = 0.0f;
+constexpr float TRIGPI_TABLE_LIMIT = 0.0f;
+#else
+constexpr float TRIG_TABLE_LIMIT = 0x1p+14f;
+constexpr float TRIGPI_TABLE_LIMIT = 0x1p+16f;
+#endif
 
 #if defined(__CUDACC__)
 static __device__ const float4 TRIG_MAIN_DEV[64] = {MPGOS_DF_TRIG_TABLE_MAIN};
@@ -676,7 +684,7 @@ MPGOS_DF_HD void sincos(dfloat a, dfloat* s, dfloat* c)
 // 2^22 the same with k/2 and both series kernels); no rounding grows with |a|.
 MPGOS_DF_HD void sincospi(dfloat a, dfloat* s, dfloat* c)
 {
-    if (std::fabs(a.hi) < 0x1p+16f) {
+    if (std::fabs(a.hi) < detail::TRIGPI_TABLE_LIMIT) {
         const float k = f_rint(f_mul(a.hi, 128.0f));
         const dfloat f = two_sum(f_sub(a.hi, f_mul(k, 0x1p-7f)), a.lo);
         const dfloat r = f * dfloat(0x1.921fb6p+1f, -0x1.777a5cp-24f);   // pi

@@ -46,6 +46,23 @@
 
 #include "df_convert.cuh"
 
+// The solver steps (begin, attempt, end) take the instance by reference from
+// one call site each. Left out of line, the whole instance lives in local
+// memory: the compiler does that for the Keller-Miksis kernels with the
+// right-hand side inlined six times (448-592 bytes of stack per thread), not
+// for the out-of-line twins that the autotuner picks for that system, nor for
+// small systems. Forcing the steps inline removes it but multiplies the
+// optimiser's time (a Keller-Miksis kernel set 57 s -> 356 s, the drop-in
+// tutorial's translation unit 95 s -> over 20 min), so it is opt-in: define
+// MPGOS_FORCE_INLINE_STEPS.
+#ifndef MPGOS_STEP_INLINE
+#if defined(MPGOS_FORCE_INLINE_STEPS)
+#define MPGOS_STEP_INLINE __forceinline__
+#else
+#define MPGOS_STEP_INLINE
+#endif
+#endif
+
 namespace mpgos {
 namespace pt {
 
@@ -372,7 +389,7 @@ struct SplitSolver {
 
     // double-float copies the right-hand side reads: all of them when an
     // instance is loaded
-    __device__ __forceinline__ static void refresh(Inst& s)
+    __device__ MPGOS_STEP_INLINE static void refresh(Inst& s)
     {
 #pragma unroll
         for (int k = 0; k < SD; k++) s.xd[k] = split_guarded(s.x[k], s.status);
@@ -387,7 +404,7 @@ struct SplitSolver {
     // after an attempt: the parameters and accessories the FP64 hooks
     // changed (compared with their values when the attempt began; where the
     // hooks never write them the compiler removes the test)
-    __device__ __forceinline__ static void refresh_changed(Inst& s, const double* cp0, const double* acc0)
+    __device__ MPGOS_STEP_INLINE static void refresh_changed(Inst& s, const double* cp0, const double* acc0)
     {
 #pragma unroll
         for (int k = 0; k < NCP; k++)
@@ -397,7 +414,7 @@ struct SplitSolver {
             if (bits_of(s.acc[k]) != bits_of(acc0[k])) s.accd[k] = split_guarded(s.acc[k], s.status);
     }
 
-    __device__ __forceinline__ static void begin(Inst& s, long long i, const Args<double>& a, const SplitStaged<S>& g)
+    __device__ MPGOS_STEP_INLINE static void begin(Inst& s, long long i, const Args<double>& a, const SplitStaged<S>& g)
     {
         const long long nt = a.nt;
         s.i = i;
@@ -442,7 +459,7 @@ struct SplitSolver {
         }
     }
 
-    __device__ __forceinline__ static void attempt(Inst& s, const Args<double>& a, const SplitStaged<S>& g)
+    __device__ MPGOS_STEP_INLINE static void attempt(Inst& s, const Args<double>& a, const SplitStaged<S>& g)
     {
         const Options<double>& o = a.o;
         if (s.attempts >= o.max_attempts) {
@@ -535,7 +552,7 @@ struct SplitSolver {
         refresh_changed(s, cp0, acc0);
     }
 
-    __device__ __forceinline__ static void end(Inst& s, const Args<double>& a, const SplitStaged<S>& g)
+    __device__ MPGOS_STEP_INLINE static void end(Inst& s, const Args<double>& a, const SplitStaged<S>& g)
     {
         const long long i = s.i, nt = a.nt;
         const int ti = static_cast<int>(i), nti = static_cast<int>(nt);
