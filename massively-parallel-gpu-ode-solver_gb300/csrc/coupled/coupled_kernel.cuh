@@ -173,6 +173,15 @@ __device__ __forceinline__ void df_dot_acc(float& sh, float& sl, dfloat m, dfloa
     sl = df::f_add(sl, df::f_add(t.lo, df::f_fma(m.hi, c.lo, df::f_fma(m.lo, c.hi, p.lo))));
 }
 
+// Unroll factor of the dense coupling loop (64 or more terms per unit and
+// stage): the whole loop unrolled is hundreds of instructions per copy, and a
+// step inlines one copy per unit of the lane and per stage.
+#ifndef MPGOS_CB_COUPLING_UNROLL
+#define MPGOS_CB_COUPLING_UNROLL 4
+#endif
+#define MPGOS_CB_PRAGMA(x) _Pragma(#x)
+#define MPGOS_CB_UNROLL(n) MPGOS_CB_PRAGMA(unroll n)
+
 template <class S, class P, class W>
 __device__ __forceinline__ P coupling_value(const P* M, const W& w, int unit, int i)
 {
@@ -180,12 +189,14 @@ __device__ __forceinline__ P coupling_value(const P* M, const W& w, int unit, in
     if constexpr (IS_DF<P> && CCI == 0 && CBW == 0) {
         const int shift = i * UPS * UPS;
         float sh = 0.0f, sl = 0.0f;
+        MPGOS_CB_UNROLL(MPGOS_CB_COUPLING_UNROLL)
         for (int col = 0; col < UPS; col++) df_dot_acc(sh, sl, M[unit + col * UPS + shift], w.cpt[col][i]);
         return df::two_sum(sh, sl);
     }
     P v = 0;
     if (CCI == 0 && CBW == 0) {
         const int shift = i * UPS * UPS;
+        MPGOS_CB_UNROLL(MPGOS_CB_COUPLING_UNROLL)
         for (int col = 0; col < UPS; col++) v += M[unit + col * UPS + shift] * w.cpt[col][i];
     } else if (CCI == 0 && CBW > 0) {
         const int shift = i * UPS * (2 * CBW + 1);
