@@ -79,3 +79,42 @@ def test_split_step_factor_is_fp64_accurate(conversions):
     corrected in FP64 lands within a few ulp of the exact root (CUDA's FP64
     pow is specified to 2 ulp)."""
     assert conversions["root_max_ulp"] <= 4.0, conversions["root_max_ulp"]
+
+
+def _trig_table():
+    """The committed table of sin / cos (j pi/128) as numbers: {name: [64 x k] floats}."""
+    import re
+    text = (HEADER_DIR / "dfloat_trig_table.h").read_text()
+    out = {}
+    for name in ("MAIN", "TAIL"):
+        body = text.split(f"#define MPGOS_DF_TRIG_TABLE_{name}")[1].split("#define")[0]
+        rows = re.findall(r"\{([^}]*)\}", body)
+        out[name] = [[float.fromhex(v.strip()[:-1]) for v in r.split(",")] for r in rows]
+    return out
+
+
+def test_trig_table_entries_are_triple_float_sines_and_cosines():
+    """sin(j pi/128) and cos(j pi/128), j = 0..63: hi + lo + lo2 within 4e-19 of
+    the long double values (the table carries ~72 bits; an x86 long double
+    angle and sine carry 64, a few 1e-20 here), every part a float and |lo| at
+    most half an ulp of hi."""
+    import numpy as np
+    t = _trig_table()
+    assert len(t["MAIN"]) == 64 and len(t["TAIL"]) == 64
+    pi = np.longdouble("3.14159265358979323846264338327950288")
+    for j, (m, tail) in enumerate(zip(t["MAIN"], t["TAIL"])):
+        a = pi * j / np.longdouble(128)
+        for (hi, lo, lo2), f in (((m[0], m[1], tail[0]), np.sin), ((m[2], m[3], tail[1]), np.cos)):
+            exact = f(a)
+            got = np.longdouble(hi) + np.longdouble(lo) + np.longdouble(lo2)
+            assert abs(got - exact) <= 4e-19, (j, float(got - exact))
+            assert np.float32(hi) == hi and np.float32(lo) == lo and np.float32(lo2) == lo2
+            if hi != 0.0:
+                assert abs(lo) <= np.spacing(np.float32(abs(hi))) / 2, (j, hi, lo)
+
+
+def test_trig_table_is_what_the_generator_writes():
+    pytest.importorskip("mpmath")
+    gen = HEADER_DIR / "gen_dfloat_trig_table.py"
+    out = subprocess.run(["python3", str(gen)], check=True, capture_output=True, text=True).stdout
+    assert out == (HEADER_DIR / "dfloat_trig_table.h").read_text()
