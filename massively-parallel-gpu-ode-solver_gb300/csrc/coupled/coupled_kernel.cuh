@@ -281,9 +281,22 @@ static __device__ __noinline__ double split_tolerance(double rtol, double atol, 
 {
     return from_bits(max_bits(bits_of(rtol * from_bits(mag_bits)), bits_of(atol)));
 }
-static __device__ __noinline__ int split_accepts(double rtol, double atol, long long mag_bits, double err)
+// The FP64 error estimate dt |sum_j e_j k_j| + 1e-18 from the double-float
+// error sum h + l, and the FP32 estimate of its log2 (float sum of the pair,
+// the leading float of dt: relative error below 2^-21)
+__device__ __forceinline__ double split_error(double dt, float h, float l)
 {
-    return bits_of(err) < bits_of(split_tolerance(rtol, atol, mag_bits));
+    return __fma_rn(dt, fabs(df::widen(h) + df::widen(l)), 1e-18);
+}
+__device__ __forceinline__ float split_log2_error(float dt_hi, float h, float l)
+{
+    return __log2f(fmaf(dt_hi, fabsf(h + l), 1e-18f));
+}
+__device__ __forceinline__ bool finite_float(float f) { return (__float_as_uint(f) & 0x7f800000u) != 0x7f800000u; }
+static __device__ __noinline__ int split_accepts(double rtol, double atol, long long mag_bits, double dt, float h,
+                                                 float l)
+{
+    return bits_of(split_error(dt, h, l)) < bits_of(split_tolerance(rtol, atol, mag_bits));
 }
 // tol_a / err_a < tol_b / err_b for positive values, by cross multiplication
 static __device__ __noinline__ bool split_ratio_less(double tol_a, double err_a, double tol_b, double err_b)
@@ -581,7 +594,7 @@ struct Solver {
     // x + dt sum b k and the error estimate dt |sum e k| + 1e-18 in FP64
     __device__ static void step_rkck45_split(long long s, int lane, Slot& w, Units& u, const dfloat* gpd,
                                              const int* igp, const dfloat* Md, const int* cidx, double t, double dt,
-                                             double (&xn)[UPL][UD], double (&err)[UPL][UD], int& finite)
+                                             double (&xn)[UPL][UD], df::prod_sum (&esum)[UPL][UD], int& finite)
     {
         using df::fma;
         using df::prod_sum;
@@ -653,11 +666,13 @@ struct Solver {
                 prod_sum_add(se, dfloat(125.0 / 594.0 - 13525.0 / 55296.0), k4[j][d]);
                 prod_sum_add(se, dfloat(0.0 - 277.0 / 14336.0), k5[j][d]);
                 prod_sum_add(se, dfloat(512.0 / 1771.0 - 1.0 / 4.0), k6[j][d]);
+                // the error sum kept as its pair: its FP64 estimate is formed
+                // by the controller where a decision or the factor needs it
                 const double b = df::widen(sb.h) + df::widen(sb.l);
-                const double e = df::widen(se.h) + df::widen(se.l);
-                xn[j][d]  = __fma_rn(dt, b, u.x[j][d]);
-                err[j][d] = __fma_rn(dt, fabs(e), 1e-18);
-                if (has(lane, j) && (!finite_bits(xn[j][d]) || !finite_bits(err[j][d]))) finite = 0;
+                xn[j][d]   = __fma_rn(dt, b, u.x[j][d]);
+                esum[j][d] = se;
+                if (has(lane, j) && (!finite_bits(xn[j][d]) || !finite_float(se.h) || !finite_float(se.l)))
+                    finite = 0;
             }
     }
 
@@ -665,22 +680,25 @@ struct Solver {
     // controller, ErrorControllers.cuh:320-423, safety factor 0.8) on FP64
     // values with exact decisions and an FP64-accurate factor: every lane
     // scans its components with FP32 log2 estimates of
-    // d = log2 tol - log2 err, deciding the accept test and its smallest ratio
-    // exactly in FP64 inside a 1e-4 band; the warp takes the smallest
-    // estimate and, where lanes tie within the band, the exact minimum of
-    // their ratios by cross-multiplied FP64 products; then
-    // q = 0.8 R^(1/5) (1/4 after a rejection) to FP64 accuracy where the
-    // clamp to [shrink, grow] does not decide it alone.
+    // d = log2 tol - log2 err (err = dt |h + l| + 1e-18 of the double-float
+    // error sum), deciding the accept test and its smallest ratio exactly in
+    // FP64 inside a 1e-4 band; the warp takes the smallest estimate and, where
+    // lanes tie within the band, the exact minimum of their ratios by
+    // cross-multiplied FP64 products; the FP64 tolerance and error are formed
+    // only for the lanes' candidates; then q = 0.8 R^(1/5) (1/4 after a
+    // rejection) to FP64 accuracy where the clamp to [shrink, grow] does not
+    // decide it alone.
     __device__ static void control_split(int lane, const Options<double>& o, float shrink_f, float grow_f, double dt,
-                                         const Units& u, const double (&xn)[UPL][UD], const double (&err)[UPL][UD],
-                                         const double* rtol, const double* atol, const float* lrtol,
-                                         const float* latol, int& update, int& finite, int& terminate,
-                                         double& new_dt, int& status)
+                                         float dt_hi, const Units& u, const double (&xn)[UPL][UD],
+                                         const df::prod_sum (&esum)[UPL][UD], const double* rtol,
+                                         const double* atol, const float* lrtol, const float* latol, int& update,
+                                         int& finite, int& terminate, double& new_dt, int& status)
     {
         float dmin = INFINITY;
         long long mag_m = 0;
+        float eh_m = 0.0f, el_m = 0.0f;
         double err_m = 1.0, rtol_m = 0.0, atol_m = 0.0, tol_m = 0.0;
-        bool tol_known = false, any = false;
+        bool tol_known = false, any = false;   // tol_known: tol_m and err_m formed
         int lane_update = 1;
 #pragma unroll
         for (int j = 0; j < UPL; j++) {
@@ -689,11 +707,12 @@ struct Solver {
             for (int d = 0; d < UD; d++) {
                 const long long mag = max_bits(abs_bits(xn[j][d]), abs_bits(u.x[j][d]));
                 const float lt = fmaxf(lrtol[d] + df::log2_estimate(from_bits(mag)), latol[d]);
-                const float di = lt - df::log2_estimate(err[j][d]);
+                const float eh = esum[j][d].h, el = esum[j][d].l;
+                const float di = lt - split_log2_error(dt_hi, eh, el);
                 int accept_i;
                 if (di > SPLIT_BAND) accept_i = 1;
                 else if (di < -SPLIT_BAND) accept_i = 0;
-                else accept_i = split_accepts(rtol[d], atol[d], mag, err[j][d]);
+                else accept_i = split_accepts(rtol[d], atol[d], mag, dt, eh, el);
                 lane_update = lane_update & accept_i;
                 bool take, settled = false;
                 if (!any || di < dmin - SPLIT_BAND) {
@@ -702,16 +721,24 @@ struct Solver {
                     take = false;
                 } else {
                     const double tol_i = split_tolerance(rtol[d], atol[d], mag);
-                    if (!tol_known) tol_m = split_tolerance(rtol_m, atol_m, mag_m);
-                    take    = split_ratio_less(tol_i, err[j][d], tol_m, err_m);
+                    const double err_i = split_error(dt, eh, el);
+                    if (!tol_known) {
+                        tol_m = split_tolerance(rtol_m, atol_m, mag_m);
+                        err_m = split_error(dt, eh_m, el_m);
+                    }
+                    take    = split_ratio_less(tol_i, err_i, tol_m, err_m);
                     settled = true;
-                    if (take) tol_m = tol_i;
+                    if (take) {
+                        tol_m = tol_i;
+                        err_m = err_i;
+                    }
                 }
                 tol_known = settled || (!take && tol_known);
                 if (take) {
                     dmin   = di;
                     mag_m  = mag;
-                    err_m  = err[j][d];
+                    eh_m   = eh;
+                    el_m   = el;
                     rtol_m = rtol[d];
                     atol_m = atol[d];
                 }
@@ -724,7 +751,10 @@ struct Solver {
         const float wmin = warp_minf(dmin);
         const bool cand = any && !(dmin > wmin + SPLIT_BAND);
         const unsigned cmask = __ballot_sync(0xffffffffu, cand);
-        if (cand && !tol_known) tol_m = from_bits(max_bits(bits_of(rtol_m * from_bits(mag_m)), bits_of(atol_m)));
+        if (cand && !tol_known) {
+            tol_m = from_bits(max_bits(bits_of(rtol_m * from_bits(mag_m)), bits_of(atol_m)));
+            err_m = split_error(dt, eh_m, el_m);
+        }
         int src = __ffs(cmask) - 1;
         double tol_w = __shfl_sync(0xffffffffu, tol_m, src);
         double err_w = __shfl_sync(0xffffffffu, err_m, src);
@@ -872,9 +902,10 @@ struct Solver {
 
             // ---- stepper
             P xn[UPL][UD], err[UPL][UD];
+            df::prod_sum esum[UPL][UD];   // SPLIT: the double-float error sums
             if constexpr (SPLIT) {
                 if (ALG == MPGOS_RK4) step_rk4_split(s, lane, w, u, gpd, igp, Md, cidx, t, dt, xn, finite);
-                else step_rkck45_split(s, lane, w, u, gpd, igp, Md, cidx, t, dt, xn, err, finite);
+                else step_rkck45_split(s, lane, w, u, gpd, igp, Md, cidx, t, dt, xn, esum, finite);
             } else if (ALG == MPGOS_RK4) {
                 step_rk4(s, lane, w, u, gp, igp, M, cidx, t, dt, xn, finite);
             } else {
@@ -894,8 +925,8 @@ struct Solver {
                 }
                 newdt = o.initial_dt;
             } else if constexpr (SPLIT) {
-                control_split(lane, o, shrink_f, grow_f, dt, u, xn, err, rtol, atol, lrtol, latol, update, finite,
-                              terminate, newdt, status);
+                control_split(lane, o, shrink_f, grow_f, dt, df::split(dt).hi, u, xn, esum, rtol, atol, lrtol, latol,
+                              update, finite, terminate, newdt, status);
             } else if constexpr (IS_DF<P>) {
                 // DF_STAGE: exact double-float accept test, step factor
                 // 0.8 * (min tol/err)^(1/5 or 1/4) from FP32 logarithms of the
