@@ -634,10 +634,11 @@ def uneven_leg(local: int, flush, periods: int) -> dict:
            "phases": periods}
     per_phase = torch.empty((periods, nt), dtype=torch.float64, device=f"cuda:{local}")
 
-    def run(mode, block=128, tune=False, outline=0, reps=2):
+    def run(mode, block=128, tune=False, outline=0, order=0, reps=2):
         with W.load_solver(case, mode=mode, block=block, device=local) as s:
             s.checkpoint_save()
             s.SolverOption(capi.Option.OutlineRhs, outline)
+            s.SolverOption(capi.Option.WorkOrder, order)
             if tune:   # one Solve() (one period) per candidate
                 s.autotune(arithmetic=mode & (capi.MODE_FAST_CONTROL | capi.MODE_DF_STAGE | capi.MODE_SPLIT))
             grid, blk, m = s.launch_config()
@@ -658,16 +659,23 @@ def uneven_leg(local: int, flush, periods: int) -> dict:
                 "grid": grid, "block": blk, "mode": m, "outline_rhs": outline}, res
 
     P = capi.MODE_PERSISTENT
-    # (mode, block, autotuned, right-hand side out of line)
-    forms = {"split_static_b32": (SPLIT, 32, False, 0), "split_persistent": (SPLIT | P, 128, False, 0),
-             "split_static_b32_outlined": (SPLIT, 32, False, 1), "split_persistent_outlined": (SPLIT | P, 128, False, 1),
-             "split_autotuned": (SPLIT, 128, True, 0), "df_static_b32": (DF, 32, False, 0),
-             "df_persistent": (DF | P, 128, False, 0), "df_static_b32_outlined": (DF, 32, False, 1),
-             "df_persistent_outlined": (DF | P, 128, False, 1), "df_autotuned": (DF, 128, True, 0),
-             "fp64_persistent": (capi.MODE_FAST_CONTROL | P, 128, False, 0)}
+    # (mode, block, autotuned, right-hand side out of line, work order: each
+    # launch (period) takes the instances longest first by the previous
+    # launch's step attempts)
+    forms = {"split_static_b32": (SPLIT, 32, False, 0, 0), "split_persistent": (SPLIT | P, 128, False, 0, 0),
+             "split_static_b32_outlined": (SPLIT, 32, False, 1, 0),
+             "split_persistent_outlined": (SPLIT | P, 128, False, 1, 0),
+             "split_static_b32_outlined_ordered": (SPLIT, 32, False, 1, 1),
+             "split_persistent_outlined_ordered": (SPLIT | P, 128, False, 1, 1),
+             "split_autotuned": (SPLIT, 128, True, 0, 0), "df_static_b32": (DF, 32, False, 0, 0),
+             "df_persistent": (DF | P, 128, False, 0, 0), "df_static_b32_outlined": (DF, 32, False, 1, 0),
+             "df_persistent_outlined": (DF | P, 128, False, 1, 0),
+             "df_persistent_outlined_ordered": (DF | P, 128, False, 1, 1), "df_autotuned": (DF, 128, True, 0, 0),
+             "fp64_persistent": (capi.MODE_FAST_CONTROL | P, 128, False, 0, 0),
+             "fp64_persistent_ordered": (capi.MODE_FAST_CONTROL | P, 128, False, 0, 1)}
     results = {}
-    for name, (mode, block, tune, outline) in forms.items():
-        out[name], results[name] = run(mode, block, tune, outline, reps=1 if name.startswith("fp64") else 2)
+    for name, (mode, block, tune, outline, order) in forms.items():
+        out[name], results[name] = run(mode, block, tune, outline, order, reps=1 if name.startswith("fp64") else 2)
     n = results["split_autotuned"]["acci"][1]
     out["steps_per_instance_min_max"] = [int(n.min()), int(n.max())]
     for arith in ("split", "df"):

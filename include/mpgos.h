@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define MPGOS_ABI_VERSION 1
+#define MPGOS_ABI_VERSION 2
 
 /* ---- status codes ------------------------------------------------------ */
 enum mpgos_status {
@@ -92,11 +92,18 @@ enum mpgos_option {
                                                 (a warp ballot; pays where lanes diverge: events, uneven
                                                 accept/reject); 0: leave it to the compiler. Default 1 for
                                                 systems with events, else 0; the autotuner tries both. */
-    MPGOS_OUTLINE_RHS                  = 36  /* DF_STAGE: 1 = the right-hand side as one out-of-line function
+    MPGOS_OUTLINE_RHS                  = 36, /* DF_STAGE: 1 = the right-hand side as one out-of-line function
                                                 (its code once in the kernel instead of once per stage; pays
                                                 for large right-hand sides that overflow the instruction
                                                 cache), 0 = inlined (default); results are identical. The
                                                 autotuner tries both for double-float kernels. */
+    MPGOS_WORK_ORDER                   = 37  /* 1: every launch integrates the instances longest first by
+                                                the step attempts of the previous launch (a counting sort on
+                                                the device before the launch; both mappings: the persistent
+                                                queue and the static lanes take instances in that order),
+                                                so the last wave of an uneven launch is short and a warp's
+                                                lanes hold instances of similar length; 0: index order
+                                                (default). Each instance's results are identical. */
 };
 
 /* ---- kernel modes (extensions) -----------------------------------------
@@ -198,6 +205,7 @@ typedef struct mpgos_pt_launch {
     int32_t*       accepted_steps;  /* [NT] or NULL */
     int32_t*       rejected_steps;  /* [NT] or NULL */
     uint32_t*      work_counter;    /* PERSISTENT: one zeroed counter */
+    const int32_t* instance_order;  /* [n_active] instance of each work item, or NULL (identity) */
 } mpgos_pt_launch;
 
 /* Adjoint tape (extension): frozen step sizes and state checkpoints of a

@@ -581,7 +581,7 @@ __global__ void MPGOS_DF_BOUNDS perthread_df_kernel(Args<double> a)
                 }
                 loaded = true;
                 if (i >= a.n_active) stop = true;
-                else Sv::begin(s, i, a, g, o);
+                else Sv::begin(s, instance_at(a, i), a, g, o);
             }
             if (!stop) Sv::attempt(s, a, g, o);
             live = __ballot_sync(live, !stop);
@@ -599,7 +599,7 @@ __global__ void MPGOS_DF_BOUNDS perthread_df_kernel(Args<double> a)
                     if (i >= a.n_active) break;
                 }
                 loaded = true;
-                Sv::begin(s, i, a, g, o);
+                Sv::begin(s, instance_at(a, i), a, g, o);
             }
             Sv::attempt(s, a, g, o);
         }

@@ -70,10 +70,19 @@ struct Args {
     int* n_acc;
     int* n_rej;
     unsigned int* work;
+    const int* order;  // instance of each work item (MPGOS_WORK_ORDER), or null: the identity
     int prefer_shared;
     Options<P> o;
     Tape tape;
 };
+
+// Instance integrated for work item k (the static mapping's lane / stride
+// index or the persistent queue's count): the runtime's order, or k itself.
+template <class P>
+__device__ __forceinline__ long long instance_at(const Args<P>& a, long long k)
+{
+    return a.order != nullptr ? static_cast<long long>(a.order[k]) : k;
+}
 
 // Registers of one instance between step attempts.
 template <class S, class P>
@@ -392,14 +401,14 @@ __global__ void __launch_bounds__(MPGOS_MAX_BLOCK) perthread_kernel(Args<P> a)
         unsigned live = __ballot_sync(__activemask(), i < a.n_active);
         if (i >= a.n_active) return;
         typename Sv::Inst s;
-        Sv::begin(s, i, a, g, cpf, accf);
+        Sv::begin(s, instance_at(a, i), a, g, cpf, accf);
         while (true) {
             bool stop = false;
             if (s.terminate) {
                 Sv::end(s, a, g);
                 i = Sv::next_index(a, total, i);
                 if (i >= a.n_active) stop = true;
-                else Sv::begin(s, i, a, g, cpf, accf);
+                else Sv::begin(s, instance_at(a, i), a, g, cpf, accf);
             }
             if (!stop) Sv::attempt(s, a, g, cpf, s_spf, accf);
             live = __ballot_sync(live, !stop);
@@ -408,13 +417,13 @@ __global__ void __launch_bounds__(MPGOS_MAX_BLOCK) perthread_kernel(Args<P> a)
     } else {
         if (i >= a.n_active) return;
         typename Sv::Inst s;
-        Sv::begin(s, i, a, g, cpf, accf);
+        Sv::begin(s, instance_at(a, i), a, g, cpf, accf);
         while (true) {
             if (s.terminate) {
                 Sv::end(s, a, g);
                 i = Sv::next_index(a, total, i);
                 if (i >= a.n_active) break;
-                Sv::begin(s, i, a, g, cpf, accf);
+                Sv::begin(s, instance_at(a, i), a, g, cpf, accf);
             }
             Sv::attempt(s, a, g, cpf, s_spf, accf);
         }
@@ -458,6 +467,7 @@ Args<P> make_args(const mpgos_pt_launch& L)
     a.n_acc         = L.accepted_steps;
     a.n_rej         = L.rejected_steps;
     a.work          = L.work_counter;
+    a.order         = L.instance_order;
     a.prefer_shared = L.prefer_shared;
     a.o.initial_dt   = static_cast<P>(L.initial_dt);
     a.o.max_dt       = static_cast<P>(L.max_dt);

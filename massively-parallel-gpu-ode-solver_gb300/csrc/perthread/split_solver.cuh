@@ -653,7 +653,7 @@ __global__ void MPGOS_SPLIT_BOUNDS perthread_split_kernel(Args<double> a)
                 }
                 loaded = true;
                 if (i >= a.n_active) stop = true;
-                else Sv::begin(s, i, a, g);
+                else Sv::begin(s, instance_at(a, i), a, g);
             }
             if (!stop) Sv::attempt(s, a, g);
             live = __ballot_sync(live, !stop);
@@ -671,7 +671,7 @@ __global__ void MPGOS_SPLIT_BOUNDS perthread_split_kernel(Args<double> a)
                     if (i >= a.n_active) break;
                 }
                 loaded = true;
-                Sv::begin(s, i, a, g);
+                Sv::begin(s, instance_at(a, i), a, g);
             }
             Sv::attempt(s, a, g);
         }

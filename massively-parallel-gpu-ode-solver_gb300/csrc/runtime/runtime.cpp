@@ -88,6 +88,11 @@ int set_error(int code, const char* msg)
 }
 }  // namespace mpgos_runtime
 
+// work_order.cu: the longest-first instance order of MPGOS_WORK_ORDER
+int mpgos_internal_order_instances(cudaStream_t stream, const int32_t* nacc, const int32_t* nrej, long long n,
+                                   unsigned* scratch, int32_t* order, int sm_count);
+int mpgos_internal_order_scratch_counters();
+
 struct mpgos_pt_solver {
     const mpgos_pt_kernels* k = nullptr;
     mpgos_pt_shape shape{};
@@ -119,6 +124,9 @@ struct mpgos_pt_solver {
     int32_t ipt = 1;  // instances per thread of the static mapping
     int32_t reconverge = -1;  // MPGOS_WARP_RECONVERGE; -1: by the system (events: 1)
     int32_t outline = 0;      // MPGOS_OUTLINE_RHS (double-float kernels)
+    int32_t work_order = 0;   // MPGOS_WORK_ORDER
+    int32_t* d_order = nullptr;           // [NT] instance of each work item
+    unsigned* d_order_scratch = nullptr;  // counting-sort buckets
     int32_t mode = MPGOS_MODE_PLAIN;
     int64_t max_attempts = 10000000;
     uint64_t generation = 1;  // bumped by every change that alters a launch
@@ -275,6 +283,14 @@ int enqueue_solve(mpgos_pt_solver* s, int32_t mode, int block)
     if (m & MPGOS_MODE_PERSISTENT) MPGOS_CUDA(cudaMemsetAsync(s->d_work, 0, sizeof(uint32_t), s->stream));
     mpgos_pt_launch L;
     fill_launch(s, L, m);
+    if (s->work_order && s->d_order != nullptr) {
+        // longest first by the attempts of the previous launch (on the stream,
+        // so a graph of phases captures it with the launch)
+        rc = mpgos_internal_order_instances(s->stream, L.accepted_steps, L.rejected_steps, s->n_active,
+                                            s->d_order_scratch, s->d_order, s->sm_count);
+        if (rc != 0) return fail(MPGOS_ERR_CUDA, "instance ordering failed: %s", cudaGetErrorString((cudaError_t)rc));
+        L.instance_order = s->d_order;
+    }
     rc = s->k->launch(&L, grid, block, dynamic_smem(s), s->stream);
     if (rc != 0) return fail(MPGOS_ERR_CUDA, "kernel launch failed: %s", cudaGetErrorString((cudaError_t)rc));
     return MPGOS_OK;
@@ -411,7 +427,8 @@ MPGOS_EXPORT int mpgos_pt_destroy(mpgos_pt_solver* s)
         if (b.host) cudaFreeHost(b.host);
         if (b.device) cudaFree(b.device);
     }
-    for (void* p : {s->d_rtol, s->d_atol, s->d_etol, static_cast<void*>(s->d_edir), static_cast<void*>(s->d_work)})
+    for (void* p : {s->d_rtol, s->d_atol, s->d_etol, static_cast<void*>(s->d_edir), static_cast<void*>(s->d_work),
+                    static_cast<void*>(s->d_order), static_cast<void*>(s->d_order_scratch)})
         if (p) cudaFree(p);
     for (void* p : s->checkpoint)
         if (p) cudaFree(p);
@@ -562,6 +579,24 @@ MPGOS_EXPORT int mpgos_pt_set_option(mpgos_pt_solver* s, int32_t option, int32_t
             if (value != 0.0 && value != 1.0) return fail(MPGOS_ERR_ARGUMENT, "OutlineRhs %g must be 0 or 1", value);
             s->outline = static_cast<int32_t>(value);
             break;
+        case MPGOS_WORK_ORDER:
+            if (value != 0.0 && value != 1.0) return fail(MPGOS_ERR_ARGUMENT, "WorkOrder %g must be 0 or 1", value);
+            if (value == 1.0 && s->d_order == nullptr) {
+                MPGOS_CUDA(cudaSetDevice(s->device));
+                const size_t counters = static_cast<size_t>(mpgos_internal_order_scratch_counters());
+                if (cudaMalloc(reinterpret_cast<void**>(&s->d_order), sizeof(int32_t) * std::max<int64_t>(s->nt, 1)) !=
+                        cudaSuccess ||
+                    cudaMalloc(reinterpret_cast<void**>(&s->d_order_scratch), sizeof(unsigned) * counters) !=
+                        cudaSuccess) {
+                    cudaFree(s->d_order);
+                    s->d_order = nullptr;
+                    s->d_order_scratch = nullptr;
+                    return fail(MPGOS_ERR_MEMORY, "work-order buffers (%lld instances) allocation failed",
+                                static_cast<long long>(s->nt));
+                }
+            }
+            s->work_order = static_cast<int32_t>(value);
+            break;
         default:
             return fail(MPGOS_ERR_ARGUMENT, "unknown solver option %d", option);
     }
@@ -603,6 +638,7 @@ MPGOS_EXPORT int mpgos_pt_get_option(const mpgos_pt_solver* s, int32_t option, i
         case MPGOS_INSTANCES_PER_THREAD: *value = s->ipt; break;
         case MPGOS_WARP_RECONVERGE: *value = s->reconverge >= 0 ? s->reconverge : (s->shape.ne > 0 ? 1 : 0); break;
         case MPGOS_OUTLINE_RHS: *value = s->outline; break;
+        case MPGOS_WORK_ORDER: *value = s->work_order; break;
         default: return fail(MPGOS_ERR_ARGUMENT, "unknown solver option %d", option);
     }
     return MPGOS_OK;

@@ -87,7 +87,8 @@ def system_lib(name: str) -> Path:
 
 def build_runtime(force: bool = False) -> Path:
     out = runtime_lib()
-    srcs = [CSRC / "runtime" / "runtime.cpp", CSRC / "runtime" / "runtime_coupled.cpp", CSRC / "runtime" / "probes.cu"]
+    srcs = [CSRC / "runtime" / "runtime.cpp", CSRC / "runtime" / "runtime_coupled.cpp", CSRC / "runtime" / "probes.cu",
+            CSRC / "runtime" / "work_order.cu"]
     deps = [*srcs, INCLUDE_DIR / "mpgos.h"]
     if not force and _newer(out, deps):
         return out

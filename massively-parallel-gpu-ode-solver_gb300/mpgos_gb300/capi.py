@@ -66,6 +66,7 @@ class Option(IntEnum):
     InstancesPerThread = 34
     WarpReconverge = 35
     OutlineRhs = 36
+    WorkOrder = 37
 
 
 MODE_PLAIN = 0
@@ -84,7 +85,7 @@ INSTANCE_ATTEMPT_LIMIT = 8
 INSTANCE_TAPE_OVERFLOW = 16
 INSTANCE_RANGE = 32
 
-ABI_VERSION = 1
+ABI_VERSION = 2
 STATIC_TAPE_BYTES = 16 * 1024 * 1024  # MPGOS_STATIC_TAPE_BYTES of mpgos.h
 
 

@@ -497,6 +497,38 @@ def test_warp_reconvergence_is_scheduling_only(native_libs):
         assert_bitwise(out[0], out[1])
 
 
+@pytest.mark.parametrize("graph", [False, True], ids=["solves", "graph"])
+def test_work_order_is_scheduling_only(graph, native_libs):
+    """WorkOrder (every launch takes the instances longest first by the
+    previous launch's step attempts, sorted on the device) changes only which
+    lane integrates which instance and when: over three periods, as separate
+    solves and as one graph of phases (the second and third launches run in
+    the sorted order), every output of every instance is bit-identical to
+    index order, in FP64, SPLIT and DF_STAGE, static and persistent. Values
+    other than 0 and 1 are refused."""
+    from mpgos_gb300.capi import MpgosError, Option
+    case = W.keller_miksis_case(n_amp=24, n_freq=40, periods=3)
+    for mode in (capi.MODE_PLAIN, capi.MODE_CHOSEN, capi.MODE_SPLIT, capi.MODE_SPLIT | capi.MODE_PERSISTENT,
+                 capi.MODE_DF_STAGE | capi.MODE_PERSISTENT):
+        out = []
+        for order in (0, 1):
+            with W.load_solver(case, mode=mode, block=64) as s:
+                s.SolverOption(Option.WorkOrder, order)
+                assert int(s.GetOption(Option.WorkOrder)) == order
+                if graph:
+                    s.SolvePhases(case.phases)
+                else:
+                    for _ in range(case.phases):
+                        s.Solve()
+                out.append(W.read_results(s))
+        assert_bitwise(out[0], out[1])
+        n = np.asarray(out[0]["nacc"]) + np.asarray(out[0]["nrej"])
+        assert n.max() > 2 * n.min()   # uneven: the order is not the identity
+    with W.load_solver(case, mode=capi.MODE_PLAIN) as s:
+        with pytest.raises(MpgosError):
+            s.SolverOption(Option.WorkOrder, 2)
+
+
 @pytest.mark.parametrize("system", ["keller_miksis", "lorenz", "duffing_rk4"])
 def test_outlined_right_hand_side_is_code_layout_only(system, native_libs):
     """OutlineRhs (double-float kernels: the right-hand side as one
