@@ -672,10 +672,12 @@ def uneven_leg(local: int, flush, periods: int) -> dict:
              "df_persistent_outlined": (DF | P, 128, False, 1, 0),
              "df_persistent_outlined_ordered": (DF | P, 128, False, 1, 1), "df_autotuned": (DF, 128, True, 0, 0),
              "fp64_persistent": (capi.MODE_FAST_CONTROL | P, 128, False, 0, 0),
-             "fp64_persistent_ordered": (capi.MODE_FAST_CONTROL | P, 128, False, 0, 1)}
+             "fp64_persistent_ordered": (capi.MODE_FAST_CONTROL | P, 128, False, 0, 1),
+             "plain_persistent_ordered": (P, 128, False, 0, 1)}
     results = {}
     for name, (mode, block, tune, outline, order) in forms.items():
-        out[name], results[name] = run(mode, block, tune, outline, order, reps=1 if name.startswith("fp64") else 2)
+        out[name], results[name] = run(mode, block, tune, outline, order,
+                                       reps=1 if name.startswith(("fp64", "plain")) else 2)
     n = results["split_autotuned"]["acci"][1]
     out["steps_per_instance_min_max"] = [int(n.min()), int(n.max())]
     for arith in ("split", "df"):
@@ -717,6 +719,11 @@ def uneven_leg(local: int, flush, periods: int) -> dict:
     out["plain_bitwise_equal_to_reference_kernel_2periods"] = bool(all(
         np.array_equal(np.asarray(p2[k]).view(np.uint8), np.asarray(r2[k]).view(np.uint8))
         for k in ("x", "t", "acc", "acci")))
+    # PLAIN with the persistent queue and the work order against the reference
+    # kernel over all periods: the reference's results, bit for bit, sooner
+    out["plain_persistent_ordered_bitwise_equal_to_reference_kernel"] = bool(all(
+        np.array_equal(np.asarray(results["plain_persistent_ordered"][k]).view(np.uint8),
+                       np.asarray(rref[k]).view(np.uint8)) for k in ("x", "t", "acc", "acci")))
     # stable instances: PLAIN (= the reference kernel) with the initial state moved by 1e-13
     end, ints = stable_sets(case, local, rref, keys=("acci",))
     out["stable"] = {"criterion": "PLAIN end state within 1e-10 (scaled) and event / step counts unchanged when "

@@ -387,6 +387,9 @@ def _main(argv=None) -> int:
     ap.add_argument("--outline", action="store_true",
                     help="double-float kernels: the right-hand side out of line (MPGOS_OUTLINE_RHS)")
     ap.add_argument("--periods", type=int, default=None, help="forcing periods (duffing_param, duffing_rk4)")
+    ap.add_argument("--work-order", action="store_true",
+                    help="every launch takes the instances longest first by the previous launch's attempts "
+                         "(MPGOS_WORK_ORDER; the first launch in index order)")
     ap.add_argument("--adjoint", type=int, default=0, metavar="SEG",
                     help="after the launches: one recording pass and one reverse pass with checkpoints every SEG steps")
     a = ap.parse_args(argv)
@@ -404,6 +407,9 @@ def _main(argv=None) -> int:
         if a.outline:
             from .capi import Option
             s.SolverOption(Option.OutlineRhs, 1)
+        if a.work_order:
+            from .capi import Option
+            s.SolverOption(Option.WorkOrder, 1)
         s.checkpoint_save()
         times = []
         for _ in range(a.launches):
