@@ -252,6 +252,30 @@ __device__ __forceinline__ float warp_minf(float v)
 }
 
 // ---- SPLIT helpers -----------------------------------------------------------------
+// Cash-Karp coefficients as double-float pairs (hi = the float nearest, lo =
+// the float nearest the rest: the values dfloat(double) gives), for the
+// split stepper's stage loop: A[i][j] the stage-input weights of stage i,
+// B the 5th-order weights, E the error weights b - b*, C the stage times.
+constexpr float ck_hi(double d) { return static_cast<float>(d); }
+constexpr float ck_lo(double d) { return static_cast<float>(d - static_cast<double>(static_cast<float>(d))); }
+#define MPGOS_CK(d) {ck_hi(d), ck_lo(d)}
+__constant__ float2 CK_A[6][5] = {
+    {MPGOS_CK(0.0), MPGOS_CK(0.0), MPGOS_CK(0.0), MPGOS_CK(0.0), MPGOS_CK(0.0)},
+    {MPGOS_CK(1.0 / 5.0), MPGOS_CK(0.0), MPGOS_CK(0.0), MPGOS_CK(0.0), MPGOS_CK(0.0)},
+    {MPGOS_CK(3.0 / 40.0), MPGOS_CK(9.0 / 40.0), MPGOS_CK(0.0), MPGOS_CK(0.0), MPGOS_CK(0.0)},
+    {MPGOS_CK(3.0 / 10.0), MPGOS_CK(-9.0 / 10.0), MPGOS_CK(6.0 / 5.0), MPGOS_CK(0.0), MPGOS_CK(0.0)},
+    {MPGOS_CK(-11.0 / 54.0), MPGOS_CK(5.0 / 2.0), MPGOS_CK(-70.0 / 27.0), MPGOS_CK(35.0 / 27.0), MPGOS_CK(0.0)},
+    {MPGOS_CK(1631.0 / 55296.0), MPGOS_CK(175.0 / 512.0), MPGOS_CK(575.0 / 13824.0), MPGOS_CK(44275.0 / 110592.0),
+     MPGOS_CK(253.0 / 4096.0)}};
+__constant__ float2 CK_B[6] = {MPGOS_CK(37.0 / 378.0), MPGOS_CK(0.0), MPGOS_CK(250.0 / 621.0),
+                               MPGOS_CK(125.0 / 594.0), MPGOS_CK(0.0), MPGOS_CK(512.0 / 1771.0)};
+__constant__ float2 CK_E[6] = {MPGOS_CK(37.0 / 378.0 - 2825.0 / 27648.0), MPGOS_CK(0.0),
+                               MPGOS_CK(250.0 / 621.0 - 18575.0 / 48384.0),
+                               MPGOS_CK(125.0 / 594.0 - 13525.0 / 55296.0), MPGOS_CK(0.0 - 277.0 / 14336.0),
+                               MPGOS_CK(512.0 / 1771.0 - 1.0 / 4.0)};
+__constant__ float2 CK_C[6] = {MPGOS_CK(0.0), MPGOS_CK(1.0 / 5.0), MPGOS_CK(3.0 / 10.0), MPGOS_CK(3.0 / 5.0),
+                               MPGOS_CK(1.0), MPGOS_CK(7.0 / 8.0)};
+#undef MPGOS_CK
 // Width (log2 units) of the band around a decision inside which the FP32
 // log2 estimates (good to ~4e-6) do not decide and the exact FP64 comparison
 // runs instead; log2(1e30), the cap of the minimum ratio
@@ -590,88 +614,87 @@ struct Solver {
     }
 
     // Cash-Karp 4(5) step of the split: stages and stage sums in
-    // double-float (the per-thread split's sums and order), the update
-    // x + dt sum b k and the error estimate dt |sum e k| + 1e-18 in FP64
+    // double-float, the update x + dt sum b k in FP64, the error sum kept as
+    // its pair. The six stages run as one loop (the unit right-hand sides
+    // and the coupling dot products inlined once instead of six times: the
+    // instruction cache holds the step) whose weights come from the
+    // constant tables above; every stage input, the solution sum and the
+    // error sum accumulate their terms in the order of the per-thread split
+    // (term j added when k_j is known), so the values are those of the
+    // straight-line form.
     __device__ static void step_rkck45_split(long long s, int lane, Slot& w, Units& u, const dfloat* gpd,
                                              const int* igp, const dfloat* Md, const int* cidx, double t, double dt,
                                              double (&xn)[UPL][UD], df::prod_sum (&esum)[UPL][UD], int& finite)
     {
-        using df::fma;
         using df::prod_sum;
         using df::prod_sum_add;
         using df::prod_sum_axpy;
-        using df::prod_sum_start;
         const dfloat td = df::split(t), dtd = df::split(dt);
-        dfloat X[UPL][UD];
-        dfloat k1[UPL][UD], k2[UPL][UD], k3[UPL][UD], k4[UPL][UD], k5[UPL][UD], k6[UPL][UD];
-        stage_rhs_split(s, lane, w, u, gpd, igp, Md, cidx, td, u.xd, k1);
-#pragma unroll
-        for (int j = 0; j < UPL; j++)
-#pragma unroll
-            for (int d = 0; d < UD; d++)
-                X[j][d] = prod_sum_axpy(dtd, prod_sum_start(dfloat(1.0 / 5.0), k1[j][d]), u.xd[j][d]);
-        stage_rhs_split(s, lane, w, u, gpd, igp, Md, cidx, fma(dtd, dfloat(1.0 / 5.0), td), X, k2);
+        prod_sum acc[5][UPL][UD], sb[UPL][UD], se[UPL][UD];
 #pragma unroll
         for (int j = 0; j < UPL; j++)
 #pragma unroll
             for (int d = 0; d < UD; d++) {
-                prod_sum sm = prod_sum_start(dfloat(3.0 / 40.0), k1[j][d]);
-                prod_sum_add(sm, dfloat(9.0 / 40.0), k2[j][d]);
-                X[j][d] = prod_sum_axpy(dtd, sm, u.xd[j][d]);
+#pragma unroll
+                for (int r = 0; r < 5; r++) acc[r][j][d] = prod_sum{0.0f, 0.0f};
+                sb[j][d] = prod_sum{0.0f, 0.0f};
+                se[j][d] = prod_sum{0.0f, 0.0f};
             }
-        stage_rhs_split(s, lane, w, u, gpd, igp, Md, cidx, fma(dtd, dfloat(3.0 / 10.0), td), X, k3);
+#pragma unroll 1
+        for (int st = 0; st < 6; st++) {
+            dfloat X[UPL][UD], k[UPL][UD];
+            // stage input x + dt (sum_j a_st,j k_j): the accumulator of stage st
 #pragma unroll
-        for (int j = 0; j < UPL; j++)
+            for (int j = 0; j < UPL; j++)
 #pragma unroll
-            for (int d = 0; d < UD; d++) {
-                prod_sum sm = prod_sum_start(dfloat(3.0 / 10.0), k1[j][d]);
-                prod_sum_add(sm, dfloat(-9.0 / 10.0), k2[j][d]);
-                prod_sum_add(sm, dfloat(6.0 / 5.0), k3[j][d]);
-                X[j][d] = prod_sum_axpy(dtd, sm, u.xd[j][d]);
+                for (int d = 0; d < UD; d++) {
+                    prod_sum a = acc[0][j][d];
+#pragma unroll
+                    for (int r = 1; r < 5; r++)
+                        if (st == r + 1) a = acc[r][j][d];
+                    X[j][d] = st == 0 ? u.xd[j][d] : prod_sum_axpy(dtd, a, u.xd[j][d]);
+                }
+            const float2 c = CK_C[st];
+            const dfloat T = st == 0 ? td : (st == 4 ? td + dtd : df::fma(dtd, dfloat(c.x, c.y), td));
+            stage_rhs_split(s, lane, w, u, gpd, igp, Md, cidx, T, X, k);
+            // k_st into the inputs of the later stages and into the two sums
+#pragma unroll
+            for (int r = 0; r < 5; r++) {
+                if (r + 1 > st) {
+                    const float2 a = CK_A[r + 1][st];
+                    const dfloat ad(a.x, a.y);
+#pragma unroll
+                    for (int j = 0; j < UPL; j++)
+#pragma unroll
+                        for (int d = 0; d < UD; d++) prod_sum_add(acc[r][j][d], ad, k[j][d]);
+                }
             }
-        stage_rhs_split(s, lane, w, u, gpd, igp, Md, cidx, fma(dtd, dfloat(3.0 / 5.0), td), X, k4);
+            const float2 b = CK_B[st], e = CK_E[st];
+            if (b.x != 0.0f) {
 #pragma unroll
-        for (int j = 0; j < UPL; j++)
+                for (int j = 0; j < UPL; j++)
 #pragma unroll
-            for (int d = 0; d < UD; d++) {
-                prod_sum sm = prod_sum_start(dfloat(-11.0 / 54.0), k1[j][d]);
-                prod_sum_add(sm, dfloat(5.0 / 2.0), k2[j][d]);
-                prod_sum_add(sm, dfloat(-70.0 / 27.0), k3[j][d]);
-                prod_sum_add(sm, dfloat(35.0 / 27.0), k4[j][d]);
-                X[j][d] = prod_sum_axpy(dtd, sm, u.xd[j][d]);
+                    for (int d = 0; d < UD; d++) prod_sum_add(sb[j][d], dfloat(b.x, b.y), k[j][d]);
             }
-        stage_rhs_split(s, lane, w, u, gpd, igp, Md, cidx, td + dtd, X, k5);
+            if (e.x != 0.0f) {
 #pragma unroll
-        for (int j = 0; j < UPL; j++)
+                for (int j = 0; j < UPL; j++)
 #pragma unroll
-            for (int d = 0; d < UD; d++) {
-                prod_sum sm = prod_sum_start(dfloat(1631.0 / 55296.0), k1[j][d]);
-                prod_sum_add(sm, dfloat(175.0 / 512.0), k2[j][d]);
-                prod_sum_add(sm, dfloat(575.0 / 13824.0), k3[j][d]);
-                prod_sum_add(sm, dfloat(44275.0 / 110592.0), k4[j][d]);
-                prod_sum_add(sm, dfloat(253.0 / 4096.0), k5[j][d]);
-                X[j][d] = prod_sum_axpy(dtd, sm, u.xd[j][d]);
+                    for (int d = 0; d < UD; d++) prod_sum_add(se[j][d], dfloat(e.x, e.y), k[j][d]);
             }
-        stage_rhs_split(s, lane, w, u, gpd, igp, Md, cidx, fma(dtd, dfloat(7.0 / 8.0), td), X, k6);
+        }
 #pragma unroll
         for (int j = 0; j < UPL; j++)
 #pragma unroll
             for (int d = 0; d < UD; d++) {
-                prod_sum sb = prod_sum_start(dfloat(37.0 / 378.0), k1[j][d]);
-                prod_sum_add(sb, dfloat(250.0 / 621.0), k3[j][d]);
-                prod_sum_add(sb, dfloat(125.0 / 594.0), k4[j][d]);
-                prod_sum_add(sb, dfloat(512.0 / 1771.0), k6[j][d]);
-                prod_sum se = prod_sum_start(dfloat(37.0 / 378.0 - 2825.0 / 27648.0), k1[j][d]);
-                prod_sum_add(se, dfloat(250.0 / 621.0 - 18575.0 / 48384.0), k3[j][d]);
-                prod_sum_add(se, dfloat(125.0 / 594.0 - 13525.0 / 55296.0), k4[j][d]);
-                prod_sum_add(se, dfloat(0.0 - 277.0 / 14336.0), k5[j][d]);
-                prod_sum_add(se, dfloat(512.0 / 1771.0 - 1.0 / 4.0), k6[j][d]);
-                // the error sum kept as its pair: its FP64 estimate is formed
-                // by the controller where a decision or the factor needs it
-                const double b = df::widen(sb.h) + df::widen(sb.l);
+                // the unnormalised sum h + l rounded once to FP64; the error
+                // sum kept as its pair (the controller forms its FP64
+                // estimate where a decision or the factor needs it)
+                const double b = df::widen(sb[j][d].h) + df::widen(sb[j][d].l);
                 xn[j][d]   = __fma_rn(dt, b, u.x[j][d]);
-                esum[j][d] = se;
-                if (has(lane, j) && (!finite_bits(xn[j][d]) || !finite_float(se.h) || !finite_float(se.l)))
+                esum[j][d] = se[j][d];
+                if (has(lane, j) && (!finite_bits(xn[j][d]) || !finite_float(se[j][d].h) ||
+                                     !finite_float(se[j][d].l)))
                     finite = 0;
             }
     }
