@@ -41,6 +41,7 @@
 #include "../perthread/numerics.cuh"
 #include "../perthread/dfloat.cuh"
 #include "../perthread/df_convert.cuh"
+#include "../perthread/ck_tableau.cuh"
 
 #ifndef MPGOS_CB_MAX_BLOCK
 #define MPGOS_CB_MAX_BLOCK 256
@@ -252,30 +253,8 @@ __device__ __forceinline__ float warp_minf(float v)
 }
 
 // ---- SPLIT helpers -----------------------------------------------------------------
-// Cash-Karp coefficients as double-float pairs (hi = the float nearest, lo =
-// the float nearest the rest: the values dfloat(double) gives), for the
-// split stepper's stage loop: A[i][j] the stage-input weights of stage i,
-// B the 5th-order weights, E the error weights b - b*, C the stage times.
-constexpr float ck_hi(double d) { return static_cast<float>(d); }
-constexpr float ck_lo(double d) { return static_cast<float>(d - static_cast<double>(static_cast<float>(d))); }
-#define MPGOS_CK(d) {ck_hi(d), ck_lo(d)}
-__constant__ float2 CK_A[6][5] = {
-    {MPGOS_CK(0.0), MPGOS_CK(0.0), MPGOS_CK(0.0), MPGOS_CK(0.0), MPGOS_CK(0.0)},
-    {MPGOS_CK(1.0 / 5.0), MPGOS_CK(0.0), MPGOS_CK(0.0), MPGOS_CK(0.0), MPGOS_CK(0.0)},
-    {MPGOS_CK(3.0 / 40.0), MPGOS_CK(9.0 / 40.0), MPGOS_CK(0.0), MPGOS_CK(0.0), MPGOS_CK(0.0)},
-    {MPGOS_CK(3.0 / 10.0), MPGOS_CK(-9.0 / 10.0), MPGOS_CK(6.0 / 5.0), MPGOS_CK(0.0), MPGOS_CK(0.0)},
-    {MPGOS_CK(-11.0 / 54.0), MPGOS_CK(5.0 / 2.0), MPGOS_CK(-70.0 / 27.0), MPGOS_CK(35.0 / 27.0), MPGOS_CK(0.0)},
-    {MPGOS_CK(1631.0 / 55296.0), MPGOS_CK(175.0 / 512.0), MPGOS_CK(575.0 / 13824.0), MPGOS_CK(44275.0 / 110592.0),
-     MPGOS_CK(253.0 / 4096.0)}};
-__constant__ float2 CK_B[6] = {MPGOS_CK(37.0 / 378.0), MPGOS_CK(0.0), MPGOS_CK(250.0 / 621.0),
-                               MPGOS_CK(125.0 / 594.0), MPGOS_CK(0.0), MPGOS_CK(512.0 / 1771.0)};
-__constant__ float2 CK_E[6] = {MPGOS_CK(37.0 / 378.0 - 2825.0 / 27648.0), MPGOS_CK(0.0),
-                               MPGOS_CK(250.0 / 621.0 - 18575.0 / 48384.0),
-                               MPGOS_CK(125.0 / 594.0 - 13525.0 / 55296.0), MPGOS_CK(0.0 - 277.0 / 14336.0),
-                               MPGOS_CK(512.0 / 1771.0 - 1.0 / 4.0)};
-__constant__ float2 CK_C[6] = {MPGOS_CK(0.0), MPGOS_CK(1.0 / 5.0), MPGOS_CK(3.0 / 10.0), MPGOS_CK(3.0 / 5.0),
-                               MPGOS_CK(1.0), MPGOS_CK(7.0 / 8.0)};
-#undef MPGOS_CK
+// The stage loop of the split stepper reads its Cash-Karp weights from
+// constant memory: CK_A, CK_B, CK_E, CK_C (ck_tableau.cuh).
 // Width (log2 units) of the band around a decision inside which the FP32
 // log2 estimates (good to ~4e-6) do not decide and the exact FP64 comparison
 // runs instead; log2(1e30), the cap of the minimum ratio

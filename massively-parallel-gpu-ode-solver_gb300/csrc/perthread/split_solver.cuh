@@ -45,6 +45,7 @@
 #pragma once
 
 #include "df_convert.cuh"
+#include "ck_tableau.cuh"
 
 // The solver steps (begin, attempt, end) take the instance by reference from
 // one call site each. Left out of line, the whole instance lives in local
@@ -186,6 +187,69 @@ __device__ __forceinline__ void step_rkck45_split(int tid, int nt, dfloat t, dou
         xn[i]   = __fma_rn(dt, sb, x[i]);
         esum[i] = e;
         if (!finite_bits(xn[i]) || !finite_float(e.h) || !finite_float(e.l)) finite = 0;
+    }
+}
+
+// The same step with the six stages as one loop (weights from constant
+// memory, the right-hand side inlined once instead of six times); every
+// stage input, the solution sum and the error sum accumulate their terms in
+// the order above (term j added when k_j is known), so the values are those
+// of the straight-line form. A plugin selects it with MPGOS_SPLIT_STAGE_LOOP.
+template <int SD, bool OUTLINE>
+__device__ __forceinline__ void step_rkck45_split_loop(int tid, int nt, dfloat t, double dt, dfloat dtd,
+                                                       const double* x, dfloat* xd, double* xn, df::prod_sum* esum,
+                                                       int& finite, dfloat* cp, dfloat* sp, int* spi, dfloat* acc,
+                                                       int* acci)
+{
+    using df::prod_sum;
+    using df::prod_sum_add;
+    using df::prod_sum_axpy;
+    prod_sum in[5][SD], sb[SD], se[SD];
+#pragma unroll
+    for (int i = 0; i < SD; i++) {
+#pragma unroll
+        for (int r = 0; r < 5; r++) in[r][i] = prod_sum{0.0f, 0.0f};
+        sb[i] = prod_sum{0.0f, 0.0f};
+        se[i] = prod_sum{0.0f, 0.0f};
+    }
+#pragma unroll 1
+    for (int st = 0; st < 6; st++) {
+        dfloat X[SD], k[SD];
+#pragma unroll
+        for (int i = 0; i < SD; i++) {
+            prod_sum a = in[0][i];
+#pragma unroll
+            for (int r = 1; r < 5; r++)
+                if (st == r + 1) a = in[r][i];
+            X[i] = st == 0 ? xd[i] : prod_sum_axpy(dtd, a, xd[i]);
+        }
+        const float2 c = CK_C[st];
+        const dfloat T = st == 0 ? t : (st == 4 ? t + dtd : df::fma(dtd, dfloat(c.x, c.y), t));
+        df_rhs<SD, OUTLINE>(tid, nt, k, X, T, cp, sp, spi, acc, acci);
+#pragma unroll
+        for (int r = 0; r < 5; r++) {
+            if (r + 1 > st) {
+                const float2 a = CK_A[r + 1][st];
+#pragma unroll
+                for (int i = 0; i < SD; i++) prod_sum_add(in[r][i], dfloat(a.x, a.y), k[i]);
+            }
+        }
+        const float2 b = CK_B[st], e = CK_E[st];
+        if (b.x != 0.0f) {
+#pragma unroll
+            for (int i = 0; i < SD; i++) prod_sum_add(sb[i], dfloat(b.x, b.y), k[i]);
+        }
+        if (e.x != 0.0f) {
+#pragma unroll
+            for (int i = 0; i < SD; i++) prod_sum_add(se[i], dfloat(e.x, e.y), k[i]);
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < SD; i++) {
+        const double b = df::widen(sb[i].h) + df::widen(sb[i].l);
+        xn[i]   = __fma_rn(dt, b, x[i]);
+        esum[i] = se[i];
+        if (!finite_bits(xn[i]) || !finite_float(se[i].h) || !finite_float(se[i].l)) finite = 0;
     }
 }
 
@@ -490,8 +554,13 @@ struct SplitSolver {
             control_rk4<double>(o, finite, s.terminate, s.new_dt, s.status);
         } else {
             df::prod_sum esum[SD];
+#ifdef MPGOS_SPLIT_STAGE_LOOP
+            step_rkck45_split_loop<SD, OUTLINE>(ti, nti, s.tdf, s.dt, dtd, s.x, s.xd, xn, esum, finite, s.cpd,
+                                                g.spd, g.spi, s.accd, s.acci);
+#else
             step_rkck45_split<SD, OUTLINE>(ti, nti, s.tdf, s.dt, dtd, s.x, s.xd, xn, esum, finite, s.cpd, g.spd,
                                            g.spi, s.accd, s.acci);
+#endif
             control_rkck45_split<SD>(o, g.shrink_f, g.grow_f, s.dt, dtd.hi, s.x, xn, esum, g.rtol, g.atol, g.lrtol,
                                      g.latol, update, finite, s.terminate, s.new_dt, s.status);
         }
