@@ -90,6 +90,14 @@ MPGOS_DF_HD float f_rint(float a)
     return std::nearbyint(a);
 #endif
 }
+MPGOS_DF_HD float f_nan()
+{
+#if defined(__CUDA_ARCH__)
+    return __int_as_float(0x7fffffff);
+#else
+    return std::nanf("");
+#endif
+}
 MPGOS_DF_HD float f_rcp(float a)
 {
 #if defined(__CUDA_ARCH__)
@@ -365,6 +373,22 @@ constexpr float TRIGPI_TABLE_LIMIT = 0.0f;
 constexpr float TRIG_TABLE_LIMIT = 0x1p+14f;
 constexpr float TRIGPI_TABLE_LIMIT = 0x1p+16f;
 #endif
+// A plugin whose sin / cos / sincos arguments stay below TRIG_TABLE_LIMIT in
+// magnitude, and its sincospi arguments below TRIGPI_TABLE_LIMIT, may define
+// MPGOS_DF_TRIG_BOUNDED: every call then runs the table path alone, without
+// the branch to the wide-range path, and an argument outside the bound (or
+// not finite) gives NaN, which the solver reports as a non-finite step.
+// Without the branch the compiler can interleave a call with the independent
+// work around it (the state arithmetic of a right-hand side, the forcing terms
+// of the other stages; sin and cos of one argument share their reduction).
+#if defined(MPGOS_DF_TRIG_BOUNDED) && defined(MPGOS_DF_TRIG_SERIES)
+#error "MPGOS_DF_TRIG_BOUNDED and MPGOS_DF_TRIG_SERIES exclude each other"
+#endif
+#ifdef MPGOS_DF_TRIG_BOUNDED
+constexpr bool TRIG_BOUNDED = true;
+#else
+constexpr bool TRIG_BOUNDED = false;
+#endif
 
 #if defined(__CUDACC__)
 static __device__ const float4 TRIG_MAIN_DEV[64] = {MPGOS_DF_TRIG_TABLE_MAIN};
@@ -435,10 +459,48 @@ MPGOS_DF_HD void sincos_table(dfloat r, int k, dfloat* s_out, dfloat* c_out)
     *c_out = table_minus(Ca, Ca2, dot2(Ca, h, Sa, s));
     *s_out = table_minus(Sa, Sa2, dot2(Sa, h, -Ca, s));
 }
+
+// sin(pi a), cos(pi a) for |a| < TRIGPI_TABLE_LIMIT: a = k/128 + f, k the
+// nearest integer to 128 a, f exact
+MPGOS_DF_HD void sincospi_table(dfloat a, dfloat* s, dfloat* c)
+{
+    const float k = f_rint(f_mul(a.hi, 128.0f));
+    const dfloat f = two_sum(f_sub(a.hi, f_mul(k, 0x1p-7f)), a.lo);
+    const dfloat r = f * dfloat(0x1.921fb6p+1f, -0x1.777a5cp-24f);   // pi
+    sincos_table(r, static_cast<int>(k), s, c);
+}
+
+// MPGOS_DF_TRIG_BOUNDED forms: the table path on the argument, on zero in its
+// place when it is outside the bound, and NaN selected for such arguments
+MPGOS_DF_HD void sincos_bounded(dfloat a, dfloat* s, dfloat* c)
+{
+    const bool in = std::fabs(a.hi) < TRIG_TABLE_LIMIT;
+    int k;
+    const dfloat r = reduce_pio128(in ? a : dfloat(0.0f), k);
+    dfloat ts, tc;
+    sincos_table(r, k, &ts, &tc);
+    const dfloat nan(f_nan(), f_nan());
+    *s = in ? ts : nan;
+    *c = in ? tc : nan;
+}
+MPGOS_DF_HD void sincospi_bounded(dfloat a, dfloat* s, dfloat* c)
+{
+    const bool in = std::fabs(a.hi) < TRIGPI_TABLE_LIMIT;
+    dfloat ts, tc;
+    sincospi_table(in ? a : dfloat(0.0f), &ts, &tc);
+    const dfloat nan(f_nan(), f_nan());
+    *s = in ? ts : nan;
+    *c = in ? tc : nan;
+}
 }  // namespace detail
 
 MPGOS_DF_HD dfloat sin(dfloat a)
 {
+    if constexpr (detail::TRIG_BOUNDED) {
+        dfloat s, c;
+        detail::sincos_bounded(a, &s, &c);
+        return s;
+    }
     if (std::fabs(a.hi) < detail::TRIG_TABLE_LIMIT) {
         int k;
         const dfloat r = detail::reduce_pio128(a, k);
@@ -458,6 +520,11 @@ MPGOS_DF_HD dfloat sin(dfloat a)
 
 MPGOS_DF_HD dfloat cos(dfloat a)
 {
+    if constexpr (detail::TRIG_BOUNDED) {
+        dfloat s, c;
+        detail::sincos_bounded(a, &s, &c);
+        return c;
+    }
     if (std::fabs(a.hi) < detail::TRIG_TABLE_LIMIT) {
         int k;
         const dfloat r = detail::reduce_pio128(a, k);
@@ -667,6 +734,10 @@ MPGOS_DF_HD void sincos_quadrant(dfloat r, int q, dfloat* s, dfloat* c)
 // sin and cos of one argument with one reduction
 MPGOS_DF_HD void sincos(dfloat a, dfloat* s, dfloat* c)
 {
+    if constexpr (detail::TRIG_BOUNDED) {
+        detail::sincos_bounded(a, s, c);
+        return;
+    }
     if (std::fabs(a.hi) < detail::TRIG_TABLE_LIMIT) {
         int k;
         const dfloat r = detail::reduce_pio128(a, k);
@@ -684,11 +755,12 @@ MPGOS_DF_HD void sincos(dfloat a, dfloat* s, dfloat* c)
 // 2^22 the same with k/2 and both series kernels); no rounding grows with |a|.
 MPGOS_DF_HD void sincospi(dfloat a, dfloat* s, dfloat* c)
 {
+    if constexpr (detail::TRIG_BOUNDED) {
+        detail::sincospi_bounded(a, s, c);
+        return;
+    }
     if (std::fabs(a.hi) < detail::TRIGPI_TABLE_LIMIT) {
-        const float k = f_rint(f_mul(a.hi, 128.0f));
-        const dfloat f = two_sum(f_sub(a.hi, f_mul(k, 0x1p-7f)), a.lo);
-        const dfloat r = f * dfloat(0x1.921fb6p+1f, -0x1.777a5cp-24f);   // pi
-        detail::sincos_table(r, static_cast<int>(k), s, c);
+        detail::sincospi_table(a, s, c);
         return;
     }
     if (!(std::fabs(a.hi) < 0x1p+22f)) {   // beyond, a is an integer or half-integer multiple

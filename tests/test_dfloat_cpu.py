@@ -118,3 +118,21 @@ def test_trig_table_is_what_the_generator_writes():
     gen = HEADER_DIR / "gen_dfloat_trig_table.py"
     out = subprocess.run(["python3", str(gen)], check=True, capture_output=True, text=True).stdout
     assert out == (HEADER_DIR / "dfloat_trig_table.h").read_text()
+
+
+@pytest.mark.parametrize("bounded", [False, True], ids=["default", "bounded"])
+def test_bounded_trig_is_the_table_path_or_nan(tmp_path, bounded):
+    """MPGOS_DF_TRIG_BOUNDED: inside the bounds (|x| < 2^14 for sin/cos,
+    2^16 for sincospi) the branch-free forms give the table path's bits, outside
+    (and for infinities and NaN) NaN in both parts; with the macro defined the
+    public sin, cos, sincos and sincospi are those forms."""
+    exe = tmp_path / "dfloat_bounded_check"
+    subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", f"-I{HEADER_DIR}",
+                    *(["-DMPGOS_DF_TRIG_BOUNDED"] if bounded else []),
+                    str(REPO / "tests" / "dfloat_bounded_check.cpp"), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout
+    got = {k: int(v) for k, v in (line.split() for line in out.strip().splitlines())}
+    assert got["bounded_in_differs"] == 0
+    assert got["bounded_out_not_nan"] == 0
+    assert got["public_differs"] == 0
+    assert got["inside"] > 100000 and got["outside"] > 10000

@@ -338,6 +338,28 @@ def test_status_flags_and_attempt_limit(mode, native_libs, oracle_libs):
     assert np.all(res["nacc"] + res["nrej"] == 10)
 
 
+@pytest.mark.parametrize("mode", [capi.MODE_SPLIT, capi.MODE_DF_STAGE], ids=["split", "df_stage"])
+def test_bounded_trig_reports_arguments_beyond_its_bound(mode, native_libs):
+    """The Duffing plugin is built with MPGOS_DF_TRIG_BOUNDED (branch-free
+    double-float cos for |t| < 2^14): one forcing period moved to start at
+    2^14 gives NaN forcing in the double-float modes, and every instance stops
+    with MPGOS_INSTANCE_NONFINITE instead of integrating a wrong cosine; the
+    FP64 kernel integrates the same period normally, and inside the bound the
+    modes agree with it."""
+    case = W.duffing_rk4_case(nt=256, periods=1)
+    res = W.run_gpu(case, mode=mode)
+    ref = W.run_gpu(case, mode=capi.MODE_PLAIN)
+    assert not np.any(res["status"]) and not np.any(ref["status"])
+    assert np.max(np.abs(res["x"] - ref["x"])) < 1e-12
+    far = case.copy()
+    far.arrays["td"][0] = 2.0 ** 14
+    far.arrays["td"][1] = 2.0 ** 14 + 2.0 * math.pi
+    res = W.run_gpu(far, mode=mode)
+    assert np.all(res["status"] & capi.INSTANCE_NONFINITE)
+    ref = W.run_gpu(far, mode=capi.MODE_PLAIN)
+    assert not np.any(ref["status"])
+
+
 def test_two_solver_objects_alternate(native_libs):
     """Two objects on one device, interleaved as T7_DoubleBuffering does."""
     c1 = W.duffing_rk4_case(nt=512, periods=4)
